@@ -1,0 +1,185 @@
+"""ctypes binding of libabie_gb300 with the reference binding's interface.
+
+``CLibABIE`` has the methods, argument meanings and error behaviour of the
+reference's abie/clibabie.py:8-194 (initialize_code, set_state, get_state,
+integrator_gr raising CloseEncounterException / CollisionException on
+return codes 1 / 2, integrator_wh, get_total_energy, ...).  It differs only
+where the reference binding is broken: the wrappers of the direct
+integrator entry points pass the full argument list (the reference omits
+r_vec), and set_additional_forces passes an integer count.  Negative return
+codes of this library raise ``AbieError``.
+
+Extra methods expose the additive entry points: explicit force forms,
+counters and the batched ensemble.
+"""
+import ctypes
+
+import numpy as np
+
+from . import FORCE_MODES, last_error, load
+from .events import AbieError, CloseEncounterException, CollisionException
+
+_c = ctypes
+
+
+def _vp(a):
+    return _c.c_void_p(a.ctypes.data)
+
+
+def _f64(a):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    return a
+
+
+class Counters(_c.Structure):
+    _fields_ = [("force_calls", _c.c_longlong), ("iterations", _c.c_longlong),
+                ("attempts", _c.c_longlong), ("accepts", _c.c_longlong),
+                ("rejects", _c.c_longlong), ("kepler_failures", _c.c_longlong),
+                ("wh_steps", _c.c_longlong), ("last_h", _c.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class CLibABIE(object):
+    def __init__(self, path=None):
+        self.lib = load(path)
+        self.max_close_encounter_events = 1
+        self.max_collision_events = 1
+
+    # -- helpers ------------------------------------------------------------
+    def _check(self, rc, what):
+        if isinstance(rc, int) and rc < 0:
+            raise AbieError(rc, "%s: %s" % (what, last_error()))
+        return rc
+
+    # -- reference interface (abie/clibabie.py) -----------------------------
+    def initialize_code(self, G, C, N_MAX, MAX_CE_EVENTS=1, MAX_COLLISION_EVENTS=1,
+                        close_encounter_distance=0, deviceID=-1):
+        rc = self.lib.initialize_code(_c.c_double(G), _c.c_double(C), _c.c_int(N_MAX),
+                                      _c.c_int(MAX_CE_EVENTS), _c.c_int(MAX_COLLISION_EVENTS),
+                                      _c.c_int(deviceID))
+        self._check(rc, "initialize_code")
+        self.lib.set_close_encounter_distance(_c.c_double(close_encounter_distance))
+        self.max_close_encounter_events = MAX_CE_EVENTS
+        self.max_collision_events = MAX_COLLISION_EVENTS
+
+    def finalize_code(self):
+        self.lib.finalize_code()
+
+    def set_state(self, pos, vel, masses, radii, N, G, C):
+        pos, vel, masses, radii = _f64(pos), _f64(vel), _f64(masses), _f64(radii)
+        self.lib.set_state(_vp(pos), _vp(vel), _vp(masses), _vp(radii), _c.c_int(N),
+                           _c.c_double(G), _c.c_double(C))
+
+    def get_state(self, pos, vel, masses, radii):
+        rc = self.lib.get_state(_vp(pos), _vp(vel), _vp(masses), _vp(radii))
+        return self._check(rc, "get_state")
+
+    def get_model_time(self):
+        return self.lib.get_model_time()
+
+    def get_close_encounter_data(self):
+        buf = np.zeros(4 * self.max_close_encounter_events)
+        self.lib.get_close_encounter_buffer(_vp(buf))
+        return buf.reshape(self.max_close_encounter_events, 4)
+
+    def get_collision_data(self):
+        buf = np.zeros(4 * self.max_collision_events)
+        self.lib.get_collision_buffer(_vp(buf))
+        return buf.reshape(self.max_collision_events, 4)
+
+    def reset_close_encounter_buffer(self):
+        self.lib.reset_close_encounter_buffer()
+
+    def reset_collision_buffer(self):
+        self.lib.reset_collision_buffer()
+
+    def set_close_encounter_distance(self, value):
+        self.lib.set_close_encounter_distance(_c.c_double(value))
+
+    def get_total_energy(self):
+        return self.lib.calculate_energy()
+
+    def set_additional_forces(self, ext_acc):
+        ext_acc = _f64(ext_acc)
+        self.lib.set_additional_forces(_c.c_int(len(ext_acc) // 3), _vp(ext_acc))
+
+    def integrator_gr(self, t, t_end, dt):
+        ret = self.lib.integrator_gr(_c.c_double(t), _c.c_double(t_end), _c.c_double(dt))
+        if ret == 1:
+            buf = self.get_close_encounter_data()
+            raise CloseEncounterException(buf[-1, 0], int(buf[-1, 1]), int(buf[-1, 2]), buf[-1, 3])
+        elif ret == 2:
+            buf = self.get_collision_data()
+            raise CollisionException(buf[-1, 0], int(buf[-1, 1]), int(buf[-1, 2]), buf[-1, 3])
+        return self._check(ret, "integrator_gr")
+
+    def integrator_rk(self, t, t_end, dt):
+        return self._check(self.lib.integrator_rk(_c.c_double(t), _c.c_double(t_end),
+                                                  _c.c_double(dt)), "integrator_rk")
+
+    def integrator_wh(self, t, t_end, dt):
+        return self._check(self.lib.integrator_wh(_c.c_double(t), _c.c_double(t_end),
+                                                  _c.c_double(dt)), "integrator_wh")
+
+    def ode_n_body_second_order(self, x, N, G, masses):
+        x, masses = _f64(x), _f64(masses)
+        acc = np.zeros(x.size, dtype=np.double)
+        radii = np.zeros(N)
+        rc = self.lib.ode_n_body_second_order(_vp(x), _c.c_size_t(N), _c.c_double(G), _vp(masses),
+                                              _vp(radii), _vp(acc))
+        if rc:
+            raise AbieError(-1, "ode_n_body_second_order: " + last_error())
+        return acc
+
+    # -- additions -----------------------------------------------------------
+    def set_force_mode(self, mode):
+        mode = FORCE_MODES.get(mode, mode)
+        return self._check(self.lib.abie_set_force_mode(_c.c_int(mode)), "set_force_mode")
+
+    def get_force_mode(self):
+        return self.lib.abie_get_force_mode()
+
+    def force(self, pos, masses, G, mode="fp64"):
+        """All-pairs accelerations of host arrays in an explicit force form."""
+        pos, masses = _f64(pos), _f64(masses)
+        acc = np.zeros(pos.size)
+        rc = self.lib.abie_force_host(_vp(pos), _vp(masses), _c.c_size_t(masses.size),
+                                      _c.c_double(G), _vp(acc), _c.c_int(FORCE_MODES.get(mode, mode)))
+        self._check(rc, "abie_force_host")
+        return acc
+
+    def energy(self, pos, vel, masses, G):
+        pos, vel, masses = _f64(pos), _f64(vel), _f64(masses)
+        return self.lib.abie_energy_host(_vp(pos), _vp(vel), _vp(masses),
+                                         _c.c_size_t(masses.size), _c.c_double(G))
+
+    def counters(self):
+        c = Counters()
+        self.lib.abie_get_counters(_c.byref(c))
+        return c.as_dict()
+
+    def reset_counters(self):
+        self.lib.abie_reset_counters()
+
+    def gr_ensemble(self, pos, vel, masses, offsets, G, t0, t_end, learned=False):
+        """Radau15 over a ragged batch of independent systems (in place)."""
+        pos, vel, masses = _f64(pos).copy(), _f64(vel).copy(), _f64(masses)
+        offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+        ns = offsets.size - 1
+        t_out = np.zeros(ns)
+        status = np.zeros(ns, dtype=np.int32)
+        steps = np.zeros(ns, dtype=np.int64)
+        rc = self.lib.abie_gr_ensemble(_vp(pos), _vp(vel), _vp(masses), _vp(offsets), _c.c_int(ns),
+                                       _c.c_double(G), _c.c_double(t0), _c.c_double(t_end),
+                                       _vp(t_out), _vp(status), _vp(steps), _c.c_int(int(learned)))
+        self._check(rc, "abie_gr_ensemble")
+        return {"pos": pos, "vel": vel, "t": t_out, "status": status, "steps": steps,
+                "seconds": self.lib.abie_last_ensemble_seconds()}
+
+    def measure_peaks(self):
+        f64, f32 = _c.c_double(0), _c.c_double(0)
+        self._check(self.lib.abie_measure_fp64_peak(_c.c_int(0), _c.byref(f64)), "fp64 probe")
+        self._check(self.lib.abie_measure_fp32_peak(_c.c_int(0), _c.byref(f32)), "fp32 probe")
+        return {"fp64_tflops": f64.value, "fp32_tflops": f32.value}

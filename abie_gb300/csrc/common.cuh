@@ -1,0 +1,137 @@
+// Shared definitions for the GB300 gravity library.
+//
+// Every translation unit is compiled with --fmad=false: a product followed
+// by a sum is rounded twice unless the code calls fma() explicitly.  The
+// bit-exact paths rely on this to reproduce the reference's C arithmetic;
+// the fast paths spell out the fma() calls they want.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stddef.h>
+#include <string.h>
+
+#include "abie_gb300.h"
+
+namespace abie {
+
+// Compact source record: predicted position and G*m of one massive body.
+struct __align__(32) Src {
+    double x, y, z, gm;
+};
+
+// Per-call error reporting (host side), defined in abi.cu.
+void set_error(int code, const char *fmt, ...);
+int cuda_fail(cudaError_t e, const char *what);
+
+#define ABIE_CUDA(call)                                                   \
+    do {                                                                  \
+        cudaError_t _e = (call);                                          \
+        if (_e != cudaSuccess) return ::abie::cuda_fail(_e, #call);       \
+    } while (0)
+
+// Device pair term for the fast FP64 form: G m / r^3 from r^2.
+//
+// A 24-bit seed y ~ r2^(-1/2) comes from the single-precision reciprocal
+// square root of r2 truncated to 20 mantissa bits; exponent and mantissa
+// are moved between the two formats with integer operations, so the FP64
+// pipe only sees the refinement.  With e = 1 - r2 y^2 (|e| < 2^-19),
+//     r2^(-3/2) = y^3 (1 - e)^(-3/2) = y^3 (1 + 3/2 e + 15/8 e^2 + O(e^3)),
+// the O(e^3) term is below 2^-55.  The 15/8 e^2 term needs only single
+// precision.  Cost: 6 FP64 operations.  r2 = 0 (a body and itself) gives a
+// finite value, so the caller's 0 * s contributes exactly zero.
+__device__ __forceinline__ int clamp_exp_f32(int hi_rebased)
+{
+    // keep the single-precision exponent in [1, 254]
+    return min(max(hi_rebased, 1 << 20), (254 << 20) | 0xFFFFF);
+}
+
+__device__ __forceinline__ double f32_bits_to_f64(int fb)
+{
+    // exact conversion of a positive normal float given by its bits
+    return __hiloint2double((fb >> 3) + ((1023 - 127) << 20), fb << 29);
+}
+
+__device__ __forceinline__ float f64_to_f32_trunc(double v)
+{
+    // |v| truncated to 20 mantissa bits, as a float (sign dropped)
+    int hi = __double2hiint(v) & 0x7FFFFFFF;
+    return __int_as_float(clamp_exp_f32(hi - ((1023 - 127) << 20)) << 3);
+}
+
+__device__ __forceinline__ double gm_inv_r3(double r2, double gm)
+{
+    float xf = f64_to_f32_trunc(r2);
+    float yf = rsqrtf(xf);
+    double y = f32_bits_to_f64(__float_as_int(yf));
+    double t = y * y;                       // exact: 24-bit squared
+    double e = fma(-r2, t, 1.0);
+    double c = (gm * y) * t;                // G m y^3
+    float ef = f64_to_f32_trunc(e);
+    float q = 1.875f * ef * ef;
+    // q underflowing to zero maps to 2^-127 here, far below an ulp of k
+    double k = fma(e, 1.5, f32_bits_to_f64(__float_as_int(q)));
+    return fma(c, k, c);
+}
+
+// Exact FP64 pair contribution, in the reference's operation order
+// (src/common.c:185-194): r = sqrt(r2); r3 = r * r2; a -= (gm*d)/r3.
+__device__ __forceinline__ void pair_exact(double xj, double yj, double zj, const Src &s,
+                                           double &ax, double &ay, double &az)
+{
+    double dx = xj - s.x;
+    double dy = yj - s.y;
+    double dz = zj - s.z;
+    double r2 = dx * dx + dy * dy + dz * dz;
+    double r1 = sqrt(r2);
+    double r3 = r1 * r2;
+    ax -= s.gm * dx / r3;
+    ay -= s.gm * dy / r3;
+    az -= s.gm * dz / r3;
+}
+
+// Fast FP64 pair contribution (15 FP64 operations).
+__device__ __forceinline__ void pair_fast(double xj, double yj, double zj, const Src &s,
+                                          double &ax, double &ay, double &az)
+{
+    double dx = xj - s.x;
+    double dy = yj - s.y;
+    double dz = zj - s.z;
+    double r2 = fma(dz, dz, fma(dy, dy, dx * dx));
+    double w = gm_inv_r3(r2, s.gm);
+    ax = fma(-w, dx, ax);
+    ay = fma(-w, dy, ay);
+    az = fma(-w, dz, az);
+}
+
+// Non-negative doubles keep their order when read as unsigned integers, so
+// a max over |v| can be an integer atomicMax.  0 encodes "no value seen";
+// NaN is skipped, like the reference's vector_max_abs (src/common.c:316-322).
+__device__ __forceinline__ unsigned long long absmax_key(double v)
+{
+    double a = fabs(v);
+    return (a == a) ? (unsigned long long)__double_as_longlong(a) + 1ull : 0ull;
+}
+
+__host__ __device__ inline double absmax_value(unsigned long long key)
+{
+#ifdef __CUDA_ARCH__
+    return key ? __longlong_as_double((long long)(key - 1ull)) : -1.7976931348623157e308;
+#else
+    if (!key) return -1.7976931348623157e308;
+    unsigned long long b = key - 1ull;
+    double d;
+    memcpy(&d, &b, sizeof d);
+    return d;
+#endif
+}
+
+__device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v)
+{
+    for (int o = 16; o > 0; o >>= 1) {
+        unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
+        v = w > v ? w : v;
+    }
+    return v;
+}
+
+}  // namespace abie

@@ -1,0 +1,409 @@
+// All-pairs Newtonian acceleration kernels (sm_103a).
+//
+//   exact : one thread per sink, sources visited in body order with the
+//           reference's operations (sqrt, r*r2, (gm*d)/r3), so every
+//           acceleration is bit-identical to src/common.c:163-201.
+//   fp64  : the production FP64 form.  A group of 1, 8 or 32 lanes shares a
+//           sink and splits its sources; partial sums meet in a fixed
+//           butterfly of warp shuffles, so results are deterministic.  The
+//           pair term is gm_inv_r3() (15 FP64 operations per interaction).
+//           Sources can also be split into chunks whose partial sums are
+//           added in chunk order by a second pass, to balance the grid.
+//   naive : one thread per sink over global memory with rsqrt, the
+//           semantics of the reference's GPU offload (src/gpuforce.cu:61-84):
+//           sources with m == 0 and coincident pairs are skipped, sinks and
+//           sources with m < 0 are not.
+//   mixed : in mixed.cu.
+#include "force.cuh"
+#include "mixed.cuh"
+
+namespace abie {
+
+static ForceShape g_shape_override = {0, 0};
+
+void force_shape_override(int lanes_per_sink, int chunks)
+{
+    g_shape_override.lanes_per_sink = lanes_per_sink;
+    g_shape_override.chunks = chunks;
+}
+
+int force_scratch_reserve(ForceScratch &s, size_t n)
+{
+    if (n <= s.cap && s.src) return 0;
+    force_scratch_free(s);
+    size_t cap = n < 1024 ? 1024 : n;
+    ABIE_CUDA(cudaMalloc(&s.src, cap * sizeof(Src)));
+    ABIE_CUDA(cudaMalloc(&s.src_body, cap * sizeof(int)));
+    ABIE_CUDA(cudaMalloc(&s.n_src, sizeof(int)));
+    s.cap = cap;
+    return 0;
+}
+
+void force_scratch_free(ForceScratch &s)
+{
+    if (s.src) cudaFree(s.src);
+    if (s.src_body) cudaFree(s.src_body);
+    if (s.n_src) cudaFree(s.n_src);
+    if (s.partial) cudaFree(s.partial);
+    s = ForceScratch();
+}
+
+// ---------------------------------------------------------------------------
+// Order-preserving compaction of the massive bodies, one block.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(1024) compact_sources_kernel(const double *__restrict__ pos,
+                                                               const double *__restrict__ m, int n,
+                                                               double G, Src *__restrict__ src,
+                                                               int *__restrict__ src_body,
+                                                               int *__restrict__ n_src)
+{
+    __shared__ int warp_count[32];
+    __shared__ int base_s;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) base_s = 0;
+    __syncthreads();
+    for (int off = 0; off < n; off += blockDim.x) {
+        int i = off + threadIdx.x;
+        bool keep = (i < n) && (m[i] > 0.0);
+        unsigned ballot = __ballot_sync(0xffffffffu, keep);
+        if (lane == 0) warp_count[warp] = __popc(ballot);
+        __syncthreads();
+        int before = 0;
+        for (int w = 0; w < warp; w++) before += warp_count[w];
+        int base = base_s;
+        if (keep) {
+            int slot = base + before + __popc(ballot & ((1u << lane) - 1u));
+            Src s;
+            s.x = pos[3 * i];
+            s.y = pos[3 * i + 1];
+            s.z = pos[3 * i + 2];
+            s.gm = G * m[i];
+            src[slot] = s;
+            src_body[slot] = i;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int tot = 0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); w++) tot += warp_count[w];
+            base_s = base + tot;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *n_src = base_s;
+}
+
+int launch_compact_sources(const double *pos, const double *m, int n, double G, Src *src,
+                           int *src_body, int *n_src, cudaStream_t st)
+{
+    compact_sources_kernel<<<1, 1024, 0, st>>>(pos, m, n, G, src, src_body, n_src);
+    ABIE_CUDA(cudaGetLastError());
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
+// exact
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) force_exact_kernel(const double *__restrict__ pos,
+                                                          const double *__restrict__ m, int n,
+                                                          const Src *__restrict__ src,
+                                                          const int *__restrict__ src_body,
+                                                          const int *__restrict__ n_src_p,
+                                                          double *__restrict__ acc)
+{
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    if (m[j] < 0.0) return;
+    const int n_src = *n_src_p;
+    double xj = pos[3 * j], yj = pos[3 * j + 1], zj = pos[3 * j + 2];
+    double ax = 0.0, ay = 0.0, az = 0.0;
+    for (int q = 0; q < n_src; q++) {
+        if (src_body[q] == j) continue;
+        pair_exact(xj, yj, zj, src[q], ax, ay, az);
+    }
+    acc[3 * j] = ax;
+    acc[3 * j + 1] = ay;
+    acc[3 * j + 2] = az;
+}
+
+// ---------------------------------------------------------------------------
+// fp64
+// ---------------------------------------------------------------------------
+template <int JS>
+__global__ void __launch_bounds__(256) force_fp64_kernel(const double *__restrict__ pos,
+                                                         const double *__restrict__ m, int n,
+                                                         const Src *__restrict__ src,
+                                                         const int *__restrict__ n_src_p,
+                                                         int chunks, double *__restrict__ acc,
+                                                         double *__restrict__ partial)
+{
+    const int groups_per_block = 256 / JS;
+    const long long group = (long long)blockIdx.x * groups_per_block + threadIdx.x / JS;
+    const int lane = threadIdx.x % JS;
+    const int n_src = *n_src_p;
+    const long long n_groups = (long long)n * chunks;
+    const bool live = group < n_groups;
+    const int j = live ? (int)(group / chunks) : 0;
+    const int c = live ? (int)(group % chunks) : 0;
+    const int per = (n_src + chunks - 1) / chunks;
+    const int q0 = c * per;
+    const int q1 = min(n_src, q0 + per);
+    double ax = 0.0, ay = 0.0, az = 0.0;
+    if (live) {
+        const double xj = pos[3 * j], yj = pos[3 * j + 1], zj = pos[3 * j + 2];
+        int q = q0 + lane;
+#pragma unroll 1
+        for (; q + 3 * JS < q1; q += 4 * JS) {
+            Src s0 = src[q], s1 = src[q + JS], s2 = src[q + 2 * JS], s3 = src[q + 3 * JS];
+            pair_fast(xj, yj, zj, s0, ax, ay, az);
+            pair_fast(xj, yj, zj, s1, ax, ay, az);
+            pair_fast(xj, yj, zj, s2, ax, ay, az);
+            pair_fast(xj, yj, zj, s3, ax, ay, az);
+        }
+        for (; q < q1; q += JS) pair_fast(xj, yj, zj, src[q], ax, ay, az);
+    }
+    if (JS > 1) {
+#pragma unroll
+        for (int o = JS / 2; o > 0; o >>= 1) {
+            ax += __shfl_xor_sync(0xffffffffu, ax, o, JS);
+            ay += __shfl_xor_sync(0xffffffffu, ay, o, JS);
+            az += __shfl_xor_sync(0xffffffffu, az, o, JS);
+        }
+    }
+    if (!live || lane != 0) return;
+    if (chunks == 1) {
+        if (m[j] < 0.0) return;
+        acc[3 * j] = ax;
+        acc[3 * j + 1] = ay;
+        acc[3 * j + 2] = az;
+    } else {
+        double *p = partial + 3 * group;
+        p[0] = ax;
+        p[1] = ay;
+        p[2] = az;
+    }
+}
+
+__global__ void sum_chunks_kernel(const double *__restrict__ partial, const double *__restrict__ m,
+                                  int n, int chunks, double *__restrict__ acc)
+{
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n || m[j] < 0.0) return;
+    const double *p = partial + 3ll * j * chunks;
+    double ax = p[0], ay = p[1], az = p[2];
+    for (int c = 1; c < chunks; c++) {
+        ax += p[3 * c];
+        ay += p[3 * c + 1];
+        az += p[3 * c + 2];
+    }
+    acc[3 * j] = ax;
+    acc[3 * j + 1] = ay;
+    acc[3 * j + 2] = az;
+}
+
+// ---------------------------------------------------------------------------
+// naive (src/gpuforce.cu:61-84 semantics)
+// ---------------------------------------------------------------------------
+__global__ void force_naive_kernel(const double *__restrict__ pos, const double *__restrict__ m,
+                                   double G, int n, double *__restrict__ acc)
+{
+    int i = blockDim.x * blockIdx.x + threadIdx.x;
+    if (i >= n) return;
+    double fx = 0.0, fy = 0.0, fz = 0.0;
+    for (int j = 0; j < n; j++) {
+        double mj = m[j];
+        if (i == j || mj == 0) continue;
+        double dx = pos[3 * i] - pos[3 * j];
+        double dy = pos[3 * i + 1] - pos[3 * j + 1];
+        double dz = pos[3 * i + 2] - pos[3 * j + 2];
+        double d2 = dx * dx + dy * dy + dz * dz;
+        if (d2 == 0.0) continue;
+        double inv = rsqrt(d2);
+        double inv3 = inv * inv * inv;
+        fx -= G * mj * dx * inv3;
+        fy -= G * mj * dy * inv3;
+        fz -= G * mj * dz * inv3;
+    }
+    acc[3 * i] = fx;
+    acc[3 * i + 1] = fy;
+    acc[3 * i + 2] = fz;
+}
+
+ForceShape force_shape_default(int n_sink, int n_src)
+{
+    ForceShape s;
+    if (g_shape_override.lanes_per_sink > 0) {
+        s.lanes_per_sink = g_shape_override.lanes_per_sink;
+        s.chunks = g_shape_override.chunks > 0 ? g_shape_override.chunks : 1;
+        return s;
+    }
+    s.lanes_per_sink = n_src <= 64 ? 1 : (n_src <= 1024 ? 8 : 32);
+    s.chunks = 1;
+    return s;
+}
+
+int launch_force(int mode, const double *pos, const double *m, int n, double G, ForceScratch &s,
+                 double *acc, cudaStream_t st)
+{
+    if (n <= 0) return 0;
+    if (mode == ABIE_FORCE_NAIVE) {
+        force_naive_kernel<<<(n + 255) / 256, 256, 0, st>>>(pos, m, G, n, acc);
+        ABIE_CUDA(cudaGetLastError());
+        return 0;
+    }
+    int rc = force_scratch_reserve(s, (size_t)n);
+    if (rc) return rc;
+    rc = launch_compact_sources(pos, m, n, G, s.src, s.src_body, s.n_src, st);
+    if (rc) return rc;
+    if (mode == ABIE_FORCE_EXACT) {
+        force_exact_kernel<<<(n + 255) / 256, 256, 0, st>>>(pos, m, n, s.src, s.src_body, s.n_src,
+                                                            acc);
+        ABIE_CUDA(cudaGetLastError());
+        return 0;
+    }
+    if (mode == ABIE_FORCE_MIXED) return launch_force_mixed(pos, m, n, G, s, acc, st);
+    // fp64: the number of sources is on the device; the shape uses n as its
+    // upper bound.
+    ForceShape sh = force_shape_default(n, n);
+    if (sh.chunks > 1) {
+        size_t need = 3ull * (size_t)n * (size_t)sh.chunks;
+        if (need > s.partial_cap) {
+            if (s.partial) cudaFree(s.partial);
+            s.partial = nullptr;
+            ABIE_CUDA(cudaMalloc(&s.partial, need * sizeof(double)));
+            s.partial_cap = need;
+        }
+    }
+    long long groups = (long long)n * sh.chunks;
+    int gpb = 256 / sh.lanes_per_sink;
+    int blocks = (int)((groups + gpb - 1) / gpb);
+    switch (sh.lanes_per_sink) {
+    case 1:
+        force_fp64_kernel<1><<<blocks, 256, 0, st>>>(pos, m, n, s.src, s.n_src, sh.chunks, acc,
+                                                     s.partial);
+        break;
+    case 8:
+        force_fp64_kernel<8><<<blocks, 256, 0, st>>>(pos, m, n, s.src, s.n_src, sh.chunks, acc,
+                                                     s.partial);
+        break;
+    case 32:
+        force_fp64_kernel<32><<<blocks, 256, 0, st>>>(pos, m, n, s.src, s.n_src, sh.chunks, acc,
+                                                      s.partial);
+        break;
+    default:
+        set_error(ABIE_ERR_ARGUMENT, "lanes_per_sink must be 1, 8 or 32");
+        return ABIE_ERR_ARGUMENT;
+    }
+    ABIE_CUDA(cudaGetLastError());
+    if (sh.chunks > 1) {
+        sum_chunks_kernel<<<(n + 255) / 256, 256, 0, st>>>(s.partial, m, n, sh.chunks, acc);
+        ABIE_CUDA(cudaGetLastError());
+    }
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Energy: src/common.c:464-481.  Each thread sums its body's kinetic term and
+// pair terms in the reference's order; thread partials are combined as
+// double-double values in a fixed tree, block results summed on the host.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void two_sum(double a, double b, double &s, double &e)
+{
+    s = a + b;
+    double bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+__device__ __forceinline__ void dd_add(double &hi, double &lo, double v)
+{
+    double s, e;
+    two_sum(hi, v, s, e);
+    e += lo;
+    two_sum(s, e, hi, lo);
+}
+
+__global__ void __launch_bounds__(256) energy_kernel(const double *__restrict__ pos,
+                                                     const double *__restrict__ vel,
+                                                     const double *__restrict__ m, int n, double G,
+                                                     double *__restrict__ partials)
+{
+    __shared__ double sh_hi[256], sh_lo[256];
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double hi = 0.0, lo = 0.0;
+    if (i < n && m[i] != 0.0) {
+        double vx = vel[3 * i], vy = vel[3 * i + 1], vz = vel[3 * i + 2];
+        double s = 0.0;
+        s += vx * vx;
+        s += vy * vy;
+        s += vz * vz;
+        double nv = sqrt(s);
+        dd_add(hi, lo, 0.5 * m[i] * (nv * nv));
+        double xi = pos[3 * i], yi = pos[3 * i + 1], zi = pos[3 * i + 2];
+        double c = 0.5 * G * m[i];
+        for (int j = 0; j < n; j++) {
+            double mj = m[j];
+            if (j == i || mj == 0.0) continue;
+            double dx = xi - pos[3 * j], dy = yi - pos[3 * j + 1], dz = zi - pos[3 * j + 2];
+            double r2 = 0.0;
+            r2 += dx * dx;
+            r2 += dy * dy;
+            r2 += dz * dz;
+            dd_add(hi, lo, -(c * mj / sqrt(r2)));
+        }
+    }
+    sh_hi[threadIdx.x] = hi;
+    sh_lo[threadIdx.x] = lo;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (threadIdx.x < w) {
+            double h2 = sh_hi[threadIdx.x], l2 = sh_lo[threadIdx.x];
+            dd_add(h2, l2, sh_hi[threadIdx.x + w]);
+            dd_add(h2, l2, sh_lo[threadIdx.x + w]);
+            sh_hi[threadIdx.x] = h2;
+            sh_lo[threadIdx.x] = l2;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        partials[2 * blockIdx.x] = sh_hi[0];
+        partials[2 * blockIdx.x + 1] = sh_lo[0];
+    }
+}
+
+int launch_energy(const double *pos, const double *vel, const double *m, int n, double G,
+                  double *d_partials, double *h_out, cudaStream_t st)
+{
+    if (n <= 0) {
+        *h_out = 0.0;
+        return 0;
+    }
+    int blocks = (n + 255) / 256;
+    energy_kernel<<<blocks, 256, 0, st>>>(pos, vel, m, n, G, d_partials);
+    ABIE_CUDA(cudaGetLastError());
+    double *host = (double *)malloc(2 * (size_t)blocks * sizeof(double));
+    if (!host) {
+        set_error(ABIE_ERR_ARGUMENT, "out of host memory");
+        return ABIE_ERR_ARGUMENT;
+    }
+    cudaError_t e = cudaMemcpyAsync(host, d_partials, 2 * (size_t)blocks * sizeof(double),
+                                    cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+        free(host);
+        return cuda_fail(e, "energy readback");
+    }
+    // host double-double sum of the block results, in block order
+    double hi = 0.0, lo = 0.0;
+    for (int b = 0; b < 2 * blocks; b++) {
+        double v = host[b];
+        double s = hi + v, bb = s - hi;
+        double err = (hi - (s - bb)) + (v - bb);
+        err += lo;
+        hi = s + err;
+        lo = err - (hi - s);
+    }
+    free(host);
+    *h_out = hi + lo;
+    return 0;
+}
+
+}  // namespace abie

@@ -1,0 +1,44 @@
+// All-pairs Newtonian acceleration on the GPU: launchers shared by the C ABI,
+// the Radau15 engine and the benchmarks.
+#pragma once
+#include "common.cuh"
+
+namespace abie {
+
+// Scratch for one standalone force evaluation: the compact list of massive
+// sources (position, G m) in body order, their body indices and count.
+struct ForceScratch {
+    Src *src = nullptr;
+    int *src_body = nullptr;
+    int *n_src = nullptr;       // device scalar
+    double *partial = nullptr;  // per (sink, source chunk) partial sums, 3 doubles each
+    size_t cap = 0;             // bodies
+    size_t partial_cap = 0;     // doubles
+};
+
+int force_scratch_reserve(ForceScratch &s, size_t n);
+void force_scratch_free(ForceScratch &s);
+
+// Order-preserving compaction of the bodies with m > 0 (src/common.c:184:
+// only positive masses act as sources).
+int launch_compact_sources(const double *pos, const double *m, int n, double G, Src *src,
+                           int *src_body, int *n_src, cudaStream_t st);
+
+// acc[3j..3j+2] for every sink j in [0, n).  Sinks with m < 0 are skipped
+// (their entries are not written), as in src/common.c:173-176.
+int launch_force(int mode, const double *pos, const double *m, int n, double G,
+                 ForceScratch &s, double *acc, cudaStream_t st);
+
+// Launch shape of the fast FP64 kernel, exposed for the autotuner.
+struct ForceShape {
+    int lanes_per_sink;   // 1, 8 or 32
+    int chunks;           // source chunks per sink (1 = no split)
+};
+ForceShape force_shape_default(int n_sink, int n_src);
+void force_shape_override(int lanes_per_sink, int chunks);  // 0,0 = automatic
+
+// Energy (src/common.c:464-481) of a state on the device, FP64.
+int launch_energy(const double *pos, const double *vel, const double *m, int n, double G,
+                  double *d_partials, double *h_out, cudaStream_t st);
+
+}  // namespace abie

@@ -1,0 +1,355 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 gravity hot path.
+
+Workload (one "step"): one all-pairs FP64 acceleration evaluation of the
+16,385-body planetesimal disk (a 1 MSun star plus 16,384 bodies of 1e-9 MSun,
+a uniform in 5..40 au, e Rayleigh 0.01, i Rayleigh 0.005; seeded synthetic
+input), 268,451,840 interactions.
+
+* ``value``: Ginteractions/s with inputs resident in GPU memory, timed with
+  CUDA events on the launching stream, L2 flushed (256 MiB write) between
+  timed steps outside the timed interval.
+* ``e2e``: the same metric through the reference-facing C entry point
+  ``ode_n_body_second_order`` on pinned host arrays: host-to-device copy of
+  positions and masses, the kernels, device-to-host copy of the
+  accelerations, every step.
+* ``roofline``: the force kernel is bound by the FP64 pipe; the peak is the
+  FMA throughput measured on this device by the library's probe kernel;
+  ``achieved`` counts 20 flop per interaction.
+* ``cpu_baseline``: the oracle (a C restatement of the reference's
+  ode_n_body_second_order, bit-identical to it) on all host cores.
+* ``ensemble``: Radau15 over a batch of independent planetary systems
+  (system-steps/s), when --ensemble-systems > 0.
+
+``--impl reference`` times the reference algorithm on the host cores instead
+(the oracle port, since the reference library itself cannot be built on the
+benchmark host) and prints the same line with "impl": "reference".
+
+Multi-GPU (torchrun): every rank runs the same workload on its own GPU
+(replicas, weak scaling); timing is the max over ranks.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from abie_gb300 import ics  # noqa: E402
+
+G = ics.G_SOLAR
+FLOP_PER_INTERACTION = 20  # the convention of the reference's tiled kernel comments
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--mode", default="fp64", choices=["fp64", "exact", "mixed", "naive"])
+    ap.add_argument("--n", type=int, default=16384, help="planetesimals (plus one star)")
+    ap.add_argument("--ensemble-systems", type=int, default=0)
+    ap.add_argument("--ensemble-years", type=float, default=1.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def interactions(m):
+    """(sink, source) pairs: sinks are bodies with m >= 0, sources bodies with
+    m > 0, a body never acting on itself."""
+    nm = int((m > 0).sum())
+    sinks = int((m >= 0).sum())
+    return sinks * nm - nm
+
+
+# ---------------------------------------------------------------------------
+class Clocks:
+    """nvidia-smi sampling while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        time.sleep(0.3)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        with open(self.path) as fh:
+            for line in fh:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        mx = [num(r[2]) for r in rows if num(r[2]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if "Active" == r[5 + k]})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(rows), "power_w_max": max(num(r[3]) or 0 for r in rows)}
+
+
+# ---------------------------------------------------------------------------
+def cpu_force_rate(p, m, threads, sinks=None, reps=1):
+    """Oracle (reference algorithm) force on host cores; returns Gint/s and details."""
+    from oracle import Oracle
+    O = Oracle()
+    n = m.size
+    j1 = n if sinks is None else min(n, sinks)
+    acc = np.zeros(p.size)
+    O.force(p, m, G, j0=0, j1=min(j1, 64), threads=threads, acc=acc)  # warm
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        O.force(p, m, G, j0=0, j1=j1, threads=threads, acc=acc)
+    dt = (time.perf_counter() - t0) / reps
+    nm = int((m > 0).sum())
+    inter = j1 * nm - int((m[:j1] > 0).sum())
+    return inter / dt / 1e9, dt, inter
+
+
+def run_reference(args):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return 0
+    p, v, m, r = ics.planetesimal_disk(n=args.n)
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_force_rate(p, m, threads, sinks=256)
+    rates, times = [], []
+    for _ in range(args.steps):
+        g, dt, inter = cpu_force_rate(p, m, threads)
+        rates.append(g)
+        times.append(dt)
+    value = float(np.mean(rates))
+    line = {
+        "impl": "reference", "metric": "Gint/s", "value": value, "unit": "Ginteractions/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * float(np.mean(times)), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "all-pairs FP64 force, planetesimal disk of %d bodies" % m.size,
+                   "bodies": int(m.size), "interactions_per_step": int(interactions(m))},
+        "cpu_baseline": {"value": value, "unit": "Ginteractions/s", "cores": threads, "kind": "port",
+                         "sample": "full force evaluation per step (all %d sinks), sinks split "
+                                   "over %d threads; oracle/abie_oracle.c orc_force, bit-identical "
+                                   "to src/common.c:163-201" % (m.size, threads)},
+        "e2e": {"value": value, "unit": "Ginteractions/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+def run_ours(args):
+    import ctypes
+
+    import torch
+
+    from abie_gb300 import FORCE_MODES, build
+    from abie_gb300.clibabie import CLibABIE
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    build.build()
+    lib = CLibABIE()
+    L = lib.lib
+    mode = FORCE_MODES[args.mode]
+
+    p, v, m, r = ics.planetesimal_disk(n=args.n)
+    inter = interactions(m)
+    dev = torch.device("cuda", local)
+    pos_d = torch.from_numpy(p).to(dev)
+    m_d = torch.from_numpy(m).to(dev)
+    acc_d = torch.zeros_like(pos_d)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MiB > L2
+    stream = torch.cuda.Stream(device=dev)
+    sp = ctypes.c_void_p(stream.cuda_stream)
+
+    def step():
+        rc = L.abie_force_device(ctypes.c_void_p(pos_d.data_ptr()), ctypes.c_void_p(m_d.data_ptr()),
+                                 ctypes.c_size_t(m.size), ctypes.c_double(G),
+                                 ctypes.c_void_p(acc_d.data_ptr()), ctypes.c_int(mode), sp)
+        if rc != 0:
+            raise RuntimeError("abie_force_device failed: %d" % rc)
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            step()
+    stream.synchronize()
+    peaks = lib.measure_peaks()
+    clocks = Clocks(local)
+    clocks.start()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    evs = []
+    with torch.cuda.stream(stream):
+        for _ in range(args.steps):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            step()
+            e1.record(stream)
+            evs.append((e0, e1))
+    stream.synchronize()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    times_ms = [a.elapsed_time(b) for a, b in evs]
+    tot_ms = float(sum(times_ms))
+    if world > 1:
+        t = torch.tensor([tot_ms], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        tot_ms = float(t.item())
+    ms_step = tot_ms / args.steps
+    value = world * inter * args.steps / (tot_ms * 1e-3) / 1e9
+
+    # e2e through the reference-facing host entry point
+    hp = torch.from_numpy(p).pin_memory()
+    hm = torch.from_numpy(m).pin_memory()
+    ha = torch.zeros(p.size, dtype=torch.float64).pin_memory()
+    hr = torch.zeros(m.size, dtype=torch.float64).pin_memory()
+    L.abie_set_force_mode(ctypes.c_int(mode))
+
+    def e2e_step():
+        rc = L.ode_n_body_second_order(ctypes.c_void_p(hp.data_ptr()), ctypes.c_size_t(m.size),
+                                       ctypes.c_double(G), ctypes.c_void_p(hm.data_ptr()),
+                                       ctypes.c_void_p(hr.data_ptr()), ctypes.c_void_p(ha.data_ptr()))
+        if rc != 0:
+            raise RuntimeError("ode_n_body_second_order failed")
+
+    for _ in range(args.warmup):
+        e2e_step()
+    if world > 1:
+        torch.distributed.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = world * inter * args.steps / e2e_s / 1e9
+
+    # roofline of the force kernel (FP64 pipe)
+    ach = FLOP_PER_INTERACTION * inter / (ms_step * 1e-3) / 1e12
+    peak = peaks["fp64_tflops"] if args.mode != "mixed" else peaks["fp32_tflops"]
+    roof = {"bound": "fp64" if args.mode != "mixed" else "fp32", "achieved": ach, "peak": peak,
+            "unit": "TFLOP/s", "frac": ach / peak if peak else None, "traffic": None,
+            "peak_source": "measured FMA throughput (abie_measure_fp64_peak) on this GPU",
+            "flop_per_interaction": FLOP_PER_INTERACTION}
+    prof = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.isfile(prof):
+        with open(prof) as fh:
+            roof["traffic"] = json.load(fh).get("force_%s_%d" % (args.mode, m.size))
+
+    extra = {}
+    if args.ensemble_systems > 0:
+        extra["ensemble"] = run_ensemble(lib, args)
+
+    if rank == 0:
+        cpu = None
+        if not args.no_cpu_baseline:
+            threads = os.cpu_count() or 1
+            g, dt, ci = cpu_force_rate(p, m, threads, reps=3)
+            cpu = {"value": g, "unit": "Ginteractions/s", "cores": threads, "kind": "port",
+                   "sample": "3 full force evaluations of the same %d-body disk, sinks split over "
+                             "%d threads (oracle/abie_oracle.c orc_force, bit-identical to "
+                             "src/common.c:163-201)" % (m.size, threads)}
+        line = {
+            "metric": "Gint/s", "value": value, "unit": "Ginteractions/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.mode != "mixed" else "f32+f64",
+            "data": "synthetic",
+            "config": {"workload": "all-pairs %s force, planetesimal disk of %d bodies (1 star + %d x 1e-9 MSun)"
+                                   % (args.mode, m.size, m.size - 1),
+                       "bodies": int(m.size), "interactions_per_step": int(inter),
+                       "force_mode": args.mode, "l2": "flushed (256 MiB write) between timed steps",
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "roofline": roof,
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": "Ginteractions/s",
+                    "h2d_bytes_per_step": int(8 * (p.size + m.size)),
+                    "d2h_bytes_per_step": int(8 * p.size),
+                    "entry_point": "ode_n_body_second_order (host arrays, pinned)"},
+            "clocks": clk,
+            "gpu_launches": 2 * args.steps,
+            "peaks_measured": peaks,
+        }
+        line.update(extra)
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def run_ensemble(lib, args):
+    P, V, M, offs = ics.ensemble(n_systems=args.ensemble_systems)
+    out = {}
+    for label, learned in (("plain", False),):
+        res = lib.gr_ensemble(P, V, M, offs, G, 0.0, args.ensemble_years, learned=learned)
+        steps = int(res["steps"].sum())
+        out[label] = {"system_steps": steps, "seconds": res["seconds"],
+                      "system_steps_per_s": steps / res["seconds"] if res["seconds"] else None}
+    return out
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,167 @@
+/*
+ * abie_gb300 -- GB300 (sm_103a) implementation of ABIE's gravity hot path.
+ *
+ * C ABI of libabie_gb300.so.  The first block keeps the exact names and
+ * argument meanings of the reference library that abie/clibabie.py loads
+ * through ctypes, so that library can be swapped for this one.  Positions,
+ * velocities and accelerations are caller-owned float64 arrays laid out
+ * x0,y0,z0,x1,... (3N entries); masses and radii hold N entries.  The
+ * library keeps one simulation state, resident in GPU memory.
+ *
+ * Size arguments declared size_t receive ctypes c_int from the reference's
+ * Python caller (abie/clibabie.py:43-46, :61); the library reads only their
+ * low 32 bits.
+ *
+ * Return codes: 0 normal; 1 and 2 keep the reference's meaning (too many
+ * close encounters / collisions, src/common.h:6-8); negative values are
+ * errors of this library (ABIE_ERR_*) with a message available from
+ * abie_last_error().  The library never exits the process.
+ */
+#ifndef ABIE_GB300_H
+#define ABIE_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ABIE_OK 0
+#define ABIE_EXIT_MAX_N_CE 1          /* src/common.h:6 */
+#define ABIE_EXIT_MAX_N_COLLISIONS 2  /* src/common.h:7 */
+#define ABIE_ERR_NO_DEVICE (-1)       /* no usable sm_103 GPU, or deviceID < 0 */
+#define ABIE_ERR_NOT_INITIALIZED (-2)
+#define ABIE_ERR_CUDA (-3)
+#define ABIE_ERR_UNSUPPORTED (-4)     /* valid call, feature not on the GPU path */
+#define ABIE_ERR_ARGUMENT (-5)
+#define ABIE_ERR_CAPACITY (-6)        /* N above the capacity given to initialize_code */
+#define ABIE_ERR_TIMEOUT (-7)         /* a device-side wait gave up */
+#define ABIE_ERR_NUMERICS (-8)        /* NaN/Inf in the state */
+
+/* Force forms (abie_set_force_mode). */
+#define ABIE_FORCE_EXACT 0  /* reference operation order per sink: bit-identical to src/common.c:163-201 */
+#define ABIE_FORCE_FP64 1   /* fast FP64: reassociated sums, refined reciprocal square root */
+#define ABIE_FORCE_MIXED 2  /* FP32 pair terms on anchored coordinates, compensated sums; heavy sources in FP64 */
+#define ABIE_FORCE_NAIVE 3  /* one thread per sink over global memory: src/gpuforce.cu:61-84 semantics */
+
+/* ---- reference-compatible entry points (src/common.h:74-122) ---------- */
+
+/* src/common.c:350-399.  Binds GPU deviceID, sizes device buffers for
+ * N_MAX bodies and the event ring buffers.  Once per process, like the
+ * reference (a second call returns 0 and does nothing). */
+int initialize_code(double G, double C, size_t N_MAX, size_t MAX_N_CE,
+                    size_t MAX_N_COLLISIONS, int deviceID);
+/* src/common.c:506-522.  Frees device and host buffers. */
+int finalize_code(void);
+/* src/common.c:433-449.  Copies the caller's arrays into device memory. */
+void set_state(double *pos, double *vel, double *m, double *r, size_t N,
+               double G, double C);
+/* src/common.c:451-462.  Copies the device state out; returns N. */
+int get_state(double *pos, double *vel, double *m, double *r);
+/* src/common.c:324-326 */
+double get_model_time(void);
+/* src/common.c:401-407 */
+void set_close_encounter_distance(double d);
+double get_close_encounter_distance(void);
+/* src/common.c:409-431 (4*MAX doubles each: t, i, j, distance) */
+void get_close_encounter_buffer(double *buf_ce);
+void get_collision_buffer(double *buf_collision);
+void reset_close_encounter_buffer(void);
+void reset_collision_buffer(void);
+/* src/common.c:488-504.  A constant 3N acceleration added to every force call. */
+size_t set_additional_forces(size_t N, double *ext_acc);
+/* src/common.c:524-527 -> src/integrator_gauss_radau15.c:287-446.
+ * Gauss-Radau 15 from t to the first accepted time past t_end, on the
+ * device-resident state; dt is ignored as in the reference. */
+int integrator_gr(double t, double t_end, double dt);
+/* src/common.c:534-537 -> src/integrator_wisdom_holman.c:513-537.
+ * Fixed-step Wisdom-Holman on a heliocentric state. */
+int integrator_wh(double t, double t_end, double dt);
+/* src/common.c:529-532.  Runge-Kutta is not part of the GPU path:
+ * returns ABIE_ERR_UNSUPPORTED. */
+int integrator_rk(double t, double t_end, double dt);
+/* src/common.c:464-481.  Total energy of the stored state (FP64). */
+double calculate_energy(void);
+/* src/common.c:163-201 (and the GPU offload src/gpuforce.cu:129-170):
+ * accelerations of N bodies from host arrays, computed on the GPU in the
+ * current force form.  Does not touch the stored simulation state. */
+size_t ode_n_body_second_order(const double *pos, size_t N, double G,
+                               const double *masses, const double *radii,
+                               double *acc);
+/* src/common.c:206-238: ode_n_body_second_order plus the external
+ * accelerations set by set_additional_forces. */
+size_t calculate_accelerations(const double *pos, const double *vel, size_t N,
+                               double G, const double *masses,
+                               const double *radii, double *acc);
+/* src/integrator_gauss_radau15.c:287: Radau15 on caller arrays (the
+ * state is uploaded, integrated on the device and copied back). */
+size_t integrator_gauss_radau15(double *pos, double *vel, double *m_vec,
+                                double *r_vec, size_t N, double G, double t,
+                                double t_end, double dt);
+/* src/integrator_wisdom_holman.c:513 on caller arrays. */
+void integrator_wisdom_holman(double *pos, double *vel, double *m_vec,
+                              double *r_vec, size_t N, double G, double t,
+                              double t_end, double dt);
+
+/* ---- additions of this library (no counterpart in the reference) ------ */
+
+typedef struct {
+    long long force_calls;       /* all-pairs evaluations */
+    long long iterations;        /* Radau15 corrector iterations */
+    long long attempts;          /* Radau15 step attempts */
+    long long accepts;
+    long long rejects;
+    long long kepler_failures;   /* WH Kepler solves that hit the iteration cap */
+    long long wh_steps;
+    double last_h;
+} abie_counters;
+
+/* Last error message ("" when none). Returns its length. */
+int abie_last_error(char *buf, size_t len);
+/* Force form used by every later call (ABIE_FORCE_*). Returns the previous one. */
+int abie_set_force_mode(int mode);
+int abie_get_force_mode(void);
+/* Counters since initialize_code or the last reset. */
+int abie_get_counters(abie_counters *out);
+void abie_reset_counters(void);
+/* Device-pointer all-pairs force: d_pos[3N], d_m[N] -> d_acc[3N], all in
+ * GPU memory of the initialized device, on the given CUDA stream (NULL for
+ * the library's stream).  Returns when the work is queued.  Allocates
+ * scratch on first use and when N grows. */
+int abie_force_device(const double *d_pos, const double *d_m, size_t N,
+                      double G, double *d_acc, int mode, void *stream);
+/* Host-pointer force in an explicit form (copies in, computes, copies out). */
+int abie_force_host(const double *pos, const double *m, size_t N, double G,
+                    double *acc, int mode);
+/* Energy of caller arrays, computed on the GPU (FP64). */
+double abie_energy_host(const double *pos, const double *vel, const double *m,
+                        size_t N, double G);
+
+/* Batched ensemble: n_systems independent systems packed ragged; system s
+ * owns bodies offsets[s] .. offsets[s+1]-1 (at most 32 bodies each).  Each
+ * system is integrated with Radau15 from t0 to the first accepted time past
+ * t_end, exactly as integrator_gr would integrate it alone.  pos/vel are
+ * updated in place, t_out[s] receives each system's final time, status[s]
+ * its return code (0, or a negative error), steps[s] its accepted steps.
+ * flags: bit 0 use the learned predictor when one is loaded. */
+int abie_gr_ensemble(double *pos, double *vel, const double *m,
+                     const long long *offsets, int n_systems, double G,
+                     double t0, double t_end, double *t_out, int *status,
+                     long long *steps, int flags);
+/* Seconds of GPU time spent in the last abie_gr_ensemble call. */
+double abie_last_ensemble_seconds(void);
+
+/* Measured FMA throughput of the bound device in TFLOP/s (one FMA = 2
+ * flops), the denominators of the compute-bound rooflines.  iters <= 0
+ * picks a default length. */
+int abie_measure_fp64_peak(int iters, double *tflops);
+int abie_measure_fp32_peak(int iters, double *tflops);
+/* Fixes the fast FP64 force kernel's launch shape: lanes_per_sink in
+ * {1, 8, 32} and the number of source chunks; (0, 0) restores the
+ * automatic choice.  For tests and the autotuner. */
+void abie_debug_force_shape(int lanes_per_sink, int chunks);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

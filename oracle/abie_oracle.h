@@ -1,0 +1,78 @@
+/*
+ * CPU oracle for ABIE's gravity hot path -- TEST INFRASTRUCTURE ONLY.
+ *
+ * A plain C99 restatement of the reference algorithms, used by tests/, by
+ * __graft_entry__.smoke() and by bench.py's CPU-baseline leg as the checker.
+ * Nothing in the product library links or calls it.  Each function cites the
+ * reference file:line it follows.  Parity of this restatement with the
+ * reference is pinned bit for bit by tests/test_oracle.py (against the
+ * reference library built by oracle/build_ref.sh, and against the committed
+ * vectors in tests/golden/).
+ */
+#ifndef ABIE_ORACLE_H
+#define ABIE_ORACLE_H
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Event ring buffers: src/common.h:49-64, src/common.c:240-282. */
+typedef struct {
+    double ce_dist;
+    size_t max_ce, max_coll;
+    size_t n_ce, n_coll;
+    double *buf_ce;   /* 4*max_ce doubles or NULL */
+    double *buf_coll; /* 4*max_coll doubles or NULL */
+} orc_events;
+
+typedef struct {
+    long force_calls;
+    long iterations;   /* corrector iterations, summed over attempts */
+    long attempts;     /* step attempts (accepted + rejected) */
+    long accepts;
+    long rejects;
+    long iter_hist[13];
+    double h_last;
+} orc_radau_stats;
+
+/* src/common.c:163-201: a_j for sinks j in [j0, j1). */
+void orc_force(const double *pos, size_t n, double G, const double *m,
+               double *acc, size_t j0, size_t j1);
+/* The same arithmetic per sink, sinks split over nthreads POSIX threads. */
+int orc_force_threads(const double *pos, size_t n, double G, const double *m,
+                      double *acc, size_t j0, size_t j1, int nthreads);
+/* src/common.c:464-481 */
+double orc_energy(const double *pos, const double *vel, const double *m,
+                  size_t n, double G);
+/* src/common.c:240-282 */
+int orc_check_events(const double *pos, const double *r, size_t n, double t,
+                     orc_events *ev);
+/* src/integrator_gauss_radau15.c:287-446 (with :75-284). Returns 0/1/2. */
+int orc_radau15(double *pos, double *vel, const double *m, const double *r,
+                size_t n, double G, double t, double t_end, orc_events *ev,
+                double *t_out, orc_radau_stats *st);
+/* src/integrator_wisdom_holman.c:513-537.  sparse=0 follows the reference's
+ * O(N^2) compute_accel; sparse=1 skips zero-mass partners (same sums, same
+ * order, for the massive terms).  Returns the number of failed Kepler solves. */
+long orc_wh(double *pos, double *vel, const double *m, size_t n, double G,
+            double t, double t_end, double dt, double *t_out, int sparse);
+/* One WH step on an already heliocentric state, accel in/out (3n). */
+long orc_wh_step(double *pos, double *vel, double *jpos, double *jvel,
+                 const double *m, size_t n, double G, double dt, double *accel,
+                 int sparse);
+/* src/integrator_wisdom_holman.c:364-451 */
+void orc_wh_accel(const double *pos, const double *jpos, const double *m,
+                  size_t n, double G, double *accel, int sparse);
+/* src/integrator_wisdom_holman.c:221-280 and :295-347 */
+void orc_helio2jacobi(const double *pos, const double *vel, const double *m,
+                      size_t n, double *jpos, double *jvel);
+void orc_jacobi2helio(const double *jpos, const double *jvel, const double *m,
+                      size_t n, double *pos, double *vel);
+/* src/integrator_wisdom_holman.c:66-147; returns 1 when not converged. */
+int orc_kepler(double *jpos, double *jvel, double gm, double dt, size_t id);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

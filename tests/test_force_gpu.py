@@ -1,0 +1,80 @@
+"""All-pairs force on the GPU against the oracle and the reference's golden
+vectors.  Tolerances: the exact form is bit-identical; the fast FP64 form
+agrees to 1e-13 relative per body (the stated bar); the naive form to 1e-12."""
+import numpy as np
+import pytest
+
+from abie_gb300 import ics
+from conftest import rel_err_per_body
+
+G = ics.G_SOLAR
+pytestmark = pytest.mark.gpu
+CASES = ["force_sys", "force_edge", "force_disk", "force_n1", "force_n2", "force_n3"]
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_exact_is_bit_identical_to_reference(clib, golden, case):
+    p, m = golden[case + "_pos"], golden[case + "_m"]
+    assert np.array_equal(clib.force(p, m, G, "exact"), golden[case + "_acc"])
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_fp64_within_1e13(clib, golden, case):
+    p, m = golden[case + "_pos"], golden[case + "_m"]
+    assert rel_err_per_body(clib.force(p, m, G, "fp64"), golden[case + "_acc"]) <= 1e-13
+
+
+def test_naive_matches_offload_semantics(clib, golden):
+    p, m = golden["force_sys_pos"], golden["force_sys_m"]
+    assert rel_err_per_body(clib.force(p, m, G, "naive"), golden["force_sys_acc"]) <= 1e-12
+
+
+def test_reference_entry_point_uses_current_form(clib, golden):
+    p, m = golden["force_disk_pos"], golden["force_disk_m"]
+    old = clib.set_force_mode("exact")
+    try:
+        acc = clib.ode_n_body_second_order(p, m.size, G, m)
+    finally:
+        clib.set_force_mode(old)
+    assert np.array_equal(acc, golden["force_disk_acc"])
+
+
+def test_full_size_disk_fp64(clib, oracle):
+    """16,385-body workload: fast FP64 vs the oracle on a sample of sinks."""
+    p, v, m, r = ics.planetesimal_disk()
+    acc = clib.force(p, m, G, "fp64")
+    sinks = np.r_[0:64, 8000:8064, m.size - 64:m.size]
+    ref = np.zeros(p.size)
+    for lo in (0, 8000, m.size - 64):
+        oracle.force(p, m, G, j0=lo, j1=lo + 64, acc=ref, threads=8)
+    idx = (3 * sinks[:, None] + np.arange(3)).reshape(-1)
+    assert rel_err_per_body(acc[idx], ref[idx]) <= 1e-13
+
+
+def test_exact_vs_oracle_cfg1(clib, oracle):
+    p, v, m, r = ics.planetary_system()
+    assert np.array_equal(clib.force(p, m, G, "exact"), oracle.force(p, m, G))
+
+
+def test_fp64_shapes_agree(clib):
+    """Every lanes-per-sink / source-chunk shape gives the same sums to 1e-13."""
+    p, v, m, r = ics.planetesimal_disk(seed=5, n=3000)
+    base = clib.force(p, m, G, "exact")
+    lib = clib.lib
+    try:
+        for lanes in (1, 8, 32):
+            for chunks in (1, 3):
+                lib.abie_debug_force_shape(lanes, chunks)
+                assert rel_err_per_body(clib.force(p, m, G, "fp64"), base) <= 1e-13
+    finally:
+        lib.abie_debug_force_shape(0, 0)
+
+
+def test_energy_matches_reference(clib, golden):
+    e = clib.energy(golden["force_disk_pos"], golden["energy_disk_vel"], golden["force_disk_m"], G)
+    assert abs(e - golden["energy_disk"][0]) <= 1e-14 * abs(golden["energy_disk"][0])
+
+
+def test_zero_and_one_body(clib):
+    assert clib.force(np.zeros(3), np.ones(1), G, "fp64").tolist() == [0.0, 0.0, 0.0]
+    assert clib.force(np.zeros(0), np.zeros(0), G, "fp64").size == 0

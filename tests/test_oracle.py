@@ -1,0 +1,93 @@
+"""The CPU oracle is pinned bit for bit: against the golden vectors produced
+by the unmodified reference library (always), and against that library live
+where it can be built (skipped elsewhere)."""
+import numpy as np
+import pytest
+
+from abie_gb300 import ics
+from abie_gb300.radau_constants import double_tables
+
+G = ics.G_SOLAR
+
+
+def test_radau_tables_match_reference_build(golden):
+    h, rs, cs = double_tables()
+    assert np.array_equal(np.array(h), golden["radau_hs"])
+    assert np.array_equal(np.array(rs).reshape(-1), golden["radau_rs"])
+    assert np.array_equal(np.array(cs).reshape(-1), golden["radau_cs"])
+
+
+@pytest.mark.parametrize("case", ["force_sys", "force_edge", "force_disk", "force_n1",
+                                  "force_n2", "force_n3"])
+def test_force_golden(oracle, golden, case):
+    p, m = golden[case + "_pos"], golden[case + "_m"]
+    acc = oracle.force(p, m, G, acc=np.zeros(p.size))
+    assert np.array_equal(acc, golden[case + "_acc"])
+
+
+def test_energy_golden(oracle, golden):
+    e = oracle.energy(golden["force_disk_pos"], golden["energy_disk_vel"], golden["force_disk_m"], G)
+    assert e == golden["energy_disk"][0]
+
+
+def test_force_threads_identical(oracle, golden):
+    p, m = golden["force_disk_pos"], golden["force_disk_m"]
+    assert np.array_equal(oracle.force(p, m, G, threads=4), golden["force_disk_acc"])
+
+
+@pytest.mark.parametrize("case", ["gr_sys", "gr_tp", "gr_ens0", "gr_ens1", "gr_ens2", "gr_ce",
+                                  "gr_coll"])
+def test_radau_golden(oracle, golden, case):
+    span = golden[case + "_span"]
+    out = oracle.radau15(golden[case + "_in_pos"], golden[case + "_in_vel"], golden[case + "_m"],
+                         golden[case + "_r"], G, span[0], span[1], ce_dist=span[2],
+                         max_ce=int(span[3]), max_coll=int(span[4]))
+    assert np.array_equal(out["pos"], golden[case + "_pos"])
+    assert np.array_equal(out["vel"], golden[case + "_vel"])
+    assert out["t"] == golden[case + "_t"][0]
+    flag, n_ce, n_coll = golden[case + "_flag"]
+    assert (out["flag"], out["n_ce"], out["n_coll"]) == (flag, n_ce, n_coll)
+    assert np.array_equal(out["buf_ce"], golden[case + "_buf_ce"])
+    assert np.array_equal(out["buf_coll"], golden[case + "_buf_coll"])
+
+
+@pytest.mark.parametrize("sparse", [False, True])
+def test_wh_golden(oracle, golden, sparse):
+    t0, t1, dt = golden["wh_span"]
+    out = oracle.wh(golden["wh_in_pos"], golden["wh_in_vel"], golden["wh_m"], G, t0, t1, dt,
+                    sparse=sparse)
+    assert np.array_equal(out["pos"], golden["wh_pos"])
+    assert np.array_equal(out["vel"], golden["wh_vel"])
+    assert out["t"] == golden["wh_t"][0]
+
+
+@pytest.mark.parametrize("seed", [101, 102, 103])
+def test_live_force_energy(oracle, reference, seed):
+    p, v, m, r = ics.planetary_system(seed=seed, n_planets=6, n_tp=50)
+    assert np.array_equal(oracle.force(p, m, G), reference.force(p, m, G))
+    assert oracle.energy(p, v, m, G) == reference.energy(p, v, m, G)
+
+
+@pytest.mark.parametrize("seed", [201, 202])
+def test_live_radau(oracle, reference, seed):
+    p, v, m, r = ics.planetary_system(seed=seed, n_planets=4, n_tp=6)
+    a = oracle.radau15(p, v, m, r, G, 0.0, 2.0)
+    b = reference.radau15(p, v, m, r, G, 0.0, 2.0)
+    assert np.array_equal(a["pos"], b["pos"]) and np.array_equal(a["vel"], b["vel"])
+    assert a["t"] == b["t"]
+
+
+def test_live_wh_sparse(oracle, reference):
+    p, v, m, r = ics.test_particle_swarm(seed=301, n_tp=300)
+    p, v = ics.to_heliocentric(p, v)
+    a = oracle.wh(p, v, m, G, 0.0, 0.5, 0.01, sparse=True)
+    b = reference.wh(p, v, m, G, 0.0, 0.5, 0.01)
+    assert np.array_equal(a["pos"], b["pos"]) and np.array_equal(a["vel"], b["vel"])
+
+
+def test_oracle_planted_mistake_is_caught(oracle, golden):
+    """The golden comparison is sensitive to a last-bit change in the oracle's output."""
+    p, m = golden["force_sys_pos"], golden["force_sys_m"]
+    acc = oracle.force(p, m, G)
+    acc[7] = np.nextafter(acc[7], np.inf)
+    assert not np.array_equal(acc, golden["force_sys_acc"])
