@@ -1,26 +1,903 @@
-// Gauss-Radau 15 on the device (placeholder until the engine lands).
+// Gauss-Radau 15 on the device for one system of any size.
+//
+// The reference (src/integrator_gauss_radau15.c:287-446) loops on the host
+// and calls the force on every Radau substep, copying positions to the GPU
+// and accelerations back each time (src/gpuforce.cu:142-156).  Here the
+// whole predictor-corrector sweep runs inside one cooperative persistent
+// kernel: per-body state (y0, dy0, F1, b[7], g[7], ...) stays in GPU memory,
+// every thread group owns a fixed set of bodies, and the grid meets at a
+// software barrier (bounded wait) once per Radau substep.  Scalars that
+// steer the sweep (t, h, convergence, accept/reject) are computed by every
+// thread from the same reduced values, so control flow stays uniform.
+//
+// The per-component arithmetic repeats the reference's expressions in the
+// reference's order, and the translation unit is built with --fmad=false,
+// so with the exact force form each substep reproduces the reference's
+// doubles; the step-size exponentiation uses the device pow(), which may
+// differ from the host libm in the last bit.
+//
+// A call runs as a series of launches, each bounded to a number of step
+// attempts (sized from the measured time of the previous launch), so no
+// launch holds the GPU for long and every wait has a limit.
+#include <stdio.h>
+
+#include <algorithm>
+#include <vector>
+
 #include "abi_state.cuh"
+#include "engine.cuh"
+#include "radau_constants.h"
 
 namespace abie {
-void free_engine_buffers() {}
+
+__constant__ double c_hs[8] = ABIE_RADAU_HS_INIT;
+__constant__ double c_rs[8][8] = ABIE_RADAU_RS_INIT;
+__constant__ double c_cs[8][8] = ABIE_RADAU_CS_INIT;
+
+static constexpr double EPSB = 1.e-4;    // src/integrator_gauss_radau15.h:58
+static constexpr double FAC = 0.25;      // :59
+static constexpr double TOLPC = 1.e-16;  // :63
+static constexpr double H_MIN = 1.e-13;  // :17
+
+struct EventRec {
+    int j, k, kind;  // kind 0: close encounter, 1: collision
+    double sep;
+};
+
+struct EngineCtl {
+    unsigned int bar;
+    int err;
+    int flag;
+    int n_ev;
+    unsigned long long red[4][4];
+    // resumable scalars
+    double t, h;
+    int loop_count;
+    int phase;  // 0: not started, 1: running, 2: done
+    int pc;     // publish counter (which position buffer is current)
+    int red_idx;
+    long long attempts_done;
+    // counters
+    long long force_calls, iterations, attempts, accepts, rejects;
+    unsigned long long n_ce, n_coll;
+    int ev_overflow;
+    int hmin_warned;
+};
+
+struct EngineArgs {
+    int n, dim, n_src;
+    const int *src_body;  // [n_src] body index of each massive body, ascending
+    const int *src_slot;  // [n] slot in the source list or -1
+    const double *m, *r, *ext;
+    double G;
+    double *y0, *dy0, *F1, *b, *g, *b6p, *ddy, *dyp;
+    double *yp[2], *ypa;
+    Src *src[2], *srca;
+    double t_end;
+    double ce_dist, thr2;
+    long long max_ce, max_coll;
+    double *buf_ce, *buf_coll;
+    EventRec *ev;
+    int ev_cap;
+    EngineCtl *ctl;
+    long long timeout_ns;
+    long long attempt_budget;
+};
+
+__device__ __forceinline__ unsigned long long gtimer()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Grid barrier: block 0 adds 2^31 - (nblocks - 1), every other block adds 1,
+// so the top bit of the counter flips exactly when all blocks have arrived.
+// The wait is bounded; on timeout the error word is set and every block
+// leaves at its next barrier.
+__device__ __forceinline__ bool grid_sync(EngineCtl *ctl, long long timeout_ns)
+{
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned int nb = gridDim.x;
+        unsigned int inc = (blockIdx.x == 0) ? (0x80000000u - (nb - 1u)) : 1u;
+        __threadfence();
+        unsigned int old = atomicAdd(&ctl->bar, inc);
+        unsigned long long t0 = gtimer();
+        unsigned int spins = 0;
+        while (((*(volatile unsigned int *)&ctl->bar ^ old) & 0x80000000u) == 0u) {
+            if ((++spins & 255u) == 0u) {
+                if (*(volatile int *)&ctl->err) break;
+                if (gtimer() - t0 > (unsigned long long)timeout_ns) {
+                    atomicCAS(&ctl->err, 0, ABIE_ERR_TIMEOUT);
+                    break;
+                }
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return *(volatile int *)&ctl->err == 0;
+}
+
+__device__ __forceinline__ Src load_src(const Src *p)
+{
+    double2 a = __ldcg(reinterpret_cast<const double2 *>(p));
+    double2 b = __ldcg(reinterpret_cast<const double2 *>(p) + 1);
+    Src s;
+    s.x = a.x;
+    s.y = a.y;
+    s.z = b.x;
+    s.gm = b.y;
+    return s;
+}
+
+// Acceleration of sink j from the published sources.  EXACT: one lane, the
+// reference's order and operations.  Otherwise JS lanes split the sources
+// and meet in a shuffle butterfly.
+template <int MODE, int JS>
+__device__ __forceinline__ void sink_accel(const EngineArgs &a, int j, const Src *src, double xj,
+                                           double yj, double zj, int lane, double &ax, double &ay,
+                                           double &az)
+{
+    ax = 0.0;
+    ay = 0.0;
+    az = 0.0;
+    if (MODE == ABIE_FORCE_EXACT) {
+        for (int q = 0; q < a.n_src; q++) {
+            if (a.src_body[q] == j) continue;
+            pair_exact(xj, yj, zj, load_src(src + q), ax, ay, az);
+        }
+    } else {
+        int q = lane;
+        for (; q + JS < a.n_src; q += 2 * JS) {
+            Src s0 = load_src(src + q), s1 = load_src(src + q + JS);
+            pair_fast(xj, yj, zj, s0, ax, ay, az);
+            pair_fast(xj, yj, zj, s1, ax, ay, az);
+        }
+        if (q < a.n_src) pair_fast(xj, yj, zj, load_src(src + q), ax, ay, az);
+        if (JS > 1) {
+#pragma unroll
+            for (int o = JS / 2; o > 0; o >>= 1) {
+                ax += __shfl_xor_sync(0xffffffffu, ax, o, JS);
+                ay += __shfl_xor_sync(0xffffffffu, ay, o, JS);
+                az += __shfl_xor_sync(0xffffffffu, az, o, JS);
+            }
+        }
+    }
+}
+
+// Predictor (src/integrator_gauss_radau15.c:122-134): spacing s, step dt.
+__device__ __forceinline__ double pred_pos(const EngineArgs &a, int i, double s, double dt)
+{
+    const int d = a.dim;
+    const double *b = a.b;
+    return a.y0[i] + dt * s * (a.dy0[i] + dt * s * (a.F1[i] + s * (b[i] / 0.3e1 + s * (b[d + i] / 0.6e1 + s * (b[2 * d + i] / 0.10e2 + s * (b[3 * d + i] / 0.15e2 + s * (b[4 * d + i] / 0.21e2 + s * (b[5 * d + i] / 0.28e2 + s * b[6 * d + i] / 0.36e2))))))) / 0.2e1);
+}
+
+__device__ __forceinline__ double pred_vel(const EngineArgs &a, int i, double s, double dt)
+{
+    const int d = a.dim;
+    const double *b = a.b;
+    return a.dy0[i] + dt * s * (a.F1[i] + s * (b[i] / 0.2e1 + s * (b[d + i] / 0.3e1 + s * (b[2 * d + i] / 0.4e1 + s * (b[3 * d + i] / 0.5e1 + s * (b[4 * d + i] / 0.6e1 + s * (b[5 * d + i] / 0.7e1 + s * b[6 * d + i] / 0.8e1)))))));
+}
+
+// Predicted position of body j at spacing s into yp, and into the source
+// list when j is massive.
+__device__ __forceinline__ void publish_body(const EngineArgs &a, int j, double s, double dt,
+                                             double *yp, Src *src)
+{
+    double p0 = pred_pos(a, 3 * j, s, dt);
+    double p1 = pred_pos(a, 3 * j + 1, s, dt);
+    double p2 = pred_pos(a, 3 * j + 2, s, dt);
+    yp[3 * j] = p0;
+    yp[3 * j + 1] = p1;
+    yp[3 * j + 2] = p2;
+    int slot = a.src_slot[j];
+    if (slot >= 0) {
+        Src v;
+        v.x = p0;
+        v.y = p1;
+        v.z = p2;
+        v.gm = a.G * a.m[j];
+        src[slot] = v;
+    }
+}
+
+// g and b after the force F at substep ih (1..7) for component i
+// (src/integrator_gauss_radau15.c:136-241; only g[ih-1] is new, the lower g
+// the reference recomputes are bitwise the stored ones).
+__device__ __forceinline__ void gb_update(const EngineArgs &a, int i, int ih, double F)
+{
+    const int d = a.dim;
+    double *g = a.g;
+    double v = (F - a.F1[i]) * c_rs[ih][0];
+    for (int l = 1; l < ih; l++) v = (v - g[(l - 1) * d + i]) * c_rs[ih][l];
+    g[(ih - 1) * d + i] = v;
+    double gl[7];
+#pragma unroll
+    for (int k = 0; k < 7; k++) gl[k] = (k == ih - 1) ? v : g[k * d + i];
+    for (int k = 0; k < ih; k++) {
+        double s = c_cs[k][k] * gl[k];
+        for (int jj = k + 1; jj < 7; jj++) s = s + c_cs[jj][k] * gl[jj];
+        a.b[k * d + i] = s;
+    }
+}
+
+// src/integrator_gauss_radau15.c:244-284 (bd is always zero there).
+__device__ __forceinline__ void refine_b(const EngineArgs &a, int i, double q)
+{
+    const int d = a.dim;
+    double *b = a.b;
+    double b0 = b[i], b1 = b[d + i], b2 = b[2 * d + i], b3 = b[3 * d + i], b4 = b[4 * d + i],
+           b5 = b[5 * d + i], b6 = b[6 * d + i];
+    double q2 = q * q, q3 = q2 * q, q4 = q2 * q2, q5 = q2 * q3, q6 = q3 * q3, q7 = q2 * q5;
+    double e0 = q * (b6 * 7.0 + b5 * 6.0 + b4 * 5.0 + b3 * 4.0 + b2 * 3.0 + b1 * 2.0 + b0);
+    double e1 = q2 * (b6 * 21.0 + b5 * 15.0 + b4 * 10.0 + b3 * 6.0 + b2 * 3.0 + b1);
+    double e2 = q3 * (b6 * 35.0 + b5 * 20.0 + b4 * 10.0 + b3 * 4.0 + b2);
+    double e3 = q4 * (b6 * 35.0 + b5 * 15.0 + b4 * 5.0 + b3);
+    double e4 = q5 * (b6 * 21.0 + b5 * 6.0 + b4);
+    double e5 = q6 * (b6 * 7.0 + b5);
+    double e6 = q7 * b6;
+    b[i] = e0 + 0.0;
+    b[d + i] = e1 + 0.0;
+    b[2 * d + i] = e2 + 0.0;
+    b[3 * d + i] = e3 + 0.0;
+    b[4 * d + i] = e4 + 0.0;
+    b[5 * d + i] = e5 + 0.0;
+    b[6 * d + i] = e6 + 0.0;
+}
+
+__device__ __forceinline__ void reduce2(EngineCtl *ctl, int idx, unsigned long long k0,
+                                        unsigned long long k1)
+{
+    k0 = warp_max_u64(k0);
+    k1 = warp_max_u64(k1);
+    if ((threadIdx.x & 31) == 0) {
+        if (k0) atomicMax(&ctl->red[idx & 3][0], k0);
+        if (k1) atomicMax(&ctl->red[idx & 3][1], k1);
+    }
+}
+
+// After the barrier that completes reduction idx: read it, and clear the
+// slot two reductions ahead (its last readers finished two barriers ago).
+__device__ __forceinline__ void read2(EngineCtl *ctl, int idx, double &v0, double &v1)
+{
+    v0 = absmax_value(*(volatile unsigned long long *)&ctl->red[idx & 3][0]);
+    v1 = absmax_value(*(volatile unsigned long long *)&ctl->red[idx & 3][1]);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        ctl->red[(idx + 2) & 3][0] = 0ull;
+        ctl->red[(idx + 2) & 3][1] = 0ull;
+    }
+}
+
+__device__ __forceinline__ void ring_put(double *buf, unsigned long long count, long long cap,
+                                         double t, int i, int j, double d)
+{
+    if (!buf || cap <= 0) return;
+    unsigned long long w = 4ull * (unsigned long long)cap;
+    buf[(4ull * count) % w] = t;
+    buf[(4ull * count + 1) % w] = (double)i;
+    buf[(4ull * count + 2) % w] = (double)j;
+    buf[(4ull * count + 3) % w] = d;
+}
+
+// Pairs j < k closer than the event thresholds (src/common.c:240-282).  A
+// pair passes the prefilter r2 <= thr2 before the reference's exact test.
+__device__ void scan_events(const EngineArgs &a, double t, int tid, int nthreads)
+{
+    EngineCtl *ctl = a.ctl;
+    for (int j = tid; j < a.n; j += nthreads) {
+        double xj = __ldcg(a.ypa + 3 * j), yj = __ldcg(a.ypa + 3 * j + 1),
+               zj = __ldcg(a.ypa + 3 * j + 2);
+        double rj = a.r[j];
+        for (int k = j + 1; k < a.n; k++) {
+            double dx = xj - __ldcg(a.ypa + 3 * k);
+            double dy = yj - __ldcg(a.ypa + 3 * k + 1);
+            double dz = zj - __ldcg(a.ypa + 3 * k + 2);
+            double r2 = dx * dx + dy * dy + dz * dz;
+            if (!(r2 <= a.thr2)) continue;
+            double sep = sqrt(r2);
+            double rr = rj + a.r[k];
+            if (sep <= a.ce_dist) {
+                int e = atomicAdd(&ctl->n_ev, 1);
+                if (e < a.ev_cap) a.ev[e] = EventRec{j, k, 0, sep};
+            }
+            if (rr > 0 && sep <= rr) {
+                int e = atomicAdd(&ctl->n_ev, 1);
+                if (e < a.ev_cap) a.ev[e] = EventRec{j, k, 1, sep};
+            }
+        }
+    }
+}
+
+// One thread: order the events of this check as the reference's loops
+// would meet them, append them to the ring buffers, compute the flag.
+__device__ void commit_events(const EngineArgs &a, double t)
+{
+    EngineCtl *ctl = a.ctl;
+    int n = *(volatile int *)&ctl->n_ev;
+    if (n > a.ev_cap) {
+        ctl->ev_overflow = 1;
+        n = a.ev_cap;
+    }
+    for (int x = 1; x < n; x++) {  // insertion sort by (j, k, kind)
+        EventRec v = a.ev[x];
+        int y = x - 1;
+        while (y >= 0) {
+            EventRec u = a.ev[y];
+            bool greater = (u.j > v.j) || (u.j == v.j && (u.k > v.k || (u.k == v.k && u.kind > v.kind)));
+            if (!greater) break;
+            a.ev[y + 1] = u;
+            y--;
+        }
+        a.ev[y + 1] = v;
+    }
+    for (int x = 0; x < n; x++) {
+        EventRec v = a.ev[x];
+        if (v.kind == 0) {
+            ring_put(a.buf_ce, ctl->n_ce, a.max_ce, t, v.j, v.k, v.sep);
+            ctl->n_ce++;
+        } else {
+            ring_put(a.buf_coll, ctl->n_coll, a.max_coll, t, v.j, v.k, v.sep);
+            ctl->n_coll++;
+        }
+    }
+    int flag = 0;
+    if (a.max_ce > 0 && ctl->n_ce >= (unsigned long long)a.max_ce) flag = 1;
+    else if (a.max_coll > 0 && ctl->n_coll >= (unsigned long long)a.max_coll) flag = 2;
+    ctl->flag = flag;
+    ctl->n_ev = 0;
+    __threadfence();
+}
+
+template <int MODE, int JS>
+__global__ void __launch_bounds__(256) radau_engine(EngineArgs a)
+{
+    EngineCtl *ctl = a.ctl;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nthreads = gridDim.x * blockDim.x;
+    const int lane = tid % JS;
+    const int gid = tid / JS;
+    const int ngroups = nthreads / JS;
+    const bool leader = (blockIdx.x == 0 && threadIdx.x == 0);
+    const long long T = a.timeout_ns;
+    const int n = a.n;
+
+    double t, h;
+    int loop_count, pc, red_idx;
+    long long my_attempts = 0;
+
+    if (ctl->phase == 0) {
+        // --- F1 = f(y0): publish y0 (spacing 0 gives y0 exactly), then force
+        for (int j = gid; j < n; j += ngroups)
+            if (lane == 0) publish_body(a, j, 0.0, 0.0, a.yp[0], a.src[0]);
+        if (!grid_sync(ctl, T)) return;
+        for (int j = gid; j < n; j += ngroups) {
+            double ax, ay, az;
+            sink_accel<MODE, JS>(a, j, a.src[0], a.y0[3 * j], a.y0[3 * j + 1], a.y0[3 * j + 2],
+                                 lane, ax, ay, az);
+            if (lane == 0) {
+                bool live = a.m[j] >= 0.0;
+                double e0 = a.ext ? a.ext[3 * j] : 0.0, e1 = a.ext ? a.ext[3 * j + 1] : 0.0,
+                       e2 = a.ext ? a.ext[3 * j + 2] : 0.0;
+                a.F1[3 * j] = (live ? ax : 0.0) + e0;
+                a.F1[3 * j + 1] = (live ? ay : 0.0) + e1;
+                a.F1[3 * j + 2] = (live ? az : 0.0) + e2;
+            }
+        }
+        if (leader) ctl->force_calls++;
+        if (!grid_sync(ctl, T)) return;
+        // --- initial_time_step (src/integrator_gauss_radau15.c:75-120): the
+        // reference scans only the first n of the 3n entries for d0 and d1
+        unsigned long long k0 = 0, k1 = 0;
+        for (int i = tid; i < n; i += nthreads) {
+            unsigned long long u = absmax_key(a.y0[i]), w = absmax_key(__ldcg(a.F1 + i));
+            k0 = u > k0 ? u : k0;
+            k1 = w > k1 ? w : k1;
+        }
+        red_idx = 0;
+        reduce2(ctl, red_idx, k0, k1);
+        if (!grid_sync(ctl, T)) return;
+        double d0, d1;
+        read2(ctl, red_idx++, d0, d1);
+        double dt0 = (d0 < 1e-5 || d1 < 1e-5) ? 1e-6 : 0.01 * (d0 / d1);
+        // Euler probe y1 = y0 + dt0 dy0 into yp[1] / src[1]
+        for (int j = gid; j < n; j += ngroups) {
+            if (lane != 0) continue;
+            double p[3];
+            for (int c = 0; c < 3; c++) {
+                p[c] = a.y0[3 * j + c] + dt0 * a.dy0[3 * j + c];
+                a.yp[1][3 * j + c] = p[c];
+            }
+            int slot = a.src_slot[j];
+            if (slot >= 0) a.src[1][slot] = Src{p[0], p[1], p[2], a.G * a.m[j]};
+        }
+        if (!grid_sync(ctl, T)) return;
+        unsigned long long k2 = 0;
+        for (int j = gid; j < n; j += ngroups) {
+            double ax, ay, az;
+            sink_accel<MODE, JS>(a, j, a.src[1], a.yp[1][3 * j], a.yp[1][3 * j + 1],
+                                 a.yp[1][3 * j + 2], lane, ax, ay, az);
+            if (lane == 0) {
+                bool live = a.m[j] >= 0.0;
+                double f[3] = {live ? ax : 0.0, live ? ay : 0.0, live ? az : 0.0};
+                for (int c = 0; c < 3; c++) {
+                    double fi = f[c] + (a.ext ? a.ext[3 * j + c] : 0.0);
+                    unsigned long long u = absmax_key(fi - a.F1[3 * j + c]);
+                    k2 = u > k2 ? u : k2;
+                }
+            }
+        }
+        if (leader) ctl->force_calls++;
+        reduce2(ctl, red_idx, k2, 0ull);
+        if (!grid_sync(ctl, T)) return;
+        double d2, unused;
+        read2(ctl, red_idx++, d2, unused);
+        d2 = d2 / dt0;
+        double dt1;
+        if (fmax(d1, d2) <= 1e-15) dt1 = fmax(1e-6, dt0 * 1e-3);
+        else dt1 = pow(0.01 / fmax(d1, d2), (1.0 / (15 + 1)));
+        h = fmin(100 * dt0, dt1);
+        t = ctl->t;
+        loop_count = 0;
+        pc = 0;
+        // first attempt's substep-1 prediction
+        for (int j = gid; j < n; j += ngroups)
+            if (lane == 0) publish_body(a, j, c_hs[1], h, a.yp[pc & 1], a.src[pc & 1]);
+        if (!grid_sync(ctl, T)) return;
+    } else {
+        t = ctl->t;
+        h = ctl->h;
+        loop_count = ctl->loop_count;
+        pc = ctl->pc;
+        red_idx = ctl->red_idx;
+    }
+
+    bool done = false;
+    while (!done && my_attempts < a.attempt_budget) {
+        // ---------------- corrector iterations ----------------
+        int iters = 0;
+        for (int ipc = 0; ipc < 12; ipc++) {
+            iters++;
+            unsigned long long kdb = 0, kf8 = 0;
+            for (int ih = 1; ih < 8; ih++) {
+                const double *yp = a.yp[pc & 1];
+                const Src *src = a.src[pc & 1];
+                for (int j = gid; j < n; j += ngroups) {
+                    double ax, ay, az;
+                    sink_accel<MODE, JS>(a, j, src, yp[3 * j], yp[3 * j + 1], yp[3 * j + 2], lane,
+                                         ax, ay, az);
+                    if (lane == 0) {
+                        bool live = a.m[j] >= 0.0;
+                        double f[3] = {live ? ax : 0.0, live ? ay : 0.0, live ? az : 0.0};
+                        for (int c = 0; c < 3; c++) {
+                            int i = 3 * j + c;
+                            double fi = f[c] + (a.ext ? a.ext[i] : 0.0);
+                            gb_update(a, i, ih, fi);
+                            if (ih == 7) {
+                                unsigned long long u = absmax_key(a.b[6 * a.dim + i] - a.b6p[i]);
+                                unsigned long long w = absmax_key(fi);
+                                kdb = u > kdb ? u : kdb;
+                                kf8 = w > kf8 ? w : kf8;
+                            }
+                        }
+                        if (ih < 7) {
+                            publish_body(a, j, c_hs[ih + 1], h, a.yp[(pc + 1) & 1],
+                                         a.src[(pc + 1) & 1]);
+                        } else {
+                            // speculative: next iteration's substep 1 and the advance
+                            publish_body(a, j, c_hs[1], h, a.yp[(pc + 1) & 1], a.src[(pc + 1) & 1]);
+                            publish_body(a, j, 1.0, h, a.ypa, a.srca);
+                            for (int c = 0; c < 3; c++) a.dyp[3 * j + c] = pred_vel(a, 3 * j + c, 1.0, h);
+                        }
+                    }
+                }
+                pc++;
+                if (ih == 7) reduce2(ctl, red_idx, kdb, kf8);
+                if (!grid_sync(ctl, T)) return;
+            }
+            if (leader) ctl->force_calls += 7;
+            double db6, f8;
+            read2(ctl, red_idx++, db6, f8);
+            if (db6 / f8 < TOLPC) break;  // src/integrator_gauss_radau15.c:366
+            for (int j = gid; j < n; j += ngroups)
+                if (lane == 0)
+                    for (int c = 0; c < 3; c++) a.b6p[3 * j + c] = a.b[6 * a.dim + 3 * j + c];
+        }
+        // ---------------- advance (spacing 1) ----------------
+        unsigned long long kb6 = 0, kdd = 0;
+        for (int j = gid; j < n; j += ngroups) {
+            double ax, ay, az;
+            sink_accel<MODE, JS>(a, j, a.srca, a.ypa[3 * j], a.ypa[3 * j + 1], a.ypa[3 * j + 2],
+                                 lane, ax, ay, az);
+            if (lane == 0) {
+                bool live = a.m[j] >= 0.0;
+                double f[3] = {live ? ax : 0.0, live ? ay : 0.0, live ? az : 0.0};
+                for (int c = 0; c < 3; c++) {
+                    int i = 3 * j + c;
+                    double fi = f[c] + (a.ext ? a.ext[i] : 0.0);
+                    a.ddy[i] = fi;
+                    unsigned long long u = absmax_key(a.b[6 * a.dim + i]);
+                    unsigned long long w = absmax_key(fi);
+                    kb6 = u > kb6 ? u : kb6;
+                    kdd = w > kdd ? w : kdd;
+                }
+            }
+        }
+        reduce2(ctl, red_idx, kb6, kdd);
+        if (!grid_sync(ctl, T)) return;
+        if (leader) {
+            ctl->force_calls += 1;
+            ctl->iterations += iters;
+            ctl->attempts += 1;
+        }
+        double mb6, mdd;
+        read2(ctl, red_idx++, mb6, mdd);
+        // ---------------- step control (src/integrator_gauss_radau15.c:379-433) ----------------
+        double estim_b6 = mb6 / mdd;
+        double err = pow(estim_b6 / EPSB, 1. / 7);
+        double dtreq = h / err;
+        bool accepted = (err <= 1 || loop_count > 100);
+        bool stop = false;
+        if (accepted) {
+            t += h;
+            loop_count = 0;
+            if (t > a.t_end) {
+                h = a.t_end - t;
+                stop = true;
+            }
+            double q = dtreq / h;
+            for (int j = gid; j < n; j += ngroups) {
+                if (lane != 0) continue;
+                for (int c = 0; c < 3; c++) {
+                    int i = 3 * j + c;
+                    a.y0[i] = a.ypa[i];
+                    a.dy0[i] = a.dyp[i];
+                    a.F1[i] = a.ddy[i];
+                    a.b6p[i] = a.b[6 * a.dim + i];
+                    refine_b(a, i, q);
+                }
+            }
+            scan_events(a, t, tid, nthreads);
+            if (leader) ctl->accepts++;
+        } else {
+            loop_count += 1;
+            if (leader) ctl->rejects++;
+        }
+        if (!stop) {
+            if (dtreq / h > 1.0 / FAC) h /= FAC;
+            else if (dtreq < 1.e-12) h *= FAC;
+            else h = dtreq;
+            if (h < H_MIN) h = H_MIN;
+            // next attempt's substep-1 prediction
+            for (int j = gid; j < n; j += ngroups)
+                if (lane == 0) publish_body(a, j, c_hs[1], h, a.yp[pc & 1], a.src[pc & 1]);
+        }
+        if (!grid_sync(ctl, T)) return;
+        if (accepted && *(volatile int *)&ctl->n_ev > 0) {
+            if (leader) commit_events(a, t);
+            if (!grid_sync(ctl, T)) return;
+            if (*(volatile int *)&ctl->flag > 0) stop = true;
+        }
+        my_attempts++;
+        if (accepted && leader) ctl->t = t;
+        done = stop;
+    }
+    if (leader) {
+        ctl->t = t;
+        ctl->h = h;
+        ctl->loop_count = loop_count;
+        ctl->pc = pc;
+        ctl->red_idx = red_idx;
+        ctl->phase = done ? 2 : 1;
+        ctl->attempts_done += my_attempts;
+        __threadfence();
+    }
+}
+
 }  // namespace abie
 
+namespace abie {
+
+struct EngineBuffers {
+    double *slab = nullptr;
+    size_t slab_n = 0;  // bodies the slab holds
+    Src *srcs = nullptr;
+    int *src_body = nullptr, *src_slot = nullptr;
+    size_t src_n = 0;
+    EngineCtl *ctl = nullptr;
+    EventRec *ev = nullptr;
+    double *d_ce = nullptr, *d_coll = nullptr;
+    size_t d_ce_n = 0, d_coll_n = 0;
+};
+static EngineBuffers g_eb;
+static const int EV_CAP = 4096;
+static const int SLAB_PER_BODY = 3 * (3 + 7 + 7 + 1 + 1 + 1 + 2 + 1);  // y0 dy0 F1 b g b6p ddy dyp yp[2] ypa
+
+void free_engine_buffers()
+{
+    EngineBuffers &e = g_eb;
+    if (e.slab) cudaFree(e.slab);
+    if (e.srcs) cudaFree(e.srcs);
+    if (e.src_body) cudaFree(e.src_body);
+    if (e.src_slot) cudaFree(e.src_slot);
+    if (e.ctl) cudaFree(e.ctl);
+    if (e.ev) cudaFree(e.ev);
+    if (e.d_ce) cudaFree(e.d_ce);
+    if (e.d_coll) cudaFree(e.d_coll);
+    e = EngineBuffers();
+}
+
+static int engine_reserve(size_t n, size_t max_ce, size_t max_coll)
+{
+    EngineBuffers &e = g_eb;
+    if (n > e.slab_n || !e.slab) {
+        if (e.slab) cudaFree(e.slab);
+        if (e.srcs) cudaFree(e.srcs);
+        if (e.src_body) cudaFree(e.src_body);
+        if (e.src_slot) cudaFree(e.src_slot);
+        e.slab = nullptr;
+        size_t c = n < 64 ? 64 : n;
+        ABIE_CUDA(cudaMalloc(&e.slab, c * SLAB_PER_BODY * sizeof(double)));
+        ABIE_CUDA(cudaMalloc(&e.srcs, 3 * c * sizeof(Src)));
+        ABIE_CUDA(cudaMalloc(&e.src_body, c * sizeof(int)));
+        ABIE_CUDA(cudaMalloc(&e.src_slot, c * sizeof(int)));
+        e.slab_n = c;
+    }
+    if (!e.ctl) ABIE_CUDA(cudaMalloc(&e.ctl, sizeof(EngineCtl)));
+    if (!e.ev) ABIE_CUDA(cudaMalloc(&e.ev, EV_CAP * sizeof(EventRec)));
+    if (4 * max_ce > e.d_ce_n || !e.d_ce) {
+        if (e.d_ce) cudaFree(e.d_ce);
+        e.d_ce_n = 4 * (max_ce ? max_ce : 1);
+        ABIE_CUDA(cudaMalloc(&e.d_ce, e.d_ce_n * sizeof(double)));
+    }
+    if (4 * max_coll > e.d_coll_n || !e.d_coll) {
+        if (e.d_coll) cudaFree(e.d_coll);
+        e.d_coll_n = 4 * (max_coll ? max_coll : 1);
+        ABIE_CUDA(cudaMalloc(&e.d_coll, e.d_coll_n * sizeof(double)));
+    }
+    return 0;
+}
+
+template <int MODE, int JS>
+static int launch_engine(const EngineArgs &a, int num_sms, cudaStream_t st, int *grid_out)
+{
+    int bps = 0;
+    ABIE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, radau_engine<MODE, JS>, 256, 0));
+    if (bps < 1) {
+        set_error(ABIE_ERR_CUDA, "radau engine does not fit on an SM");
+        return ABIE_ERR_CUDA;
+    }
+    long long want = ((long long)a.n * JS + 255) / 256;
+    long long grid = std::min<long long>((long long)bps * num_sms, std::max<long long>(want, 1));
+    EngineArgs args = a;
+    void *params[] = {&args};
+    ABIE_CUDA(cudaLaunchCooperativeKernel((const void *)radau_engine<MODE, JS>, dim3((unsigned)grid),
+                                          dim3(256), params, 0, st));
+    *grid_out = (int)grid;
+    return 0;
+}
+
+static int dispatch_engine(int mode, int js, const EngineArgs &a, int num_sms, cudaStream_t st,
+                           int *grid)
+{
+    if (mode == ABIE_FORCE_EXACT) return launch_engine<ABIE_FORCE_EXACT, 1>(a, num_sms, st, grid);
+    if (js == 1) return launch_engine<ABIE_FORCE_FP64, 1>(a, num_sms, st, grid);
+    if (js == 8) return launch_engine<ABIE_FORCE_FP64, 8>(a, num_sms, st, grid);
+    return launch_engine<ABIE_FORCE_FP64, 32>(a, num_sms, st, grid);
+}
+
+int radau_run(const SystemView &sys, double t, double t_end, int mode, EventState *evs,
+              double *t_out, abie_counters *ctr, cudaStream_t st)
+{
+    const int n = sys.n;
+    if (n <= 0) {
+        *t_out = t;
+        return 0;
+    }
+    if (mode == ABIE_FORCE_NAIVE || mode == ABIE_FORCE_MIXED) mode = ABIE_FORCE_FP64;
+    size_t max_ce = evs ? evs->max_ce : 0, max_coll = evs ? evs->max_coll : 0;
+    int rc = engine_reserve((size_t)n, max_ce, max_coll);
+    if (rc) return rc;
+    EngineBuffers &e = g_eb;
+    const size_t d = 3 * (size_t)n;
+
+    // source list: massive bodies in body order
+    std::vector<int> body, slot(n, -1);
+    double rmax = 0.0;
+    for (int j = 0; j < n; j++) {
+        if (sys.h_m[j] > 0.0) {
+            slot[j] = (int)body.size();
+            body.push_back(j);
+        }
+        if (sys.h_r && sys.h_r[j] > rmax) rmax = sys.h_r[j];
+    }
+    int n_src = (int)body.size();
+    if (n_src) ABIE_CUDA(cudaMemcpyAsync(e.src_body, body.data(), n_src * sizeof(int), cudaMemcpyHostToDevice, st));
+    ABIE_CUDA(cudaMemcpyAsync(e.src_slot, slot.data(), n * sizeof(int), cudaMemcpyHostToDevice, st));
+
+    ABIE_CUDA(cudaMemsetAsync(e.slab, 0, (size_t)n * SLAB_PER_BODY * sizeof(double), st));
+    EngineArgs a = {};
+    a.n = n;
+    a.dim = (int)d;
+    a.n_src = n_src;
+    a.src_body = e.src_body;
+    a.src_slot = e.src_slot;
+    a.m = sys.m;
+    a.r = sys.r;
+    a.ext = sys.ext;
+    a.G = sys.G;
+    double *p = e.slab;
+    a.y0 = p; p += d;
+    a.dy0 = p; p += d;
+    a.F1 = p; p += d;
+    a.b = p; p += 7 * d;
+    a.g = p; p += 7 * d;
+    a.b6p = p; p += d;
+    a.ddy = p; p += d;
+    a.dyp = p; p += d;
+    a.yp[0] = p; p += d;
+    a.yp[1] = p; p += d;
+    a.ypa = p; p += d;
+    a.src[0] = e.srcs;
+    a.src[1] = e.srcs + n;
+    a.srca = e.srcs + 2 * n;
+    a.t_end = t_end;
+    double ce = evs ? evs->ce_dist : 0.0;
+    a.ce_dist = ce;
+    double thr = std::max(ce, 2.0 * rmax);
+    a.thr2 = thr * thr * (1.0 + 1e-12);
+    a.max_ce = (long long)max_ce;
+    a.max_coll = (long long)max_coll;
+    a.buf_ce = max_ce ? e.d_ce : nullptr;
+    a.buf_coll = max_coll ? e.d_coll : nullptr;
+    a.ev = e.ev;
+    a.ev_cap = EV_CAP;
+    a.ctl = e.ctl;
+    a.timeout_ns = 2000000000ll + 12ll * (long long)n * (long long)std::max(n_src, 1);
+
+    ABIE_CUDA(cudaMemcpyAsync(a.y0, sys.pos, d * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    ABIE_CUDA(cudaMemcpyAsync(a.dy0, sys.vel, d * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    if (evs && max_ce)
+        ABIE_CUDA(cudaMemcpyAsync(e.d_ce, evs->buf_ce->data(), 4 * max_ce * sizeof(double),
+                                  cudaMemcpyHostToDevice, st));
+    if (evs && max_coll)
+        ABIE_CUDA(cudaMemcpyAsync(e.d_coll, evs->buf_coll->data(), 4 * max_coll * sizeof(double),
+                                  cudaMemcpyHostToDevice, st));
+    EngineCtl c0;
+    memset(&c0, 0, sizeof c0);
+    c0.t = t;
+    c0.n_ce = evs ? *evs->n_ce : 0;
+    c0.n_coll = evs ? *evs->n_coll : 0;
+    ABIE_CUDA(cudaMemcpyAsync(e.ctl, &c0, sizeof c0, cudaMemcpyHostToDevice, st));
+    ABIE_CUDA(cudaStreamSynchronize(st));
+
+    int js = 1;
+    if (mode != ABIE_FORCE_EXACT) js = n_src <= 64 ? 1 : (n_src <= 1024 ? 8 : 32);
+    EngineCtl c;
+    long long budget = 4;
+    for (;;) {
+        a.attempt_budget = budget;
+        cudaEvent_t e0, e1;
+        ABIE_CUDA(cudaEventCreate(&e0));
+        ABIE_CUDA(cudaEventCreate(&e1));
+        ABIE_CUDA(cudaEventRecord(e0, st));
+        int grid = 0;
+        rc = dispatch_engine(mode, js, a, g_sim.num_sms, st, &grid);
+        if (rc) return rc;
+        ABIE_CUDA(cudaEventRecord(e1, st));
+        ABIE_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        ABIE_CUDA(cudaMemcpy(&c, e.ctl, sizeof c, cudaMemcpyDeviceToHost));
+        if (c.err) {
+            set_error(c.err, "radau engine stopped (code %d, t=%g)", c.err, c.t);
+            return c.err;
+        }
+        if (c.phase == 2) break;
+        // aim each launch at about 100 ms of GPU time
+        double per = ms / (double)std::max<long long>(budget, 1);
+        long long next = per > 0 ? (long long)(100.0 / per) : budget * 4;
+        budget = std::max<long long>(1, std::min<long long>(next, budget * 8));
+        budget = std::min<long long>(budget, 1 << 20);
+    }
+    if (c.ev_overflow) {
+        set_error(ABIE_ERR_CAPACITY, "more than %d events in one check; ring buffers incomplete",
+                  EV_CAP);
+    }
+    ABIE_CUDA(cudaMemcpyAsync(sys.pos, a.y0, d * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    ABIE_CUDA(cudaMemcpyAsync(sys.vel, a.dy0, d * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    if (evs && max_ce)
+        ABIE_CUDA(cudaMemcpyAsync(evs->buf_ce->data(), e.d_ce, 4 * max_ce * sizeof(double),
+                                  cudaMemcpyDeviceToHost, st));
+    if (evs && max_coll)
+        ABIE_CUDA(cudaMemcpyAsync(evs->buf_coll->data(), e.d_coll, 4 * max_coll * sizeof(double),
+                                  cudaMemcpyDeviceToHost, st));
+    ABIE_CUDA(cudaStreamSynchronize(st));
+    if (evs) {
+        *evs->n_ce = (size_t)c.n_ce;
+        *evs->n_coll = (size_t)c.n_coll;
+    }
+    *t_out = c.t;
+    if (ctr) {
+        ctr->force_calls += c.force_calls;
+        ctr->iterations += c.iterations;
+        ctr->attempts += c.attempts;
+        ctr->accepts += c.accepts;
+        ctr->rejects += c.rejects;
+        ctr->last_h = c.h;
+    }
+    return c.flag;
+}
+
+}  // namespace abie
+
+using namespace abie;
+
 extern "C" {
+
 int integrator_gr(double t, double t_end, double dt)
 {
-    (void)t; (void)t_end; (void)dt;
-    abie::set_error(ABIE_ERR_UNSUPPORTED, "integrator_gr: engine not built yet");
-    return ABIE_ERR_UNSUPPORTED;
+    (void)dt;  // ignored, as in the reference (h comes from initial_time_step)
+    Sim &s = g_sim;
+    if (!s.inited) {
+        set_error(ABIE_ERR_NOT_INITIALIZED, "integrator_gr before initialize_code");
+        return ABIE_ERR_NOT_INITIALIZED;
+    }
+    if (s.C > 0.0) {
+        set_error(ABIE_ERR_UNSUPPORTED,
+                  "post-Newtonian terms (C > 0, src/additional_forces.c) are not on the GPU path");
+        return ABIE_ERR_UNSUPPORTED;
+    }
+    SystemView v{s.pos, s.vel, s.m, s.r, s.ext_enabled ? s.ext_acc : nullptr,
+                 s.h_m.data(), s.h_r.data(), (int)s.n, s.G};
+    EventState ev{s.ce_dist, s.max_ce, s.max_coll, &s.n_ce, &s.n_coll, &s.buf_ce, &s.buf_coll};
+    double t_out = t;
+    int rc = radau_run(v, t, t_end, s.force_mode, &ev, &t_out, &s.ctr, s.st);
+    if (rc >= 0) s.t = t_out;
+    return rc;
 }
+
 size_t integrator_gauss_radau15(double *pos, double *vel, double *m_vec, double *r_vec, size_t N,
                                 double G, double t, double t_end, double dt)
 {
-    (void)pos; (void)vel; (void)m_vec; (void)r_vec; (void)N; (void)G; (void)t; (void)t_end; (void)dt;
-    return (size_t)(long long)ABIE_ERR_UNSUPPORTED;
+    (void)dt;
+    int rc = ensure_device(-1);
+    if (rc) return (size_t)(long long)rc;
+    Sim &s = g_sim;
+    N &= 0xffffffffull;
+    double *dp = nullptr, *dv = nullptr, *dm = nullptr, *dr = nullptr;
+    size_t cp = 0, cv = 0, cm = 0, cr = 0;
+    if ((rc = reserve(&dp, &cp, 3 * N)) || (rc = reserve(&dv, &cv, 3 * N)) ||
+        (rc = reserve(&dm, &cm, N)) || (rc = reserve(&dr, &cr, N)))
+        return (size_t)(long long)rc;
+    cudaMemcpy(dp, pos, 3 * N * 8, cudaMemcpyHostToDevice);
+    cudaMemcpy(dv, vel, 3 * N * 8, cudaMemcpyHostToDevice);
+    cudaMemcpy(dm, m_vec, N * 8, cudaMemcpyHostToDevice);
+    cudaMemcpy(dr, r_vec, N * 8, cudaMemcpyHostToDevice);
+    SystemView v{dp, dv, dm, dr, nullptr, m_vec, r_vec, (int)N, G};
+    EventState ev{s.ce_dist, s.max_ce, s.max_coll, &s.n_ce, &s.n_coll, &s.buf_ce, &s.buf_coll};
+    double t_out = t;
+    rc = radau_run(v, t, t_end, s.force_mode, s.inited ? &ev : nullptr, &t_out, &s.ctr, s.st);
+    if (rc >= 0) {
+        cudaMemcpy(pos, dp, 3 * N * 8, cudaMemcpyDeviceToHost);
+        cudaMemcpy(vel, dv, 3 * N * 8, cudaMemcpyDeviceToHost);
+        s.t = t_out;
+    }
+    cudaFree(dp);
+    cudaFree(dv);
+    cudaFree(dm);
+    cudaFree(dr);
+    return (size_t)(long long)rc;
 }
+
 int integrator_wh(double t, double t_end, double dt)
 {
     (void)t; (void)t_end; (void)dt;
+    set_error(ABIE_ERR_UNSUPPORTED, "integrator_wh: not built yet");
     return ABIE_ERR_UNSUPPORTED;
 }
 void integrator_wisdom_holman(double *pos, double *vel, double *m_vec, double *r_vec, size_t N,
