@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "abi_state.cuh"
+#include "engine.cuh"
 #include "force.cuh"
 
 namespace abie {
@@ -216,6 +217,7 @@ int finalize_code(void)
     s.tmp_pos_cap = s.tmp_m_cap = s.tmp_acc_cap = s.energy_cap = 0;
     force_scratch_free(s.fs);
     free_engine_buffers();
+    free_wh_buffers();
     // like the reference, a finalized library is not re-initialized in the
     // same process (src/common.c:506-522 leaves code_inited set)
     return 0;

@@ -30,4 +30,10 @@ struct EventState {
 int radau_run(const SystemView &sys, double t, double t_end, int mode, EventState *ev,
               double *t_out, abie_counters *ctr, cudaStream_t st);
 
+// Wisdom-Holman (wh.cu) from t while t < t_end in steps of dt on a
+// heliocentric state; *t_out gets the accumulated time.
+int wh_run(const SystemView &sys, double t, double t_end, double dt, double *t_out,
+           abie_counters *ctr, cudaStream_t st);
+void free_wh_buffers();
+
 }  // namespace abie

@@ -1,0 +1,594 @@
+// Batched Gauss-Radau 15 over many independent small systems.
+//
+// One warp integrates one system (at most 21 bodies) from a work queue; a
+// finished warp takes the next system, so systems of uneven size and
+// difficulty do not wait for each other.  Each lane owns up to two of the
+// system's 3N components and keeps their Radau state (y0, dy0, F1, b[7],
+// g[7], previous b6) in registers.  For the force, the predicted positions
+// go to shared memory and the pairs spread over the lanes: L = 32/N lanes
+// per sink, each summing every L-th source, partial sums added in lane
+// order (L = 1 and the reference's operations in the exact form).  The
+// sweep itself -- predictor, g/b updates, convergence test, step control,
+// refine_bs -- is the reference's (src/integrator_gauss_radau15.c:287-446)
+// component by component, as in the single-system engine.
+//
+// Launches are bounded in time: a warp that has run past the launch's time
+// budget saves its system's state and leaves; the host launches again over
+// the systems not yet done.
+#include <algorithm>
+#include <vector>
+
+#include "abi_state.cuh"
+#include "ensemble.cuh"
+#include "radau_constants.h"
+
+namespace abie {
+
+__constant__ double e_hs[8] = ABIE_RADAU_HS_INIT;
+__constant__ double e_rs[8][8] = ABIE_RADAU_RS_INIT;
+__constant__ double e_cs[8][8] = ABIE_RADAU_CS_INIT;
+
+static constexpr double EPSB = 1.e-4;
+static constexpr double FAC = 0.25;
+static constexpr double TOLPC = 1.e-16;
+static constexpr double H_MIN = 1.e-13;
+static constexpr int ENS_MAX_BODIES = 21;  // 3N <= 64: two components per lane
+static constexpr int WARPS = 4;            // warps per block
+static constexpr int STATE_PER_COMP = 18;  // y0 dy0 F1 b[7] g[7] b6p
+
+struct EnsScalars {
+    double t, h;
+    int loop_count, phase;  // phase 0: fresh, 1: running, 2: done
+    long long steps, attempts, iterations, force_calls;
+    int status;
+    int pad;
+};
+
+struct EnsArgs {
+    const long long *offsets;
+    const double *m;
+    double *pos, *vel;  // packed 3*total, updated at the end
+    double *state;      // STATE_PER_COMP * 3 * total
+    EnsScalars *sc;     // per system
+    const int *active;  // systems to run in this launch
+    int n_active;
+    int *queue;
+    double G, t_end;
+    unsigned long long budget_ns;    // a warp yields once this long after the launch began
+    const LearnedPredictor *mlp;     // null: plain predictor
+};
+
+__device__ __forceinline__ unsigned long long ens_timer()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Component state of one lane.
+struct Comp {
+    double y0, dy0, F1, b[7], g[7], b6p;
+};
+
+template <int MODE>
+__device__ __forceinline__ double e_pred_pos(const Comp &c, double s, double dt)
+{
+    const double *b = c.b;
+    if (MODE == ABIE_FORCE_EXACT)
+        return c.y0 + dt * s * (c.dy0 + dt * s * (c.F1 + s * (b[0] / 0.3e1 + s * (b[1] / 0.6e1 + s * (b[2] / 0.10e2 + s * (b[3] / 0.15e2 + s * (b[4] / 0.21e2 + s * (b[5] / 0.28e2 + s * b[6] / 0.36e2))))))) / 0.2e1);
+    // same polynomial with the divisions as products by rounded reciprocals
+    double u = s * (b[6] * (1.0 / 36.0));
+    u = s * fma(b[5], 1.0 / 28.0, u);
+    u = s * fma(b[4], 1.0 / 21.0, u);
+    u = s * fma(b[3], 1.0 / 15.0, u);
+    u = s * fma(b[2], 1.0 / 10.0, u);
+    u = s * fma(b[1], 1.0 / 6.0, u);
+    u = s * fma(b[0], 1.0 / 3.0, u);
+    double ds = dt * s;
+    return fma(ds, fma(0.5 * ds, c.F1 + u, c.dy0), c.y0);
+}
+
+template <int MODE>
+__device__ __forceinline__ double e_pred_vel(const Comp &c, double s, double dt)
+{
+    const double *b = c.b;
+    if (MODE == ABIE_FORCE_EXACT)
+        return c.dy0 + dt * s * (c.F1 + s * (b[0] / 0.2e1 + s * (b[1] / 0.3e1 + s * (b[2] / 0.4e1 + s * (b[3] / 0.5e1 + s * (b[4] / 0.6e1 + s * (b[5] / 0.7e1 + s * b[6] / 0.8e1)))))));
+    double u = s * (b[6] * 0.125);
+    u = s * fma(b[5], 1.0 / 7.0, u);
+    u = s * fma(b[4], 1.0 / 6.0, u);
+    u = s * fma(b[3], 0.2, u);
+    u = s * fma(b[2], 0.25, u);
+    u = s * fma(b[1], 1.0 / 3.0, u);
+    u = s * fma(b[0], 0.5, u);
+    return fma(dt * s, c.F1 + u, c.dy0);
+}
+
+__device__ __forceinline__ void e_gb_update(Comp &c, int ih, double F)
+{
+    double v = (F - c.F1) * e_rs[ih][0];
+#pragma unroll
+    for (int l = 1; l < 7; l++)
+        if (l < ih) v = (v - c.g[l - 1]) * e_rs[ih][l];
+#pragma unroll
+    for (int k = 0; k < 7; k++)
+        if (k == ih - 1) c.g[k] = v;
+#pragma unroll
+    for (int k = 0; k < 7; k++) {
+        if (k < ih) {
+            double s = e_cs[k][k] * c.g[k];
+#pragma unroll
+            for (int jj = k + 1; jj < 7; jj++) s = s + e_cs[jj][k] * c.g[jj];
+            c.b[k] = s;
+        }
+    }
+}
+
+__device__ __forceinline__ void e_refine(Comp &c, double q)
+{
+    double *b = c.b;
+    double q2 = q * q, q3 = q2 * q, q4 = q2 * q2, q5 = q2 * q3, q6 = q3 * q3, q7 = q2 * q5;
+    double e0 = q * (b[6] * 7.0 + b[5] * 6.0 + b[4] * 5.0 + b[3] * 4.0 + b[2] * 3.0 + b[1] * 2.0 + b[0]);
+    double e1 = q2 * (b[6] * 21.0 + b[5] * 15.0 + b[4] * 10.0 + b[3] * 6.0 + b[2] * 3.0 + b[1]);
+    double e2 = q3 * (b[6] * 35.0 + b[5] * 20.0 + b[4] * 10.0 + b[3] * 4.0 + b[2]);
+    double e3 = q4 * (b[6] * 35.0 + b[5] * 15.0 + b[4] * 5.0 + b[3]);
+    double e4 = q5 * (b[6] * 21.0 + b[5] * 6.0 + b[4]);
+    double e5 = q6 * (b[6] * 7.0 + b[5]);
+    double e6 = q7 * b[6];
+    b[0] = e0 + 0.0;
+    b[1] = e1 + 0.0;
+    b[2] = e2 + 0.0;
+    b[3] = e3 + 0.0;
+    b[4] = e4 + 0.0;
+    b[5] = e5 + 0.0;
+    b[6] = e6 + 0.0;
+}
+
+__device__ __forceinline__ double warp_maxd(double v)
+{
+    // the values are non-negative magnitudes or -DBL_MAX; plain max is exact
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+__device__ __forceinline__ double absmax_or_none(double v)
+{
+    double a = fabs(v);
+    return (a == a) ? a : -1.7976931348623157e308;
+}
+
+// Accelerations of the n bodies whose predicted positions and G m are in
+// sp[k] = {x, y, z, Gm}; the result of sink i goes to sa[i].
+template <int MODE>
+__device__ __forceinline__ void warp_force(int n, const double (*sp)[4], double (*sa)[3], int lane,
+                                           int L)
+{
+    const int g = lane / L, hh = lane % L;
+    double ax = 0.0, ay = 0.0, az = 0.0;
+    if (g < n) {
+        const double xi = sp[g][0], yi = sp[g][1], zi = sp[g][2];
+        for (int k = hh; k < n; k += L) {
+            double gm = sp[k][3];
+            if (k == g || !(gm > 0.0)) continue;
+            Src s{sp[k][0], sp[k][1], sp[k][2], gm};
+            if (MODE == ABIE_FORCE_EXACT) pair_exact(xi, yi, zi, s, ax, ay, az);
+            else pair_fast(xi, yi, zi, s, ax, ay, az);
+        }
+    }
+    if (L > 1) {
+        const int base = (g < 32 ? g : 0) * L;
+        double sx = ax, sy = ay, sz = az;
+        for (int k = 1; k < L; k++) {
+            int src = base + k;
+            src = src < 32 ? src : 31;
+            double ox = __shfl_sync(0xffffffffu, ax, src);
+            double oy = __shfl_sync(0xffffffffu, ay, src);
+            double oz = __shfl_sync(0xffffffffu, az, src);
+            sx += ox;
+            sy += oy;
+            sz += oz;
+        }
+        ax = sx;
+        ay = sy;
+        az = sz;
+    }
+    if (g < n && hh == 0) {
+        sa[g][0] = ax;
+        sa[g][1] = ay;
+        sa[g][2] = az;
+    }
+    __syncwarp();
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(32 * WARPS) ensemble_kernel(EnsArgs a)
+{
+    __shared__ double s_pos[WARPS][32][4];
+    __shared__ double s_acc[WARPS][32][3];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    double(*sp)[4] = s_pos[w];
+    double(*sa)[3] = s_acc[w];
+    const unsigned long long deadline = ens_timer() + a.budget_ns;
+
+    for (;;) {
+        int qi = 0;
+        if (lane == 0) qi = atomicAdd(a.queue, 1);
+        qi = __shfl_sync(0xffffffffu, qi, 0);
+        if (qi >= a.n_active) break;
+        const int sid = a.active[qi];
+        const long long off = a.offsets[sid];
+        const int n = (int)(a.offsets[sid + 1] - off);
+        const int dim = 3 * n;
+        const int L = MODE == ABIE_FORCE_EXACT ? 1 : max(1, 32 / max(n, 1));
+        const double *m = a.m + off;
+        EnsScalars S = a.sc[sid];
+        // lane's components c0 = lane, c1 = lane + 32
+        const bool has0 = lane < dim, has1 = lane + 32 < dim;
+        Comp C[2];
+        double *st = a.state + (size_t)STATE_PER_COMP * 3 * off;
+        auto slot = [&](int c, int k) -> double & { return st[(size_t)k * dim + c]; };
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            const int c = lane + 32 * u;
+            const bool has = u == 0 ? has0 : has1;
+            Comp &X = C[u];
+            if (!has) {
+                X.y0 = X.dy0 = X.F1 = X.b6p = 0.0;
+                for (int k = 0; k < 7; k++) X.b[k] = X.g[k] = 0.0;
+                continue;
+            }
+            if (S.phase == 0) {
+                X.y0 = a.pos[3 * off + c];
+                X.dy0 = a.vel[3 * off + c];
+                X.F1 = 0.0;
+                X.b6p = 0.0;
+                for (int k = 0; k < 7; k++) X.b[k] = X.g[k] = 0.0;
+            } else {
+                X.y0 = slot(c, 0);
+                X.dy0 = slot(c, 1);
+                X.F1 = slot(c, 2);
+                for (int k = 0; k < 7; k++) X.b[k] = slot(c, 3 + k);
+                for (int k = 0; k < 7; k++) X.g[k] = slot(c, 10 + k);
+                X.b6p = slot(c, 17);
+            }
+        }
+        const double G = a.G;
+        // publish a predicted position for every body (components of a
+        // body may sit on different lanes, so go through shared memory)
+        auto publish = [&](double p0, double p1) {
+            if (has0) sp[lane / 3][lane % 3] = p0;
+            if (has1) sp[(lane + 32) / 3][(lane + 32) % 3] = p1;
+            if (lane < n) sp[lane][3] = m[lane] > 0.0 ? G * m[lane] : 0.0;
+            __syncwarp();
+        };
+        auto force_of = [&](int u) -> double {
+            int c = lane + 32 * u;
+            int i = c / 3;
+            return (m[i] >= 0.0) ? sa[i][c % 3] : 0.0;
+        };
+
+        if (S.phase == 0) {
+            // F1 = f(y0), then initial_time_step (:75-120)
+            publish(C[0].y0, C[1].y0);
+            warp_force<MODE>(n, sp, sa, lane, L);
+            if (has0) C[0].F1 = force_of(0);
+            if (has1) C[1].F1 = force_of(1);
+            S.force_calls++;
+            // d0, d1 over the first n of the 3n entries, as the reference does
+            double d0 = -1.7976931348623157e308, d1 = d0;
+            if (lane < n) {
+                d0 = absmax_or_none(C[0].y0);
+                d1 = absmax_or_none(C[0].F1);
+            }
+            if (lane + 32 < n) {
+                d0 = fmax(d0, absmax_or_none(C[1].y0));
+                d1 = fmax(d1, absmax_or_none(C[1].F1));
+            }
+            d0 = warp_maxd(d0);
+            d1 = warp_maxd(d1);
+            double dt0 = (d0 < 1e-5 || d1 < 1e-5) ? 1e-6 : 0.01 * (d0 / d1);
+            __syncwarp();
+            publish(C[0].y0 + dt0 * C[0].dy0, C[1].y0 + dt0 * C[1].dy0);
+            warp_force<MODE>(n, sp, sa, lane, L);
+            S.force_calls++;
+            double d2 = -1.7976931348623157e308;
+            if (has0) d2 = absmax_or_none(force_of(0) - C[0].F1);
+            if (has1) d2 = fmax(d2, absmax_or_none(force_of(1) - C[1].F1));
+            d2 = warp_maxd(d2) / dt0;
+            double dt1;
+            if (fmax(d1, d2) <= 1e-15) dt1 = fmax(1e-6, dt0 * 1e-3);
+            else dt1 = pow(0.01 / fmax(d1, d2), (1.0 / (15 + 1)));
+            S.h = fmin(100 * dt0, dt1);
+            S.loop_count = 0;
+            S.phase = 1;
+            __syncwarp();
+        }
+
+        double t = S.t, h = S.h;
+        int loop_count = S.loop_count;
+        bool done = false;
+        while (!done) {
+            if (ens_timer() > deadline) break;
+            int iters = 0;
+            for (int ipc = 0; ipc < 12; ipc++) {
+                iters++;
+                double f8 = -1.7976931348623157e308, db6 = f8;
+                for (int ih = 1; ih < 8; ih++) {
+                    __syncwarp();
+                    publish(e_pred_pos<MODE>(C[0], e_hs[ih], h), e_pred_pos<MODE>(C[1], e_hs[ih], h));
+                    warp_force<MODE>(n, sp, sa, lane, L);
+#pragma unroll
+                    for (int u = 0; u < 2; u++) {
+                        if (!(u == 0 ? has0 : has1)) continue;
+                        double F = force_of(u);
+                        e_gb_update(C[u], ih, F);
+                        if (ih == 7) {
+                            f8 = fmax(f8, absmax_or_none(F));
+                            db6 = fmax(db6, absmax_or_none(C[u].b[6] - C[u].b6p));
+                        }
+                    }
+                }
+                S.force_calls += 7;
+                f8 = warp_maxd(f8);
+                db6 = warp_maxd(db6);
+                if (db6 / f8 < TOLPC) break;
+#pragma unroll
+                for (int u = 0; u < 2; u++) C[u].b6p = C[u].b[6];
+            }
+            S.iterations += iters;
+            S.attempts++;
+            // advance
+            __syncwarp();
+            double ya0 = e_pred_pos<MODE>(C[0], 1.0, h), ya1 = e_pred_pos<MODE>(C[1], 1.0, h);
+            double va0 = e_pred_vel<MODE>(C[0], 1.0, h), va1 = e_pred_vel<MODE>(C[1], 1.0, h);
+            publish(ya0, ya1);
+            warp_force<MODE>(n, sp, sa, lane, L);
+            S.force_calls++;
+            double dd0 = has0 ? force_of(0) : 0.0, dd1 = has1 ? force_of(1) : 0.0;
+            bool bad = (has0 && !isfinite(ya0 + dd0 + va0)) || (has1 && !isfinite(ya1 + dd1 + va1));
+            if (__any_sync(0xffffffffu, bad)) {  // non-finite state: report, stop this system
+                S.status = ABIE_ERR_NUMERICS;
+                done = true;
+                break;
+            }
+            double mb6 = -1.7976931348623157e308, mdd = mb6;
+            if (has0) {
+                mb6 = absmax_or_none(C[0].b[6]);
+                mdd = absmax_or_none(dd0);
+            }
+            if (has1) {
+                mb6 = fmax(mb6, absmax_or_none(C[1].b[6]));
+                mdd = fmax(mdd, absmax_or_none(dd1));
+            }
+            mb6 = warp_maxd(mb6);
+            mdd = warp_maxd(mdd);
+            double estim_b6 = mb6 / mdd;
+            double err = pow(estim_b6 / EPSB, 1. / 7);
+            double dtreq = h / err;
+            if (!(err == err)) {  // NaN step control: the state is not finite
+                S.status = ABIE_ERR_NUMERICS;
+                done = true;
+                break;
+            }
+            if (err <= 1 || loop_count > 100) {
+                t += h;
+                loop_count = 0;
+                S.steps++;
+                bool stop = false;
+                if (t > a.t_end) {
+                    h = a.t_end - t;
+                    stop = true;
+                }
+                double q = dtreq / h;
+                C[0].y0 = ya0;
+                C[0].dy0 = va0;
+                C[0].F1 = dd0;
+                C[0].b6p = C[0].b[6];
+                C[1].y0 = ya1;
+                C[1].dy0 = va1;
+                C[1].F1 = dd1;
+                C[1].b6p = C[1].b[6];
+                if (!stop) {
+                    e_refine(C[0], q);
+                    e_refine(C[1], q);
+                }
+                if (stop) {
+                    done = true;
+                    break;
+                }
+            } else {
+                loop_count += 1;
+            }
+            if (dtreq / h > 1.0 / FAC) h /= FAC;
+            else if (dtreq < 1.e-12) h *= FAC;
+            else h = dtreq;
+            if (h < H_MIN) h = H_MIN;
+        }
+        S.t = t;
+        S.h = h;
+        S.loop_count = loop_count;
+        if (done) S.phase = 2;
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            const int c = lane + 32 * u;
+            if (!(u == 0 ? has0 : has1)) continue;
+            const Comp &X = C[u];
+            if (done) {
+                a.pos[3 * off + c] = X.y0;
+                a.vel[3 * off + c] = X.dy0;
+            } else {
+                slot(c, 0) = X.y0;
+                slot(c, 1) = X.dy0;
+                slot(c, 2) = X.F1;
+                for (int k = 0; k < 7; k++) slot(c, 3 + k) = X.b[k];
+                for (int k = 0; k < 7; k++) slot(c, 10 + k) = X.g[k];
+                slot(c, 17) = X.b6p;
+            }
+        }
+        if (lane == 0) a.sc[sid] = S;
+        __syncwarp();
+    }
+}
+
+static double g_last_seconds = 0.0;
+
+static void launch_ensemble(int mode, int blocks, const EnsArgs &a, cudaStream_t st)
+{
+    if (mode == ABIE_FORCE_EXACT)
+        ensemble_kernel<ABIE_FORCE_EXACT><<<blocks, 32 * WARPS, 0, st>>>(a);
+    else
+        ensemble_kernel<ABIE_FORCE_FP64><<<blocks, 32 * WARPS, 0, st>>>(a);
+}
+
+int ensemble_run(double *pos, double *vel, const double *m, const long long *offsets, int ns,
+                 double G, double t0, double t_end, double *t_out, int *status, long long *steps,
+                 int mode, const LearnedPredictor *mlp, cudaStream_t st, EnsembleStats *stats)
+{
+    if (ns <= 0) return 0;
+    long long total = offsets[ns];
+    for (int s = 0; s < ns; s++) {
+        long long k = offsets[s + 1] - offsets[s];
+        if (k < 1 || k > ENS_MAX_BODIES) {
+            set_error(ABIE_ERR_ARGUMENT, "ensemble system %d has %lld bodies (1..%d supported)", s,
+                      k, ENS_MAX_BODIES);
+            return ABIE_ERR_ARGUMENT;
+        }
+    }
+    if (mode == ABIE_FORCE_NAIVE || mode == ABIE_FORCE_MIXED) mode = ABIE_FORCE_FP64;
+    double *d_pos, *d_vel, *d_m, *d_state;
+    long long *d_off;
+    EnsScalars *d_sc;
+    int *d_active, *d_queue;
+    ABIE_CUDA(cudaMalloc(&d_pos, 3 * total * sizeof(double)));
+    ABIE_CUDA(cudaMalloc(&d_vel, 3 * total * sizeof(double)));
+    ABIE_CUDA(cudaMalloc(&d_m, total * sizeof(double)));
+    ABIE_CUDA(cudaMalloc(&d_state, (size_t)STATE_PER_COMP * 3 * total * sizeof(double)));
+    ABIE_CUDA(cudaMalloc(&d_off, (ns + 1) * sizeof(long long)));
+    ABIE_CUDA(cudaMalloc(&d_sc, ns * sizeof(EnsScalars)));
+    ABIE_CUDA(cudaMalloc(&d_active, ns * sizeof(int)));
+    ABIE_CUDA(cudaMalloc(&d_queue, sizeof(int)));
+    std::vector<EnsScalars> sc(ns);
+    for (int s = 0; s < ns; s++) {
+        memset(&sc[s], 0, sizeof(EnsScalars));
+        sc[s].t = t0;
+    }
+    std::vector<int> active(ns);
+    for (int s = 0; s < ns; s++) active[s] = s;
+    ABIE_CUDA(cudaMemcpyAsync(d_pos, pos, 3 * total * sizeof(double), cudaMemcpyHostToDevice, st));
+    ABIE_CUDA(cudaMemcpyAsync(d_vel, vel, 3 * total * sizeof(double), cudaMemcpyHostToDevice, st));
+    ABIE_CUDA(cudaMemcpyAsync(d_m, m, total * sizeof(double), cudaMemcpyHostToDevice, st));
+    ABIE_CUDA(cudaMemcpyAsync(d_off, offsets, (ns + 1) * sizeof(long long), cudaMemcpyHostToDevice, st));
+    ABIE_CUDA(cudaMemcpyAsync(d_sc, sc.data(), ns * sizeof(EnsScalars), cudaMemcpyHostToDevice, st));
+    ABIE_CUDA(cudaStreamSynchronize(st));
+
+    int bps = 0;
+    const void *fn = mode == ABIE_FORCE_EXACT ? (const void *)ensemble_kernel<ABIE_FORCE_EXACT>
+                                              : (const void *)ensemble_kernel<ABIE_FORCE_FP64>;
+    ABIE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fn, 32 * WARPS, 0));
+    bps = std::max(bps, 1);
+    cudaEvent_t e0, e1;
+    ABIE_CUDA(cudaEventCreate(&e0));
+    ABIE_CUDA(cudaEventCreate(&e1));
+    double gpu_ms = 0.0;
+    int launches = 0;
+    int n_active = ns;
+    while (n_active > 0) {
+        ABIE_CUDA(cudaMemcpyAsync(d_active, active.data(), n_active * sizeof(int),
+                                  cudaMemcpyHostToDevice, st));
+        ABIE_CUDA(cudaMemsetAsync(d_queue, 0, sizeof(int), st));
+        EnsArgs a;
+        a.offsets = d_off;
+        a.m = d_m;
+        a.pos = d_pos;
+        a.vel = d_vel;
+        a.state = d_state;
+        a.sc = d_sc;
+        a.active = d_active;
+        a.n_active = n_active;
+        a.queue = d_queue;
+        a.G = G;
+        a.t_end = t_end;
+        a.mlp = mlp;
+        a.budget_ns = 2000000000ull;  // each launch yields after about two seconds
+        int blocks = std::min<long long>((long long)bps * g_sim.num_sms,
+                                         (n_active + WARPS - 1) / WARPS);
+        blocks = std::max(blocks, 1);
+        ABIE_CUDA(cudaEventRecord(e0, st));
+        launch_ensemble(mode, blocks, a, st);
+        ABIE_CUDA(cudaGetLastError());
+        ABIE_CUDA(cudaEventRecord(e1, st));
+        ABIE_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        gpu_ms += ms;
+        launches++;
+        ABIE_CUDA(cudaMemcpy(sc.data(), d_sc, ns * sizeof(EnsScalars), cudaMemcpyDeviceToHost));
+        int k = 0;
+        for (int s = 0; s < ns; s++)
+            if (sc[s].phase != 2 && sc[s].status == 0) active[k++] = s;
+        n_active = k;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    ABIE_CUDA(cudaMemcpy(pos, d_pos, 3 * total * sizeof(double), cudaMemcpyDeviceToHost));
+    ABIE_CUDA(cudaMemcpy(vel, d_vel, 3 * total * sizeof(double), cudaMemcpyDeviceToHost));
+    for (int s = 0; s < ns; s++) {
+        if (t_out) t_out[s] = sc[s].t;
+        if (status) status[s] = sc[s].status;
+        if (steps) steps[s] = sc[s].steps;
+        if (stats) {
+            stats->attempts += sc[s].attempts;
+            stats->iterations += sc[s].iterations;
+            stats->force_calls += sc[s].force_calls;
+            stats->steps += sc[s].steps;
+        }
+    }
+    if (stats) stats->launches += launches;
+    g_last_seconds = gpu_ms * 1e-3;
+    cudaFree(d_pos);
+    cudaFree(d_vel);
+    cudaFree(d_m);
+    cudaFree(d_state);
+    cudaFree(d_off);
+    cudaFree(d_sc);
+    cudaFree(d_active);
+    cudaFree(d_queue);
+    return 0;
+}
+
+double ensemble_last_seconds() { return g_last_seconds; }
+
+}  // namespace abie
+
+using namespace abie;
+
+extern "C" {
+
+int abie_gr_ensemble(double *pos, double *vel, const double *m, const long long *offsets,
+                     int n_systems, double G, double t0, double t_end, double *t_out, int *status,
+                     long long *steps, int flags)
+{
+    int rc = ensure_device(-1);
+    if (rc) return rc;
+    const LearnedPredictor *mlp = (flags & 1) ? learned_predictor_current() : nullptr;
+    EnsembleStats st = {};
+    rc = ensemble_run(pos, vel, m, offsets, n_systems, G, t0, t_end, t_out, status, steps,
+                      g_sim.force_mode, mlp, g_sim.st, &st);
+    if (rc == 0) {
+        g_sim.ctr.attempts += st.attempts;
+        g_sim.ctr.iterations += st.iterations;
+        g_sim.ctr.force_calls += st.force_calls;
+        g_sim.ctr.accepts += st.steps;
+        g_sim.ctr.rejects += st.attempts - st.steps;
+    }
+    return rc;
+}
+
+double abie_last_ensemble_seconds(void) { return ensemble_last_seconds(); }
+
+}  // extern "C"
+
+namespace abie {
+// No learned predictor is loaded yet in this build.
+const LearnedPredictor *learned_predictor_current() { return nullptr; }
+}  // namespace abie

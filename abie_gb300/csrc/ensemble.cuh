@@ -1,0 +1,20 @@
+// Batched Radau15 ensemble (ensemble.cu) and the learned predictor hook.
+#pragma once
+#include "abi_state.cuh"
+
+namespace abie {
+
+// Learned b-coefficient predictor (mlp.cu); null when none is loaded.
+struct LearnedPredictor;
+const LearnedPredictor *learned_predictor_current();
+
+struct EnsembleStats {
+    long long attempts, iterations, force_calls, steps, launches;
+};
+
+int ensemble_run(double *pos, double *vel, const double *m, const long long *offsets, int ns,
+                 double G, double t0, double t_end, double *t_out, int *status, long long *steps,
+                 int mode, const LearnedPredictor *mlp, cudaStream_t st, EnsembleStats *stats);
+double ensemble_last_seconds();
+
+}  // namespace abie

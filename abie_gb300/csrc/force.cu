@@ -407,3 +407,4 @@ int launch_energy(const double *pos, const double *vel, const double *m, int n, 
 }
 
 }  // namespace abie
+

@@ -168,28 +168,53 @@ __device__ __forceinline__ void sink_accel(const EngineArgs &a, int j, const Src
 }
 
 // Predictor (src/integrator_gauss_radau15.c:122-134): spacing s, step dt.
+// The exact form keeps the reference's divisions by constants; the fast
+// form multiplies by the rounded reciprocals (about one tenth of the FP64
+// work, results within an ulp or two).
+template <int MODE>
 __device__ __forceinline__ double pred_pos(const EngineArgs &a, int i, double s, double dt)
 {
     const int d = a.dim;
     const double *b = a.b;
-    return a.y0[i] + dt * s * (a.dy0[i] + dt * s * (a.F1[i] + s * (b[i] / 0.3e1 + s * (b[d + i] / 0.6e1 + s * (b[2 * d + i] / 0.10e2 + s * (b[3 * d + i] / 0.15e2 + s * (b[4 * d + i] / 0.21e2 + s * (b[5 * d + i] / 0.28e2 + s * b[6 * d + i] / 0.36e2))))))) / 0.2e1);
+    if (MODE == ABIE_FORCE_EXACT)
+        return a.y0[i] + dt * s * (a.dy0[i] + dt * s * (a.F1[i] + s * (b[i] / 0.3e1 + s * (b[d + i] / 0.6e1 + s * (b[2 * d + i] / 0.10e2 + s * (b[3 * d + i] / 0.15e2 + s * (b[4 * d + i] / 0.21e2 + s * (b[5 * d + i] / 0.28e2 + s * b[6 * d + i] / 0.36e2))))))) / 0.2e1);
+    double u = s * (b[6 * d + i] * (1.0 / 36.0));
+    u = s * fma(b[5 * d + i], 1.0 / 28.0, u);
+    u = s * fma(b[4 * d + i], 1.0 / 21.0, u);
+    u = s * fma(b[3 * d + i], 1.0 / 15.0, u);
+    u = s * fma(b[2 * d + i], 1.0 / 10.0, u);
+    u = s * fma(b[d + i], 1.0 / 6.0, u);
+    u = s * fma(b[i], 1.0 / 3.0, u);
+    double ds = dt * s;
+    return fma(ds, fma(0.5 * ds, a.F1[i] + u, a.dy0[i]), a.y0[i]);
 }
 
+template <int MODE>
 __device__ __forceinline__ double pred_vel(const EngineArgs &a, int i, double s, double dt)
 {
     const int d = a.dim;
     const double *b = a.b;
-    return a.dy0[i] + dt * s * (a.F1[i] + s * (b[i] / 0.2e1 + s * (b[d + i] / 0.3e1 + s * (b[2 * d + i] / 0.4e1 + s * (b[3 * d + i] / 0.5e1 + s * (b[4 * d + i] / 0.6e1 + s * (b[5 * d + i] / 0.7e1 + s * b[6 * d + i] / 0.8e1)))))));
+    if (MODE == ABIE_FORCE_EXACT)
+        return a.dy0[i] + dt * s * (a.F1[i] + s * (b[i] / 0.2e1 + s * (b[d + i] / 0.3e1 + s * (b[2 * d + i] / 0.4e1 + s * (b[3 * d + i] / 0.5e1 + s * (b[4 * d + i] / 0.6e1 + s * (b[5 * d + i] / 0.7e1 + s * b[6 * d + i] / 0.8e1)))))));
+    double u = s * (b[6 * d + i] * 0.125);
+    u = s * fma(b[5 * d + i], 1.0 / 7.0, u);
+    u = s * fma(b[4 * d + i], 1.0 / 6.0, u);
+    u = s * fma(b[3 * d + i], 0.2, u);
+    u = s * fma(b[2 * d + i], 0.25, u);
+    u = s * fma(b[d + i], 1.0 / 3.0, u);
+    u = s * fma(b[i], 0.5, u);
+    return fma(dt * s, a.F1[i] + u, a.dy0[i]);
 }
 
 // Predicted position of body j at spacing s into yp, and into the source
 // list when j is massive.
+template <int MODE>
 __device__ __forceinline__ void publish_body(const EngineArgs &a, int j, double s, double dt,
                                              double *yp, Src *src)
 {
-    double p0 = pred_pos(a, 3 * j, s, dt);
-    double p1 = pred_pos(a, 3 * j + 1, s, dt);
-    double p2 = pred_pos(a, 3 * j + 2, s, dt);
+    double p0 = pred_pos<MODE>(a, 3 * j, s, dt);
+    double p1 = pred_pos<MODE>(a, 3 * j + 1, s, dt);
+    double p2 = pred_pos<MODE>(a, 3 * j + 2, s, dt);
     yp[3 * j] = p0;
     yp[3 * j + 1] = p1;
     yp[3 * j + 2] = p2;
@@ -371,7 +396,7 @@ __global__ void __launch_bounds__(256) radau_engine(EngineArgs a)
     if (ctl->phase == 0) {
         // --- F1 = f(y0): publish y0 (spacing 0 gives y0 exactly), then force
         for (int j = gid; j < n; j += ngroups)
-            if (lane == 0) publish_body(a, j, 0.0, 0.0, a.yp[0], a.src[0]);
+            if (lane == 0) publish_body<MODE>(a, j, 0.0, 0.0, a.yp[0], a.src[0]);
         if (!grid_sync(ctl, T)) return;
         for (int j = gid; j < n; j += ngroups) {
             double ax, ay, az;
@@ -444,7 +469,7 @@ __global__ void __launch_bounds__(256) radau_engine(EngineArgs a)
         pc = 0;
         // first attempt's substep-1 prediction
         for (int j = gid; j < n; j += ngroups)
-            if (lane == 0) publish_body(a, j, c_hs[1], h, a.yp[pc & 1], a.src[pc & 1]);
+            if (lane == 0) publish_body<MODE>(a, j, c_hs[1], h, a.yp[pc & 1], a.src[pc & 1]);
         if (!grid_sync(ctl, T)) return;
     } else {
         t = ctl->t;
@@ -483,13 +508,13 @@ __global__ void __launch_bounds__(256) radau_engine(EngineArgs a)
                             }
                         }
                         if (ih < 7) {
-                            publish_body(a, j, c_hs[ih + 1], h, a.yp[(pc + 1) & 1],
+                            publish_body<MODE>(a, j, c_hs[ih + 1], h, a.yp[(pc + 1) & 1],
                                          a.src[(pc + 1) & 1]);
                         } else {
                             // speculative: next iteration's substep 1 and the advance
-                            publish_body(a, j, c_hs[1], h, a.yp[(pc + 1) & 1], a.src[(pc + 1) & 1]);
-                            publish_body(a, j, 1.0, h, a.ypa, a.srca);
-                            for (int c = 0; c < 3; c++) a.dyp[3 * j + c] = pred_vel(a, 3 * j + c, 1.0, h);
+                            publish_body<MODE>(a, j, c_hs[1], h, a.yp[(pc + 1) & 1], a.src[(pc + 1) & 1]);
+                            publish_body<MODE>(a, j, 1.0, h, a.ypa, a.srca);
+                            for (int c = 0; c < 3; c++) a.dyp[3 * j + c] = pred_vel<MODE>(a, 3 * j + c, 1.0, h);
                         }
                     }
                 }
@@ -518,6 +543,7 @@ __global__ void __launch_bounds__(256) radau_engine(EngineArgs a)
                     int i = 3 * j + c;
                     double fi = f[c] + (a.ext ? a.ext[i] : 0.0);
                     a.ddy[i] = fi;
+                    if (!isfinite(fi + a.ypa[i] + a.dyp[i])) atomicCAS(&ctl->err, 0, ABIE_ERR_NUMERICS);
                     unsigned long long u = absmax_key(a.b[6 * a.dim + i]);
                     unsigned long long w = absmax_key(fi);
                     kb6 = u > kb6 ? u : kb6;
@@ -572,7 +598,7 @@ __global__ void __launch_bounds__(256) radau_engine(EngineArgs a)
             if (h < H_MIN) h = H_MIN;
             // next attempt's substep-1 prediction
             for (int j = gid; j < n; j += ngroups)
-                if (lane == 0) publish_body(a, j, c_hs[1], h, a.yp[pc & 1], a.src[pc & 1]);
+                if (lane == 0) publish_body<MODE>(a, j, c_hs[1], h, a.yp[pc & 1], a.src[pc & 1]);
         }
         if (!grid_sync(ctl, T)) return;
         if (accepted && *(volatile int *)&ctl->n_ev > 0) {
@@ -894,24 +920,4 @@ size_t integrator_gauss_radau15(double *pos, double *vel, double *m_vec, double 
     return (size_t)(long long)rc;
 }
 
-int integrator_wh(double t, double t_end, double dt)
-{
-    (void)t; (void)t_end; (void)dt;
-    set_error(ABIE_ERR_UNSUPPORTED, "integrator_wh: not built yet");
-    return ABIE_ERR_UNSUPPORTED;
-}
-void integrator_wisdom_holman(double *pos, double *vel, double *m_vec, double *r_vec, size_t N,
-                              double G, double t, double t_end, double dt)
-{
-    (void)pos; (void)vel; (void)m_vec; (void)r_vec; (void)N; (void)G; (void)t; (void)t_end; (void)dt;
-}
-int abie_gr_ensemble(double *pos, double *vel, const double *m, const long long *offsets,
-                     int n_systems, double G, double t0, double t_end, double *t_out, int *status,
-                     long long *steps, int flags)
-{
-    (void)pos; (void)vel; (void)m; (void)offsets; (void)n_systems; (void)G; (void)t0; (void)t_end;
-    (void)t_out; (void)status; (void)steps; (void)flags;
-    return ABIE_ERR_UNSUPPORTED;
-}
-double abie_last_ensemble_seconds(void) { return 0.0; }
 }

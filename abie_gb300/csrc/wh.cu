@@ -1,0 +1,525 @@
+// Wisdom-Holman kick-drift-kick on the device.
+//
+// Reference: src/integrator_wisdom_holman.c:471-537.  Bodies split into
+//   head: 0 .. the last body with nonzero mass (at least body 1), and
+//   tail: the massless bodies after it.
+// Massless bodies add exact zeros to every running sum of the reference
+// (Jacobi centres of mass, interior masses, indirect and pairwise terms),
+// so every tail body sees the same head quantities: the centre of mass
+// and momentum that shift it into and out of Jacobi coordinates, the
+// Kepler parameter G m0 eta/eta and the indirect and accel2 terms.  A
+// one-block kernel computes the head (its sequential prefixes in the
+// reference's order, its Kepler drifts in parallel) and publishes those
+// quantities; a one-thread-per-body kernel then runs the whole step for
+// each tail body.  Steps are replayed from a captured CUDA graph.
+#include <algorithm>
+#include <vector>
+
+#include "abi_state.cuh"
+#include "engine.cuh"
+
+namespace abie {
+
+static constexpr double KEPLER_TOL = 1e-12;  // src/integrator_wisdom_holman.h:7
+static constexpr double TOL_ENERGY = 0.0;    // :11
+static constexpr int KEPLER_MAX_IT = 500;    // :12
+static constexpr int WH_HEAD_MAX = 4096;
+
+// Quantities the head publishes for the tail.
+struct WhShared {
+    double R[3], V[3];    // helio -> Jacobi shift for tail bodies
+    double Rp[3], Vp[3];  // Jacobi -> helio shift after the drift
+    double ind[3];        // indirect term
+    double a2[3];         // accel2 carried past the head
+    double gm_tail;       // Kepler parameter of a massless body
+    unsigned long long kepler_failures;
+};
+
+struct WhArgs {
+    int n, head;        // bodies, head size (head_end + 1)
+    double G, dt;
+    double *pos, *vel, *acc;  // heliocentric state and last acceleration (3n)
+    const double *m;
+    double *jpos, *jvel;      // head Jacobi state (3 * head)
+    double *eta, *gm;         // head interior masses and Kepler parameters
+    double *ir3h, *ir3j;      // head inverse cubes
+    WhShared *sh;
+};
+
+// x^3 rounded once: x*x with its exact error (fma), times x (Dekker-style
+// error-free products), so the value matches a correctly rounded pow(x, 3).
+__device__ __forceinline__ double cube_cr(double x)
+{
+    double p = x * x;
+    double e = fma(x, x, -p);
+    double q = p * x;
+    double f = fma(p, x, -q);
+    return q + fma(e, x, f);
+}
+
+__device__ __forceinline__ double norm3(double a, double b, double c)
+{
+    double s = 0.0;
+    s += a * a;
+    s += b * b;
+    s += c * c;
+    return sqrt(s);
+}
+
+// src/integrator_wisdom_holman.c:30-47
+__device__ __forceinline__ void stumpff(double psi, double &c2, double &c3)
+{
+    if (psi > 1.e-10) {
+        double sp = sqrt(psi), s, c;
+        sincos(sp, &s, &c);
+        c2 = (1.0 - c) / psi;
+        c3 = (sp - s) / sqrt(cube_cr(psi));
+    } else if (psi < -1.e-6) {
+        double sp = sqrt(-psi);
+        c2 = (1 - cosh(sp)) / psi;
+        c3 = (sinh(sp) - sp) / sqrt(-cube_cr(psi));
+    } else {
+        c2 = 0.5;
+        c3 = 1.0 / 6.0;
+    }
+}
+
+// src/integrator_wisdom_holman.c:66-147 on one body's Jacobi state.
+// Returns 1 when Newton did not converge within the iteration cap.
+__device__ int kepler_drift(double r0v[3], double v0v[3], double gm, double dt)
+{
+    double r0 = norm3(r0v[0], r0v[1], r0v[2]);
+    double v0 = norm3(v0v[0], v0v[1], v0v[2]);
+    double sqrtgm = sqrt(gm);
+    double xi = 0.5 * v0 * v0 - gm / r0;
+    double sma = -gm / (2 * xi);
+    double alpha = 1.0 / sma;
+    double rv = r0v[0] * v0v[0] + r0v[1] * v0v[1] + r0v[2] * v0v[2];
+    double chi0;
+    if (alpha > TOL_ENERGY) {
+        chi0 = sqrtgm * dt * alpha;
+    } else if (alpha < TOL_ENERGY) {
+        double sg = (double)((dt > 0) - (dt < 0));
+        chi0 = sg * (sqrt(-sma) * log(-2.0 * gm * alpha * dt / (rv + sqrt(-gm * sma) * (1.0 - r0 * alpha))));
+    } else {
+        double c0 = r0v[1] * v0v[2] - r0v[2] * v0v[1];
+        double c1 = r0v[2] * v0v[0] - r0v[0] * v0v[2];
+        double c2_ = r0v[0] * v0v[1] - r0v[1] * v0v[0];
+        double cn = sqrt(c0 * c0 + c1 * c1 + c2_ * c2_);
+        double p = cn * cn / gm;
+        double s = 0.5 * atan(1.0 / (3.0 * sqrt(gm / cube_cr(p)) * dt));
+        double w = atan(pow(tan(s), 1.0 / 3.0));
+        chi0 = sqrt(p) * 2 / tan(2 * w);
+    }
+    double chi = 0.0, r = 0.0, c2 = 0.0, c3 = 0.0, psi = 0.0;
+    const double rvs = rv / sqrtgm;
+    for (int it = 0; it < KEPLER_MAX_IT; it++) {
+        psi = chi0 * chi0 * alpha;
+        stumpff(psi, c2, c3);
+        r = chi0 * chi0 * c2 + rvs * chi0 * (1.0 - psi * c3) + r0 * (1 - psi * c2);
+        chi = chi0 + (sqrtgm * dt - cube_cr(chi0) * c3 - rvs * (chi0 * chi0) * c2 - r0 * chi0 * (1.0 - psi * c3)) / r;
+        if (fabs(chi - chi0) < KEPLER_TOL) break;
+        chi0 = chi;
+    }
+    int failed = fabs(chi - chi0) > KEPLER_TOL;
+    double f = 1.0 - chi * chi / r0 * c2;
+    double g = dt - cube_cr(chi) / sqrtgm * c3;
+    double dg = 1.0 - chi * chi / r * c2;
+    double df = sqrtgm / (r * r0) * chi * (psi * c3 - 1.0);
+    double nr[3], nv[3];
+    for (int c = 0; c < 3; c++) {
+        nr[c] = f * r0v[c] + g * v0v[c];
+        nv[c] = df * r0v[c] + dg * v0v[c];
+    }
+    for (int c = 0; c < 3; c++) {
+        r0v[c] = nr[c];
+        v0v[c] = nv[c];
+    }
+    return failed;
+}
+
+// One block.  init != 0: only Jacobi coordinates and accelerations (the
+// set-up at the start of integrator_wh, :524-525); otherwise a full step.
+__global__ void __launch_bounds__(256) wh_head_kernel(WhArgs a, int init)
+{
+    const int H = a.head, n = a.n;
+    const double dt = a.dt, half = dt / 2;
+    const double *m = a.m;
+    WhShared *sh = a.sh;
+    if (!init)
+        for (int i = 1 + threadIdx.x; i < H; i += blockDim.x)
+            for (int c = 0; c < 3; c++) a.vel[3 * i + c] += a.acc[3 * i + c] * half;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        // interior masses and Kepler parameters (:189-206, :224-229)
+        a.eta[0] = m[0];
+        for (int i = 1; i < H; i++) a.eta[i] = m[i] + a.eta[i - 1];
+        double eta0 = m[0];
+        for (int i = 1; i < H; i++) {
+            double eta = eta0 + m[i];
+            a.gm[i] = a.G * m[0] * eta / eta0;
+            eta0 = eta;
+        }
+        {
+            double eta = eta0 + 0.0;
+            sh->gm_tail = a.G * m[0] * eta / eta0;
+        }
+        // helio -> Jacobi for the head (:221-280)
+        double *jp = a.jpos, *jv = a.jvel;
+        for (int c = 0; c < 3; c++) {
+            jp[c] = 0.0;
+            jv[c] = 0.0;
+            jp[3 + c] = a.pos[3 + c];
+            jv[3 + c] = a.vel[3 + c];
+        }
+        double aR[3], aV[3], R[3], V[3];
+        for (int c = 0; c < 3; c++) {
+            aR[c] = m[1] * a.pos[3 + c];
+            aV[c] = m[1] * a.vel[3 + c];
+            R[c] = aR[c] / a.eta[1];
+            V[c] = aV[c] / a.eta[1];
+        }
+        for (int i = 2; i < H; i++) {
+            for (int c = 0; c < 3; c++) {
+                jp[3 * i + c] = a.pos[3 * i + c] - R[c];
+                jv[3 * i + c] = a.vel[3 * i + c] - V[c];
+            }
+            if (i < n - 1) {
+                for (int c = 0; c < 3; c++) {
+                    aR[c] += (m[i] * a.pos[3 * i + c]);
+                    aV[c] += (m[i] * a.vel[3 * i + c]);
+                    R[c] = aR[c] / a.eta[i];
+                    V[c] = aV[c] / a.eta[i];
+                }
+            }
+        }
+        for (int c = 0; c < 3; c++) {
+            sh->R[c] = R[c];
+            sh->V[c] = V[c];
+        }
+    }
+    __syncthreads();
+    if (!init) {
+        // drift the head bodies (:189-206), independent given Jacobi states
+        for (int i = 1 + threadIdx.x; i < H; i += blockDim.x) {
+            double r[3] = {a.jpos[3 * i], a.jpos[3 * i + 1], a.jpos[3 * i + 2]};
+            double v[3] = {a.jvel[3 * i], a.jvel[3 * i + 1], a.jvel[3 * i + 2]};
+            if (kepler_drift(r, v, a.gm[i], dt)) atomicAdd(&sh->kepler_failures, 1ull);
+            for (int c = 0; c < 3; c++) {
+                a.jpos[3 * i + c] = r[c];
+                a.jvel[3 * i + c] = v[c];
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            // Jacobi -> helio for the head (:295-347)
+            const double *jp = a.jpos, *jv = a.jvel;
+            for (int c = 0; c < 3; c++) {
+                a.pos[3 + c] = jp[3 + c];
+                a.vel[3 + c] = jv[3 + c];
+                a.pos[c] = 0.0;
+                a.vel[c] = 0.0;
+            }
+            double R[3], V[3];
+            for (int c = 0; c < 3; c++) {
+                R[c] = m[1] * jp[3 + c] / a.eta[1];
+                V[c] = m[1] * jv[3 + c] / a.eta[1];
+            }
+            for (int i = 2; i < H; i++) {
+                for (int c = 0; c < 3; c++) {
+                    a.pos[3 * i + c] = jp[3 * i + c] + R[c];
+                    a.vel[3 * i + c] = jv[3 * i + c] + V[c];
+                }
+                if (i < n - 1) {
+                    for (int c = 0; c < 3; c++) {
+                        R[c] += m[i] * jp[3 * i + c] / a.eta[i];
+                        V[c] += m[i] * jv[3 * i + c] / a.eta[i];
+                    }
+                }
+            }
+            for (int c = 0; c < 3; c++) {
+                sh->Rp[c] = R[c];
+                sh->Vp[c] = V[c];
+            }
+        }
+        __syncthreads();
+    }
+    // accelerations of the head (:364-451)
+    for (int i = threadIdx.x; i < H; i += blockDim.x) {
+        double h = 0.0, j = 0.0;
+        if (i >= 2) {
+            h = cube_cr(1.0 / norm3(a.pos[3 * i], a.pos[3 * i + 1], a.pos[3 * i + 2]));
+            j = cube_cr(1.0 / norm3(a.jpos[3 * i], a.jpos[3 * i + 1], a.jpos[3 * i + 2]));
+        }
+        a.ir3h[i] = h;
+        a.ir3j[i] = j;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double ind[3] = {0.0, 0.0, 0.0};
+        for (int i = 2; i < H; i++)
+            for (int c = 0; c < 3; c++) ind[c] -= a.G * m[i] * a.pos[3 * i + c] * a.ir3h[i];
+        double a2[3] = {0.0, 0.0, 0.0};
+        double etai = m[0];
+        for (int i = 2; i < H; i++) {
+            etai += m[i - 1];
+            for (int c = 0; c < 3; c++)
+                a2[c] = a2[c] + a.G * m[i] * m[0] * a.ir3j[i] / etai * a.jpos[3 * i + c];
+            for (int c = 0; c < 3; c++) a.acc[3 * i + c] = a2[c];  // temporarily: accel2[i]
+        }
+        for (int c = 0; c < 3; c++) {
+            sh->ind[c] = ind[c];
+            sh->a2[c] = a2[c];
+            a.acc[c] = 0.0;
+            a.acc[3 + c] = 0.0;
+        }
+    }
+    __syncthreads();
+    // per head body: a3 in the reference's order (pairs with i < j first,
+    // ascending, then pairs with k > j, ascending), then the sum
+    for (int j = threadIdx.x; j < H; j += blockDim.x) {
+        double a3[3] = {0.0, 0.0, 0.0};
+        if (j >= 1) {
+            for (int i = 1; i < j; i++) {
+                if (m[i] == 0.0) continue;
+                double d[3];
+                for (int c = 0; c < 3; c++) d[c] = a.pos[3 * j + c] - a.pos[3 * i + c];
+                double aux = 1.0 / cube_cr(norm3(d[0], d[1], d[2]));
+                for (int c = 0; c < 3; c++) a3[c] -= a.G * m[i] * aux * d[c];
+            }
+            for (int k = j + 1; k < H; k++) {
+                if (m[k] == 0.0) continue;
+                double d[3];
+                for (int c = 0; c < 3; c++) d[c] = a.pos[3 * k + c] - a.pos[3 * j + c];
+                double aux = 1.0 / cube_cr(norm3(d[0], d[1], d[2]));
+                for (int c = 0; c < 3; c++) a3[c] += a.G * m[k] * aux * d[c];
+            }
+        }
+        for (int c = 0; c < 3; c++) {
+            double ind = (j >= 1) ? sh->ind[c] : 0.0;
+            double cent = 0.0;
+            if (j >= 2)
+                cent = a.G * m[0] * (a.jpos[3 * j + c] * a.ir3j[j] - a.pos[3 * j + c] * a.ir3h[j]);
+            double acc2 = (j >= 2) ? a.acc[3 * j + c] : 0.0;
+            double tot = ind + cent + acc2 + a3[c];
+            a.acc[3 * j + c] = tot;
+        }
+    }
+    __syncthreads();
+    if (!init)
+        for (int i = 1 + threadIdx.x; i < H; i += blockDim.x)
+            for (int c = 0; c < 3; c++) a.vel[3 * i + c] += a.acc[3 * i + c] * half;
+}
+
+// One thread per tail body: the whole step (kick, Jacobi shift, drift, shift
+// back, acceleration, kick) with the head's published quantities.
+__global__ void __launch_bounds__(256) wh_tail_kernel(WhArgs a, int init)
+{
+    extern __shared__ double hs[];  // 4 doubles per massive head body: x y z G*m
+    __shared__ int n_src;
+    const int H = a.head;
+    if (threadIdx.x == 0) {
+        int q = 0;
+        for (int i = 1; i < H; i++) {
+            if (a.m[i] == 0.0) continue;
+            hs[4 * q] = a.pos[3 * i];
+            hs[4 * q + 1] = a.pos[3 * i + 1];
+            hs[4 * q + 2] = a.pos[3 * i + 2];
+            hs[4 * q + 3] = a.G * a.m[i];
+            q++;
+        }
+        n_src = q;
+    }
+    __syncthreads();
+    const long long i = (long long)H + (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    const WhShared *sh = a.sh;
+    const double half = a.dt / 2;
+    double p[3], v[3], jp[3], jv[3];
+    for (int c = 0; c < 3; c++) {
+        p[c] = a.pos[3 * i + c];
+        v[c] = a.vel[3 * i + c];
+        if (!init) v[c] += a.acc[3 * i + c] * half;
+        jp[c] = p[c] - sh->R[c];
+        jv[c] = v[c] - sh->V[c];
+    }
+    if (!init) {
+        if (kepler_drift(jp, jv, sh->gm_tail, a.dt)) atomicAdd(&a.sh->kepler_failures, 1ull);
+        for (int c = 0; c < 3; c++) {
+            p[c] = jp[c] + sh->Rp[c];
+            v[c] = jv[c] + sh->Vp[c];
+        }
+    }
+    double ir3h = cube_cr(1.0 / norm3(p[0], p[1], p[2]));
+    double ir3j = cube_cr(1.0 / norm3(jp[0], jp[1], jp[2]));
+    double a3[3] = {0.0, 0.0, 0.0};
+    for (int q = 0; q < n_src; q++) {
+        double d[3];
+        for (int c = 0; c < 3; c++) d[c] = p[c] - hs[4 * q + c];
+        double aux = 1.0 / cube_cr(norm3(d[0], d[1], d[2]));
+        for (int c = 0; c < 3; c++) a3[c] -= hs[4 * q + 3] * aux * d[c];
+    }
+    const double Gm0 = a.G * a.m[0];
+    for (int c = 0; c < 3; c++) {
+        double cent = Gm0 * (jp[c] * ir3j - p[c] * ir3h);
+        double acc = sh->ind[c] + cent + sh->a2[c] + a3[c];
+        a.acc[3 * i + c] = acc;
+        if (!init) v[c] += acc * half;
+        a.pos[3 * i + c] = p[c];
+        a.vel[3 * i + c] = v[c];
+    }
+}
+
+struct WhBuffers {
+    double *acc = nullptr, *scratch = nullptr;
+    size_t acc_n = 0;
+    WhShared *sh = nullptr;
+};
+static WhBuffers g_wh;
+
+void free_wh_buffers()
+{
+    if (g_wh.acc) cudaFree(g_wh.acc);
+    if (g_wh.scratch) cudaFree(g_wh.scratch);
+    if (g_wh.sh) cudaFree(g_wh.sh);
+    g_wh = WhBuffers();
+}
+
+static int wh_launch_step(const WhArgs &a, int init, int n_src, cudaStream_t st)
+{
+    wh_head_kernel<<<1, 256, 0, st>>>(a, init);
+    long long tail = (long long)a.n - a.head;
+    if (tail > 0) {
+        unsigned blocks = (unsigned)((tail + 255) / 256);
+        wh_tail_kernel<<<blocks, 256, 4 * sizeof(double) * (size_t)std::max(n_src, 1), st>>>(a, init);
+    }
+    return 0;
+}
+
+int wh_run(const SystemView &sys, double t, double t_end, double dt, double *t_out,
+           abie_counters *ctr, cudaStream_t st)
+{
+    const int n = sys.n;
+    if (n < 2) {
+        set_error(ABIE_ERR_ARGUMENT, "integrator_wh needs at least two bodies (N=%d)", n);
+        return ABIE_ERR_ARGUMENT;
+    }
+    int last = 1;
+    for (int i = 0; i < n; i++)
+        if (sys.h_m[i] != 0.0) last = std::max(last, i);
+    int H = last + 1;
+    if (H > WH_HEAD_MAX) {
+        set_error(ABIE_ERR_CAPACITY, "integrator_wh: %d bodies before the last massive one (max %d)",
+                  H, WH_HEAD_MAX);
+        return ABIE_ERR_CAPACITY;
+    }
+    int n_src = 0;
+    for (int i = 1; i < H; i++) n_src += (sys.h_m[i] != 0.0);
+    int rc;
+    if ((rc = reserve(&g_wh.acc, &g_wh.acc_n, 3 * (size_t)n))) return rc;
+    if (!g_wh.scratch) ABIE_CUDA(cudaMalloc(&g_wh.scratch, (size_t)WH_HEAD_MAX * 10 * sizeof(double)));
+    if (!g_wh.sh) ABIE_CUDA(cudaMalloc(&g_wh.sh, sizeof(WhShared)));
+    ABIE_CUDA(cudaMemsetAsync(g_wh.sh, 0, sizeof(WhShared), st));
+    WhArgs a;
+    a.n = n;
+    a.head = H;
+    a.G = sys.G;
+    a.dt = dt;
+    a.pos = sys.pos;
+    a.vel = sys.vel;
+    a.acc = g_wh.acc;
+    a.m = sys.m;
+    double *s = g_wh.scratch;
+    a.jpos = s;
+    a.jvel = s + 3 * WH_HEAD_MAX;
+    a.eta = s + 6 * WH_HEAD_MAX;
+    a.gm = s + 7 * WH_HEAD_MAX;
+    a.ir3h = s + 8 * WH_HEAD_MAX;
+    a.ir3j = s + 9 * WH_HEAD_MAX;
+    a.sh = g_wh.sh;
+
+    long long steps = 0;
+    double tt = t;
+    while (tt < t_end) {  // :528-535, the same accumulation of t
+        tt += dt;
+        steps++;
+    }
+    size_t smem = 4 * sizeof(double) * (size_t)std::max(n_src, 1);
+    if (smem > 48 * 1024)
+        ABIE_CUDA(cudaFuncSetAttribute(wh_tail_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem));
+    rc = wh_launch_step(a, 1, n_src, st);
+    ABIE_CUDA(cudaGetLastError());
+    if (steps > 0) {
+        const int CH = 32;
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        long long full = steps / CH;
+        if (full > 0) {
+            ABIE_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+            for (int k = 0; k < CH; k++) wh_launch_step(a, 0, n_src, st);
+            ABIE_CUDA(cudaStreamEndCapture(st, &graph));
+            ABIE_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+            for (long long k = 0; k < full; k++) ABIE_CUDA(cudaGraphLaunch(exec, st));
+        }
+        for (long long k = full * CH; k < steps; k++) wh_launch_step(a, 0, n_src, st);
+        ABIE_CUDA(cudaGetLastError());
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+    }
+    WhShared h;
+    ABIE_CUDA(cudaMemcpyAsync(&h, g_wh.sh, sizeof h, cudaMemcpyDeviceToHost, st));
+    ABIE_CUDA(cudaStreamSynchronize(st));
+    if (ctr) {
+        ctr->kepler_failures += (long long)h.kepler_failures;
+        ctr->wh_steps += steps;
+    }
+    *t_out = tt;
+    return 0;
+}
+
+}  // namespace abie
+
+using namespace abie;
+
+extern "C" {
+
+int integrator_wh(double t, double t_end, double dt)
+{
+    Sim &s = g_sim;
+    if (!s.inited) {
+        set_error(ABIE_ERR_NOT_INITIALIZED, "integrator_wh before initialize_code");
+        return ABIE_ERR_NOT_INITIALIZED;
+    }
+    SystemView v{s.pos, s.vel, s.m, s.r, nullptr, s.h_m.data(), s.h_r.data(), (int)s.n, s.G};
+    double t_out = t;
+    int rc = wh_run(v, t, t_end, dt, &t_out, &s.ctr, s.st);
+    if (rc == 0 && t_out != t) s.t = t_out;
+    return rc;
+}
+
+void integrator_wisdom_holman(double *pos, double *vel, double *m_vec, double *r_vec, size_t N,
+                              double G, double t, double t_end, double dt)
+{
+    if (ensure_device(-1)) return;
+    Sim &s = g_sim;
+    N &= 0xffffffffull;
+    double *dp = nullptr, *dv = nullptr, *dm = nullptr;
+    size_t cp = 0, cv = 0, cm = 0;
+    if (reserve(&dp, &cp, 3 * N) || reserve(&dv, &cv, 3 * N) || reserve(&dm, &cm, N)) return;
+    cudaMemcpy(dp, pos, 3 * N * 8, cudaMemcpyHostToDevice);
+    cudaMemcpy(dv, vel, 3 * N * 8, cudaMemcpyHostToDevice);
+    cudaMemcpy(dm, m_vec, N * 8, cudaMemcpyHostToDevice);
+    SystemView v{dp, dv, dm, nullptr, nullptr, m_vec, r_vec, (int)N, G};
+    double t_out = t;
+    if (wh_run(v, t, t_end, dt, &t_out, &s.ctr, s.st) == 0) {
+        cudaMemcpy(pos, dp, 3 * N * 8, cudaMemcpyDeviceToHost);
+        cudaMemcpy(vel, dv, 3 * N * 8, cudaMemcpyDeviceToHost);
+        if (t_out != t) s.t = t_out;
+    }
+    cudaFree(dp);
+    cudaFree(dv);
+    cudaFree(dm);
+}
+
+}  // extern "C"

@@ -56,8 +56,11 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--mode", default="fp64", choices=["fp64", "exact", "mixed", "naive"])
     ap.add_argument("--n", type=int, default=16384, help="planetesimals (plus one star)")
-    ap.add_argument("--ensemble-systems", type=int, default=0)
+    ap.add_argument("--ensemble-systems", type=int, default=4096)
     ap.add_argument("--ensemble-years", type=float, default=1.0)
+    ap.add_argument("--wh-steps", type=int, default=20)
+    ap.add_argument("--gr-years", type=float, default=1.0)
+    ap.add_argument("--no-extras", action="store_true", help="only the headline force line")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
 
@@ -293,8 +296,13 @@ def run_ours(args):
             roof["traffic"] = json.load(fh).get("force_%s_%d" % (args.mode, m.size))
 
     extra = {}
-    if args.ensemble_systems > 0:
-        extra["ensemble"] = run_ensemble(lib, args)
+    if not args.no_extras and rank == 0:
+        if args.ensemble_systems > 0:
+            extra["ensemble"] = run_ensemble(lib, args)
+        if args.wh_steps > 0:
+            extra["wh"] = run_wh(lib, args)
+        if args.gr_years > 0:
+            extra["radau_1009"] = run_radau_single(lib, args)
 
     if rank == 0:
         cpu = None
@@ -333,14 +341,84 @@ def run_ours(args):
     return 0
 
 
+def _energy_errors(P0, V0, P1, V1, M, offs):
+    from oracle import Oracle
+    O = Oracle()
+    worst = 0.0
+    for s in range(offs.size - 1):
+        a, b = offs[s], offs[s + 1]
+        e0 = O.energy(P0[3 * a:3 * b], V0[3 * a:3 * b], M[a:b], G)
+        e1 = O.energy(P1[3 * a:3 * b], V1[3 * a:3 * b], M[a:b], G)
+        worst = max(worst, abs((e1 - e0) / e0))
+    return worst
+
+
 def run_ensemble(lib, args):
+    """Radau15 over independent systems (4,096 systems of 4..13 bodies:
+    a 0.5..1.5 MSun star and 3..12 planets) for a bounded slice of time."""
     P, V, M, offs = ics.ensemble(n_systems=args.ensemble_systems)
-    out = {}
-    for label, learned in (("plain", False),):
-        res = lib.gr_ensemble(P, V, M, offs, G, 0.0, args.ensemble_years, learned=learned)
+    out = {"systems": int(offs.size - 1), "bodies": int(M.size), "years": args.ensemble_years}
+    base = None
+    for label, mode in (("fp64", "fp64"), ("plain_fp64", "exact")):
+        old = lib.set_force_mode(mode)
+        lib.reset_counters()
+        res = lib.gr_ensemble(P, V, M, offs, G, 0.0, args.ensemble_years)
+        c = lib.counters()
+        lib.set_force_mode(old)
         steps = int(res["steps"].sum())
-        out[label] = {"system_steps": steps, "seconds": res["seconds"],
-                      "system_steps_per_s": steps / res["seconds"] if res["seconds"] else None}
+        rate = steps / res["seconds"] if res["seconds"] else None
+        out[label] = {"system_steps": steps, "seconds": res["seconds"], "system_steps_per_s": rate,
+                      "corrector_iterations_per_attempt": c["iterations"] / max(c["attempts"], 1),
+                      "max_abs_dE_over_E": _energy_errors(P, V, res["pos"], res["vel"], M, offs),
+                      "failed_systems": int((res["status"] != 0).sum())}
+        if label == "fp64":
+            base = rate
+    if base and out["plain_fp64"]["system_steps_per_s"]:
+        out["speedup_fp64_vs_plain"] = base / out["plain_fp64"]["system_steps_per_s"]
+    out["note"] = ("plain_fp64 = the reference's FP64 operations (divisions, sqrt) in the same "
+                   "batched kernel; fp64 = reassociated FP64 pair terms and predictor")
+    return out
+
+
+def run_wh(lib, args):
+    """Wisdom-Holman, 1 MSun star + 5 planets + 1,048,576 test particles, dt = 0.01 yr."""
+    import time as _t
+    p, v, m, r = ics.test_particle_swarm()
+    p, v = ics.to_heliocentric(p, v)
+    n = m.size
+    lib.initialize_code(G, 0.0, max(n, 1 << 21), MAX_CE_EVENTS=3, MAX_COLLISION_EVENTS=2, deviceID=0)
+    lib.set_state(p, v, m, r, n, G, 0.0)
+    lib.integrator_wh(0.0, 0.02, 0.01)  # warm-up (graph capture, first launches)
+    lib.set_state(p, v, m, r, n, G, 0.0)
+    lib.reset_counters()
+    t0 = _t.perf_counter()
+    lib.integrator_wh(0.0, args.wh_steps * 0.01 - 1e-9, 0.01)
+    dt = _t.perf_counter() - t0
+    c = lib.counters()
+    steps = c["wh_steps"]
+    return {"bodies": int(n), "steps": int(steps), "seconds": dt, "steps_per_s": steps / dt,
+            "kepler_solves_per_s": steps * (n - 1) / dt, "kepler_failures": c["kepler_failures"],
+            "timing": "wall clock around integrator_wh (device-resident state)"}
+
+
+def run_radau_single(lib, args):
+    """Radau15 on the 1,009-body system (1 star, 8 planets, 1,000 test particles)."""
+    import time as _t
+    p, v, m, r = ics.planetary_system()
+    lib.initialize_code(G, 0.0, 1 << 21, MAX_CE_EVENTS=3, MAX_COLLISION_EVENTS=2, deviceID=0)
+    out = {"bodies": int(m.size), "years": args.gr_years}
+    for mode in ("fp64", "exact"):
+        old = lib.set_force_mode(mode)
+        lib.set_state(p, v, m, r, m.size, G, 0.0)
+        lib.reset_counters()
+        t0 = _t.perf_counter()
+        lib.integrator_gr(0.0, args.gr_years, 1.0)
+        dt = _t.perf_counter() - t0
+        c = lib.counters()
+        lib.set_force_mode(old)
+        out[mode] = {"seconds": dt, "accepts": c["accepts"], "attempts": c["attempts"],
+                     "ms_per_attempt": 1e3 * dt / max(c["attempts"], 1),
+                     "force_calls": c["force_calls"]}
     return out
 
 

@@ -64,3 +64,12 @@ def rel_err_per_body(a, b):
     out[ok] = num[ok] / den[ok]
     out[~ok] = num[~ok]
     return out.max() if out.size else 0.0
+
+
+@pytest.fixture(scope="session")
+def sim(clib):
+    """The stateful library, initialized once per process as the reference
+    requires: capacity 2^21 bodies, 3 close-encounter and 2 collision slots."""
+    clib.initialize_code(4 * np.pi ** 2, 0.0, 1 << 21, MAX_CE_EVENTS=3, MAX_COLLISION_EVENTS=2,
+                         close_encounter_distance=0.0, deviceID=0)
+    return clib

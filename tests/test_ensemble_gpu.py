@@ -1,0 +1,92 @@
+"""Batched Radau15 ensemble: each system is integrated as integrator_gr would
+integrate it alone.  Compared at a common time (see test_radau_gpu.py) to
+the reference's golden runs and to the oracle; energy conservation over the
+batch; a system with a non-finite state is reported without disturbing the
+others."""
+import numpy as np
+import pytest
+
+from abie_gb300 import ics
+from conftest import rel_err_per_body
+from test_radau_gpu import TIME_TOL, TOL, at_time
+
+pytestmark = pytest.mark.gpu
+G = ics.G_SOLAR
+
+
+def _pack(systems):
+    P = np.concatenate([s[0] for s in systems])
+    V = np.concatenate([s[1] for s in systems])
+    M = np.concatenate([s[2] for s in systems])
+    offs = np.concatenate([[0], np.cumsum([s[2].size for s in systems])]).astype(np.int64)
+    return P, V, M, offs
+
+
+def _sl(offs, s):
+    return slice(3 * offs[s], 3 * offs[s + 1]), slice(offs[s], offs[s + 1])
+
+
+@pytest.mark.parametrize("mode", ["exact", "fp64"])
+def test_golden_systems(clib, oracle, golden, mode):
+    cases = ["gr_ens0", "gr_ens1", "gr_ens2"]
+    systems = [(golden[c + "_in_pos"], golden[c + "_in_vel"], golden[c + "_m"]) for c in cases]
+    P, V, M, offs = _pack(systems)
+    old = clib.set_force_mode(mode)
+    try:
+        out = clib.gr_ensemble(P, V, M, offs, G, 0.0, 20.0)
+    finally:
+        clib.set_force_mode(old)
+    assert (out["status"] == 0).all()
+    for s, c in enumerate(cases):
+        sv, sm = _sl(offs, s)
+        t_ref = golden[c + "_t"][0]
+        assert abs(out["t"][s] - t_ref) <= TIME_TOL * t_ref
+        p, v = at_time(out["pos"][sv], out["vel"][sv], M[sm], out["t"][s], t_ref, oracle)
+        assert rel_err_per_body(p, golden[c + "_pos"]) <= TOL
+        assert rel_err_per_body(v, golden[c + "_vel"]) <= TOL
+
+
+def test_random_batch_vs_oracle(clib, oracle):
+    P, V, M, offs = ics.ensemble(n_systems=48, seed0=500)
+    out = clib.gr_ensemble(P, V, M, offs, G, 0.0, 0.5)
+    assert (out["status"] == 0).all()
+    for s in range(48):
+        sv, sm = _sl(offs, s)
+        ref = oracle.radau15(P[sv], V[sv], M[sm], np.zeros(M[sm].size), G, 0.0, 0.5)
+        assert abs(out["t"][s] - ref["t"]) <= TIME_TOL * ref["t"]
+        assert out["steps"][s] > 0
+        p, v = at_time(out["pos"][sv], out["vel"][sv], M[sm], out["t"][s], ref["t"], oracle)
+        assert rel_err_per_body(p, ref["pos"]) <= TOL
+        assert rel_err_per_body(v, ref["vel"]) <= TOL
+
+
+def test_energy_conservation_batch(clib, oracle):
+    P, V, M, offs = ics.ensemble(n_systems=256, seed0=900)
+    out = clib.gr_ensemble(P, V, M, offs, G, 0.0, 2.0)
+    assert (out["status"] == 0).all()
+    worst = 0.0
+    for s in range(256):
+        sv, sm = _sl(offs, s)
+        e0 = oracle.energy(P[sv], V[sv], M[sm], G)
+        e1 = oracle.energy(out["pos"][sv], out["vel"][sv], M[sm], G)
+        worst = max(worst, abs((e1 - e0) / e0))
+    assert worst <= 1e-12, worst
+
+
+def test_nonfinite_system_is_isolated(clib):
+    P, V, M, offs = ics.ensemble(n_systems=6, seed0=77)
+    P = P.copy()
+    sv, _ = _sl(offs, 2)
+    P[sv.start + 3] = np.nan  # planet 1 of system 2
+    out = clib.gr_ensemble(P, V, M, offs, G, 0.0, 0.2)
+    assert out["status"][2] < 0
+    others = [s for s in range(6) if s != 2]
+    assert (out["status"][others] == 0).all()
+    assert all(out["t"][s] > 0.2 for s in others)
+
+
+def test_rejects_oversized_system(clib):
+    from abie_gb300.events import AbieError
+    P, V, M, offs = ics.ensemble(n_systems=1, seed0=1, n_planets=(25, 25))
+    with pytest.raises(AbieError):
+        clib.gr_ensemble(P, V, M, offs, G, 0.0, 0.1)

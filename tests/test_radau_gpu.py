@@ -1,0 +1,152 @@
+"""Gauss-Radau 15 on the device against the reference's golden trajectories
+and the oracle.
+
+The device sweep repeats the reference's arithmetic per component; the
+exact force form reproduces its accelerations bit for bit, but the step-size
+exponentiation uses the device pow(), whose last bit can differ from the
+host libm's.  The step size is h / err, so a last-bit change moves every
+later step and the time at which the integrator stops past t_end (by up to
+~1e-9 relative here).  Trajectories are therefore compared at a common
+time: the device's final state is carried to the reference's final time by
+a second-order Taylor step (|dt| ~ 1e-9, so the neglected term is ~1e-27),
+and then positions and velocities must agree to 1e-10 relative, max over
+bodies (measured: 1e-15 .. 6e-12 for the same 1-ulp perturbation injected
+into the oracle's pow).  Final times agree to 1e-8 relative; event flags,
+counts and body indices exactly."""
+import numpy as np
+import pytest
+
+from abie_gb300 import ics
+from abie_gb300.clibabie import CLibABIE
+from abie_gb300.events import CloseEncounterException, CollisionException
+from conftest import rel_err_per_body
+
+pytestmark = pytest.mark.gpu
+G = ics.G_SOLAR
+TOL = 1e-10
+TIME_TOL = 1e-8
+
+
+def at_time(pos, vel, m, t_from, t_to, oracle):
+    """Carry a state from t_from to t_to with a second-order Taylor step."""
+    dt = t_to - t_from
+    acc = oracle.force(pos, m, G)
+    return pos + vel * dt + 0.5 * acc * dt * dt, vel + acc * dt
+GR_CASES = ["gr_sys", "gr_tp", "gr_ens0", "gr_ens1", "gr_ens2"]
+
+
+def _direct(clib, pos, vel, m, r, t0, t1, mode):
+    """integrator_gauss_radau15 on caller arrays (src/integrator_gauss_radau15.c:287)."""
+    import ctypes as C
+    lib = clib.lib
+    old = clib.set_force_mode(mode)
+    p, v = np.array(pos, dtype=np.float64), np.array(vel, dtype=np.float64)
+    mm, rr = np.array(m, dtype=np.float64), np.array(r, dtype=np.float64)
+    lib.integrator_gauss_radau15.restype = C.c_ssize_t
+    rc = lib.integrator_gauss_radau15(C.c_void_p(p.ctypes.data), C.c_void_p(v.ctypes.data),
+                                      C.c_void_p(mm.ctypes.data), C.c_void_p(rr.ctypes.data),
+                                      C.c_size_t(mm.size), C.c_double(G), C.c_double(t0),
+                                      C.c_double(t1), C.c_double(1.0))
+    clib.set_force_mode(old)
+    return rc, p, v, lib.get_model_time()
+
+
+@pytest.mark.parametrize("mode", ["exact", "fp64"])
+@pytest.mark.parametrize("case", GR_CASES)
+def test_golden_trajectories(clib, oracle, golden, case, mode):
+    span = golden[case + "_span"]
+    m = golden[case + "_m"]
+    rc, p, v, t = _direct(clib, golden[case + "_in_pos"], golden[case + "_in_vel"],
+                          m, golden[case + "_r"], span[0], span[1], mode)
+    assert rc == 0
+    t_ref = golden[case + "_t"][0]
+    assert abs(t - t_ref) <= TIME_TOL * abs(t_ref)
+    p, v = at_time(p, v, m, t, t_ref, oracle)
+    assert rel_err_per_body(p, golden[case + "_pos"]) <= TOL
+    assert rel_err_per_body(v, golden[case + "_vel"]) <= TOL
+
+
+def test_energy_conservation_cfg1(clib, oracle):
+    """1,009-body workload over 5 yr: energy drift at the reference's level."""
+    p, v, m, r = ics.planetary_system()
+    rc, p1, v1, t = _direct(clib, p, v, m, r, 0.0, 5.0, "fp64")
+    assert rc == 0 and t > 5.0
+    e0 = oracle.energy(p, v, m, G)
+    e1 = oracle.energy(p1, v1, m, G)
+    assert abs((e1 - e0) / e0) < 1e-13
+
+
+def test_cfg1_against_oracle_short(clib, oracle):
+    p, v, m, r = ics.planetary_system()
+    ref = oracle.radau15(p, v, m, r, G, 0.0, 0.5)
+    rc, p1, v1, t = _direct(clib, p, v, m, r, 0.0, 0.5, "exact")
+    assert rc == 0
+    assert abs(t - ref["t"]) <= TIME_TOL * ref["t"]
+    p1, v1 = at_time(p1, v1, m, t, ref["t"], oracle)
+    assert rel_err_per_body(p1, ref["pos"]) <= TOL
+    assert rel_err_per_body(v1, ref["vel"]) <= TOL
+
+
+@pytest.mark.parametrize("case,exc_type", [("gr_ce", CloseEncounterException),
+                                           ("gr_coll", CollisionException)])
+def test_events_through_integrator_gr(sim, oracle, golden, case, exc_type):
+    """Close-encounter / collision flag, counts and ring buffers via the
+    stateful reference entry points (initialize_code, set_state, integrator_gr)."""
+    span = golden[case + "_span"]
+    old = sim.set_force_mode("exact")
+    sim.set_close_encounter_distance(span[2])
+    sim.reset_close_encounter_buffer()
+    sim.reset_collision_buffer()
+    m = golden[case + "_m"]
+    sim.set_state(golden[case + "_in_pos"], golden[case + "_in_vel"], m, golden[case + "_r"],
+                  m.size, G, 0.0)
+    with pytest.raises(exc_type) as exc:
+        sim.integrator_gr(span[0], span[1], 1.0)
+    if case == "gr_ce":
+        buf, gold = sim.get_close_encounter_data().reshape(-1), golden[case + "_buf_ce"]
+    else:
+        buf, gold = sim.get_collision_data().reshape(-1), golden[case + "_buf_coll"]
+    assert np.array_equal(buf[1::4], gold[1::4]) and np.array_equal(buf[2::4], gold[2::4])
+    assert np.allclose(buf, gold, rtol=TIME_TOL, atol=0)
+    assert exc.value.obj1 == int(gold[-3]) and exc.value.obj2 == int(gold[-2])
+    pos, vel = np.zeros(3 * m.size), np.zeros(3 * m.size)
+    assert sim.get_state(pos, vel, np.zeros(m.size), np.zeros(m.size)) == m.size
+    t, t_ref = sim.get_model_time(), golden[case + "_t"][0]
+    assert abs(t - t_ref) <= TIME_TOL * t_ref
+    pos, vel = at_time(pos, vel, m, t, t_ref, oracle)
+    assert rel_err_per_body(pos, golden[case + "_pos"]) <= TOL
+    sim.set_force_mode(old)
+    sim.set_close_encounter_distance(0.0)
+    sim.reset_close_encounter_buffer()
+    sim.reset_collision_buffer()
+
+
+def test_stateful_chunked_run_matches_oracle(sim, oracle):
+    """The Python driver's store_dt chunking (abie/integrator.py:181-188):
+    every chunk restarts Radau15 from the stored state."""
+    p, v, m, r = ics.planetary_system(seed=9, n_planets=5, n_tp=20)
+    sim.set_force_mode("exact")
+    sim.set_state(p, v, m, r, m.size, G, 0.0)
+    ref_p, ref_v, t_ref = p.copy(), v.copy(), 0.0
+    t, t_end, dt = 0.0, 3.0, 1.0
+    while t < t_end:
+        next_t = t + dt - ((t + dt) % dt)
+        sim.integrator_gr(t, next_t, 1.0)
+        t = sim.get_model_time()
+        out = oracle.radau15(ref_p, ref_v, m, r, G, t_ref, next_t)
+        ref_p, ref_v, t_ref = out["pos"], out["vel"], out["t"]
+    sim.set_force_mode("fp64")
+    pos, vel = np.zeros(p.size), np.zeros(p.size)
+    sim.get_state(pos, vel, np.zeros(m.size), np.zeros(m.size))
+    assert abs(t - t_ref) <= TIME_TOL * t_ref
+    pos, vel = at_time(pos, vel, m, t, t_ref, oracle)
+    assert rel_err_per_body(pos, ref_p) <= TOL and rel_err_per_body(vel, ref_v) <= TOL
+
+
+def test_counters_reported(clib):
+    clib.reset_counters()
+    p, v, m, r = ics.planetary_system(seed=3, n_planets=3, n_tp=0)
+    _direct(clib, p, v, m, r, 0.0, 1.0, "fp64")
+    c = clib.counters()
+    assert c["accepts"] > 0 and c["attempts"] == c["accepts"] + c["rejects"]
+    assert c["force_calls"] >= 7 * c["iterations"] + c["attempts"]
