@@ -408,3 +408,33 @@ int launch_energy(const double *pos, const double *vel, const double *m, int n, 
 
 }  // namespace abie
 
+namespace abie {
+
+// Fast FP64 force with scratch the caller provides (compact source list,
+// its body indices and count); launches the compaction and one force kernel
+// and allocates nothing.
+int launch_force_fp64_scratch(const double *pos, const double *m, int n, double G, Src *src,
+                              int *src_body, int *n_src, double *acc, cudaStream_t st)
+{
+    if (n <= 0) return 0;
+    compact_sources_kernel<<<1, 1024, 0, st>>>(pos, m, n, G, src, src_body, n_src);
+    ABIE_CUDA(cudaGetLastError());
+    ForceShape sh = force_shape_default(n, n);
+    int gpb = 256 / sh.lanes_per_sink;
+    int blocks = (n + gpb - 1) / gpb;
+    switch (sh.lanes_per_sink) {
+    case 1:
+        force_fp64_kernel<1><<<blocks, 256, 0, st>>>(pos, m, n, src, n_src, 1, acc, nullptr);
+        break;
+    case 8:
+        force_fp64_kernel<8><<<blocks, 256, 0, st>>>(pos, m, n, src, n_src, 1, acc, nullptr);
+        break;
+    default:
+        force_fp64_kernel<32><<<blocks, 256, 0, st>>>(pos, m, n, src, n_src, 1, acc, nullptr);
+        break;
+    }
+    ABIE_CUDA(cudaGetLastError());
+    return 0;
+}
+
+}  // namespace abie

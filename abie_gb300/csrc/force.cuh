@@ -29,6 +29,11 @@ int launch_compact_sources(const double *pos, const double *m, int n, double G, 
 int launch_force(int mode, const double *pos, const double *m, int n, double G,
                  ForceScratch &s, double *acc, cudaStream_t st);
 
+// Fast FP64 force with caller-provided scratch (src / src_body sized for n
+// entries, n_src one int); allocates nothing.  Uses one source chunk.
+int launch_force_fp64_scratch(const double *pos, const double *m, int n, double G, Src *src,
+                              int *src_body, int *n_src, double *acc, cudaStream_t st);
+
 // Launch shape of the fast FP64 kernel, exposed for the autotuner.
 struct ForceShape {
     int lanes_per_sink;   // 1, 8 or 32

@@ -156,6 +156,20 @@ double abie_last_ensemble_seconds(void);
  * picks a default length. */
 int abie_measure_fp64_peak(int iters, double *tflops);
 int abie_measure_fp32_peak(int iters, double *tflops);
+/* No counterpart in the reference.  The fast FP64 all-pairs force on device
+ * pointers, like abie_force_device with mode ABIE_FORCE_FP64, for callers
+ * that cannot allocate GPU memory (inside a stream capture that must hold
+ * no allocation, in a loop that may not wait on the allocator, or under a
+ * budget that allows only their own buffers).  Scratch is a fixed area
+ * compiled into the library, held by every GPU that loads it until exit:
+ * N above ABIE_NOALLOC_MAX_BODIES returns ABIE_ERR_CAPACITY.  Calls share
+ * that area, so calls that overlap on the GPU race; order them on one
+ * stream.  The first call on each device (with it current) looks up the
+ * area's device address; make it before any stream capture.  Runs on the
+ * given stream (NULL: the default stream) and returns once queued. */
+#define ABIE_NOALLOC_MAX_BODIES 65536
+int abie_force_device_noalloc(const double *d_pos, const double *d_m, size_t N,
+                              double G, double *d_acc, void *stream);
 /* Fixes the fast FP64 force kernel's launch shape: lanes_per_sink in
  * {1, 8, 32} and the number of source chunks; (0, 0) restores the
  * automatic choice.  For tests and the autotuner. */
