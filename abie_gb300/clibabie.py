@@ -163,8 +163,10 @@ class CLibABIE(object):
     def reset_counters(self):
         self.lib.abie_reset_counters()
 
-    def gr_ensemble(self, pos, vel, masses, offsets, G, t0, t_end, learned=False):
-        """Radau15 over a ragged batch of independent systems (in place)."""
+    def gr_ensemble(self, pos, vel, masses, offsets, G, t0, t_end, learned=False, collect=False):
+        """Radau15 over a ragged batch of independent systems.  learned: start
+        each step from the learned predictor's guess; collect: append
+        training samples to the predictor's store."""
         pos, vel, masses = _f64(pos).copy(), _f64(vel).copy(), _f64(masses)
         offsets = np.ascontiguousarray(offsets, dtype=np.int64)
         ns = offsets.size - 1
@@ -173,7 +175,8 @@ class CLibABIE(object):
         steps = np.zeros(ns, dtype=np.int64)
         rc = self.lib.abie_gr_ensemble(_vp(pos), _vp(vel), _vp(masses), _vp(offsets), _c.c_int(ns),
                                        _c.c_double(G), _c.c_double(t0), _c.c_double(t_end),
-                                       _vp(t_out), _vp(status), _vp(steps), _c.c_int(int(learned)))
+                                       _vp(t_out), _vp(status), _vp(steps),
+                                       _c.c_int(int(bool(learned)) | (2 if collect else 0)))
         self._check(rc, "abie_gr_ensemble")
         return {"pos": pos, "vel": vel, "t": t_out, "status": status, "steps": steps,
                 "seconds": self.lib.abie_last_ensemble_seconds()}
@@ -183,3 +186,59 @@ class CLibABIE(object):
         self._check(self.lib.abie_measure_fp64_peak(_c.c_int(0), _c.byref(f64)), "fp64 probe")
         self._check(self.lib.abie_measure_fp32_peak(_c.c_int(0), _c.byref(f32)), "fp32 probe")
         return {"fp64_tflops": f64.value, "fp32_tflops": f32.value}
+
+    # -- learned Radau15 predictor -----------------------------------------------
+    def _mlp_sig(self):
+        L = self.lib
+        L.abie_mlp_init.argtypes = [_c.c_int, _c.c_double]
+        L.abie_mlp_train.argtypes = [_c.c_int, _c.c_int, _c.c_double, _c.c_int, _c.c_void_p]
+        L.abie_mlp_load_samples.argtypes = [_c.c_void_p, _c.c_longlong]
+        L.abie_mlp_get_samples.argtypes = [_c.c_void_p, _c.c_longlong]
+        L.abie_mlp_sample_count.restype = _c.c_longlong
+        L.abie_mlp_set_params.argtypes = [_c.c_void_p, _c.c_int, _c.c_double]
+        L.abie_mlp_get_params.argtypes = [_c.c_void_p, _c.c_int]
+        L.abie_mlp_set_capacity.argtypes = [_c.c_longlong]
+        return L
+
+    def mlp_init(self, seed=0, tau=1.0):
+        self._check(self._mlp_sig().abie_mlp_init(int(seed), float(tau)), "abie_mlp_init")
+
+    def mlp_enable(self, on=True):
+        self.lib.abie_mlp_enable(_c.c_int(int(bool(on))))
+
+    def mlp_clear_samples(self):
+        self.lib.abie_mlp_clear_samples()
+
+    def mlp_set_capacity(self, samples):
+        self._mlp_sig().abie_mlp_set_capacity(int(samples))
+
+    def mlp_samples(self):
+        L = self._mlp_sig()
+        n = L.abie_mlp_sample_count()
+        out = np.zeros((max(n, 0), 64), dtype=np.float32)
+        if n > 0:
+            L.abie_mlp_get_samples(out.ctypes.data, n)
+        return out
+
+    def mlp_load_samples(self, samples):
+        samples = np.ascontiguousarray(samples, dtype=np.float32)
+        self._check(self._mlp_sig().abie_mlp_load_samples(samples.ctypes.data, samples.shape[0]),
+                    "abie_mlp_load_samples")
+
+    def mlp_train(self, steps, batch, lr, seed=0):
+        loss = _c.c_double(0)
+        self._check(self._mlp_sig().abie_mlp_train(int(steps), int(batch), float(lr), int(seed),
+                                                   _c.byref(loss)), "abie_mlp_train")
+        return loss.value
+
+    def mlp_params(self):
+        L = self._mlp_sig()
+        n = L.abie_mlp_n_params()
+        out = np.zeros(n, dtype=np.float32)
+        self._check(L.abie_mlp_get_params(out.ctypes.data, n), "abie_mlp_get_params")
+        return out
+
+    def mlp_set_params(self, params, tau):
+        params = np.ascontiguousarray(params, dtype=np.float32)
+        self._check(self._mlp_sig().abie_mlp_set_params(params.ctypes.data, params.size, float(tau)),
+                    "abie_mlp_set_params")

@@ -20,6 +20,7 @@
 
 #include "abi_state.cuh"
 #include "ensemble.cuh"
+#include "mlp.cuh"
 #include "radau_constants.h"
 
 namespace abie {
@@ -55,8 +56,63 @@ struct EnsArgs {
     int *queue;
     double G, t_end;
     unsigned long long budget_ns;    // a warp yields once this long after the launch began
-    const LearnedPredictor *mlp;     // null: plain predictor
+    const LearnedPredictor *mlp;     // device view of the learned predictor; null: plain predictor
+    float *samples;                  // training-sample store (null: no collection)
+    long long sample_cap;
+    unsigned long long *sample_count;
+    float tau;                       // output scale of the learned predictor's targets
 };
+
+// Per-warp shared buffers of the learned predictor (systems of at most 16 bodies).
+constexpr int LP_ROWS = 16;
+struct LearnSmem {
+    float row[LP_ROWS][MLP_OUT_PAD];                     // staging; later the network output
+    __nv_bfloat16 xh2[LP_ROWS][MLP_HID + 8];             // features (ld 40), then H2 (ld 136)
+    __nv_bfloat16 h1[LP_ROWS][MLP_HID + 8];
+    float pfeat[LP_ROWS][MLP_FEAT];                      // features of the pending sample
+    float pE[LP_ROWS][MLP_OUT];                          // plain guess / scale of the pending sample
+    float ps[LP_ROWS];                                   // scale of the pending sample
+    float scale[LP_ROWS];
+};
+
+// Network outputs for LP_ROWS rows of features (bf16, ld 40, in xh2) into
+// row[][] (fp32).  One warp; weights from global memory.
+__device__ __noinline__ void mlp_warp_forward(const LearnedPredictor *P, LearnSmem &L)
+{
+    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    const __nv_bfloat16 *W1 = P->W1, *W2 = P->W2, *W3 = P->W3;
+    const float *b1 = P->b1, *b2 = P->b2, *b3 = P->b3;
+    const __nv_bfloat16 *X = &L.xh2[0][0];
+    for (int n0 = 0; n0 < MLP_HID; n0 += 8) {
+        float c[4];
+        mma_tile(X, 40, W1, MLP_IN, 0, n0, MLP_IN, c);
+        for (int e = 0; e < 4; e++) {
+            int r = g + (e >> 1) * 8, n = n0 + 2 * t + (e & 1);
+            L.h1[r][n] = __float2bfloat16_rn(fmaxf(c[e] + b1[n], 0.0f));
+        }
+    }
+    __syncwarp();
+    __nv_bfloat16 *H2 = &L.xh2[0][0];  // features are dead now
+    for (int n0 = 0; n0 < MLP_HID; n0 += 8) {
+        float c[4];
+        mma_tile(&L.h1[0][0], MLP_HID + 8, W2, MLP_HID, 0, n0, MLP_HID, c);
+        __syncwarp();  // every lane has read its A fragments of this tile before H2 overwrites
+        for (int e = 0; e < 4; e++) {
+            int r = g + (e >> 1) * 8, n = n0 + 2 * t + (e & 1);
+            H2[r * (MLP_HID + 8) + n] = __float2bfloat16_rn(fmaxf(c[e] + b2[n], 0.0f));
+        }
+    }
+    __syncwarp();
+    for (int n0 = 0; n0 < MLP_OUT_PAD; n0 += 8) {
+        float c[4];
+        mma_tile(H2, MLP_HID + 8, W3, MLP_HID, 0, n0, MLP_HID, c);
+        for (int e = 0; e < 4; e++) {
+            int r = g + (e >> 1) * 8, n = n0 + 2 * t + (e & 1);
+            L.row[r][n] = c[e] + b3[n];
+        }
+    }
+    __syncwarp();
+}
 
 __device__ __forceinline__ unsigned long long ens_timer()
 {
@@ -200,12 +256,107 @@ __device__ __forceinline__ void warp_force(int n, const double (*sp)[4], double 
     __syncwarp();
 }
 
+// At an accepted step (not the last): emit the pending training sample
+// when this step was reached by a single attempt after the previous accept,
+// then replace refine_bs's plain guess E by E + s tau out (network output)
+// when a network is active, and remember this step's features and E.
+__device__ __forceinline__ void learned_refine(const EnsArgs &a, LearnSmem &L, Comp C[2], int n,
+                                               int lane, bool has0, bool has1, double q, double h,
+                                               double dtreq, const double *m, bool &pend_valid,
+                                               bool first_attempt)
+{
+    double h_next = (dtreq / h > 1.0 / FAC) ? h / FAC : ((dtreq < 1.e-12) ? h * FAC : dtreq);
+    if (h_next < H_MIN) h_next = H_MIN;
+    // converged b of this step, per body row (7 per component)
+#pragma unroll
+    for (int u = 0; u < 2; u++) {
+        if (!(u == 0 ? has0 : has1)) continue;
+        int c = lane + 32 * u, i = c / 3, d = c % 3;
+        for (int k = 0; k < 7; k++) L.row[i][7 * d + k] = (float)C[u].b[k];
+    }
+    __syncwarp();
+    if (lane < n) {
+        float sc = 0.0f;
+        for (int k = 0; k < MLP_OUT; k++) sc = fmaxf(sc, fabsf(L.row[lane][k]));
+        L.scale[lane] = (sc > 0.0f && isfinite(sc)) ? sc : 1.0f;
+    }
+    __syncwarp();
+    // the pending sample: features of the previous accept, target from this b
+    if (a.samples && pend_valid && first_attempt) {
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(a.sample_count, (unsigned long long)n);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base + (unsigned long long)n <= (unsigned long long)a.sample_cap) {
+            for (int e = lane; e < n * MLP_IN; e += 32) {
+                int i = e / MLP_IN, k = e % MLP_IN;
+                a.samples[(base + i) * MLP_SAMPLE + k] = k < MLP_FEAT ? L.pfeat[i][k] : 0.0f;
+            }
+            for (int e = lane; e < n * (MLP_OUT_PAD - MLP_OUT); e += 32) {
+                int i = e / (MLP_OUT_PAD - MLP_OUT), k = MLP_OUT + e % (MLP_OUT_PAD - MLP_OUT);
+                a.samples[(base + i) * MLP_SAMPLE + MLP_IN + k] = 0.0f;
+            }
+#pragma unroll
+            for (int u = 0; u < 2; u++) {
+                if (!(u == 0 ? has0 : has1)) continue;
+                int c = lane + 32 * u, i = c / 3, d = c % 3;
+                for (int k = 0; k < 7; k++) {
+                    float tgt = ((float)(C[u].b[k] / (double)L.ps[i]) - L.pE[i][7 * d + k]) / a.tau;
+                    a.samples[(base + i) * MLP_SAMPLE + MLP_IN + 7 * d + k] = tgt;
+                }
+            }
+        }
+    }
+    // features of this step (into xh2 as bf16, ld 40) and the plain guess E
+    __syncwarp();
+    float lq = fminf(fmaxf(log2f((float)q), -8.0f), 8.0f) * 0.25f;
+    float lh = fminf(fmaxf(log2f((float)(h_next / h)), -8.0f), 8.0f) * 0.25f;
+#pragma unroll
+    for (int u = 0; u < 2; u++) {
+        if (!(u == 0 ? has0 : has1)) continue;
+        int c = lane + 32 * u, i = c / 3, d = c % 3;
+        float sc = L.scale[i];
+        for (int k = 0; k < 7; k++) {
+            float f = L.row[i][7 * d + k] / sc;
+            L.xh2[i][7 * d + k] = __float2bfloat16_rn(f);
+            L.pfeat[i][7 * d + k] = f;
+        }
+        e_refine(C[u], q);
+        for (int k = 0; k < 7; k++) L.pE[i][7 * d + k] = (float)(C[u].b[k] / (double)sc);
+    }
+    for (int e = lane; e < LP_ROWS * 40; e += 32) {
+        int i = e / 40, k = e % 40;
+        if (i < n && k < MLP_OUT) continue;
+        float f = 0.0f;
+        if (i < n && k == 21) f = lq;
+        if (i < n && k == 22) f = lh;
+        if (i < n && k == 23) f = log10f(fmaxf((float)(m[i] / m[0]), 1e-20f)) * 0.1f;
+        L.xh2[i][k] = __float2bfloat16_rn(f);
+        if (i < n && k < MLP_FEAT) L.pfeat[i][k] = f;
+    }
+    if (lane < n) L.ps[lane] = L.scale[lane];
+    pend_valid = a.samples != nullptr;
+    __syncwarp();
+    if (a.mlp) {
+        mlp_warp_forward(a.mlp, L);
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            if (!(u == 0 ? has0 : has1)) continue;
+            int c = lane + 32 * u, i = c / 3, d = c % 3;
+            double f = (double)L.scale[i] * (double)a.tau;
+            for (int k = 0; k < 7; k++) C[u].b[k] += f * (double)L.row[i][7 * d + k];
+        }
+        __syncwarp();
+    }
+}
+
 template <int MODE>
 __global__ void __launch_bounds__(32 * WARPS) ensemble_kernel(EnsArgs a)
 {
     __shared__ double s_pos[WARPS][32][4];
     __shared__ double s_acc[WARPS][32][3];
+    extern __shared__ __align__(16) unsigned char ens_dyn[];  // learned path only
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    LearnSmem &LS = reinterpret_cast<LearnSmem *>(ens_dyn)[w];
     double(*sp)[4] = s_pos[w];
     double(*sa)[3] = s_acc[w];
     const unsigned long long deadline = ens_timer() + a.budget_ns;
@@ -307,6 +458,9 @@ __global__ void __launch_bounds__(32 * WARPS) ensemble_kernel(EnsArgs a)
         double t = S.t, h = S.h;
         int loop_count = S.loop_count;
         bool done = false;
+        // learned predictor: pending training sample, first attempt after an accept
+        const bool learn = (a.mlp != nullptr || a.samples != nullptr) && n <= LP_ROWS;
+        bool pend_valid = false, first_attempt = false;
         while (!done) {
             if (ens_timer() > deadline) break;
             int iters = 0;
@@ -388,16 +542,21 @@ __global__ void __launch_bounds__(32 * WARPS) ensemble_kernel(EnsArgs a)
                 C[1].dy0 = va1;
                 C[1].F1 = dd1;
                 C[1].b6p = C[1].b[6];
-                if (!stop) {
+                if (!stop && learn) {
+                    learned_refine(a, LS, C, n, lane, has0, has1, q, h, dtreq, m, pend_valid,
+                                   first_attempt);
+                } else if (!stop) {
                     e_refine(C[0], q);
                     e_refine(C[1], q);
                 }
+                first_attempt = true;
                 if (stop) {
                     done = true;
                     break;
                 }
             } else {
                 loop_count += 1;
+                first_attempt = false;
             }
             if (dtreq / h > 1.0 / FAC) h /= FAC;
             else if (dtreq < 1.e-12) h *= FAC;
@@ -432,17 +591,26 @@ __global__ void __launch_bounds__(32 * WARPS) ensemble_kernel(EnsArgs a)
 
 static double g_last_seconds = 0.0;
 
-static void launch_ensemble(int mode, int blocks, const EnsArgs &a, cudaStream_t st)
+static size_t learn_smem(const EnsArgs &a)
 {
+    return (a.mlp || a.samples) ? WARPS * sizeof(LearnSmem) : 0;
+}
+
+static int launch_ensemble(int mode, int blocks, const EnsArgs &a, cudaStream_t st)
+{
+    size_t dyn = learn_smem(a);
     if (mode == ABIE_FORCE_EXACT)
-        ensemble_kernel<ABIE_FORCE_EXACT><<<blocks, 32 * WARPS, 0, st>>>(a);
+        ensemble_kernel<ABIE_FORCE_EXACT><<<blocks, 32 * WARPS, dyn, st>>>(a);
     else
-        ensemble_kernel<ABIE_FORCE_FP64><<<blocks, 32 * WARPS, 0, st>>>(a);
+        ensemble_kernel<ABIE_FORCE_FP64><<<blocks, 32 * WARPS, dyn, st>>>(a);
+    ABIE_CUDA(cudaGetLastError());
+    return 0;
 }
 
 int ensemble_run(double *pos, double *vel, const double *m, const long long *offsets, int ns,
                  double G, double t0, double t_end, double *t_out, int *status, long long *steps,
-                 int mode, const LearnedPredictor *mlp, cudaStream_t st, EnsembleStats *stats)
+                 int mode, const LearnedPredictor *mlp, cudaStream_t st, EnsembleStats *stats,
+                 const EnsembleLearnIO *learn_io)
 {
     if (ns <= 0) return 0;
     long long total = offsets[ns];
@@ -484,7 +652,11 @@ int ensemble_run(double *pos, double *vel, const double *m, const long long *off
     int bps = 0;
     const void *fn = mode == ABIE_FORCE_EXACT ? (const void *)ensemble_kernel<ABIE_FORCE_EXACT>
                                               : (const void *)ensemble_kernel<ABIE_FORCE_FP64>;
-    ABIE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fn, 32 * WARPS, 0));
+    const bool learning = mlp || (learn_io && learn_io->samples);
+    const size_t dyn = learning ? WARPS * sizeof(LearnSmem) : 0;
+    ABIE_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)(WARPS * sizeof(LearnSmem))));
+    ABIE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fn, 32 * WARPS, dyn));
     bps = std::max(bps, 1);
     cudaEvent_t e0, e1;
     ABIE_CUDA(cudaEventCreate(&e0));
@@ -509,13 +681,17 @@ int ensemble_run(double *pos, double *vel, const double *m, const long long *off
         a.G = G;
         a.t_end = t_end;
         a.mlp = mlp;
+        a.samples = learn_io ? learn_io->samples : nullptr;
+        a.sample_cap = learn_io ? learn_io->cap : 0;
+        a.sample_count = learn_io ? learn_io->count : nullptr;
+        a.tau = learn_io ? learn_io->tau : 1.0f;
         a.budget_ns = 2000000000ull;  // each launch yields after about two seconds
         int blocks = std::min<long long>((long long)bps * g_sim.num_sms,
                                          (n_active + WARPS - 1) / WARPS);
         blocks = std::max(blocks, 1);
         ABIE_CUDA(cudaEventRecord(e0, st));
-        launch_ensemble(mode, blocks, a, st);
-        ABIE_CUDA(cudaGetLastError());
+        int lrc = launch_ensemble(mode, blocks, a, st);
+        if (lrc) return lrc;
         ABIE_CUDA(cudaEventRecord(e1, st));
         ABIE_CUDA(cudaEventSynchronize(e1));
         float ms = 0.f;
@@ -571,9 +747,19 @@ int abie_gr_ensemble(double *pos, double *vel, const double *m, const long long 
     int rc = ensure_device(-1);
     if (rc) return rc;
     const LearnedPredictor *mlp = (flags & 1) ? learned_predictor_current() : nullptr;
+    if ((flags & 1) && !mlp) {
+        set_error(ABIE_ERR_ARGUMENT, "abie_gr_ensemble: learned predictor requested, none enabled");
+        return ABIE_ERR_ARGUMENT;
+    }
+    EnsembleLearnIO io = {};
+    if (flags & 2) {
+        rc = mlp_collect_begin(&io);
+        if (rc) return rc;
+    }
     EnsembleStats st = {};
     rc = ensemble_run(pos, vel, m, offsets, n_systems, G, t0, t_end, t_out, status, steps,
-                      g_sim.force_mode, mlp, g_sim.st, &st);
+                      g_sim.force_mode, mlp, g_sim.st, &st, (flags & 2) ? &io : nullptr);
+    if (flags & 2) mlp_collect_end(&io);
     if (rc == 0) {
         g_sim.ctr.attempts += st.attempts;
         g_sim.ctr.iterations += st.iterations;
@@ -587,8 +773,3 @@ int abie_gr_ensemble(double *pos, double *vel, const double *m, const long long 
 double abie_last_ensemble_seconds(void) { return ensemble_last_seconds(); }
 
 }  // extern "C"
-
-namespace abie {
-// No learned predictor is loaded yet in this build.
-const LearnedPredictor *learned_predictor_current() { return nullptr; }
-}  // namespace abie

@@ -8,13 +8,24 @@ namespace abie {
 struct LearnedPredictor;
 const LearnedPredictor *learned_predictor_current();
 
+// Device store that the ensemble appends training samples to.
+struct EnsembleLearnIO {
+    float *samples;
+    long long cap;
+    unsigned long long *count;  // device counter
+    float tau;
+};
+int mlp_collect_begin(EnsembleLearnIO *io);
+void mlp_collect_end(EnsembleLearnIO *io);
+
 struct EnsembleStats {
     long long attempts, iterations, force_calls, steps, launches;
 };
 
 int ensemble_run(double *pos, double *vel, const double *m, const long long *offsets, int ns,
                  double G, double t0, double t_end, double *t_out, int *status, long long *steps,
-                 int mode, const LearnedPredictor *mlp, cudaStream_t st, EnsembleStats *stats);
+                 int mode, const LearnedPredictor *mlp, cudaStream_t st, EnsembleStats *stats,
+                 const EnsembleLearnIO *learn_io);
 double ensemble_last_seconds();
 
 }  // namespace abie

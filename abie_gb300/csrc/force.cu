@@ -45,6 +45,7 @@ void force_scratch_free(ForceScratch &s)
     if (s.src_body) cudaFree(s.src_body);
     if (s.n_src) cudaFree(s.n_src);
     if (s.partial) cudaFree(s.partial);
+    if (s.gm_max) cudaFree(s.gm_max);
     s = ForceScratch();
 }
 

@@ -12,6 +12,7 @@ struct ForceScratch {
     int *src_body = nullptr;
     int *n_src = nullptr;       // device scalar
     double *partial = nullptr;  // per (sink, source chunk) partial sums, 3 doubles each
+    unsigned long long *gm_max = nullptr;  // mixed form: largest G m (as ordered bits)
     size_t cap = 0;             // bodies
     size_t partial_cap = 0;     // doubles
 };

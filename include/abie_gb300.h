@@ -143,13 +143,35 @@ double abie_energy_host(const double *pos, const double *vel, const double *m,
  * t_end, exactly as integrator_gr would integrate it alone.  pos/vel are
  * updated in place, t_out[s] receives each system's final time, status[s]
  * its return code (0, or a negative error), steps[s] its accepted steps.
- * flags: bit 0 use the learned predictor when one is loaded. */
+ * flags: bit 0 learned predictor, bit 1 collect training samples (below). */
 int abie_gr_ensemble(double *pos, double *vel, const double *m,
                      const long long *offsets, int n_systems, double G,
                      double t0, double t_end, double *t_out, int *status,
                      long long *steps, int flags);
 /* Seconds of GPU time spent in the last abie_gr_ensemble call. */
 double abie_last_ensemble_seconds(void);
+
+/* Learned Radau15 predictor (BF16 MLP 24 -> 128 -> 128 -> 21; see
+ * abie_gb300/csrc/mlp.cuh for features and targets).  abie_gr_ensemble
+ * flags: bit 0 starts every step from the network's guess (requires
+ * abie_mlp_enable(1)), bit 1 appends training samples (64 floats each:
+ * 32 features, 32 targets) to the device sample store. */
+int abie_mlp_init(int seed, double tau);             /* fresh weights, zero output layer */
+int abie_mlp_set_params(const float *params, int n, double tau);
+int abie_mlp_get_params(float *params, int n);
+int abie_mlp_n_params(void);
+void abie_mlp_enable(int on);
+void abie_mlp_set_capacity(long long samples);      /* sample store size for collection */
+int abie_mlp_load_samples(const float *samples, long long rows);
+long long abie_mlp_sample_count(void);
+int abie_mlp_get_samples(float *out, long long rows);
+void abie_mlp_clear_samples(void);
+/* Network outputs (rows x 32) on the first rows stored samples. */
+int abie_mlp_forward(long long rows, float *Y);
+/* Loss and summed gradient over the first rows stored samples. */
+int abie_mlp_loss_grad(long long rows, float *grad, double *loss);
+/* Adam on random minibatches of the stored samples. */
+int abie_mlp_train(int steps, int batch, double lr, int seed, double *last_loss);
 
 /* Measured FMA throughput of the bound device in TFLOP/s (one FMA = 2
  * flops), the denominators of the compute-bound rooflines.  iters <= 0

@@ -8,7 +8,7 @@ import pytest
 
 from abie_gb300 import ics
 from conftest import rel_err_per_body
-from test_radau_gpu import TIME_TOL, TOL, at_time
+from test_radau_gpu import TIME_TOL, TIME_TOL_FAST, TOL, at_time
 
 pytestmark = pytest.mark.gpu
 G = ics.G_SOLAR
@@ -40,7 +40,7 @@ def test_golden_systems(clib, oracle, golden, mode):
     for s, c in enumerate(cases):
         sv, sm = _sl(offs, s)
         t_ref = golden[c + "_t"][0]
-        assert abs(out["t"][s] - t_ref) <= TIME_TOL * t_ref
+        assert abs(out["t"][s] - t_ref) <= (TIME_TOL if mode == "exact" else TIME_TOL_FAST) * t_ref
         p, v = at_time(out["pos"][sv], out["vel"][sv], M[sm], out["t"][s], t_ref, oracle)
         assert rel_err_per_body(p, golden[c + "_pos"]) <= TOL
         assert rel_err_per_body(v, golden[c + "_vel"]) <= TOL
@@ -53,7 +53,7 @@ def test_random_batch_vs_oracle(clib, oracle):
     for s in range(48):
         sv, sm = _sl(offs, s)
         ref = oracle.radau15(P[sv], V[sv], M[sm], np.zeros(M[sm].size), G, 0.0, 0.5)
-        assert abs(out["t"][s] - ref["t"]) <= TIME_TOL * ref["t"]
+        assert abs(out["t"][s] - ref["t"]) <= TIME_TOL_FAST * ref["t"]
         assert out["steps"][s] > 0
         p, v = at_time(out["pos"][sv], out["vel"][sv], M[sm], out["t"][s], ref["t"], oracle)
         assert rel_err_per_body(p, ref["pos"]) <= TOL

@@ -1,0 +1,63 @@
+"""Learned Radau15 predictor inside the batched ensemble.
+
+* An untrained network (zero output layer) reproduces the plain predictor
+  bit for bit (the guess is E + s tau * 0).
+* Samples collected from the ensemble's own runs train a network whose
+  held-out loss beats the plain predictor's, and which then lowers the
+  corrector iterations per step attempt on systems it has not seen, while
+  their final states agree with the plain run's at a common time to 1e-10
+  (the corrector's convergence test is unchanged)."""
+import numpy as np
+import pytest
+
+from abie_gb300 import ics
+from abie_gb300.learned import collect_samples, train_predictor
+from conftest import rel_err_per_body
+from test_radau_gpu import TIME_TOL_FAST, TOL, at_time
+
+pytestmark = pytest.mark.gpu
+G = ics.G_SOLAR
+
+
+def test_untrained_network_is_the_plain_predictor(clib):
+    P, V, M, offs = ics.ensemble(n_systems=64, seed0=3000)
+    plain = clib.gr_ensemble(P, V, M, offs, G, 0.0, 0.3)
+    clib.mlp_init(1, tau=1.0)
+    clib.mlp_enable(True)
+    try:
+        learned = clib.gr_ensemble(P, V, M, offs, G, 0.0, 0.3, learned=True)
+    finally:
+        clib.mlp_enable(False)
+    assert np.array_equal(plain["pos"], learned["pos"])
+    assert np.array_equal(plain["t"], learned["t"])
+
+
+def test_collect_train_and_fewer_iterations(clib, oracle):
+    P, V, M, offs = ics.ensemble(n_systems=1024, seed0=20000)
+    samples, _ = collect_samples(clib, P, V, M, offs, G, 1.0)
+    assert len(samples) > 10000 and np.isfinite(samples).all()
+    info = train_predictor(clib, samples, steps=1500, batch=2048, lr=1e-3)
+    print(info)
+    assert info["holdout_loss"] < 0.8 * info["holdout_loss_plain"]
+    # unseen systems
+    P2, V2, M2, offs2 = ics.ensemble(n_systems=512, seed0=40000)
+    clib.mlp_enable(False)
+    clib.reset_counters()
+    plain = clib.gr_ensemble(P2, V2, M2, offs2, G, 0.0, 0.5)
+    cp = clib.counters()
+    clib.mlp_enable(True)
+    clib.reset_counters()
+    learned = clib.gr_ensemble(P2, V2, M2, offs2, G, 0.0, 0.5, learned=True)
+    cl = clib.counters()
+    clib.mlp_enable(False)
+    it_plain = cp["iterations"] / cp["attempts"]
+    it_learned = cl["iterations"] / cl["attempts"]
+    print("iterations per attempt: plain %.3f learned %.3f" % (it_plain, it_learned))
+    assert it_learned < it_plain
+    for s in range(0, 512, 37):
+        a, b = offs2[s], offs2[s + 1]
+        tp, tl = plain["t"][s], learned["t"][s]
+        assert abs(tp - tl) <= TIME_TOL_FAST * tp
+        p, v = at_time(learned["pos"][3 * a:3 * b], learned["vel"][3 * a:3 * b], M2[a:b], tl, tp,
+                       oracle)
+        assert rel_err_per_body(p, plain["pos"][3 * a:3 * b]) <= TOL
