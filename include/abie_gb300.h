@@ -138,7 +138,7 @@ double abie_energy_host(const double *pos, const double *vel, const double *m,
                         size_t N, double G);
 
 /* Batched ensemble: n_systems independent systems packed ragged; system s
- * owns bodies offsets[s] .. offsets[s+1]-1 (at most 32 bodies each).  Each
+ * owns bodies offsets[s] .. offsets[s+1]-1 (at most 21 bodies each).  Each
  * system is integrated with Radau15 from t0 to the first accepted time past
  * t_end, exactly as integrator_gr would integrate it alone.  pos/vel are
  * updated in place, t_out[s] receives each system's final time, status[s]
