@@ -163,10 +163,12 @@ class CLibABIE(object):
     def reset_counters(self):
         self.lib.abie_reset_counters()
 
-    def gr_ensemble(self, pos, vel, masses, offsets, G, t0, t_end, learned=False, collect=False):
+    def gr_ensemble(self, pos, vel, masses, offsets, G, t0, t_end, learned=False, collect=False,
+                    consistent=False):
         """Radau15 over a ragged batch of independent systems.  learned: start
-        each step from the learned predictor's guess; collect: append
-        training samples to the predictor's store."""
+        each step from the learned predictor's guess (with consistent g);
+        consistent: the plain guess with g made consistent with it; collect:
+        append training samples to the predictor's store."""
         pos, vel, masses = _f64(pos).copy(), _f64(vel).copy(), _f64(masses)
         offsets = np.ascontiguousarray(offsets, dtype=np.int64)
         ns = offsets.size - 1
@@ -176,7 +178,8 @@ class CLibABIE(object):
         rc = self.lib.abie_gr_ensemble(_vp(pos), _vp(vel), _vp(masses), _vp(offsets), _c.c_int(ns),
                                        _c.c_double(G), _c.c_double(t0), _c.c_double(t_end),
                                        _vp(t_out), _vp(status), _vp(steps),
-                                       _c.c_int(int(bool(learned)) | (2 if collect else 0)))
+                                       _c.c_int(int(bool(learned)) | (2 if collect else 0) |
+                                                (4 if consistent else 0)))
         self._check(rc, "abie_gr_ensemble")
         return {"pos": pos, "vel": vel, "t": t_out, "status": status, "steps": steps,
                 "seconds": self.lib.abie_last_ensemble_seconds()}
@@ -190,18 +193,25 @@ class CLibABIE(object):
     # -- learned Radau15 predictor -----------------------------------------------
     def _mlp_sig(self):
         L = self.lib
-        L.abie_mlp_init.argtypes = [_c.c_int, _c.c_double]
+        L.abie_mlp_init.argtypes = [_c.c_int, _c.c_void_p]
         L.abie_mlp_train.argtypes = [_c.c_int, _c.c_int, _c.c_double, _c.c_int, _c.c_void_p]
         L.abie_mlp_load_samples.argtypes = [_c.c_void_p, _c.c_longlong]
         L.abie_mlp_get_samples.argtypes = [_c.c_void_p, _c.c_longlong]
         L.abie_mlp_sample_count.restype = _c.c_longlong
-        L.abie_mlp_set_params.argtypes = [_c.c_void_p, _c.c_int, _c.c_double]
+        L.abie_mlp_set_params.argtypes = [_c.c_void_p, _c.c_int, _c.c_void_p]
         L.abie_mlp_get_params.argtypes = [_c.c_void_p, _c.c_int]
         L.abie_mlp_set_capacity.argtypes = [_c.c_longlong]
         return L
 
-    def mlp_init(self, seed=0, tau=1.0):
-        self._check(self._mlp_sig().abie_mlp_init(int(seed), float(tau)), "abie_mlp_init")
+    @staticmethod
+    def _tau7(tau):
+        t = np.ones(7) if tau is None else np.broadcast_to(np.asarray(tau, dtype=np.float64), (7,))
+        return np.ascontiguousarray(t, dtype=np.float64)
+
+    def mlp_init(self, seed=0, tau=None):
+        """Fresh weights (zero output layer); tau: 7 output scales (or one)."""
+        t = self._tau7(tau)
+        self._check(self._mlp_sig().abie_mlp_init(int(seed), t.ctypes.data), "abie_mlp_init")
 
     def mlp_enable(self, on=True):
         self.lib.abie_mlp_enable(_c.c_int(int(bool(on))))
@@ -238,7 +248,8 @@ class CLibABIE(object):
         self._check(L.abie_mlp_get_params(out.ctypes.data, n), "abie_mlp_get_params")
         return out
 
-    def mlp_set_params(self, params, tau):
+    def mlp_set_params(self, params, tau=None):
         params = np.ascontiguousarray(params, dtype=np.float32)
-        self._check(self._mlp_sig().abie_mlp_set_params(params.ctypes.data, params.size, float(tau)),
-                    "abie_mlp_set_params")
+        t = self._tau7(tau)
+        self._check(self._mlp_sig().abie_mlp_set_params(params.ctypes.data, params.size,
+                                                        t.ctypes.data), "abie_mlp_set_params")

@@ -31,14 +31,19 @@ int cuda_fail(cudaError_t e, const char *what);
 
 // Device pair term for the fast FP64 form: G m / r^3 from r^2.
 //
-// A 24-bit seed y ~ r2^(-1/2) comes from the single-precision reciprocal
-// square root of r2 truncated to 20 mantissa bits; exponent and mantissa
-// are moved between the two formats with integer operations, so the FP64
-// pipe only sees the refinement.  With e = 1 - r2 y^2 (|e| < 2^-19),
-//     r2^(-3/2) = y^3 (1 - e)^(-3/2) = y^3 (1 + 3/2 e + 15/8 e^2 + O(e^3)),
-// the O(e^3) term is below 2^-55.  The 15/8 e^2 term needs only single
-// precision.  Cost: 6 FP64 operations.  r2 = 0 (a body and itself) gives a
-// finite value, so the caller's 0 * s contributes exactly zero.
+// Seed: r2 truncated to 23 mantissa bits as a float, its single-precision
+// reciprocal square root y truncated to a 21-bit significand m, so that
+// y = m 2^E.  Then y^2 = m^2 2^2E (m^2 < 2^42) is exact in a double and
+// y^3 = m^3 2^3E (m^3 < 2^63) exact in a 64-bit integer; both are
+// assembled into doubles by integer instructions (y^3 truncated to 53
+// bits), so the FP64 pipe does not compute them.  With e = 1 - r2 y^2
+// (|e| < 2^-18),
+//     r2^(-3/2) = y^3 (1 - e)^(-3/2) = y^3 (1 + 3/2 e + 15/8 e^2 + 35/16 e^3 + O(e^4)),
+// the quadratic and cubic terms taken in FP32 (they need only 2^-19
+// relative accuracy).  Cost: 4 FP64 instructions (e, G m y^3, the
+// correction factor, the product); at most ~4 ulp from the exact value.
+// r2 = 0 (a body and itself) gives a finite value, so the caller's 0 * w
+// contributes exactly zero.
 __device__ __forceinline__ int clamp_exp_f32(int hi_rebased)
 {
     // keep the single-precision exponent in [1, 254]
@@ -58,18 +63,46 @@ __device__ __forceinline__ float f64_to_f32_trunc(double v)
     return __int_as_float(clamp_exp_f32(hi - ((1023 - 127) << 20)) << 3);
 }
 
+__device__ __forceinline__ float f64_to_f32_trunc23(double v)
+{
+    // |v| truncated to 23 mantissa bits, as a float (sign dropped)
+    int hi = __double2hiint(v) & 0x7FFFFFFF;
+    unsigned lo = (unsigned)__double2loint(v);
+    return __uint_as_float(((unsigned)clamp_exp_f32(hi - ((1023 - 127) << 20)) << 3) | (lo >> 29));
+}
+
+__device__ __forceinline__ double f32_to_f64_signed(float f)
+{
+    // exact conversion of a normal (or zero) float, sign kept
+    unsigned b = __float_as_uint(f);
+    unsigned sgn = b & 0x80000000u;
+    b &= 0x7FFFFFFFu;
+    if (b == 0u) return 0.0;
+    return __hiloint2double((int)(((b >> 3) + ((1023 - 127) << 20)) | sgn), (int)(b << 29));
+}
+
 __device__ __forceinline__ double gm_inv_r3(double r2, double gm)
 {
-    float xf = f64_to_f32_trunc(r2);
-    float yf = rsqrtf(xf);
-    double y = f32_bits_to_f64(__float_as_int(yf));
-    double t = y * y;                       // exact: 24-bit squared
-    double e = fma(-r2, t, 1.0);
-    double c = (gm * y) * t;                // G m y^3
-    float ef = f64_to_f32_trunc(e);
-    float q = 1.875f * ef * ef;
-    // q underflowing to zero maps to 2^-127 here, far below an ulp of k
-    double k = fma(e, 1.5, f32_bits_to_f64(__float_as_int(q)));
+    const float yf = rsqrtf(f64_to_f32_trunc23(r2));
+    const unsigned yb = __float_as_uint(yf);
+    const unsigned long long m = (unsigned long long)(((yb & 0x7FFFFFu) | 0x800000u) >> 3);
+    const int E = (int)(yb >> 23) - 147;  // y = m 2^E
+    const unsigned long long m2 = m * m;  // [2^40, 2^42)
+    const int p2 = 40 + (int)(m2 >> 41);
+    const unsigned long long t_bits =
+        ((unsigned long long)(long long)(p2 + 2 * E + 1023) << 52) | ((m2 << (52 - p2)) & 0xFFFFFFFFFFFFFull);
+    const unsigned long long m3 = m2 * m;  // [2^60, 2^63)
+    const int p3 = 60 + (m3 >= (1ull << 61)) + (m3 >= (1ull << 62));
+    const unsigned long long y3_bits =
+        ((unsigned long long)(long long)(p3 + 3 * E + 1023) << 52) | ((m3 >> (p3 - 52)) & 0xFFFFFFFFFFFFFull);
+    const double t = __longlong_as_double((long long)t_bits);
+    const double y3 = __longlong_as_double((long long)y3_bits);
+    const double e = fma(-r2, t, 1.0);
+    const double c = gm * y3;
+    float ef = f64_to_f32_trunc23(e);
+    ef = (__double2hiint(e) < 0) ? -ef : ef;
+    const float q = ef * ef * fmaf(2.1875f, ef, 1.875f);
+    const double k = fma(e, 1.5, f32_to_f64_signed(q));
     return fma(c, k, c);
 }
 
@@ -89,7 +122,8 @@ __device__ __forceinline__ void pair_exact(double xj, double yj, double zj, cons
     az -= s.gm * dz / r3;
 }
 
-// Fast FP64 pair contribution (15 FP64 operations).
+// Fast FP64 pair contribution (13 FP64 operations: 3 differences, 3 for r^2,
+// 4 for G m r^-3, 3 accumulations).
 __device__ __forceinline__ void pair_fast(double xj, double yj, double zj, const Src &s,
                                           double &ax, double &ay, double &az)
 {

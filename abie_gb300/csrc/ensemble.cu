@@ -60,7 +60,8 @@ struct EnsArgs {
     float *samples;                  // training-sample store (null: no collection)
     long long sample_cap;
     unsigned long long *sample_count;
-    float tau;                       // output scale of the learned predictor's targets
+    float tau[7];                    // output scales of the learned predictor's targets
+    int consistent_g;                // set g = C^-1 b after the guess (learned or plain)
 };
 
 // Per-warp shared buffers of the learned predictor (systems of at most 16 bodies).
@@ -71,8 +72,8 @@ struct LearnSmem {
     __nv_bfloat16 h1[LP_ROWS][MLP_HID + 8];
     float pfeat[LP_ROWS][MLP_FEAT];                      // features of the pending sample
     float pE[LP_ROWS][MLP_OUT];                          // plain guess / scale of the pending sample
-    float ps[LP_ROWS];                                   // scale of the pending sample
-    float scale[LP_ROWS];
+    float ps[LP_ROWS][7];                                // per-order scales of the pending sample
+    float scale[LP_ROWS][7];                             // per-order scales of this step
 };
 
 // Network outputs for LP_ROWS rows of features (bf16, ld 40, in xh2) into
@@ -256,10 +257,27 @@ __device__ __forceinline__ void warp_force(int n, const double (*sp)[4], double 
     __syncwarp();
 }
 
+// g = C^-1 b for one component: back-substitution through the triangular
+// change of basis b_k = sum_{j>=k} cs[j][k] g_j, so that the corrector's
+// first sweep starts from the polynomial the guess describes.  (The
+// reference keeps the previous step's g, which the first sweep mixes into
+// every b it rebuilds, src/integrator_gauss_radau15.c:189-241.)
+__device__ __forceinline__ void consistent_g(Comp &c)
+{
+#pragma unroll
+    for (int k = 6; k >= 0; k--) {
+        double v = c.b[k];
+#pragma unroll
+        for (int j = k + 1; j < 7; j++) v -= e_cs[j][k] * c.g[j];
+        c.g[k] = v;
+    }
+}
+
 // At an accepted step (not the last): emit the pending training sample
 // when this step was reached by a single attempt after the previous accept,
-// then replace refine_bs's plain guess E by E + s tau out (network output)
-// when a network is active, and remember this step's features and E.
+// then replace refine_bs's plain guess E_k by E_k + s_k tau_k out_k (network
+// output) when a network is active, and remember this step's features and
+// E.  Scales s_k are per coefficient order: the largest |b_k| of the body.
 __device__ __forceinline__ void learned_refine(const EnsArgs &a, LearnSmem &L, Comp C[2], int n,
                                                int lane, bool has0, bool has1, double q, double h,
                                                double dtreq, const double *m, bool &pend_valid,
@@ -275,10 +293,10 @@ __device__ __forceinline__ void learned_refine(const EnsArgs &a, LearnSmem &L, C
         for (int k = 0; k < 7; k++) L.row[i][7 * d + k] = (float)C[u].b[k];
     }
     __syncwarp();
-    if (lane < n) {
-        float sc = 0.0f;
-        for (int k = 0; k < MLP_OUT; k++) sc = fmaxf(sc, fabsf(L.row[lane][k]));
-        L.scale[lane] = (sc > 0.0f && isfinite(sc)) ? sc : 1.0f;
+    for (int e = lane; e < n * 7; e += 32) {
+        int i = e / 7, k = e % 7;
+        float sc = fmaxf(fmaxf(fabsf(L.row[i][k]), fabsf(L.row[i][7 + k])), fabsf(L.row[i][14 + k]));
+        L.scale[i][k] = (sc > 0.0f && isfinite(sc)) ? sc : 1.0f;
     }
     __syncwarp();
     // the pending sample: features of the previous accept, target from this b
@@ -300,7 +318,7 @@ __device__ __forceinline__ void learned_refine(const EnsArgs &a, LearnSmem &L, C
                 if (!(u == 0 ? has0 : has1)) continue;
                 int c = lane + 32 * u, i = c / 3, d = c % 3;
                 for (int k = 0; k < 7; k++) {
-                    float tgt = ((float)(C[u].b[k] / (double)L.ps[i]) - L.pE[i][7 * d + k]) / a.tau;
+                    float tgt = ((float)(C[u].b[k] / (double)L.ps[i][k]) - L.pE[i][7 * d + k]) / a.tau[k];
                     a.samples[(base + i) * MLP_SAMPLE + MLP_IN + 7 * d + k] = tgt;
                 }
             }
@@ -314,26 +332,29 @@ __device__ __forceinline__ void learned_refine(const EnsArgs &a, LearnSmem &L, C
     for (int u = 0; u < 2; u++) {
         if (!(u == 0 ? has0 : has1)) continue;
         int c = lane + 32 * u, i = c / 3, d = c % 3;
-        float sc = L.scale[i];
         for (int k = 0; k < 7; k++) {
-            float f = L.row[i][7 * d + k] / sc;
+            float f = L.row[i][7 * d + k] / L.scale[i][k];
             L.xh2[i][7 * d + k] = __float2bfloat16_rn(f);
             L.pfeat[i][7 * d + k] = f;
         }
         e_refine(C[u], q);
-        for (int k = 0; k < 7; k++) L.pE[i][7 * d + k] = (float)(C[u].b[k] / (double)sc);
+        for (int k = 0; k < 7; k++) L.pE[i][7 * d + k] = (float)(C[u].b[k] / (double)L.scale[i][k]);
     }
     for (int e = lane; e < LP_ROWS * 40; e += 32) {
         int i = e / 40, k = e % 40;
         if (i < n && k < MLP_OUT) continue;
         float f = 0.0f;
-        if (i < n && k == 21) f = lq;
-        if (i < n && k == 22) f = lh;
-        if (i < n && k == 23) f = log10f(fmaxf((float)(m[i] / m[0]), 1e-20f)) * 0.1f;
+        if (i < n) {
+            if (k == 21) f = lq;
+            else if (k == 22) f = lh;
+            else if (k == 23) f = log10f(fmaxf((float)(m[i] / m[0]), 1e-20f)) * 0.1f;
+            else if (k >= 24 && k < 30)
+                f = fminf(fmaxf(log10f(L.scale[i][k - 23] / L.scale[i][0]), -30.0f), 30.0f) * 0.1f;
+        }
         L.xh2[i][k] = __float2bfloat16_rn(f);
         if (i < n && k < MLP_FEAT) L.pfeat[i][k] = f;
     }
-    if (lane < n) L.ps[lane] = L.scale[lane];
+    for (int e = lane; e < n * 7; e += 32) L.ps[e / 7][e % 7] = L.scale[e / 7][e % 7];
     pend_valid = a.samples != nullptr;
     __syncwarp();
     if (a.mlp) {
@@ -342,10 +363,14 @@ __device__ __forceinline__ void learned_refine(const EnsArgs &a, LearnSmem &L, C
         for (int u = 0; u < 2; u++) {
             if (!(u == 0 ? has0 : has1)) continue;
             int c = lane + 32 * u, i = c / 3, d = c % 3;
-            double f = (double)L.scale[i] * (double)a.tau;
-            for (int k = 0; k < 7; k++) C[u].b[k] += f * (double)L.row[i][7 * d + k];
+            for (int k = 0; k < 7; k++)
+                C[u].b[k] += (double)L.scale[i][k] * (double)a.tau[k] * (double)L.row[i][7 * d + k];
         }
         __syncwarp();
+    }
+    if (a.consistent_g) {
+        if (has0) consistent_g(C[0]);
+        if (has1) consistent_g(C[1]);
     }
 }
 
@@ -548,6 +573,10 @@ __global__ void __launch_bounds__(32 * WARPS) ensemble_kernel(EnsArgs a)
                 } else if (!stop) {
                     e_refine(C[0], q);
                     e_refine(C[1], q);
+                    if (a.consistent_g) {
+                        consistent_g(C[0]);
+                        consistent_g(C[1]);
+                    }
                 }
                 first_attempt = true;
                 if (stop) {
@@ -610,7 +639,7 @@ static int launch_ensemble(int mode, int blocks, const EnsArgs &a, cudaStream_t 
 int ensemble_run(double *pos, double *vel, const double *m, const long long *offsets, int ns,
                  double G, double t0, double t_end, double *t_out, int *status, long long *steps,
                  int mode, const LearnedPredictor *mlp, cudaStream_t st, EnsembleStats *stats,
-                 const EnsembleLearnIO *learn_io)
+                 const EnsembleLearnIO *learn_io, bool consistent, const float *mlp_tau)
 {
     if (ns <= 0) return 0;
     long long total = offsets[ns];
@@ -684,7 +713,8 @@ int ensemble_run(double *pos, double *vel, const double *m, const long long *off
         a.samples = learn_io ? learn_io->samples : nullptr;
         a.sample_cap = learn_io ? learn_io->cap : 0;
         a.sample_count = learn_io ? learn_io->count : nullptr;
-        a.tau = learn_io ? learn_io->tau : 1.0f;
+        for (int k = 0; k < 7; k++) a.tau[k] = learn_io ? learn_io->tau[k] : (mlp_tau ? mlp_tau[k] : 1.0f);
+        a.consistent_g = consistent ? 1 : 0;
         a.budget_ns = 2000000000ull;  // each launch yields after about two seconds
         int blocks = std::min<long long>((long long)bps * g_sim.num_sms,
                                          (n_active + WARPS - 1) / WARPS);
@@ -758,7 +788,8 @@ int abie_gr_ensemble(double *pos, double *vel, const double *m, const long long 
     }
     EnsembleStats st = {};
     rc = ensemble_run(pos, vel, m, offsets, n_systems, G, t0, t_end, t_out, status, steps,
-                      g_sim.force_mode, mlp, g_sim.st, &st, (flags & 2) ? &io : nullptr);
+                      g_sim.force_mode, mlp, g_sim.st, &st, (flags & 2) ? &io : nullptr,
+                      (flags & 1) || (flags & 4), mlp ? learned_predictor_tau() : nullptr);
     if (flags & 2) mlp_collect_end(&io);
     if (rc == 0) {
         g_sim.ctr.attempts += st.attempts;

@@ -13,7 +13,7 @@ struct EnsembleLearnIO {
     float *samples;
     long long cap;
     unsigned long long *count;  // device counter
-    float tau;
+    float tau[7];
 };
 int mlp_collect_begin(EnsembleLearnIO *io);
 void mlp_collect_end(EnsembleLearnIO *io);
@@ -25,7 +25,9 @@ struct EnsembleStats {
 int ensemble_run(double *pos, double *vel, const double *m, const long long *offsets, int ns,
                  double G, double t0, double t_end, double *t_out, int *status, long long *steps,
                  int mode, const LearnedPredictor *mlp, cudaStream_t st, EnsembleStats *stats,
-                 const EnsembleLearnIO *learn_io);
+                 const EnsembleLearnIO *learn_io, bool consistent_g, const float *mlp_tau);
+// Host copy of the output scales of the enabled learned predictor.
+const float *learned_predictor_tau();
 double ensemble_last_seconds();
 
 }  // namespace abie

@@ -6,7 +6,9 @@
 //   fp64  : the production FP64 form.  A group of 1, 8 or 32 lanes shares a
 //           sink and splits its sources; partial sums meet in a fixed
 //           butterfly of warp shuffles, so results are deterministic.  The
-//           pair term is gm_inv_r3() (15 FP64 operations per interaction).
+//           pair term is gm_inv_r3() (13 FP64 operations per interaction).
+//           Sinks are handed out to lane groups from an atomic counter, so
+//           the grid has no tail of idle SMs.
 //           Sources can also be split into chunks whose partial sums are
 //           added in chunk order by a second pass, to balance the grid.
 //   naive : one thread per sink over global memory with rsqrt, the
@@ -14,6 +16,8 @@
 //           sources with m == 0 and coincident pairs are skipped, sinks and
 //           sources with m < 0 are not.
 //   mixed : in mixed.cu.
+#include <algorithm>
+
 #include "force.cuh"
 #include "mixed.cuh"
 
@@ -35,6 +39,7 @@ int force_scratch_reserve(ForceScratch &s, size_t n)
     ABIE_CUDA(cudaMalloc(&s.src, cap * sizeof(Src)));
     ABIE_CUDA(cudaMalloc(&s.src_body, cap * sizeof(int)));
     ABIE_CUDA(cudaMalloc(&s.n_src, sizeof(int)));
+    ABIE_CUDA(cudaMalloc(&s.next, sizeof(unsigned int)));
     s.cap = cap;
     return 0;
 }
@@ -46,6 +51,7 @@ void force_scratch_free(ForceScratch &s)
     if (s.n_src) cudaFree(s.n_src);
     if (s.partial) cudaFree(s.partial);
     if (s.gm_max) cudaFree(s.gm_max);
+    if (s.next) cudaFree(s.next);
     s = ForceScratch();
 }
 
@@ -184,6 +190,54 @@ __global__ void __launch_bounds__(256) force_fp64_kernel(const double *__restric
     }
 }
 
+// Persistent form: a grid that fills the GPU once, lane groups take sinks
+// from an atomic counter (*next must be zero at launch).
+template <int JS>
+__global__ void __launch_bounds__(256) force_fp64_dyn_kernel(const double *__restrict__ pos,
+                                                             const double *__restrict__ m, int n,
+                                                             const Src *__restrict__ src,
+                                                             const int *__restrict__ n_src_p,
+                                                             double *__restrict__ acc,
+                                                             unsigned int *__restrict__ next)
+{
+    const int lane = threadIdx.x % JS;
+    const int gl = threadIdx.x / JS;  // group within the block
+    const int n_src = *n_src_p;
+    const unsigned mask = JS == 32 ? 0xffffffffu : (((1u << JS) - 1u) << ((threadIdx.x & 31) / JS * JS));
+    for (;;) {
+        int j = 0;
+        if (lane == 0) j = (int)atomicAdd(next, 1u);
+        j = __shfl_sync(mask, j, (threadIdx.x & 31) / JS * JS);
+        if (j >= n) break;
+        const double xj = pos[3 * j], yj = pos[3 * j + 1], zj = pos[3 * j + 2];
+        double ax = 0.0, ay = 0.0, az = 0.0;
+        int q = lane;
+#pragma unroll 1
+        for (; q + 3 * JS < n_src; q += 4 * JS) {
+            Src s0 = src[q], s1 = src[q + JS], s2 = src[q + 2 * JS], s3 = src[q + 3 * JS];
+            pair_fast(xj, yj, zj, s0, ax, ay, az);
+            pair_fast(xj, yj, zj, s1, ax, ay, az);
+            pair_fast(xj, yj, zj, s2, ax, ay, az);
+            pair_fast(xj, yj, zj, s3, ax, ay, az);
+        }
+        for (; q < n_src; q += JS) pair_fast(xj, yj, zj, src[q], ax, ay, az);
+        if (JS > 1) {
+#pragma unroll
+            for (int o = JS / 2; o > 0; o >>= 1) {
+                ax += __shfl_xor_sync(mask, ax, o, JS);
+                ay += __shfl_xor_sync(mask, ay, o, JS);
+                az += __shfl_xor_sync(mask, az, o, JS);
+            }
+        }
+        if (lane == 0 && m[j] >= 0.0) {
+            acc[3 * j] = ax;
+            acc[3 * j + 1] = ay;
+            acc[3 * j + 2] = az;
+        }
+    }
+    (void)gl;
+}
+
 __global__ void sum_chunks_kernel(const double *__restrict__ partial, const double *__restrict__ m,
                                   int n, int chunks, double *__restrict__ acc)
 {
@@ -273,6 +327,33 @@ int launch_force(int mode, const double *pos, const double *m, int n, double G, 
             ABIE_CUDA(cudaMalloc(&s.partial, need * sizeof(double)));
             s.partial_cap = need;
         }
+    }
+    if (sh.chunks == 1 && s.next) {
+        // persistent grid, sinks from an atomic counter
+        int dev = 0, sms = 152;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        int bps = 0;
+        const void *fn = sh.lanes_per_sink == 1 ? (const void *)force_fp64_dyn_kernel<1>
+                         : sh.lanes_per_sink == 8 ? (const void *)force_fp64_dyn_kernel<8>
+                                                  : (const void *)force_fp64_dyn_kernel<32>;
+        ABIE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fn, 256, 0));
+        long long want = ((long long)n * sh.lanes_per_sink + 255) / 256;
+        int blocks = (int)std::max<long long>(1, std::min<long long>((long long)sms * std::max(bps, 1), want));
+        ABIE_CUDA(cudaMemsetAsync(s.next, 0, sizeof(unsigned int), st));
+        switch (sh.lanes_per_sink) {
+        case 1:
+            force_fp64_dyn_kernel<1><<<blocks, 256, 0, st>>>(pos, m, n, s.src, s.n_src, acc, s.next);
+            break;
+        case 8:
+            force_fp64_dyn_kernel<8><<<blocks, 256, 0, st>>>(pos, m, n, s.src, s.n_src, acc, s.next);
+            break;
+        default:
+            force_fp64_dyn_kernel<32><<<blocks, 256, 0, st>>>(pos, m, n, s.src, s.n_src, acc, s.next);
+            break;
+        }
+        ABIE_CUDA(cudaGetLastError());
+        return 0;
     }
     long long groups = (long long)n * sh.chunks;
     int gpb = 256 / sh.lanes_per_sink;

@@ -13,6 +13,7 @@ struct ForceScratch {
     int *n_src = nullptr;       // device scalar
     double *partial = nullptr;  // per (sink, source chunk) partial sums, 3 doubles each
     unsigned long long *gm_max = nullptr;  // mixed form: largest G m (as ordered bits)
+    unsigned int *next = nullptr;          // fp64 form: next sink to hand out
     size_t cap = 0;             // bodies
     size_t partial_cap = 0;     // doubles
 };

@@ -38,7 +38,7 @@ struct MlpState {
     int *idx = nullptr;
     long long idx_cap = 0;
     long long adam_t = 0;
-    float tau = 1.0f;
+    float tau[7] = {1, 1, 1, 1, 1, 1, 1};
     bool ready = false, enabled = false;
     LearnedPredictor view = {};
     LearnedPredictor *view_dev = nullptr;
@@ -321,7 +321,7 @@ int mlp_refresh(cudaStream_t st)
     v.b1 = s.master + MLP_OFF_B1;
     v.b2 = s.master + MLP_OFF_B2;
     v.b3 = s.master + MLP_OFF_B3;
-    v.tau = s.tau;
+    for (int k = 0; k < 7; k++) v.tau[k] = s.tau[k];
     ABIE_CUDA(cudaMemcpyAsync(s.view_dev, &v, sizeof v, cudaMemcpyHostToDevice, st));
     ABIE_CUDA(cudaStreamSynchronize(st));
     s.ready = true;
@@ -396,6 +396,8 @@ const LearnedPredictor *learned_predictor_device()
 
 const LearnedPredictor *learned_predictor_current() { return learned_predictor_device(); }
 
+const float *learned_predictor_tau() { return g_mlp.tau; }
+
 static unsigned long long *g_sample_counter = nullptr;
 static long long g_collect_cap = 1 << 20;
 
@@ -416,7 +418,7 @@ int mlp_collect_begin(EnsembleLearnIO *io)
     io->samples = s.samples;
     io->cap = s.sample_cap;
     io->count = g_sample_counter;
-    io->tau = s.tau;
+    for (int k = 0; k < 7; k++) io->tau[k] = s.tau[k];
     return 0;
 }
 
@@ -433,7 +435,7 @@ using namespace abie;
 
 extern "C" {
 
-int abie_mlp_init(int seed, double tau)
+int abie_mlp_init(int seed, const double *tau)
 {
     int rc = ensure_device(-1);
     if (rc) return rc;
@@ -457,11 +459,11 @@ int abie_mlp_init(int seed, double tau)
     ABIE_CUDA(cudaMemset(s.adam_m, 0, MLP_N_PARAMS * sizeof(float)));
     ABIE_CUDA(cudaMemset(s.adam_v, 0, MLP_N_PARAMS * sizeof(float)));
     s.adam_t = 0;
-    s.tau = (float)tau;
+    for (int k = 0; k < 7; k++) s.tau[k] = tau ? (float)tau[k] : 1.0f;
     return mlp_refresh(g_sim.st);
 }
 
-int abie_mlp_set_params(const float *params, int n, double tau)
+int abie_mlp_set_params(const float *params, int n, const double *tau)
 {
     if (n != MLP_N_PARAMS) {
         set_error(ABIE_ERR_ARGUMENT, "abie_mlp_set_params: %d values, expected %d", n, MLP_N_PARAMS);
@@ -471,7 +473,7 @@ int abie_mlp_set_params(const float *params, int n, double tau)
     if (rc) return rc;
     if ((rc = mlp_alloc())) return rc;
     ABIE_CUDA(cudaMemcpy(g_mlp.master, params, n * sizeof(float), cudaMemcpyHostToDevice));
-    g_mlp.tau = (float)tau;
+    for (int k = 0; k < 7; k++) g_mlp.tau[k] = tau ? (float)tau[k] : 1.0f;
     return mlp_refresh(g_sim.st);
 }
 

@@ -1,15 +1,16 @@
 // Learned Radau15 predictor: a BF16 multilayer perceptron that proposes the
 // next step's b coefficients of a body.
 //
-//   in  (32, 24 used): the body's converged b of the step just accepted,
-//        b_k[d] / s for k < 7, d < 3 (s = max |b|), log2 of the requested
-//        and the actual step ratio (dtreq/h, h_next/h) / 4, and
-//        log10(m / m_star) / 10
+//   in  (32, 30 used): the body's converged b of the step just accepted,
+//        b_k[d] / s_k for k < 7, d < 3 (s_k = max_d |b_k[d]|, one scale per
+//        order), log2 of the requested and the actual step ratio
+//        (dtreq/h, h_next/h) / 4, log10(m / m_star) / 10 and
+//        log10(s_k / s_0) / 10 for k = 1..6
 //   H1 = relu(in W1^T + b1), H2 = relu(H1 W2^T + b2)      (128, 128)
-//   out = H2 W3^T + b3     (32, 21 used): (b_next - E(q)) / (s * tau)
-// where E(q) is the reference's plain predictor (refine_bs) and tau a fixed
-// output scale.  The guess handed to the corrector is E + s * tau * out, so
-// an all-zero output layer is exactly the plain predictor.
+//   out = H2 W3^T + b3     (32, 21 used): (b_next,k - E_k(q)) / (s_k tau_k)
+// where E(q) is the reference's plain predictor (refine_bs) and tau_k fixed
+// output scales.  The guess handed to the corrector is E_k + s_k tau_k out,
+// so an all-zero output layer is exactly the plain predictor.
 //
 // Tensor-core operands are BF16, accumulation FP32 (mma.sync m16n8k16).
 #pragma once
@@ -20,7 +21,7 @@
 
 namespace abie {
 
-constexpr int MLP_IN = 32, MLP_HID = 128, MLP_OUT = 21, MLP_OUT_PAD = 32, MLP_FEAT = 24;
+constexpr int MLP_IN = 32, MLP_HID = 128, MLP_OUT = 21, MLP_OUT_PAD = 32, MLP_FEAT = 30;
 constexpr int MLP_N_PARAMS = MLP_HID * MLP_IN + MLP_HID + MLP_HID * MLP_HID + MLP_HID +
                              MLP_OUT_PAD * MLP_HID + MLP_OUT_PAD;
 // offsets of the tensors in the flat FP32 parameter vector
@@ -37,7 +38,7 @@ struct LearnedPredictor {
     const __nv_bfloat16 *W1, *W2, *W3;
     const __nv_bfloat16 *W1t, *W2t, *W3t;
     const float *b1, *b2, *b3;
-    float tau;  // output scale
+    float tau[7];  // output scale per coefficient order
 };
 
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi)

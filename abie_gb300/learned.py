@@ -2,14 +2,16 @@
 
 The batched Radau15 ensemble, run with the plain predictor, records for
 every step reached in one attempt a training sample: the features of the
-previous accepted step (its converged b coefficients scaled by their
-largest magnitude, the requested and actual step ratios, the body's mass
-ratio) and the target (this step's converged b minus the plain guess
-refine_bs made for it, in the same scale).  The targets are normalised by
-a robust scale tau (their 95th percentile magnitude, clipped at 20 tau),
-the network is trained on the GPU with the library's own forward/backward
+previous accepted step (its converged b coefficients scaled per order by
+their largest magnitude s_k, the requested and actual step ratios, the
+body's mass ratio, the log ratios of the scales) and the target (this
+step's converged b minus the plain guess refine_bs made for it, per order
+in units of s_k).  Each order's targets are normalised by a robust scale
+tau_k (their 95th percentile magnitude; targets clipped at 20 tau_k), the
+network is trained on the GPU with the library's own forward/backward
 kernels (Adam), and is then switched on: later steps start from
-E + s tau out instead of E.  The convergence test of the corrector is
+E_k + s_k tau_k out_k instead of E_k, with the g coefficients made
+consistent with that guess.  The convergence test of the corrector is
 unchanged, so the solution is the same; only the number of corrector
 iterations changes.
 """
@@ -21,7 +23,7 @@ TARGETS = slice(32, 32 + 21)
 
 
 def collect_samples(lib: CLibABIE, P, V, M, offs, G, years, capacity=1 << 20, seed=0):
-    lib.mlp_init(seed, tau=1.0)
+    lib.mlp_init(seed, tau=None)
     lib.mlp_enable(False)
     lib.mlp_clear_samples()
     lib.mlp_set_capacity(capacity)
@@ -33,9 +35,9 @@ def train_predictor(lib: CLibABIE, samples, steps=2000, batch=2048, lr=1e-3, see
                     holdout=0.1):
     S = np.array(samples, dtype=np.float32, copy=True)
     S = S[np.isfinite(S).all(axis=1)]
-    T = S[:, TARGETS]
-    tau = float(np.quantile(np.abs(T), 0.95)) or 1.0
-    S[:, TARGETS] = np.clip(T / tau, -20.0, 20.0)
+    T = S[:, TARGETS].reshape(-1, 3, 7)          # [sample][d][k]
+    tau = np.array([float(np.quantile(np.abs(T[:, :, k]), 0.95)) or 1.0 for k in range(7)])
+    S[:, TARGETS] = np.clip(T / tau, -20.0, 20.0).reshape(-1, 21)
     rng = np.random.default_rng(seed)
     rng.shuffle(S)
     n_hold = int(len(S) * holdout)
@@ -53,5 +55,5 @@ def train_predictor(lib: CLibABIE, samples, steps=2000, batch=2048, lr=1e-3, see
     L.abie_mlp_loss_grad(len(hold), grad.ctypes.data, ctypes.byref(loss))
     plain = float((hold[:, TARGETS] ** 2).mean())
     lib.mlp_enable(True)
-    return {"samples": int(len(S)), "tau": tau, "train_loss": last, "holdout_loss": loss.value,
-            "holdout_loss_plain": plain}
+    return {"samples": int(len(S)), "tau": tau.tolist(), "train_loss": last,
+            "holdout_loss": loss.value, "holdout_loss_plain": plain}

@@ -42,6 +42,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+from abie_gb300 import dist as D  # noqa: E402
 from abie_gb300 import ics  # noqa: E402
 
 G = ics.G_SOLAR
@@ -66,10 +67,7 @@ def parse():
 
 
 def dist_env():
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return rank, world, local
+    return D.rank_info()
 
 
 def interactions(m):
@@ -247,13 +245,9 @@ def run_ours(args):
     torch.cuda.synchronize()
     clk = clocks.stop()
     times_ms = [a.elapsed_time(b) for a, b in evs]
-    tot_ms = float(sum(times_ms))
-    if world > 1:
-        t = torch.tensor([tot_ms], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        tot_ms = float(t.item())
-    ms_step = tot_ms / args.steps
-    value = world * inter * args.steps / (tot_ms * 1e-3) / 1e9
+    tot_s, units = D.reduce_timing(1e-3 * float(sum(times_ms)), inter * args.steps, device=dev)
+    ms_step = 1e3 * tot_s / args.steps
+    value = units / tot_s / 1e9
 
     # e2e through the reference-facing host entry point
     hp = torch.from_numpy(p).pin_memory()
@@ -276,12 +270,8 @@ def run_ours(args):
     t0 = time.perf_counter()
     for _ in range(args.steps):
         e2e_step()
-    e2e_s = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_value = world * inter * args.steps / e2e_s / 1e9
+    e2e_s, e2e_units = D.reduce_timing(time.perf_counter() - t0, inter * args.steps, device=dev)
+    e2e_value = e2e_units / e2e_s / 1e9
 
     # roofline of the force kernel (FP64 pipe)
     ach = FLOP_PER_INTERACTION * inter / (ms_step * 1e-3) / 1e12
@@ -296,9 +286,9 @@ def run_ours(args):
             roof["traffic"] = json.load(fh).get("force_%s_%d" % (args.mode, m.size))
 
     extra = {}
-    if not args.no_extras and rank == 0:
+    if not args.no_extras:
         if args.ensemble_systems > 0:
-            extra["ensemble"] = run_ensemble(lib, args)
+            extra["ensemble"] = run_ensemble(lib, args, rank, dev)
         if args.wh_steps > 0:
             extra["wh"] = run_wh(lib, args)
         if args.gr_years > 0:
@@ -353,10 +343,12 @@ def _energy_errors(P0, V0, P1, V1, M, offs):
     return worst
 
 
-def run_ensemble(lib, args):
-    """Radau15 over independent systems (4,096 systems of 4..13 bodies:
-    a 0.5..1.5 MSun star and 3..12 planets) for a bounded slice of time."""
-    P, V, M, offs = ics.ensemble(n_systems=args.ensemble_systems)
+def run_ensemble(lib, args, rank, dev):
+    """Radau15 over independent systems (4,096 systems per GPU of 4..13
+    bodies: a 0.5..1.5 MSun star and 3..12 planets) for a bounded slice of
+    time.  Every rank draws its own systems (weak scaling)."""
+    P, V, M, offs = ics.ensemble(n_systems=args.ensemble_systems,
+                                 seed0=D.ensemble_seed0(10000, rank, args.ensemble_systems))
     out = {"systems": int(offs.size - 1), "bodies": int(M.size), "years": args.ensemble_years}
     base = None
     for label, mode in (("fp64", "fp64"), ("plain_fp64", "exact")):
@@ -365,9 +357,9 @@ def run_ensemble(lib, args):
         res = lib.gr_ensemble(P, V, M, offs, G, 0.0, args.ensemble_years)
         c = lib.counters()
         lib.set_force_mode(old)
-        steps = int(res["steps"].sum())
-        rate = steps / res["seconds"] if res["seconds"] else None
-        out[label] = {"system_steps": steps, "seconds": res["seconds"], "system_steps_per_s": rate,
+        secs, steps = D.reduce_timing(res["seconds"], int(res["steps"].sum()), device=dev)
+        rate = steps / secs if secs else None
+        out[label] = {"system_steps": int(steps), "seconds": secs, "system_steps_per_s": rate,
                       "corrector_iterations_per_attempt": c["iterations"] / max(c["attempts"], 1),
                       "max_abs_dE_over_E": _energy_errors(P, V, res["pos"], res["vel"], M, offs),
                       "failed_systems": int((res["status"] != 0).sum())}

@@ -143,7 +143,8 @@ double abie_energy_host(const double *pos, const double *vel, const double *m,
  * t_end, exactly as integrator_gr would integrate it alone.  pos/vel are
  * updated in place, t_out[s] receives each system's final time, status[s]
  * its return code (0, or a negative error), steps[s] its accepted steps.
- * flags: bit 0 learned predictor, bit 1 collect training samples (below). */
+ * flags: bit 0 learned predictor, bit 1 collect training samples, bit 2
+ * consistent-g plain predictor (below). */
 int abie_gr_ensemble(double *pos, double *vel, const double *m,
                      const long long *offsets, int n_systems, double G,
                      double t0, double t_end, double *t_out, int *status,
@@ -151,13 +152,16 @@ int abie_gr_ensemble(double *pos, double *vel, const double *m,
 /* Seconds of GPU time spent in the last abie_gr_ensemble call. */
 double abie_last_ensemble_seconds(void);
 
-/* Learned Radau15 predictor (BF16 MLP 24 -> 128 -> 128 -> 21; see
+/* Learned Radau15 predictor (BF16 MLP 30 -> 128 -> 128 -> 21; see
  * abie_gb300/csrc/mlp.cuh for features and targets).  abie_gr_ensemble
- * flags: bit 0 starts every step from the network's guess (requires
- * abie_mlp_enable(1)), bit 1 appends training samples (64 floats each:
- * 32 features, 32 targets) to the device sample store. */
-int abie_mlp_init(int seed, double tau);             /* fresh weights, zero output layer */
-int abie_mlp_set_params(const float *params, int n, double tau);
+ * flags: bit 0 starts every step from the network's guess, with the g
+ * coefficients made consistent with it (requires abie_mlp_enable(1));
+ * bit 2 the same consistent g with the plain guess and no network; bit 1
+ * appends training samples (64 floats each: 32 features, 32 targets) to the
+ * device sample store.  tau: 7 output scales, one per coefficient order
+ * (NULL: all 1). */
+int abie_mlp_init(int seed, const double *tau);       /* fresh weights, zero output layer */
+int abie_mlp_set_params(const float *params, int n, const double *tau);
 int abie_mlp_get_params(float *params, int n);
 int abie_mlp_n_params(void);
 void abie_mlp_enable(int on);

@@ -2,7 +2,7 @@
 
 A float64 NumPy statement of the network the library runs on the GPU:
 
-    H1 = relu(bf16(X)  @ bf16(W1)^T + b1)      X: rows x 32 (24 features, zero padded)
+    H1 = relu(bf16(X)  @ bf16(W1)^T + b1)      X: rows x 32 (30 features, zero padded)
     H2 = relu(bf16(H1) @ bf16(W2)^T + b2)      W1: 128 x 32, W2: 128 x 128
     Y  =      bf16(H2) @ bf16(W3)^T + b3       W3: 32 x 128 (21 outputs, zero padded)
     loss = sum over rows and the 21 outputs of (Y - T)^2 / (rows * 21)

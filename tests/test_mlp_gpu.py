@@ -14,8 +14,8 @@ pytestmark = pytest.mark.gpu
 
 def _lib(clib):
     L = clib.lib
-    L.abie_mlp_init.argtypes = [C.c_int, C.c_double]
-    L.abie_mlp_set_params.argtypes = [C.c_void_p, C.c_int, C.c_double]
+    L.abie_mlp_init.argtypes = [C.c_int, C.c_void_p]
+    L.abie_mlp_set_params.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
     L.abie_mlp_get_params.argtypes = [C.c_void_p, C.c_int]
     L.abie_mlp_load_samples.argtypes = [C.c_void_p, C.c_longlong]
     L.abie_mlp_forward.argtypes = [C.c_longlong, C.c_void_p]
@@ -33,7 +33,7 @@ def _random_params(rng):
 
 def _samples(rng, rows):
     X = np.zeros((rows, R.IN), np.float32)
-    X[:, :24] = rng.normal(size=(rows, 24))
+    X[:, :30] = rng.normal(size=(rows, 30))
     T = np.zeros((rows, R.OUT_PAD), np.float32)
     T[:, :R.OUT] = rng.normal(size=(rows, R.OUT))
     return X, T, np.ascontiguousarray(np.concatenate([X, T], axis=1))
@@ -47,7 +47,7 @@ def test_forward_and_gradients_match_checker(clib):
     L = _lib(clib)
     rng = np.random.default_rng(1)
     params, flat = _random_params(rng)
-    assert L.abie_mlp_set_params(flat.ctypes.data, flat.size, 1.0) == 0
+    assert L.abie_mlp_set_params(flat.ctypes.data, flat.size, None) == 0
     rows = 200  # several CTAs of 64 and a ragged last one
     X, T, S = _samples(rng, rows)
     assert L.abie_mlp_load_samples(S.ctypes.data, rows) == 0
@@ -70,19 +70,20 @@ def test_forward_and_gradients_match_checker(clib):
 def test_training_lowers_loss(clib):
     L = _lib(clib)
     rng = np.random.default_rng(2)
-    assert L.abie_mlp_init(7, 1.0) == 0
+    assert L.abie_mlp_init(7, None) == 0
     rows = 4096
     X = np.zeros((rows, R.IN), np.float32)
-    X[:, :24] = rng.normal(size=(rows, 24))
-    A = rng.normal(0, 0.3, (24, R.OUT))
+    X[:, :30] = rng.normal(size=(rows, 30))
+    A = rng.normal(0, 0.3, (30, R.OUT))
     T = np.zeros((rows, R.OUT_PAD), np.float32)
-    T[:, :R.OUT] = np.tanh(X[:, :24] @ A)
+    T[:, :R.OUT] = np.tanh(X[:, :30] @ A)
     S = np.ascontiguousarray(np.concatenate([X, T], axis=1))
     assert L.abie_mlp_load_samples(S.ctypes.data, rows) == 0
+    grad = np.zeros(R.N_PARAMS, np.float32)  # kept alive across the calls
     l0 = C.c_double(0)
-    L.abie_mlp_loss_grad(rows, np.zeros(R.N_PARAMS, np.float32).ctypes.data, C.byref(l0))
+    assert L.abie_mlp_loss_grad(rows, grad.ctypes.data, C.byref(l0)) == 0
     last = C.c_double(0)
     assert L.abie_mlp_train(400, 256, 3e-3, 5, C.byref(last)) == 0
     l1 = C.c_double(0)
-    L.abie_mlp_loss_grad(rows, np.zeros(R.N_PARAMS, np.float32).ctypes.data, C.byref(l1))
+    assert L.abie_mlp_loss_grad(rows, grad.ctypes.data, C.byref(l1)) == 0
     assert l1.value < 0.2 * l0.value, (l0.value, l1.value)
