@@ -161,23 +161,38 @@ __device__ __forceinline__ double e_pred_vel(const Comp &c, double s, double dt)
     return fma(dt * s, c.F1 + u, c.dy0);
 }
 
+// g and b after the force F of substep IH (src/integrator_gauss_radau15.c:136-241);
+// one fully static variant per substep keeps the coefficients in registers.
+template <int MODE, int IH>
+__device__ __forceinline__ void e_gb_update_ih(Comp &c, double F)
+{
+    double v = (F - c.F1) * e_rs[IH][0];
+#pragma unroll
+    for (int l = 1; l < IH; l++) v = (v - c.g[l - 1]) * e_rs[IH][l];
+    c.g[IH - 1] = v;
+#pragma unroll
+    for (int k = 0; k < IH; k++) {
+        double s = e_cs[k][k] * c.g[k];
+#pragma unroll
+        for (int jj = k + 1; jj < 7; jj++) {
+            if (MODE == ABIE_FORCE_EXACT) s = s + e_cs[jj][k] * c.g[jj];  // reference roundings
+            else s = fma(e_cs[jj][k], c.g[jj], s);
+        }
+        c.b[k] = s;
+    }
+}
+
+template <int MODE>
 __device__ __forceinline__ void e_gb_update(Comp &c, int ih, double F)
 {
-    double v = (F - c.F1) * e_rs[ih][0];
-#pragma unroll
-    for (int l = 1; l < 7; l++)
-        if (l < ih) v = (v - c.g[l - 1]) * e_rs[ih][l];
-#pragma unroll
-    for (int k = 0; k < 7; k++)
-        if (k == ih - 1) c.g[k] = v;
-#pragma unroll
-    for (int k = 0; k < 7; k++) {
-        if (k < ih) {
-            double s = e_cs[k][k] * c.g[k];
-#pragma unroll
-            for (int jj = k + 1; jj < 7; jj++) s = s + e_cs[jj][k] * c.g[jj];
-            c.b[k] = s;
-        }
+    switch (ih) {
+    case 1: e_gb_update_ih<MODE, 1>(c, F); break;
+    case 2: e_gb_update_ih<MODE, 2>(c, F); break;
+    case 3: e_gb_update_ih<MODE, 3>(c, F); break;
+    case 4: e_gb_update_ih<MODE, 4>(c, F); break;
+    case 5: e_gb_update_ih<MODE, 5>(c, F); break;
+    case 6: e_gb_update_ih<MODE, 6>(c, F); break;
+    default: e_gb_update_ih<MODE, 7>(c, F); break;
     }
 }
 
@@ -290,6 +305,7 @@ __device__ __forceinline__ void learned_refine(const EnsArgs &a, LearnSmem &L, C
     for (int u = 0; u < 2; u++) {
         if (!(u == 0 ? has0 : has1)) continue;
         int c = lane + 32 * u, i = c / 3, d = c % 3;
+        #pragma unroll
         for (int k = 0; k < 7; k++) L.row[i][7 * d + k] = (float)C[u].b[k];
     }
     __syncwarp();
@@ -317,6 +333,7 @@ __device__ __forceinline__ void learned_refine(const EnsArgs &a, LearnSmem &L, C
             for (int u = 0; u < 2; u++) {
                 if (!(u == 0 ? has0 : has1)) continue;
                 int c = lane + 32 * u, i = c / 3, d = c % 3;
+                #pragma unroll
                 for (int k = 0; k < 7; k++) {
                     float tgt = ((float)(C[u].b[k] / (double)L.ps[i][k]) - L.pE[i][7 * d + k]) / a.tau[k];
                     a.samples[(base + i) * MLP_SAMPLE + MLP_IN + 7 * d + k] = tgt;
@@ -332,12 +349,14 @@ __device__ __forceinline__ void learned_refine(const EnsArgs &a, LearnSmem &L, C
     for (int u = 0; u < 2; u++) {
         if (!(u == 0 ? has0 : has1)) continue;
         int c = lane + 32 * u, i = c / 3, d = c % 3;
+        #pragma unroll
         for (int k = 0; k < 7; k++) {
             float f = L.row[i][7 * d + k] / L.scale[i][k];
             L.xh2[i][7 * d + k] = __float2bfloat16_rn(f);
             L.pfeat[i][7 * d + k] = f;
         }
         e_refine(C[u], q);
+        #pragma unroll
         for (int k = 0; k < 7; k++) L.pE[i][7 * d + k] = (float)(C[u].b[k] / (double)L.scale[i][k]);
     }
     for (int e = lane; e < LP_ROWS * 40; e += 32) {
@@ -363,8 +382,14 @@ __device__ __forceinline__ void learned_refine(const EnsArgs &a, LearnSmem &L, C
         for (int u = 0; u < 2; u++) {
             if (!(u == 0 ? has0 : has1)) continue;
             int c = lane + 32 * u, i = c / 3, d = c % 3;
-            for (int k = 0; k < 7; k++)
-                C[u].b[k] += (double)L.scale[i][k] * (double)a.tau[k] * (double)L.row[i][7 * d + k];
+            #pragma unroll
+            for (int k = 0; k < 7; k++) {
+                // outside the training range (|target| <= 20) or non-finite:
+                // keep the plain guess for this coefficient
+                float o = L.row[i][7 * d + k];
+                o = (isfinite(o) && fabsf(o) <= 20.0f) ? o : 0.0f;
+                C[u].b[k] += (double)L.scale[i][k] * (double)a.tau[k] * (double)o;
+            }
         }
         __syncwarp();
     }
@@ -374,8 +399,8 @@ __device__ __forceinline__ void learned_refine(const EnsArgs &a, LearnSmem &L, C
     }
 }
 
-template <int MODE>
-__global__ void __launch_bounds__(32 * WARPS) ensemble_kernel(EnsArgs a)
+template <int MODE, int NC>
+__global__ void __launch_bounds__(32 * WARPS, NC == 1 ? 4 : 2) ensemble_kernel(EnsArgs a)
 {
     __shared__ double s_pos[WARPS][32][4];
     __shared__ double s_acc[WARPS][32][3];
@@ -399,7 +424,9 @@ __global__ void __launch_bounds__(32 * WARPS) ensemble_kernel(EnsArgs a)
         const double *m = a.m + off;
         EnsScalars S = a.sc[sid];
         // lane's components c0 = lane, c1 = lane + 32
-        const bool has0 = lane < dim, has1 = lane + 32 < dim;
+        // NC = 1: systems of at most 10 bodies, one component per lane; the
+        // second component's state is then compiled out
+        const bool has0 = lane < dim, has1 = (NC > 1) && (lane + 32 < dim);
         Comp C[2];
         double *st = a.state + (size_t)STATE_PER_COMP * 3 * off;
         auto slot = [&](int c, int k) -> double & { return st[(size_t)k * dim + c]; };
@@ -410,6 +437,7 @@ __global__ void __launch_bounds__(32 * WARPS) ensemble_kernel(EnsArgs a)
             Comp &X = C[u];
             if (!has) {
                 X.y0 = X.dy0 = X.F1 = X.b6p = 0.0;
+                #pragma unroll
                 for (int k = 0; k < 7; k++) X.b[k] = X.g[k] = 0.0;
                 continue;
             }
@@ -418,12 +446,15 @@ __global__ void __launch_bounds__(32 * WARPS) ensemble_kernel(EnsArgs a)
                 X.dy0 = a.vel[3 * off + c];
                 X.F1 = 0.0;
                 X.b6p = 0.0;
+                #pragma unroll
                 for (int k = 0; k < 7; k++) X.b[k] = X.g[k] = 0.0;
             } else {
                 X.y0 = slot(c, 0);
                 X.dy0 = slot(c, 1);
                 X.F1 = slot(c, 2);
+                #pragma unroll
                 for (int k = 0; k < 7; k++) X.b[k] = slot(c, 3 + k);
+                #pragma unroll
                 for (int k = 0; k < 7; k++) X.g[k] = slot(c, 10 + k);
                 X.b6p = slot(c, 17);
             }
@@ -500,7 +531,7 @@ __global__ void __launch_bounds__(32 * WARPS) ensemble_kernel(EnsArgs a)
                     for (int u = 0; u < 2; u++) {
                         if (!(u == 0 ? has0 : has1)) continue;
                         double F = force_of(u);
-                        e_gb_update(C[u], ih, F);
+                        e_gb_update<MODE>(C[u], ih, F);
                         if (ih == 7) {
                             f8 = fmax(f8, absmax_or_none(F));
                             db6 = fmax(db6, absmax_or_none(C[u].b[6] - C[u].b6p));
@@ -608,7 +639,9 @@ __global__ void __launch_bounds__(32 * WARPS) ensemble_kernel(EnsArgs a)
                 slot(c, 0) = X.y0;
                 slot(c, 1) = X.dy0;
                 slot(c, 2) = X.F1;
+                #pragma unroll
                 for (int k = 0; k < 7; k++) slot(c, 3 + k) = X.b[k];
+                #pragma unroll
                 for (int k = 0; k < 7; k++) slot(c, 10 + k) = X.g[k];
                 slot(c, 17) = X.b6p;
             }
@@ -625,16 +658,30 @@ static size_t learn_smem(const EnsArgs &a)
     return (a.mlp || a.samples) ? WARPS * sizeof(LearnSmem) : 0;
 }
 
-static int launch_ensemble(int mode, int blocks, const EnsArgs &a, cudaStream_t st)
+static int launch_ensemble(int mode, int nc, int blocks, const EnsArgs &a, cudaStream_t st)
 {
     size_t dyn = learn_smem(a);
-    if (mode == ABIE_FORCE_EXACT)
-        ensemble_kernel<ABIE_FORCE_EXACT><<<blocks, 32 * WARPS, dyn, st>>>(a);
-    else
-        ensemble_kernel<ABIE_FORCE_FP64><<<blocks, 32 * WARPS, dyn, st>>>(a);
+    if (mode == ABIE_FORCE_EXACT) {
+        if (nc == 1) ensemble_kernel<ABIE_FORCE_EXACT, 1><<<blocks, 32 * WARPS, dyn, st>>>(a);
+        else ensemble_kernel<ABIE_FORCE_EXACT, 2><<<blocks, 32 * WARPS, dyn, st>>>(a);
+    } else {
+        if (nc == 1) ensemble_kernel<ABIE_FORCE_FP64, 1><<<blocks, 32 * WARPS, dyn, st>>>(a);
+        else ensemble_kernel<ABIE_FORCE_FP64, 2><<<blocks, 32 * WARPS, dyn, st>>>(a);
+    }
     ABIE_CUDA(cudaGetLastError());
     return 0;
 }
+
+static const void *ensemble_fn(int mode, int nc)
+{
+    if (mode == ABIE_FORCE_EXACT)
+        return nc == 1 ? (const void *)ensemble_kernel<ABIE_FORCE_EXACT, 1>
+                       : (const void *)ensemble_kernel<ABIE_FORCE_EXACT, 2>;
+    return nc == 1 ? (const void *)ensemble_kernel<ABIE_FORCE_FP64, 1>
+                   : (const void *)ensemble_kernel<ABIE_FORCE_FP64, 2>;
+}
+
+static cudaStream_t g_ens_stream2 = nullptr;
 
 int ensemble_run(double *pos, double *vel, const double *m, const long long *offsets, int ns,
                  double G, double t0, double t_end, double *t_out, int *status, long long *steps,
@@ -663,7 +710,7 @@ int ensemble_run(double *pos, double *vel, const double *m, const long long *off
     ABIE_CUDA(cudaMalloc(&d_off, (ns + 1) * sizeof(long long)));
     ABIE_CUDA(cudaMalloc(&d_sc, ns * sizeof(EnsScalars)));
     ABIE_CUDA(cudaMalloc(&d_active, ns * sizeof(int)));
-    ABIE_CUDA(cudaMalloc(&d_queue, sizeof(int)));
+    ABIE_CUDA(cudaMalloc(&d_queue, 2 * sizeof(int)));
     std::vector<EnsScalars> sc(ns);
     for (int s = 0; s < ns; s++) {
         memset(&sc[s], 0, sizeof(EnsScalars));
@@ -678,25 +725,36 @@ int ensemble_run(double *pos, double *vel, const double *m, const long long *off
     ABIE_CUDA(cudaMemcpyAsync(d_sc, sc.data(), ns * sizeof(EnsScalars), cudaMemcpyHostToDevice, st));
     ABIE_CUDA(cudaStreamSynchronize(st));
 
-    int bps = 0;
-    const void *fn = mode == ABIE_FORCE_EXACT ? (const void *)ensemble_kernel<ABIE_FORCE_EXACT>
-                                              : (const void *)ensemble_kernel<ABIE_FORCE_FP64>;
     const bool learning = mlp || (learn_io && learn_io->samples);
     const size_t dyn = learning ? WARPS * sizeof(LearnSmem) : 0;
-    ABIE_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)(WARPS * sizeof(LearnSmem))));
-    ABIE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fn, 32 * WARPS, dyn));
-    bps = std::max(bps, 1);
-    cudaEvent_t e0, e1;
+    int bps[2] = {1, 1};
+    for (int k = 0; k < 2; k++) {
+        const void *fn = ensemble_fn(mode, k + 1);
+        ABIE_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)(WARPS * sizeof(LearnSmem))));
+        ABIE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps[k], fn, 32 * WARPS, dyn));
+        bps[k] = std::max(bps[k], 1);
+    }
+    if (!g_ens_stream2) ABIE_CUDA(cudaStreamCreateWithFlags(&g_ens_stream2, cudaStreamNonBlocking));
+    cudaEvent_t e0, e1, ej;
     ABIE_CUDA(cudaEventCreate(&e0));
     ABIE_CUDA(cudaEventCreate(&e1));
+    ABIE_CUDA(cudaEventCreateWithFlags(&ej, cudaEventDisableTiming));
     double gpu_ms = 0.0;
     int launches = 0;
     int n_active = ns;
+    std::vector<int> part(ns);
     while (n_active > 0) {
-        ABIE_CUDA(cudaMemcpyAsync(d_active, active.data(), n_active * sizeof(int),
+        // small systems (3n <= 32) first, then the rest
+        int n_small = 0;
+        for (int q = 0; q < n_active; q++)
+            if (3 * (offsets[active[q] + 1] - offsets[active[q]]) <= 32) part[n_small++] = active[q];
+        int k2 = n_small;
+        for (int q = 0; q < n_active; q++)
+            if (3 * (offsets[active[q] + 1] - offsets[active[q]]) > 32) part[k2++] = active[q];
+        ABIE_CUDA(cudaMemcpyAsync(d_active, part.data(), n_active * sizeof(int),
                                   cudaMemcpyHostToDevice, st));
-        ABIE_CUDA(cudaMemsetAsync(d_queue, 0, sizeof(int), st));
+        ABIE_CUDA(cudaMemsetAsync(d_queue, 0, 2 * sizeof(int), st));
         EnsArgs a;
         a.offsets = d_off;
         a.m = d_m;
@@ -704,9 +762,6 @@ int ensemble_run(double *pos, double *vel, const double *m, const long long *off
         a.vel = d_vel;
         a.state = d_state;
         a.sc = d_sc;
-        a.active = d_active;
-        a.n_active = n_active;
-        a.queue = d_queue;
         a.G = G;
         a.t_end = t_end;
         a.mlp = mlp;
@@ -716,12 +771,23 @@ int ensemble_run(double *pos, double *vel, const double *m, const long long *off
         for (int k = 0; k < 7; k++) a.tau[k] = learn_io ? learn_io->tau[k] : (mlp_tau ? mlp_tau[k] : 1.0f);
         a.consistent_g = consistent ? 1 : 0;
         a.budget_ns = 2000000000ull;  // each launch yields after about two seconds
-        int blocks = std::min<long long>((long long)bps * g_sim.num_sms,
-                                         (n_active + WARPS - 1) / WARPS);
-        blocks = std::max(blocks, 1);
         ABIE_CUDA(cudaEventRecord(e0, st));
-        int lrc = launch_ensemble(mode, blocks, a, st);
-        if (lrc) return lrc;
+        ABIE_CUDA(cudaEventRecord(ej, st));
+        ABIE_CUDA(cudaStreamWaitEvent(g_ens_stream2, ej, 0));
+        for (int k = 0; k < 2; k++) {
+            int cnt = k == 0 ? n_small : n_active - n_small;
+            if (cnt == 0) continue;
+            EnsArgs ak = a;
+            ak.active = d_active + (k == 0 ? 0 : n_small);
+            ak.n_active = cnt;
+            ak.queue = d_queue + k;
+            int blocks = (int)std::min<long long>((long long)bps[k] * g_sim.num_sms, (cnt + WARPS - 1) / WARPS);
+            blocks = std::max(blocks, 1);
+            int lrc = launch_ensemble(mode, k + 1, blocks, ak, k == 0 ? st : g_ens_stream2);
+            if (lrc) return lrc;
+        }
+        ABIE_CUDA(cudaEventRecord(ej, g_ens_stream2));
+        ABIE_CUDA(cudaStreamWaitEvent(st, ej, 0));
         ABIE_CUDA(cudaEventRecord(e1, st));
         ABIE_CUDA(cudaEventSynchronize(e1));
         float ms = 0.f;
@@ -730,10 +796,11 @@ int ensemble_run(double *pos, double *vel, const double *m, const long long *off
         launches++;
         ABIE_CUDA(cudaMemcpy(sc.data(), d_sc, ns * sizeof(EnsScalars), cudaMemcpyDeviceToHost));
         int k = 0;
-        for (int s = 0; s < ns; s++)
-            if (sc[s].phase != 2 && sc[s].status == 0) active[k++] = s;
+        for (int s2 = 0; s2 < ns; s2++)
+            if (sc[s2].phase != 2 && sc[s2].status == 0) active[k++] = s2;
         n_active = k;
     }
+    cudaEventDestroy(ej);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     ABIE_CUDA(cudaMemcpy(pos, d_pos, 3 * total * sizeof(double), cudaMemcpyDeviceToHost));

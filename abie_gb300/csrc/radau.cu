@@ -232,6 +232,7 @@ __device__ __forceinline__ void publish_body(const EngineArgs &a, int j, double 
 // g and b after the force F at substep ih (1..7) for component i
 // (src/integrator_gauss_radau15.c:136-241; only g[ih-1] is new, the lower g
 // the reference recomputes are bitwise the stored ones).
+template <int MODE>
 __device__ __forceinline__ void gb_update(const EngineArgs &a, int i, int ih, double F)
 {
     const int d = a.dim;
@@ -244,7 +245,10 @@ __device__ __forceinline__ void gb_update(const EngineArgs &a, int i, int ih, do
     for (int k = 0; k < 7; k++) gl[k] = (k == ih - 1) ? v : g[k * d + i];
     for (int k = 0; k < ih; k++) {
         double s = c_cs[k][k] * gl[k];
-        for (int jj = k + 1; jj < 7; jj++) s = s + c_cs[jj][k] * gl[jj];
+        for (int jj = k + 1; jj < 7; jj++) {
+            if (MODE == ABIE_FORCE_EXACT) s = s + c_cs[jj][k] * gl[jj];  // reference roundings
+            else s = fma(c_cs[jj][k], gl[jj], s);
+        }
         a.b[k * d + i] = s;
     }
 }
@@ -499,7 +503,7 @@ __global__ void __launch_bounds__(256) radau_engine(EngineArgs a)
                         for (int c = 0; c < 3; c++) {
                             int i = 3 * j + c;
                             double fi = f[c] + (a.ext ? a.ext[i] : 0.0);
-                            gb_update(a, i, ih, fi);
+                            gb_update<MODE>(a, i, ih, fi);
                             if (ih == 7) {
                                 unsigned long long u = absmax_key(a.b[6 * a.dim + i] - a.b6p[i]);
                                 unsigned long long w = absmax_key(fi);
