@@ -35,7 +35,8 @@ class Counters(_c.Structure):
     _fields_ = [("force_calls", _c.c_longlong), ("iterations", _c.c_longlong),
                 ("attempts", _c.c_longlong), ("accepts", _c.c_longlong),
                 ("rejects", _c.c_longlong), ("kepler_failures", _c.c_longlong),
-                ("wh_steps", _c.c_longlong), ("last_h", _c.c_double)]
+                ("wh_steps", _c.c_longlong), ("last_h", _c.c_double),
+                ("learned_fallbacks", _c.c_longlong)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -42,7 +42,7 @@ struct EnsScalars {
     int loop_count, phase;  // phase 0: fresh, 1: running, 2: done
     long long steps, attempts, iterations, force_calls;
     int status;
-    int pad;
+    int fallbacks;  // attempts redone from the plain guess after the network's guess failed
 };
 
 struct EnsArgs {
@@ -74,6 +74,7 @@ struct LearnSmem {
     float pE[LP_ROWS][MLP_OUT];                          // plain guess / scale of the pending sample
     float ps[LP_ROWS][7];                                // per-order scales of the pending sample
     float scale[LP_ROWS][7];                             // per-order scales of this step
+    double plain[3 * LP_ROWS][8];                        // plain guess b and b6p, kept while the network's is tried
 };
 
 // Network outputs for LP_ROWS rows of features (bf16, ld 40, in xh2) into
@@ -296,7 +297,7 @@ __device__ __forceinline__ void consistent_g(Comp &c)
 __device__ __forceinline__ void learned_refine(const EnsArgs &a, LearnSmem &L, Comp C[2], int n,
                                                int lane, bool has0, bool has1, double q, double h,
                                                double dtreq, const double *m, bool &pend_valid,
-                                               bool first_attempt)
+                                               bool first_attempt, bool &net_guess)
 {
     double h_next = (dtreq / h > 1.0 / FAC) ? h / FAC : ((dtreq < 1.e-12) ? h * FAC : dtreq);
     if (h_next < H_MIN) h_next = H_MIN;
@@ -383,6 +384,9 @@ __device__ __forceinline__ void learned_refine(const EnsArgs &a, LearnSmem &L, C
             if (!(u == 0 ? has0 : has1)) continue;
             int c = lane + 32 * u, i = c / 3, d = c % 3;
             #pragma unroll
+            for (int k = 0; k < 7; k++) L.plain[c][k] = C[u].b[k];
+            L.plain[c][7] = C[u].b6p;
+            #pragma unroll
             for (int k = 0; k < 7; k++) {
                 // outside the training range (|target| <= 20) or non-finite:
                 // keep the plain guess for this coefficient
@@ -392,10 +396,26 @@ __device__ __forceinline__ void learned_refine(const EnsArgs &a, LearnSmem &L, C
             }
         }
         __syncwarp();
+        net_guess = true;
     }
     if (a.consistent_g) {
         if (has0) consistent_g(C[0]);
         if (has1) consistent_g(C[1]);
+    }
+}
+
+// Back to the plain guess (consistent g) that learned_refine kept.
+__device__ __forceinline__ void restore_plain_guess(LearnSmem &L, Comp C[2], int lane, bool has0,
+                                                 bool has1)
+{
+#pragma unroll
+    for (int u = 0; u < 2; u++) {
+        if (!(u == 0 ? has0 : has1)) continue;
+        const int c = lane + 32 * u;
+#pragma unroll
+        for (int k = 0; k < 7; k++) C[u].b[k] = L.plain[c][k];
+        C[u].b6p = L.plain[c][7];
+        consistent_g(C[u]);
     }
 }
 
@@ -517,6 +537,7 @@ __global__ void __launch_bounds__(32 * WARPS, NC == 1 ? 4 : 2) ensemble_kernel(E
         // learned predictor: pending training sample, first attempt after an accept
         const bool learn = (a.mlp != nullptr || a.samples != nullptr) && n <= LP_ROWS;
         bool pend_valid = false, first_attempt = false;
+        bool net_guess = false;  // this attempt started from the network's guess
         while (!done) {
             if (ens_timer() > deadline) break;
             int iters = 0;
@@ -556,8 +577,16 @@ __global__ void __launch_bounds__(32 * WARPS, NC == 1 ? 4 : 2) ensemble_kernel(E
             S.force_calls++;
             double dd0 = has0 ? force_of(0) : 0.0, dd1 = has1 ? force_of(1) : 0.0;
             bool bad = (has0 && !isfinite(ya0 + dd0 + va0)) || (has1 && !isfinite(ya1 + dd1 + va1));
-            if (__any_sync(0xffffffffu, bad)) {  // non-finite state: report, stop this system
-                S.status = ABIE_ERR_NUMERICS;
+            if (__any_sync(0xffffffffu, bad)) {
+                if (net_guess) {
+                    // the network's guess led the corrector astray: redo the
+                    // attempt from the plain guess
+                    restore_plain_guess(LS, C, lane, has0, has1);
+                    net_guess = false;
+                    S.fallbacks++;
+                    continue;
+                }
+                S.status = ABIE_ERR_NUMERICS;  // non-finite state: report, stop this system
                 done = true;
                 break;
             }
@@ -576,10 +605,17 @@ __global__ void __launch_bounds__(32 * WARPS, NC == 1 ? 4 : 2) ensemble_kernel(E
             double err = pow(estim_b6 / EPSB, 1. / 7);
             double dtreq = h / err;
             if (!(err == err)) {  // NaN step control: the state is not finite
+                if (net_guess) {
+                    restore_plain_guess(LS, C, lane, has0, has1);
+                    net_guess = false;
+                    S.fallbacks++;
+                    continue;
+                }
                 S.status = ABIE_ERR_NUMERICS;
                 done = true;
                 break;
             }
+            net_guess = false;
             if (err <= 1 || loop_count > 100) {
                 t += h;
                 loop_count = 0;
@@ -600,7 +636,7 @@ __global__ void __launch_bounds__(32 * WARPS, NC == 1 ? 4 : 2) ensemble_kernel(E
                 C[1].b6p = C[1].b[6];
                 if (!stop && learn) {
                     learned_refine(a, LS, C, n, lane, has0, has1, q, h, dtreq, m, pend_valid,
-                                   first_attempt);
+                                   first_attempt, net_guess);
                 } else if (!stop) {
                     e_refine(C[0], q);
                     e_refine(C[1], q);
@@ -814,6 +850,7 @@ int ensemble_run(double *pos, double *vel, const double *m, const long long *off
             stats->iterations += sc[s].iterations;
             stats->force_calls += sc[s].force_calls;
             stats->steps += sc[s].steps;
+            stats->fallbacks += sc[s].fallbacks;
         }
     }
     if (stats) stats->launches += launches;
@@ -864,6 +901,7 @@ int abie_gr_ensemble(double *pos, double *vel, const double *m, const long long 
         g_sim.ctr.force_calls += st.force_calls;
         g_sim.ctr.accepts += st.steps;
         g_sim.ctr.rejects += st.attempts - st.steps;
+        g_sim.ctr.learned_fallbacks += st.fallbacks;
     }
     return rc;
 }

@@ -19,7 +19,7 @@ int mlp_collect_begin(EnsembleLearnIO *io);
 void mlp_collect_end(EnsembleLearnIO *io);
 
 struct EnsembleStats {
-    long long attempts, iterations, force_calls, steps, launches;
+    long long attempts, iterations, force_calls, steps, launches, fallbacks;
 };
 
 int ensemble_run(double *pos, double *vel, const double *m, const long long *offsets, int ns,

@@ -35,6 +35,10 @@ def train_predictor(lib: CLibABIE, samples, steps=2000, batch=2048, lr=1e-3, see
                     holdout=0.1):
     S = np.array(samples, dtype=np.float32, copy=True)
     S = S[np.isfinite(S).all(axis=1)]
+    # warps append samples in a run-dependent order: sort rows by content so
+    # that training depends only on the sample set and the seed
+    S = S[np.argsort(np.ascontiguousarray(S).view(np.dtype((np.void, S.shape[1] * 4))).ravel(),
+                     kind="stable")]
     T = S[:, TARGETS].reshape(-1, 3, 7)          # [sample][d][k]
     tau = np.array([float(np.quantile(np.abs(T[:, :, k]), 0.95)) or 1.0 for k in range(7)])
     S[:, TARGETS] = np.clip(T / tau, -20.0, 20.0).reshape(-1, 21)

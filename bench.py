@@ -62,6 +62,10 @@ def parse():
     ap.add_argument("--wh-steps", type=int, default=20)
     ap.add_argument("--gr-years", type=float, default=1.0)
     ap.add_argument("--no-extras", action="store_true", help="only the headline force line")
+    ap.add_argument("--extras", default="ensemble,wh,radau",
+                    help="comma list of sub-measurements: ensemble, wh, radau")
+    ap.add_argument("--ensemble-forms", default="plain_fp64,fp64,fp64_consistent,learned",
+                    help="comma list of ensemble forms to time")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
 
@@ -287,11 +291,12 @@ def run_ours(args):
 
     extra = {}
     if not args.no_extras:
-        if args.ensemble_systems > 0:
+        which = set(args.extras.split(","))
+        if args.ensemble_systems > 0 and "ensemble" in which:
             extra["ensemble"] = run_ensemble(lib, args, rank, dev)
-        if args.wh_steps > 0:
+        if args.wh_steps > 0 and "wh" in which:
             extra["wh"] = run_wh(lib, args)
-        if args.gr_years > 0:
+        if args.gr_years > 0 and "radau" in which:
             extra["radau_1009"] = run_radau_single(lib, args)
 
     if rank == 0:
@@ -331,14 +336,13 @@ def run_ours(args):
     return 0
 
 
-def _energy_errors(P0, V0, P1, V1, M, offs):
-    from oracle import Oracle
-    O = Oracle()
+def _energy_errors(lib, P0, V0, P1, V1, M, offs):
+    """Largest |dE/E| over the systems, energies from the library's FP64 energy kernel."""
     worst = 0.0
     for s in range(offs.size - 1):
         a, b = offs[s], offs[s + 1]
-        e0 = O.energy(P0[3 * a:3 * b], V0[3 * a:3 * b], M[a:b], G)
-        e1 = O.energy(P1[3 * a:3 * b], V1[3 * a:3 * b], M[a:b], G)
+        e0 = lib.energy(P0[3 * a:3 * b], V0[3 * a:3 * b], M[a:b], G)
+        e1 = lib.energy(P1[3 * a:3 * b], V1[3 * a:3 * b], M[a:b], G)
         worst = max(worst, abs((e1 - e0) / e0))
     return worst
 
@@ -346,29 +350,50 @@ def _energy_errors(P0, V0, P1, V1, M, offs):
 def run_ensemble(lib, args, rank, dev):
     """Radau15 over independent systems (4,096 systems per GPU of 4..13
     bodies: a 0.5..1.5 MSun star and 3..12 planets) for a bounded slice of
-    time.  Every rank draws its own systems (weak scaling)."""
+    time.  Every rank draws its own systems (weak scaling).
+
+    Forms: plain_fp64 = the reference's FP64 operations and predictor in the
+    batched kernel (the comparator); fp64 = 13-instruction pair terms, FMA
+    sweep; fp64_consistent = the same with g made consistent with the
+    predicted b; learned = that plus the BF16 network, trained online on
+    samples the ensemble records on a separate set of systems."""
+    import time as _t
+
+    from abie_gb300.learned import collect_samples, train_predictor
     P, V, M, offs = ics.ensemble(n_systems=args.ensemble_systems,
                                  seed0=D.ensemble_seed0(10000, rank, args.ensemble_systems))
     out = {"systems": int(offs.size - 1), "bodies": int(M.size), "years": args.ensemble_years}
-    base = None
-    for label, mode in (("fp64", "fp64"), ("plain_fp64", "exact")):
+    # online training on other systems
+    wanted = set(args.ensemble_forms.split(","))
+    if "learned" in wanted:
+        t0 = _t.perf_counter()
+        TP, TV, TM, toffs = ics.ensemble(n_systems=2048, seed0=900000 + 4096 * rank)
+        samples, _ = collect_samples(lib, TP, TV, TM, toffs, G, 1.0)
+        info = train_predictor(lib, samples, steps=1500, batch=2048, lr=1e-3)
+        out["training"] = {"systems": 2048, "years": 1.0, "samples": info["samples"],
+                           "seconds": _t.perf_counter() - t0, "holdout_loss": info["holdout_loss"],
+                           "holdout_loss_plain_guess": info["holdout_loss_plain"]}
+    forms = (("plain_fp64", "exact", {}), ("fp64", "fp64", {}),
+             ("fp64_consistent", "fp64", {"consistent": True}), ("learned", "fp64", {"learned": True}))
+    for label, mode, kw in forms:
+        if label not in wanted:
+            continue
         old = lib.set_force_mode(mode)
         lib.reset_counters()
-        res = lib.gr_ensemble(P, V, M, offs, G, 0.0, args.ensemble_years)
+        res = lib.gr_ensemble(P, V, M, offs, G, 0.0, args.ensemble_years, **kw)
         c = lib.counters()
         lib.set_force_mode(old)
         secs, steps = D.reduce_timing(res["seconds"], int(res["steps"].sum()), device=dev)
         rate = steps / secs if secs else None
         out[label] = {"system_steps": int(steps), "seconds": secs, "system_steps_per_s": rate,
                       "corrector_iterations_per_attempt": c["iterations"] / max(c["attempts"], 1),
-                      "max_abs_dE_over_E": _energy_errors(P, V, res["pos"], res["vel"], M, offs),
+                      "max_abs_dE_over_E": _energy_errors(lib, P, V, res["pos"], res["vel"], M, offs),
                       "failed_systems": int((res["status"] != 0).sum())}
-        if label == "fp64":
-            base = rate
-    if base and out["plain_fp64"]["system_steps_per_s"]:
-        out["speedup_fp64_vs_plain"] = base / out["plain_fp64"]["system_steps_per_s"]
-    out["note"] = ("plain_fp64 = the reference's FP64 operations (divisions, sqrt) in the same "
-                   "batched kernel; fp64 = reassociated FP64 pair terms and predictor")
+    lib.mlp_enable(False)
+    base = out.get("plain_fp64", {}).get("system_steps_per_s")
+    for label in ("fp64", "fp64_consistent", "learned"):
+        if base and label in out and out[label]["system_steps_per_s"]:
+            out[label]["speedup_vs_plain_fp64"] = out[label]["system_steps_per_s"] / base
     return out
 
 

@@ -114,6 +114,8 @@ typedef struct {
     long long kepler_failures;   /* WH Kepler solves that hit the iteration cap */
     long long wh_steps;
     double last_h;
+    long long learned_fallbacks; /* ensemble attempts redone from the plain guess after the
+                                    learned guess gave a non-finite state */
 } abie_counters;
 
 /* Last error message ("" when none). Returns its length. */
