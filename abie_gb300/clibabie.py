@@ -185,6 +185,13 @@ class CLibABIE(object):
         return {"pos": pos, "vel": vel, "t": t_out, "status": status, "steps": steps,
                 "seconds": self.lib.abie_last_ensemble_seconds()}
 
+    def measure_fp64_issue(self, active_lanes):
+        """FP64 FMA rate counted over whole warps with only active_lanes lanes working."""
+        v = _c.c_double(0)
+        self._check(self.lib.abie_measure_fp64_issue(_c.c_int(active_lanes), _c.byref(v)),
+                    "fp64 issue probe")
+        return v.value
+
     def measure_peaks(self):
         f64, f32 = _c.c_double(0), _c.c_double(0)
         self._check(self.lib.abie_measure_fp64_peak(_c.c_int(0), _c.byref(f64)), "fp64 probe")

@@ -6,11 +6,22 @@
 // system's 3N components and keeps their Radau state (y0, dy0, F1, b[7],
 // g[7], previous b6) in registers.  For the force, the predicted positions
 // go to shared memory and the pairs spread over the lanes: L = 32/N lanes
-// per sink, each summing every L-th source, partial sums added in lane
-// order (L = 1 and the reference's operations in the exact form).  The
+// per sink, each summing every L-th source, partial sums added as a fixed
+// tree (L = 1 and the reference's operations in the exact form).  The
 // sweep itself -- predictor, g/b updates, convergence test, step control,
 // refine_bs -- is the reference's (src/integrator_gauss_radau15.c:287-446)
-// component by component, as in the single-system engine.
+// component by component, as in the single-system engine.  The fast form
+// runs the corrector on the Newton-form coefficients g alone: predicted
+// positions come straight from g with tabulated weights, b = C g is formed
+// once per accepted step for refine_bs, and the next step starts from g
+// consistent with the refined guess.  Far fewer FP64 instructions per
+// substep (on this GPU each FP64 warp instruction holds the SM
+// sub-partition's FP64 pipe for ~64 cycles whatever the number of active
+// lanes, so the instruction count sets the time per substep), the same
+// converged solution, and fewer corrector iterations.
+//
+// Systems start longest first (shortest two-body time scale first), since
+// a batch lasts at least as long as its slowest system.
 //
 // Launches are bounded in time: a warp that has run past the launch's time
 // budget saves its system's state and leaves; the host launches again over
@@ -28,6 +39,9 @@ namespace abie {
 __constant__ double e_hs[8] = ABIE_RADAU_HS_INIT;
 __constant__ double e_rs[8][8] = ABIE_RADAU_RS_INIT;
 __constant__ double e_cs[8][8] = ABIE_RADAU_CS_INIT;
+__constant__ double e_rsp[8][8] = ABIE_RADAU_RSP_INIT;  // fast sweep: expanded g recurrence
+__constant__ double e_wg[9][7] = ABIE_RADAU_WG_INIT;    // fast sweep: position weights on g, row 8 = spacing 1
+__constant__ double e_vg[7] = ABIE_RADAU_VG_INIT;       // fast sweep: velocity weights on g at spacing 1
 
 static constexpr double EPSB = 1.e-4;
 static constexpr double FAC = 0.25;
@@ -36,6 +50,12 @@ static constexpr double H_MIN = 1.e-13;
 static constexpr int ENS_MAX_BODIES = 21;  // 3N <= 64: two components per lane
 static constexpr int WARPS = 4;            // warps per block
 static constexpr int STATE_PER_COMP = 18;  // y0 dy0 F1 b[7] g[7] b6p
+#ifndef ENS_BLOCKS_NC1
+#define ENS_BLOCKS_NC1 4  // blocks per SM the plain one-component variant is built for
+#endif
+#ifndef ENS_BLOCKS_NC2
+#define ENS_BLOCKS_NC2 2
+#endif
 
 struct EnsScalars {
     double t, h;
@@ -128,38 +148,57 @@ struct Comp {
     double y0, dy0, F1, b[7], g[7], b6p;
 };
 
+// Predicted position at spacing s = e_hs[row] (row 8: s = 1) of a step dt.
+// Exact form: the reference's Horner polynomial in b with its divisions.
+// Fast form: the same polynomial written on the Newton-form coefficients
+// g (b = C g), y0 + ds dy0 + hh (F1 + sum_j g_j W_j(s)) with the weights
+// W_j(s) = sum_{k<=j} cs[j][k] s^(k+1) / ((k+2)(k+3)/2) tabulated, and
+// ds = dt s, hh = ds^2 / 2 once per substep: 10 FP64 instructions, and b
+// is never needed inside the corrector.
 template <int MODE>
-__device__ __forceinline__ double e_pred_pos(const Comp &c, double s, double dt)
+__device__ __forceinline__ double e_pred_pos(const Comp &c, int row, double s, double dt, double ds,
+                                             double hh)
 {
     const double *b = c.b;
     if (MODE == ABIE_FORCE_EXACT)
         return c.y0 + dt * s * (c.dy0 + dt * s * (c.F1 + s * (b[0] / 0.3e1 + s * (b[1] / 0.6e1 + s * (b[2] / 0.10e2 + s * (b[3] / 0.15e2 + s * (b[4] / 0.21e2 + s * (b[5] / 0.28e2 + s * b[6] / 0.36e2))))))) / 0.2e1);
-    // same polynomial with the divisions as products by rounded reciprocals
-    double u = s * (b[6] * (1.0 / 36.0));
-    u = s * fma(b[5], 1.0 / 28.0, u);
-    u = s * fma(b[4], 1.0 / 21.0, u);
-    u = s * fma(b[3], 1.0 / 15.0, u);
-    u = s * fma(b[2], 1.0 / 10.0, u);
-    u = s * fma(b[1], 1.0 / 6.0, u);
-    u = s * fma(b[0], 1.0 / 3.0, u);
-    double ds = dt * s;
-    return fma(ds, fma(0.5 * ds, c.F1 + u, c.dy0), c.y0);
+    const double *w = e_wg[row];
+    const double *g = c.g;
+    double u = g[6] * w[6];
+    u = fma(g[5], w[5], u);
+    u = fma(g[4], w[4], u);
+    u = fma(g[3], w[3], u);
+    u = fma(g[2], w[2], u);
+    u = fma(g[1], w[1], u);
+    u = fma(g[0], w[0], u);
+    return fma(hh, c.F1 + u, fma(ds, c.dy0, c.y0));
 }
 
+// Predicted velocity at spacing 1 (the advance).
 template <int MODE>
-__device__ __forceinline__ double e_pred_vel(const Comp &c, double s, double dt)
+__device__ __forceinline__ double e_pred_vel(const Comp &c, double dt)
 {
     const double *b = c.b;
-    if (MODE == ABIE_FORCE_EXACT)
+    if (MODE == ABIE_FORCE_EXACT) {
+        const double s = 1.0;
         return c.dy0 + dt * s * (c.F1 + s * (b[0] / 0.2e1 + s * (b[1] / 0.3e1 + s * (b[2] / 0.4e1 + s * (b[3] / 0.5e1 + s * (b[4] / 0.6e1 + s * (b[5] / 0.7e1 + s * b[6] / 0.8e1)))))));
-    double u = s * (b[6] * 0.125);
-    u = s * fma(b[5], 1.0 / 7.0, u);
-    u = s * fma(b[4], 1.0 / 6.0, u);
-    u = s * fma(b[3], 0.2, u);
-    u = s * fma(b[2], 0.25, u);
-    u = s * fma(b[1], 1.0 / 3.0, u);
-    u = s * fma(b[0], 0.5, u);
-    return fma(dt * s, c.F1 + u, c.dy0);
+    }
+    const double *g = c.g;
+    double u = g[6] * e_vg[6];
+    u = fma(g[5], e_vg[5], u);
+    u = fma(g[4], e_vg[4], u);
+    u = fma(g[3], e_vg[3], u);
+    u = fma(g[2], e_vg[2], u);
+    u = fma(g[1], e_vg[1], u);
+    u = fma(g[0], e_vg[0], u);
+    return fma(dt, c.F1 + u, c.dy0);
+}
+
+// b6 of the corrector: b_6 = cs[6][6] g_6 = g_6, read from g in the fast form.
+template <int MODE>
+__device__ __forceinline__ double e_b6(const Comp &c)
+{
+    return MODE == ABIE_FORCE_EXACT ? c.b[6] : c.g[6];
 }
 
 // g and b after the force F of substep IH (src/integrator_gauss_radau15.c:136-241);
@@ -183,17 +222,53 @@ __device__ __forceinline__ void e_gb_update_ih(Comp &c, double F)
     }
 }
 
+// Fast form: only the new Newton coefficient, g_{IH-1} from the expanded
+// recurrence (F - F1) rsp[IH][0] - sum_{l<IH-1} g_l rsp[IH][l+1]; b is
+// formed from g once per accepted step (e_b_from_g).
+template <int IH>
+__device__ __forceinline__ void e_g_update_ih(Comp &c, double F)
+{
+    double v = (F - c.F1) * e_rsp[IH][0];
+#pragma unroll
+    for (int l = 1; l < IH; l++) v = fma(-c.g[l - 1], e_rsp[IH][l], v);
+    c.g[IH - 1] = v;
+}
+
 template <int MODE>
 __device__ __forceinline__ void e_gb_update(Comp &c, int ih, double F)
 {
+    if (MODE == ABIE_FORCE_EXACT) {
+        switch (ih) {
+        case 1: e_gb_update_ih<MODE, 1>(c, F); break;
+        case 2: e_gb_update_ih<MODE, 2>(c, F); break;
+        case 3: e_gb_update_ih<MODE, 3>(c, F); break;
+        case 4: e_gb_update_ih<MODE, 4>(c, F); break;
+        case 5: e_gb_update_ih<MODE, 5>(c, F); break;
+        case 6: e_gb_update_ih<MODE, 6>(c, F); break;
+        default: e_gb_update_ih<MODE, 7>(c, F); break;
+        }
+        return;
+    }
     switch (ih) {
-    case 1: e_gb_update_ih<MODE, 1>(c, F); break;
-    case 2: e_gb_update_ih<MODE, 2>(c, F); break;
-    case 3: e_gb_update_ih<MODE, 3>(c, F); break;
-    case 4: e_gb_update_ih<MODE, 4>(c, F); break;
-    case 5: e_gb_update_ih<MODE, 5>(c, F); break;
-    case 6: e_gb_update_ih<MODE, 6>(c, F); break;
-    default: e_gb_update_ih<MODE, 7>(c, F); break;
+    case 1: e_g_update_ih<1>(c, F); break;
+    case 2: e_g_update_ih<2>(c, F); break;
+    case 3: e_g_update_ih<3>(c, F); break;
+    case 4: e_g_update_ih<4>(c, F); break;
+    case 5: e_g_update_ih<5>(c, F); break;
+    case 6: e_g_update_ih<6>(c, F); break;
+    default: e_g_update_ih<7>(c, F); break;
+    }
+}
+
+// b_k = sum_{j>=k} cs[j][k] g_j for every k (fast form, at an accept).
+__device__ __forceinline__ void e_b_from_g(Comp &c)
+{
+#pragma unroll
+    for (int k = 0; k < 7; k++) {
+        double s = c.g[k];  // cs[k][k] = 1
+#pragma unroll
+        for (int j = k + 1; j < 7; j++) s = fma(e_cs[j][k], c.g[j], s);
+        c.b[k] = s;
     }
 }
 
@@ -248,22 +323,20 @@ __device__ __forceinline__ void warp_force(int n, const double (*sp)[4], double 
             else pair_fast(xi, yi, zi, s, ax, ay, az);
         }
     }
-    if (L > 1) {
-        const int base = (g < 32 ? g : 0) * L;
-        double sx = ax, sy = ay, sz = az;
-        for (int k = 1; k < L; k++) {
-            int src = base + k;
-            src = src < 32 ? src : 31;
-            double ox = __shfl_sync(0xffffffffu, ax, src);
-            double oy = __shfl_sync(0xffffffffu, ay, src);
-            double oz = __shfl_sync(0xffffffffu, az, src);
-            sx += ox;
-            sy += oy;
-            sz += oz;
+    // partial sums of the lanes of one sink that hold work (the first
+    // min(L, n)), added as a fixed tree: lane hh takes lane hh + o
+    const int W = L < n ? L : n;
+    for (int o = 1; o < W; o <<= 1) {
+        int src = lane + o;
+        src = src < 32 ? src : 31;
+        double ox = __shfl_sync(0xffffffffu, ax, src);
+        double oy = __shfl_sync(0xffffffffu, ay, src);
+        double oz = __shfl_sync(0xffffffffu, az, src);
+        if (hh + o < W) {
+            ax += ox;
+            ay += oy;
+            az += oz;
         }
-        ax = sx;
-        ay = sy;
-        az = sz;
     }
     if (g < n && hh == 0) {
         sa[g][0] = ax;
@@ -297,7 +370,8 @@ __device__ __forceinline__ void consistent_g(Comp &c)
 __device__ __forceinline__ void learned_refine(const EnsArgs &a, LearnSmem &L, Comp C[2], int n,
                                                int lane, bool has0, bool has1, double q, double h,
                                                double dtreq, const double *m, bool &pend_valid,
-                                               bool first_attempt, bool &net_guess)
+                                               bool first_attempt, bool &net_guess,
+                                               bool make_consistent)
 {
     double h_next = (dtreq / h > 1.0 / FAC) ? h / FAC : ((dtreq < 1.e-12) ? h * FAC : dtreq);
     if (h_next < H_MIN) h_next = H_MIN;
@@ -398,7 +472,7 @@ __device__ __forceinline__ void learned_refine(const EnsArgs &a, LearnSmem &L, C
         __syncwarp();
         net_guess = true;
     }
-    if (a.consistent_g) {
+    if (make_consistent) {
         if (has0) consistent_g(C[0]);
         if (has1) consistent_g(C[1]);
     }
@@ -419,8 +493,14 @@ __device__ __forceinline__ void restore_plain_guess(LearnSmem &L, Comp C[2], int
     }
 }
 
-template <int MODE, int NC>
-__global__ void __launch_bounds__(32 * WARPS, NC == 1 ? 4 : 2) ensemble_kernel(EnsArgs a)
+// Blocks per SM the register budget is sized for, per variant.
+template <int NC, bool LEARN>
+struct EnsOccupancy {
+    static constexpr int value = LEARN ? (NC == 1 ? 4 : 2) : (NC == 1 ? ENS_BLOCKS_NC1 : ENS_BLOCKS_NC2);
+};
+
+template <int MODE, int NC, bool LEARN>
+__global__ void __launch_bounds__(32 * WARPS, (EnsOccupancy<NC, LEARN>::value)) ensemble_kernel(EnsArgs a)
 {
     __shared__ double s_pos[WARPS][32][4];
     __shared__ double s_acc[WARPS][32][3];
@@ -535,7 +615,7 @@ __global__ void __launch_bounds__(32 * WARPS, NC == 1 ? 4 : 2) ensemble_kernel(E
         int loop_count = S.loop_count;
         bool done = false;
         // learned predictor: pending training sample, first attempt after an accept
-        const bool learn = (a.mlp != nullptr || a.samples != nullptr) && n <= LP_ROWS;
+        const bool learn = LEARN && (a.mlp != nullptr || a.samples != nullptr) && n <= LP_ROWS;
         bool pend_valid = false, first_attempt = false;
         bool net_guess = false;  // this attempt started from the network's guess
         while (!done) {
@@ -546,7 +626,9 @@ __global__ void __launch_bounds__(32 * WARPS, NC == 1 ? 4 : 2) ensemble_kernel(E
                 double f8 = -1.7976931348623157e308, db6 = f8;
                 for (int ih = 1; ih < 8; ih++) {
                     __syncwarp();
-                    publish(e_pred_pos<MODE>(C[0], e_hs[ih], h), e_pred_pos<MODE>(C[1], e_hs[ih], h));
+                    const double sh = e_hs[ih], ds = h * sh, hh = 0.5 * ds * ds;
+                    publish(e_pred_pos<MODE>(C[0], ih, sh, h, ds, hh),
+                            e_pred_pos<MODE>(C[1], ih, sh, h, ds, hh));
                     warp_force<MODE>(n, sp, sa, lane, L);
 #pragma unroll
                     for (int u = 0; u < 2; u++) {
@@ -555,7 +637,7 @@ __global__ void __launch_bounds__(32 * WARPS, NC == 1 ? 4 : 2) ensemble_kernel(E
                         e_gb_update<MODE>(C[u], ih, F);
                         if (ih == 7) {
                             f8 = fmax(f8, absmax_or_none(F));
-                            db6 = fmax(db6, absmax_or_none(C[u].b[6] - C[u].b6p));
+                            db6 = fmax(db6, absmax_or_none(e_b6<MODE>(C[u]) - C[u].b6p));
                         }
                     }
                 }
@@ -564,14 +646,16 @@ __global__ void __launch_bounds__(32 * WARPS, NC == 1 ? 4 : 2) ensemble_kernel(E
                 db6 = warp_maxd(db6);
                 if (db6 / f8 < TOLPC) break;
 #pragma unroll
-                for (int u = 0; u < 2; u++) C[u].b6p = C[u].b[6];
+                for (int u = 0; u < 2; u++) C[u].b6p = e_b6<MODE>(C[u]);
             }
             S.iterations += iters;
             S.attempts++;
             // advance
             __syncwarp();
-            double ya0 = e_pred_pos<MODE>(C[0], 1.0, h), ya1 = e_pred_pos<MODE>(C[1], 1.0, h);
-            double va0 = e_pred_vel<MODE>(C[0], 1.0, h), va1 = e_pred_vel<MODE>(C[1], 1.0, h);
+            const double hh1 = 0.5 * h * h;
+            double ya0 = e_pred_pos<MODE>(C[0], 8, 1.0, h, h, hh1),
+                   ya1 = e_pred_pos<MODE>(C[1], 8, 1.0, h, h, hh1);
+            double va0 = e_pred_vel<MODE>(C[0], h), va1 = e_pred_vel<MODE>(C[1], h);
             publish(ya0, ya1);
             warp_force<MODE>(n, sp, sa, lane, L);
             S.force_calls++;
@@ -592,11 +676,11 @@ __global__ void __launch_bounds__(32 * WARPS, NC == 1 ? 4 : 2) ensemble_kernel(E
             }
             double mb6 = -1.7976931348623157e308, mdd = mb6;
             if (has0) {
-                mb6 = absmax_or_none(C[0].b[6]);
+                mb6 = absmax_or_none(e_b6<MODE>(C[0]));
                 mdd = absmax_or_none(dd0);
             }
             if (has1) {
-                mb6 = fmax(mb6, absmax_or_none(C[1].b[6]));
+                mb6 = fmax(mb6, absmax_or_none(e_b6<MODE>(C[1])));
                 mdd = fmax(mdd, absmax_or_none(dd1));
             }
             mb6 = warp_maxd(mb6);
@@ -626,6 +710,10 @@ __global__ void __launch_bounds__(32 * WARPS, NC == 1 ? 4 : 2) ensemble_kernel(E
                     stop = true;
                 }
                 double q = dtreq / h;
+                if (MODE != ABIE_FORCE_EXACT) {  // the fast form carries g only
+                    e_b_from_g(C[0]);
+                    e_b_from_g(C[1]);
+                }
                 C[0].y0 = ya0;
                 C[0].dy0 = va0;
                 C[0].F1 = dd0;
@@ -634,13 +722,15 @@ __global__ void __launch_bounds__(32 * WARPS, NC == 1 ? 4 : 2) ensemble_kernel(E
                 C[1].dy0 = va1;
                 C[1].F1 = dd1;
                 C[1].b6p = C[1].b[6];
+                // the fast form always continues from g consistent with the guess
+                const bool make_consistent = a.consistent_g || MODE != ABIE_FORCE_EXACT;
                 if (!stop && learn) {
                     learned_refine(a, LS, C, n, lane, has0, has1, q, h, dtreq, m, pend_valid,
-                                   first_attempt, net_guess);
+                                   first_attempt, net_guess, make_consistent);
                 } else if (!stop) {
                     e_refine(C[0], q);
                     e_refine(C[1], q);
-                    if (a.consistent_g) {
+                    if (make_consistent) {
                         consistent_g(C[0]);
                         consistent_g(C[1]);
                     }
@@ -694,27 +784,30 @@ static size_t learn_smem(const EnsArgs &a)
     return (a.mlp || a.samples) ? WARPS * sizeof(LearnSmem) : 0;
 }
 
-static int launch_ensemble(int mode, int nc, int blocks, const EnsArgs &a, cudaStream_t st)
+template <int MODE, bool LEARN>
+static const void *ensemble_fn_l(int nc)
 {
-    size_t dyn = learn_smem(a);
-    if (mode == ABIE_FORCE_EXACT) {
-        if (nc == 1) ensemble_kernel<ABIE_FORCE_EXACT, 1><<<blocks, 32 * WARPS, dyn, st>>>(a);
-        else ensemble_kernel<ABIE_FORCE_EXACT, 2><<<blocks, 32 * WARPS, dyn, st>>>(a);
-    } else {
-        if (nc == 1) ensemble_kernel<ABIE_FORCE_FP64, 1><<<blocks, 32 * WARPS, dyn, st>>>(a);
-        else ensemble_kernel<ABIE_FORCE_FP64, 2><<<blocks, 32 * WARPS, dyn, st>>>(a);
-    }
-    ABIE_CUDA(cudaGetLastError());
-    return 0;
+    return nc == 1 ? (const void *)ensemble_kernel<MODE, 1, LEARN>
+                   : (const void *)ensemble_kernel<MODE, 2, LEARN>;
 }
 
-static const void *ensemble_fn(int mode, int nc)
+// The kernel for a force form, components per lane and whether the learned
+// predictor (or sample collection) is in use: without it the variant leaves
+// the predictor's code out and fits more warps per SM.
+static const void *ensemble_fn(int mode, int nc, bool learn)
 {
     if (mode == ABIE_FORCE_EXACT)
-        return nc == 1 ? (const void *)ensemble_kernel<ABIE_FORCE_EXACT, 1>
-                       : (const void *)ensemble_kernel<ABIE_FORCE_EXACT, 2>;
-    return nc == 1 ? (const void *)ensemble_kernel<ABIE_FORCE_FP64, 1>
-                   : (const void *)ensemble_kernel<ABIE_FORCE_FP64, 2>;
+        return learn ? ensemble_fn_l<ABIE_FORCE_EXACT, true>(nc) : ensemble_fn_l<ABIE_FORCE_EXACT, false>(nc);
+    return learn ? ensemble_fn_l<ABIE_FORCE_FP64, true>(nc) : ensemble_fn_l<ABIE_FORCE_FP64, false>(nc);
+}
+
+static int launch_ensemble(int mode, int nc, int blocks, const EnsArgs &a, cudaStream_t st)
+{
+    const bool learn = a.mlp || a.samples;
+    size_t dyn = learn ? WARPS * sizeof(LearnSmem) : 0;
+    void *args[] = {const_cast<EnsArgs *>(&a)};
+    ABIE_CUDA(cudaLaunchKernel(ensemble_fn(mode, nc, learn), dim3(blocks), dim3(32 * WARPS), args, dyn, st));
+    return 0;
 }
 
 static cudaStream_t g_ens_stream2 = nullptr;
@@ -752,8 +845,29 @@ int ensemble_run(double *pos, double *vel, const double *m, const long long *off
         memset(&sc[s], 0, sizeof(EnsScalars));
         sc[s].t = t0;
     }
+    // Longest-first order: a system's step count follows its shortest
+    // two-body time scale sqrt(r_ij^3 / G(m_i + m_j)), and the batch takes
+    // at least as long as its slowest system, so those start first.
+    std::vector<double> rate(ns, 0.0);
+    {
+        std::vector<double> hp(3 * (size_t)total), hm(m, m + total);
+        memcpy(hp.data(), pos, 3 * total * sizeof(double));
+        for (int s = 0; s < ns; s++) {
+            double best = 0.0;
+            for (long long i = offsets[s]; i < offsets[s + 1]; i++)
+                for (long long j = i + 1; j < offsets[s + 1]; j++) {
+                    double mu = G * (std::max(hm[i], 0.0) + std::max(hm[j], 0.0));
+                    double dx = hp[3 * i] - hp[3 * j], dy = hp[3 * i + 1] - hp[3 * j + 1],
+                           dz = hp[3 * i + 2] - hp[3 * j + 2];
+                    double r2 = dx * dx + dy * dy + dz * dz;
+                    if (mu > 0.0 && r2 > 0.0) best = std::max(best, sqrt(mu / (r2 * sqrt(r2))));
+                }
+            rate[s] = best;
+        }
+    }
     std::vector<int> active(ns);
     for (int s = 0; s < ns; s++) active[s] = s;
+    std::stable_sort(active.begin(), active.end(), [&](int x, int y) { return rate[x] > rate[y]; });
     ABIE_CUDA(cudaMemcpyAsync(d_pos, pos, 3 * total * sizeof(double), cudaMemcpyHostToDevice, st));
     ABIE_CUDA(cudaMemcpyAsync(d_vel, vel, 3 * total * sizeof(double), cudaMemcpyHostToDevice, st));
     ABIE_CUDA(cudaMemcpyAsync(d_m, m, total * sizeof(double), cudaMemcpyHostToDevice, st));
@@ -765,9 +879,10 @@ int ensemble_run(double *pos, double *vel, const double *m, const long long *off
     const size_t dyn = learning ? WARPS * sizeof(LearnSmem) : 0;
     int bps[2] = {1, 1};
     for (int k = 0; k < 2; k++) {
-        const void *fn = ensemble_fn(mode, k + 1);
-        ABIE_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)(WARPS * sizeof(LearnSmem))));
+        const void *fn = ensemble_fn(mode, k + 1, learning);
+        if (learning)
+            ABIE_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)(WARPS * sizeof(LearnSmem))));
         ABIE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps[k], fn, 32 * WARPS, dyn));
         bps[k] = std::max(bps[k], 1);
     }
@@ -832,8 +947,10 @@ int ensemble_run(double *pos, double *vel, const double *m, const long long *off
         launches++;
         ABIE_CUDA(cudaMemcpy(sc.data(), d_sc, ns * sizeof(EnsScalars), cudaMemcpyDeviceToHost));
         int k = 0;
-        for (int s2 = 0; s2 < ns; s2++)
+        for (int q = 0; q < n_active; q++) {  // keeps the longest-first order
+            const int s2 = active[q];
             if (sc[s2].phase != 2 && sc[s2].status == 0) active[k++] = s2;
+        }
         n_active = k;
     }
     cudaEventDestroy(ej);

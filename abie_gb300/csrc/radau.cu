@@ -33,6 +33,9 @@ namespace abie {
 __constant__ double c_hs[8] = ABIE_RADAU_HS_INIT;
 __constant__ double c_rs[8][8] = ABIE_RADAU_RS_INIT;
 __constant__ double c_cs[8][8] = ABIE_RADAU_CS_INIT;
+__constant__ double c_rsp[8][8] = ABIE_RADAU_RSP_INIT;  // fast form: expanded g recurrence
+__constant__ double c_wg[9][7] = ABIE_RADAU_WG_INIT;    // fast form: position weights on g
+__constant__ double c_vg[7] = ABIE_RADAU_VG_INIT;       // fast form: velocity weights on g at spacing 1
 
 static constexpr double EPSB = 1.e-4;    // src/integrator_gauss_radau15.h:58
 static constexpr double FAC = 0.25;      // :59
@@ -132,9 +135,11 @@ __device__ __forceinline__ Src load_src(const Src *p)
     return s;
 }
 
-// Acceleration of sink j from the published sources.  EXACT: one lane, the
-// reference's order and operations.  Otherwise JS lanes split the sources
-// and meet in a shuffle butterfly.
+// Acceleration of sink j from the published sources, returned to every
+// lane of the sink's group.  EXACT: lane 0 alone, in the reference's order
+// and operations, then broadcast.  Otherwise the JS lanes split the sources
+// and meet in a shuffle butterfly.  All 32 lanes of the warp call this
+// together (the sink loops are warp-uniform).
 template <int MODE, int JS>
 __device__ __forceinline__ void sink_accel(const EngineArgs &a, int j, const Src *src, double xj,
                                            double yj, double zj, int lane, double &ax, double &ay,
@@ -144,9 +149,16 @@ __device__ __forceinline__ void sink_accel(const EngineArgs &a, int j, const Src
     ay = 0.0;
     az = 0.0;
     if (MODE == ABIE_FORCE_EXACT) {
-        for (int q = 0; q < a.n_src; q++) {
-            if (a.src_body[q] == j) continue;
-            pair_exact(xj, yj, zj, load_src(src + q), ax, ay, az);
+        if (lane == 0) {
+            for (int q = 0; q < a.n_src; q++) {
+                if (a.src_body[q] == j) continue;
+                pair_exact(xj, yj, zj, load_src(src + q), ax, ay, az);
+            }
+        }
+        if (JS > 1) {
+            ax = __shfl_sync(0xffffffffu, ax, 0, JS);
+            ay = __shfl_sync(0xffffffffu, ay, 0, JS);
+            az = __shfl_sync(0xffffffffu, az, 0, JS);
         }
     } else {
         int q = lane;
@@ -167,89 +179,176 @@ __device__ __forceinline__ void sink_accel(const EngineArgs &a, int j, const Src
     }
 }
 
-// Predictor (src/integrator_gauss_radau15.c:122-134): spacing s, step dt.
-// The exact form keeps the reference's divisions by constants; the fast
-// form multiplies by the rounded reciprocals (about one tenth of the FP64
-// work, results within an ulp or two).
+// f[c] without a dynamically indexed local array.
+__device__ __forceinline__ double pick3(const double f[3], int c)
+{
+    return c == 0 ? f[0] : (c == 1 ? f[1] : f[2]);
+}
+
+// Components of a body handled by a lane of its group: with JS >= 4 lanes
+// 0, 1, 2 take x, y, z; with JS == 1 the single lane takes all three.
+template <int JS>
+__device__ __forceinline__ int comp_lo(int lane) { return JS >= 4 ? lane : 0; }
+template <int JS>
+__device__ __forceinline__ int comp_hi(int lane) { return JS >= 4 ? (lane < 3 ? lane + 1 : 0) : 3; }
+
+// Predicted position of component i at spacing s = c_hs[row] (row 8:
+// s = 1) of a step dt (src/integrator_gauss_radau15.c:122-134).  Exact
+// form: the reference's Horner polynomial in b with its divisions by
+// constants.  Fast form: the same polynomial on the Newton-form
+// coefficients g (b = C g), y0 + ds dy0 + hh (F1 + sum_j g_j W_j(s)), the
+// weights tabulated and ds = dt s, hh = ds^2 / 2 computed once per substep
+// (10 FP64 instructions instead of 19, and b is not needed in the corrector).
 template <int MODE>
-__device__ __forceinline__ double pred_pos(const EngineArgs &a, int i, double s, double dt)
+__device__ __forceinline__ double pred_pos(const EngineArgs &a, int i, int row, double s, double dt,
+                                           double ds, double hh)
 {
     const int d = a.dim;
-    const double *b = a.b;
-    if (MODE == ABIE_FORCE_EXACT)
+    if (MODE == ABIE_FORCE_EXACT) {
+        const double *b = a.b;
         return a.y0[i] + dt * s * (a.dy0[i] + dt * s * (a.F1[i] + s * (b[i] / 0.3e1 + s * (b[d + i] / 0.6e1 + s * (b[2 * d + i] / 0.10e2 + s * (b[3 * d + i] / 0.15e2 + s * (b[4 * d + i] / 0.21e2 + s * (b[5 * d + i] / 0.28e2 + s * b[6 * d + i] / 0.36e2))))))) / 0.2e1);
-    double u = s * (b[6 * d + i] * (1.0 / 36.0));
-    u = s * fma(b[5 * d + i], 1.0 / 28.0, u);
-    u = s * fma(b[4 * d + i], 1.0 / 21.0, u);
-    u = s * fma(b[3 * d + i], 1.0 / 15.0, u);
-    u = s * fma(b[2 * d + i], 1.0 / 10.0, u);
-    u = s * fma(b[d + i], 1.0 / 6.0, u);
-    u = s * fma(b[i], 1.0 / 3.0, u);
-    double ds = dt * s;
-    return fma(ds, fma(0.5 * ds, a.F1[i] + u, a.dy0[i]), a.y0[i]);
+    }
+    const double *g = a.g;
+    const double *w = c_wg[row];
+    double u = g[6 * d + i] * w[6];
+    u = fma(g[5 * d + i], w[5], u);
+    u = fma(g[4 * d + i], w[4], u);
+    u = fma(g[3 * d + i], w[3], u);
+    u = fma(g[2 * d + i], w[2], u);
+    u = fma(g[d + i], w[1], u);
+    u = fma(g[i], w[0], u);
+    return fma(hh, a.F1[i] + u, fma(ds, a.dy0[i], a.y0[i]));
 }
 
+// Predicted velocity at spacing 1 (the advance).
 template <int MODE>
-__device__ __forceinline__ double pred_vel(const EngineArgs &a, int i, double s, double dt)
+__device__ __forceinline__ double pred_vel(const EngineArgs &a, int i, double dt)
 {
     const int d = a.dim;
-    const double *b = a.b;
-    if (MODE == ABIE_FORCE_EXACT)
+    if (MODE == ABIE_FORCE_EXACT) {
+        const double *b = a.b;
+        const double s = 1.0;
         return a.dy0[i] + dt * s * (a.F1[i] + s * (b[i] / 0.2e1 + s * (b[d + i] / 0.3e1 + s * (b[2 * d + i] / 0.4e1 + s * (b[3 * d + i] / 0.5e1 + s * (b[4 * d + i] / 0.6e1 + s * (b[5 * d + i] / 0.7e1 + s * b[6 * d + i] / 0.8e1)))))));
-    double u = s * (b[6 * d + i] * 0.125);
-    u = s * fma(b[5 * d + i], 1.0 / 7.0, u);
-    u = s * fma(b[4 * d + i], 1.0 / 6.0, u);
-    u = s * fma(b[3 * d + i], 0.2, u);
-    u = s * fma(b[2 * d + i], 0.25, u);
-    u = s * fma(b[d + i], 1.0 / 3.0, u);
-    u = s * fma(b[i], 0.5, u);
-    return fma(dt * s, a.F1[i] + u, a.dy0[i]);
+    }
+    const double *g = a.g;
+    double u = g[6 * d + i] * c_vg[6];
+    u = fma(g[5 * d + i], c_vg[5], u);
+    u = fma(g[4 * d + i], c_vg[4], u);
+    u = fma(g[3 * d + i], c_vg[3], u);
+    u = fma(g[2 * d + i], c_vg[2], u);
+    u = fma(g[d + i], c_vg[1], u);
+    u = fma(g[i], c_vg[0], u);
+    return fma(dt, a.F1[i] + u, a.dy0[i]);
 }
 
-// Predicted position of body j at spacing s into yp, and into the source
-// list when j is massive.
+// The corrector's b6 (b_6 = cs[6][6] g_6 = g_6: read from g in the fast form).
 template <int MODE>
-__device__ __forceinline__ void publish_body(const EngineArgs &a, int j, double s, double dt,
-                                             double *yp, Src *src)
+__device__ __forceinline__ double b6_at(const EngineArgs &a, int i)
 {
-    double p0 = pred_pos<MODE>(a, 3 * j, s, dt);
-    double p1 = pred_pos<MODE>(a, 3 * j + 1, s, dt);
-    double p2 = pred_pos<MODE>(a, 3 * j + 2, s, dt);
-    yp[3 * j] = p0;
-    yp[3 * j + 1] = p1;
-    yp[3 * j + 2] = p2;
-    int slot = a.src_slot[j];
+    return MODE == ABIE_FORCE_EXACT ? a.b[6 * a.dim + i] : a.g[6 * a.dim + i];
+}
+
+// Predicted component c of body j into yp, and into the source list when j
+// is massive (lane of component 0 also writes G m).
+template <int MODE>
+__device__ __forceinline__ void publish_comp(const EngineArgs &a, int j, int c, int row, double s,
+                                             double dt, double ds, double hh, double *yp, Src *src)
+{
+    const int i = 3 * j + c;
+    const double p = pred_pos<MODE>(a, i, row, s, dt, ds, hh);
+    yp[i] = p;
+    const int slot = a.src_slot[j];
     if (slot >= 0) {
-        Src v;
-        v.x = p0;
-        v.y = p1;
-        v.z = p2;
-        v.gm = a.G * a.m[j];
-        src[slot] = v;
+        double *rec = reinterpret_cast<double *>(src + slot);
+        rec[c] = p;
+        if (c == 0) rec[3] = a.G * a.m[j];
     }
 }
 
-// g and b after the force F at substep ih (1..7) for component i
-// (src/integrator_gauss_radau15.c:136-241; only g[ih-1] is new, the lower g
-// the reference recomputes are bitwise the stored ones).
-template <int MODE>
-__device__ __forceinline__ void gb_update(const EngineArgs &a, int i, int ih, double F)
+// Exact form: g and b after the force F at substep IH (1..7) for component
+// i (src/integrator_gauss_radau15.c:136-241; only g[IH-1] is new, the lower
+// g the reference recomputes are bitwise the stored ones), in the
+// reference's order and roundings.  Fast form: only g[IH-1], from the
+// expanded recurrence (F - F1) rsp[IH][0] - sum_{l<IH-1} g_l rsp[IH][l+1];
+// b is formed from g once per accepted step.  One static variant per
+// substep keeps every index a constant.
+template <int MODE, int IH>
+__device__ __forceinline__ void gb_update_ih(const EngineArgs &a, int i, double F)
 {
     const int d = a.dim;
     double *g = a.g;
-    double v = (F - a.F1[i]) * c_rs[ih][0];
-    for (int l = 1; l < ih; l++) v = (v - g[(l - 1) * d + i]) * c_rs[ih][l];
-    g[(ih - 1) * d + i] = v;
-    double gl[7];
+    if (MODE == ABIE_FORCE_EXACT) {
+        double gl[7];
 #pragma unroll
-    for (int k = 0; k < 7; k++) gl[k] = (k == ih - 1) ? v : g[k * d + i];
-    for (int k = 0; k < ih; k++) {
-        double s = c_cs[k][k] * gl[k];
-        for (int jj = k + 1; jj < 7; jj++) {
-            if (MODE == ABIE_FORCE_EXACT) s = s + c_cs[jj][k] * gl[jj];  // reference roundings
-            else s = fma(c_cs[jj][k], gl[jj], s);
+        for (int k = 0; k < 7; k++) gl[k] = g[k * d + i];
+        double v = (F - a.F1[i]) * c_rs[IH][0];
+#pragma unroll
+        for (int l = 1; l < IH; l++) v = (v - gl[l - 1]) * c_rs[IH][l];
+        g[(IH - 1) * d + i] = v;
+        gl[IH - 1] = v;
+#pragma unroll
+        for (int k = 0; k < IH; k++) {
+            double s = c_cs[k][k] * gl[k];
+#pragma unroll
+            for (int jj = k + 1; jj < 7; jj++) s = s + c_cs[jj][k] * gl[jj];  // reference roundings
+            a.b[k * d + i] = s;
         }
-        a.b[k * d + i] = s;
+        return;
+    }
+    double v = (F - a.F1[i]) * c_rsp[IH][0];
+#pragma unroll
+    for (int l = 1; l < IH; l++) v = fma(-g[(l - 1) * d + i], c_rsp[IH][l], v);
+    g[(IH - 1) * d + i] = v;
+}
+
+template <int MODE>
+__device__ __forceinline__ void gb_update(const EngineArgs &a, int i, int ih, double F)
+{
+    switch (ih) {
+    case 1: gb_update_ih<MODE, 1>(a, i, F); break;
+    case 2: gb_update_ih<MODE, 2>(a, i, F); break;
+    case 3: gb_update_ih<MODE, 3>(a, i, F); break;
+    case 4: gb_update_ih<MODE, 4>(a, i, F); break;
+    case 5: gb_update_ih<MODE, 5>(a, i, F); break;
+    case 6: gb_update_ih<MODE, 6>(a, i, F); break;
+    default: gb_update_ih<MODE, 7>(a, i, F); break;
+    }
+}
+
+// Fast form at an accepted step: b = C g, the previous-b6 record, the
+// reference's refine_bs guess E(q), and g = C^-1 E so that the next step's
+// corrector starts from the polynomial the guess describes.
+__device__ __forceinline__ void refine_g(const EngineArgs &a, int i, double q, bool last)
+{
+    const int d = a.dim;
+    double gl[7], b[7];
+#pragma unroll
+    for (int k = 0; k < 7; k++) gl[k] = a.g[k * d + i];
+#pragma unroll
+    for (int k = 0; k < 7; k++) {
+        double s = gl[k];  // cs[k][k] = 1
+#pragma unroll
+        for (int j = k + 1; j < 7; j++) s = fma(c_cs[j][k], gl[j], s);
+        b[k] = s;
+    }
+    a.b6p[i] = b[6];
+    if (last) return;
+    double q2 = q * q, q3 = q2 * q, q4 = q2 * q2, q5 = q2 * q3, q6 = q3 * q3, q7 = q2 * q5;
+    double e[7];
+    e[0] = q * (b[6] * 7.0 + b[5] * 6.0 + b[4] * 5.0 + b[3] * 4.0 + b[2] * 3.0 + b[1] * 2.0 + b[0]);
+    e[1] = q2 * (b[6] * 21.0 + b[5] * 15.0 + b[4] * 10.0 + b[3] * 6.0 + b[2] * 3.0 + b[1]);
+    e[2] = q3 * (b[6] * 35.0 + b[5] * 20.0 + b[4] * 10.0 + b[3] * 4.0 + b[2]);
+    e[3] = q4 * (b[6] * 35.0 + b[5] * 15.0 + b[4] * 5.0 + b[3]);
+    e[4] = q5 * (b[6] * 21.0 + b[5] * 6.0 + b[4]);
+    e[5] = q6 * (b[6] * 7.0 + b[5]);
+    e[6] = q7 * b[6];
+#pragma unroll
+    for (int k = 6; k >= 0; k--) {
+        double v = e[k];
+#pragma unroll
+        for (int j = k + 1; j < 7; j++) v -= c_cs[j][k] * gl[j];
+        gl[k] = v;
+        a.g[k * d + i] = v;
     }
 }
 
@@ -392,6 +491,11 @@ __global__ void __launch_bounds__(256) radau_engine(EngineArgs a)
     const bool leader = (blockIdx.x == 0 && threadIdx.x == 0);
     const long long T = a.timeout_ns;
     const int n = a.n;
+    // sink loops run to a multiple of the groups in a warp, so every lane of
+    // a warp takes part in each iteration's shuffles; jj >= n is a dummy
+    const int gpw = 32 / JS;
+    const int n_loop = (n + gpw - 1) / gpw * gpw;
+    const int c0 = comp_lo<JS>(lane), c1 = comp_hi<JS>(lane);
 
     double t, h;
     int loop_count, pc, red_idx;
@@ -400,20 +504,19 @@ __global__ void __launch_bounds__(256) radau_engine(EngineArgs a)
     if (ctl->phase == 0) {
         // --- F1 = f(y0): publish y0 (spacing 0 gives y0 exactly), then force
         for (int j = gid; j < n; j += ngroups)
-            if (lane == 0) publish_body<MODE>(a, j, 0.0, 0.0, a.yp[0], a.src[0]);
+            for (int c = c0; c < c1; c++)
+                publish_comp<MODE>(a, j, c, 0, 0.0, 0.0, 0.0, 0.0, a.yp[0], a.src[0]);
         if (!grid_sync(ctl, T)) return;
-        for (int j = gid; j < n; j += ngroups) {
-            double ax, ay, az;
+        for (int jj = gid; jj < n_loop; jj += ngroups) {
+            const bool live = jj < n;
+            const int j = live ? jj : n - 1;
+            double f[3];
             sink_accel<MODE, JS>(a, j, a.src[0], a.y0[3 * j], a.y0[3 * j + 1], a.y0[3 * j + 2],
-                                 lane, ax, ay, az);
-            if (lane == 0) {
-                bool live = a.m[j] >= 0.0;
-                double e0 = a.ext ? a.ext[3 * j] : 0.0, e1 = a.ext ? a.ext[3 * j + 1] : 0.0,
-                       e2 = a.ext ? a.ext[3 * j + 2] : 0.0;
-                a.F1[3 * j] = (live ? ax : 0.0) + e0;
-                a.F1[3 * j + 1] = (live ? ay : 0.0) + e1;
-                a.F1[3 * j + 2] = (live ? az : 0.0) + e2;
-            }
+                                 lane, f[0], f[1], f[2]);
+            if (!live) continue;
+            const bool alive = a.m[j] >= 0.0;
+            for (int c = c0; c < c1; c++)
+                a.F1[3 * j + c] = (alive ? pick3(f, c) : 0.0) + (a.ext ? a.ext[3 * j + c] : 0.0);
         }
         if (leader) ctl->force_calls++;
         if (!grid_sync(ctl, T)) return;
@@ -433,29 +536,31 @@ __global__ void __launch_bounds__(256) radau_engine(EngineArgs a)
         double dt0 = (d0 < 1e-5 || d1 < 1e-5) ? 1e-6 : 0.01 * (d0 / d1);
         // Euler probe y1 = y0 + dt0 dy0 into yp[1] / src[1]
         for (int j = gid; j < n; j += ngroups) {
-            if (lane != 0) continue;
-            double p[3];
-            for (int c = 0; c < 3; c++) {
-                p[c] = a.y0[3 * j + c] + dt0 * a.dy0[3 * j + c];
-                a.yp[1][3 * j + c] = p[c];
+            const int slot = a.src_slot[j];
+            for (int c = c0; c < c1; c++) {
+                const double p = a.y0[3 * j + c] + dt0 * a.dy0[3 * j + c];
+                a.yp[1][3 * j + c] = p;
+                if (slot >= 0) {
+                    double *rec = reinterpret_cast<double *>(a.src[1] + slot);
+                    rec[c] = p;
+                    if (c == 0) rec[3] = a.G * a.m[j];
+                }
             }
-            int slot = a.src_slot[j];
-            if (slot >= 0) a.src[1][slot] = Src{p[0], p[1], p[2], a.G * a.m[j]};
         }
         if (!grid_sync(ctl, T)) return;
         unsigned long long k2 = 0;
-        for (int j = gid; j < n; j += ngroups) {
-            double ax, ay, az;
+        for (int jj = gid; jj < n_loop; jj += ngroups) {
+            const bool live = jj < n;
+            const int j = live ? jj : n - 1;
+            double f[3];
             sink_accel<MODE, JS>(a, j, a.src[1], a.yp[1][3 * j], a.yp[1][3 * j + 1],
-                                 a.yp[1][3 * j + 2], lane, ax, ay, az);
-            if (lane == 0) {
-                bool live = a.m[j] >= 0.0;
-                double f[3] = {live ? ax : 0.0, live ? ay : 0.0, live ? az : 0.0};
-                for (int c = 0; c < 3; c++) {
-                    double fi = f[c] + (a.ext ? a.ext[3 * j + c] : 0.0);
-                    unsigned long long u = absmax_key(fi - a.F1[3 * j + c]);
-                    k2 = u > k2 ? u : k2;
-                }
+                                 a.yp[1][3 * j + 2], lane, f[0], f[1], f[2]);
+            if (!live) continue;
+            const bool alive = a.m[j] >= 0.0;
+            for (int c = c0; c < c1; c++) {
+                double fi = (alive ? pick3(f, c) : 0.0) + (a.ext ? a.ext[3 * j + c] : 0.0);
+                unsigned long long u = absmax_key(fi - a.F1[3 * j + c]);
+                k2 = u > k2 ? u : k2;
             }
         }
         if (leader) ctl->force_calls++;
@@ -472,8 +577,12 @@ __global__ void __launch_bounds__(256) radau_engine(EngineArgs a)
         loop_count = 0;
         pc = 0;
         // first attempt's substep-1 prediction
-        for (int j = gid; j < n; j += ngroups)
-            if (lane == 0) publish_body<MODE>(a, j, c_hs[1], h, a.yp[pc & 1], a.src[pc & 1]);
+        {
+            const double ds = h * c_hs[1], hh = 0.5 * ds * ds;
+            for (int j = gid; j < n; j += ngroups)
+                for (int c = c0; c < c1; c++)
+                    publish_comp<MODE>(a, j, c, 1, c_hs[1], h, ds, hh, a.yp[pc & 1], a.src[pc & 1]);
+        }
         if (!grid_sync(ctl, T)) return;
     } else {
         t = ctl->t;
@@ -493,32 +602,35 @@ __global__ void __launch_bounds__(256) radau_engine(EngineArgs a)
             for (int ih = 1; ih < 8; ih++) {
                 const double *yp = a.yp[pc & 1];
                 const Src *src = a.src[pc & 1];
-                for (int j = gid; j < n; j += ngroups) {
-                    double ax, ay, az;
+                // spacing of the next publication: substep ih + 1, or at
+                // ih = 7 the next iteration's substep 1 (speculative)
+                const int nrow = ih < 7 ? ih + 1 : 1;
+                const double ns = c_hs[nrow], nds = h * ns, nhh = 0.5 * nds * nds;
+                const double hh1 = 0.5 * h * h;
+                for (int jj = gid; jj < n_loop; jj += ngroups) {
+                    const bool live = jj < n;
+                    const int j = live ? jj : n - 1;
+                    double f[3];
                     sink_accel<MODE, JS>(a, j, src, yp[3 * j], yp[3 * j + 1], yp[3 * j + 2], lane,
-                                         ax, ay, az);
-                    if (lane == 0) {
-                        bool live = a.m[j] >= 0.0;
-                        double f[3] = {live ? ax : 0.0, live ? ay : 0.0, live ? az : 0.0};
-                        for (int c = 0; c < 3; c++) {
-                            int i = 3 * j + c;
-                            double fi = f[c] + (a.ext ? a.ext[i] : 0.0);
-                            gb_update<MODE>(a, i, ih, fi);
-                            if (ih == 7) {
-                                unsigned long long u = absmax_key(a.b[6 * a.dim + i] - a.b6p[i]);
-                                unsigned long long w = absmax_key(fi);
-                                kdb = u > kdb ? u : kdb;
-                                kf8 = w > kf8 ? w : kf8;
-                            }
+                                         f[0], f[1], f[2]);
+                    if (!live) continue;
+                    const bool alive = a.m[j] >= 0.0;
+                    for (int c = c0; c < c1; c++) {
+                        const int i = 3 * j + c;
+                        const double fi = (alive ? pick3(f, c) : 0.0) + (a.ext ? a.ext[i] : 0.0);
+                        gb_update<MODE>(a, i, ih, fi);
+                        if (ih == 7) {
+                            unsigned long long u = absmax_key(b6_at<MODE>(a, i) - a.b6p[i]);
+                            unsigned long long w = absmax_key(fi);
+                            kdb = u > kdb ? u : kdb;
+                            kf8 = w > kf8 ? w : kf8;
                         }
-                        if (ih < 7) {
-                            publish_body<MODE>(a, j, c_hs[ih + 1], h, a.yp[(pc + 1) & 1],
-                                         a.src[(pc + 1) & 1]);
-                        } else {
-                            // speculative: next iteration's substep 1 and the advance
-                            publish_body<MODE>(a, j, c_hs[1], h, a.yp[(pc + 1) & 1], a.src[(pc + 1) & 1]);
-                            publish_body<MODE>(a, j, 1.0, h, a.ypa, a.srca);
-                            for (int c = 0; c < 3; c++) a.dyp[3 * j + c] = pred_vel<MODE>(a, 3 * j + c, 1.0, h);
+                        publish_comp<MODE>(a, j, c, nrow, ns, h, nds, nhh, a.yp[(pc + 1) & 1],
+                                           a.src[(pc + 1) & 1]);
+                        if (ih == 7) {
+                            // speculative advance (spacing 1)
+                            publish_comp<MODE>(a, j, c, 8, 1.0, h, h, hh1, a.ypa, a.srca);
+                            a.dyp[i] = pred_vel<MODE>(a, i, h);
                         }
                     }
                 }
@@ -531,28 +643,27 @@ __global__ void __launch_bounds__(256) radau_engine(EngineArgs a)
             read2(ctl, red_idx++, db6, f8);
             if (db6 / f8 < TOLPC) break;  // src/integrator_gauss_radau15.c:366
             for (int j = gid; j < n; j += ngroups)
-                if (lane == 0)
-                    for (int c = 0; c < 3; c++) a.b6p[3 * j + c] = a.b[6 * a.dim + 3 * j + c];
+                for (int c = c0; c < c1; c++) a.b6p[3 * j + c] = b6_at<MODE>(a, 3 * j + c);
         }
         // ---------------- advance (spacing 1) ----------------
         unsigned long long kb6 = 0, kdd = 0;
-        for (int j = gid; j < n; j += ngroups) {
-            double ax, ay, az;
+        for (int jj = gid; jj < n_loop; jj += ngroups) {
+            const bool live = jj < n;
+            const int j = live ? jj : n - 1;
+            double f[3];
             sink_accel<MODE, JS>(a, j, a.srca, a.ypa[3 * j], a.ypa[3 * j + 1], a.ypa[3 * j + 2],
-                                 lane, ax, ay, az);
-            if (lane == 0) {
-                bool live = a.m[j] >= 0.0;
-                double f[3] = {live ? ax : 0.0, live ? ay : 0.0, live ? az : 0.0};
-                for (int c = 0; c < 3; c++) {
-                    int i = 3 * j + c;
-                    double fi = f[c] + (a.ext ? a.ext[i] : 0.0);
-                    a.ddy[i] = fi;
-                    if (!isfinite(fi + a.ypa[i] + a.dyp[i])) atomicCAS(&ctl->err, 0, ABIE_ERR_NUMERICS);
-                    unsigned long long u = absmax_key(a.b[6 * a.dim + i]);
-                    unsigned long long w = absmax_key(fi);
-                    kb6 = u > kb6 ? u : kb6;
-                    kdd = w > kdd ? w : kdd;
-                }
+                                 lane, f[0], f[1], f[2]);
+            if (!live) continue;
+            const bool alive = a.m[j] >= 0.0;
+            for (int c = c0; c < c1; c++) {
+                const int i = 3 * j + c;
+                const double fi = (alive ? pick3(f, c) : 0.0) + (a.ext ? a.ext[i] : 0.0);
+                a.ddy[i] = fi;
+                if (!isfinite(fi + a.ypa[i] + a.dyp[i])) atomicCAS(&ctl->err, 0, ABIE_ERR_NUMERICS);
+                unsigned long long u = absmax_key(b6_at<MODE>(a, i));
+                unsigned long long w = absmax_key(fi);
+                kb6 = u > kb6 ? u : kb6;
+                kdd = w > kdd ? w : kdd;
             }
         }
         reduce2(ctl, red_idx, kb6, kdd);
@@ -579,14 +690,17 @@ __global__ void __launch_bounds__(256) radau_engine(EngineArgs a)
             }
             double q = dtreq / h;
             for (int j = gid; j < n; j += ngroups) {
-                if (lane != 0) continue;
-                for (int c = 0; c < 3; c++) {
+                for (int c = c0; c < c1; c++) {
                     int i = 3 * j + c;
                     a.y0[i] = a.ypa[i];
                     a.dy0[i] = a.dyp[i];
                     a.F1[i] = a.ddy[i];
-                    a.b6p[i] = a.b[6 * a.dim + i];
-                    refine_b(a, i, q);
+                    if (MODE == ABIE_FORCE_EXACT) {
+                        a.b6p[i] = a.b[6 * a.dim + i];
+                        refine_b(a, i, q);
+                    } else {
+                        refine_g(a, i, q, stop);
+                    }
                 }
             }
             scan_events(a, t, tid, nthreads);
@@ -601,8 +715,10 @@ __global__ void __launch_bounds__(256) radau_engine(EngineArgs a)
             else h = dtreq;
             if (h < H_MIN) h = H_MIN;
             // next attempt's substep-1 prediction
+            const double ds = h * c_hs[1], hh = 0.5 * ds * ds;
             for (int j = gid; j < n; j += ngroups)
-                if (lane == 0) publish_body<MODE>(a, j, c_hs[1], h, a.yp[pc & 1], a.src[pc & 1]);
+                for (int c = c0; c < c1; c++)
+                    publish_comp<MODE>(a, j, c, 1, c_hs[1], h, ds, hh, a.yp[pc & 1], a.src[pc & 1]);
         }
         if (!grid_sync(ctl, T)) return;
         if (accepted && *(volatile int *)&ctl->n_ev > 0) {
@@ -691,31 +807,80 @@ static int engine_reserve(size_t n, size_t max_ce, size_t max_coll)
 }
 
 template <int MODE, int JS>
-static int launch_engine(const EngineArgs &a, int num_sms, cudaStream_t st, int *grid_out)
+static int launch_engine(const EngineArgs &a, int num_sms, int block, cudaStream_t st, int *grid_out)
 {
     int bps = 0;
-    ABIE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, radau_engine<MODE, JS>, 256, 0));
+    ABIE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, radau_engine<MODE, JS>, block, 0));
     if (bps < 1) {
         set_error(ABIE_ERR_CUDA, "radau engine does not fit on an SM");
         return ABIE_ERR_CUDA;
     }
-    long long want = ((long long)a.n * JS + 255) / 256;
+    const int gpw = 32 / JS;
+    long long want = ((long long)(a.n + gpw - 1) / gpw * 32 + block - 1) / block;
     long long grid = std::min<long long>((long long)bps * num_sms, std::max<long long>(want, 1));
     EngineArgs args = a;
     void *params[] = {&args};
     ABIE_CUDA(cudaLaunchCooperativeKernel((const void *)radau_engine<MODE, JS>, dim3((unsigned)grid),
-                                          dim3(256), params, 0, st));
+                                          dim3(block), params, 0, st));
     *grid_out = (int)grid;
     return 0;
 }
 
-static int dispatch_engine(int mode, int js, const EngineArgs &a, int num_sms, cudaStream_t st,
-                           int *grid)
+static int dispatch_engine(int mode, int js, int block, const EngineArgs &a, int num_sms,
+                           cudaStream_t st, int *grid)
 {
-    if (mode == ABIE_FORCE_EXACT) return launch_engine<ABIE_FORCE_EXACT, 1>(a, num_sms, st, grid);
-    if (js == 1) return launch_engine<ABIE_FORCE_FP64, 1>(a, num_sms, st, grid);
-    if (js == 8) return launch_engine<ABIE_FORCE_FP64, 8>(a, num_sms, st, grid);
-    return launch_engine<ABIE_FORCE_FP64, 32>(a, num_sms, st, grid);
+    if (mode == ABIE_FORCE_EXACT) {
+        if (js == 4) return launch_engine<ABIE_FORCE_EXACT, 4>(a, num_sms, block, st, grid);
+        return launch_engine<ABIE_FORCE_EXACT, 1>(a, num_sms, block, st, grid);
+    }
+    switch (js) {
+    case 1: return launch_engine<ABIE_FORCE_FP64, 1>(a, num_sms, block, st, grid);
+    case 4: return launch_engine<ABIE_FORCE_FP64, 4>(a, num_sms, block, st, grid);
+    case 8: return launch_engine<ABIE_FORCE_FP64, 8>(a, num_sms, block, st, grid);
+    case 16: return launch_engine<ABIE_FORCE_FP64, 16>(a, num_sms, block, st, grid);
+    default: return launch_engine<ABIE_FORCE_FP64, 32>(a, num_sms, block, st, grid);
+    }
+}
+
+static int g_engine_js = 0, g_engine_block = 0;  // debug override (0: automatic)
+
+// Launch shape.  Each FP64 warp instruction occupies an SM sub-partition's
+// FP64 pipe for about 64 cycles however many lanes are active, so the time
+// of a substep is about (warps per sub-partition) x (FP64 instructions per
+// warp).  With JS lanes per body, lanes 0..2 own x, y, z (JS >= 4) and the
+// sources split JS ways; with one lane per body that lane does everything.
+// The shape minimising that estimate is taken (small systems spread thin,
+// large ones keep every lane busy), with blocks small enough that every SM
+// gets work.
+static void engine_shape(int mode, int n, int n_src, int num_sms, int *js, int *block)
+{
+    const long long subparts = 4LL * num_sms;
+    const int cand_fast[5] = {1, 4, 8, 16, 32}, cand_exact[2] = {1, 4};
+    const int *cand = mode == ABIE_FORCE_EXACT ? cand_exact : cand_fast;
+    const int nc = mode == ABIE_FORCE_EXACT ? 2 : 5;
+    const double pair = mode == ABIE_FORCE_EXACT ? 20.0 : 13.0;  // FP64 instructions per pair
+    const double sweep = mode == ABIE_FORCE_EXACT ? 50.0 : 30.0; // per component and substep
+    double best = 0.0;
+    for (int k = 0; k < nc; k++) {
+        const int w = cand[k];
+        const long long warps = ((long long)n * w + 31) / 32;
+        const long long per_sub = (warps + subparts - 1) / subparts;
+        double force = mode == ABIE_FORCE_EXACT ? pair * n_src : pair * ((n_src + w - 1) / w);
+        int lg = 0;
+        while ((1 << lg) < w) lg++;
+        const double instr = force + 3.0 * lg + (w >= 4 ? sweep : 3.0 * sweep);
+        const double cost = (double)per_sub * instr;
+        if (k == 0 || cost < best) {
+            best = cost;
+            *js = w;
+        }
+    }
+    const long long threads = ((long long)n * *js + 31) / 32 * 32;
+    long long b = (threads + num_sms - 1) / num_sms;  // one block per SM when that is enough
+    b = (b + 31) / 32 * 32;
+    *block = (int)std::max<long long>(32, std::min<long long>(256, b));
+    if (g_engine_js > 0) *js = g_engine_js;
+    if (g_engine_block > 0) *block = g_engine_block;
 }
 
 int radau_run(const SystemView &sys, double t, double t_end, int mode, EventState *evs,
@@ -803,8 +968,8 @@ int radau_run(const SystemView &sys, double t, double t_end, int mode, EventStat
     ABIE_CUDA(cudaMemcpyAsync(e.ctl, &c0, sizeof c0, cudaMemcpyHostToDevice, st));
     ABIE_CUDA(cudaStreamSynchronize(st));
 
-    int js = 1;
-    if (mode != ABIE_FORCE_EXACT) js = n_src <= 64 ? 1 : (n_src <= 1024 ? 8 : 32);
+    int js = 1, block = 256;
+    engine_shape(mode, n, n_src, g_sim.num_sms, &js, &block);
     EngineCtl c;
     long long budget = 4;
     for (;;) {
@@ -814,7 +979,7 @@ int radau_run(const SystemView &sys, double t, double t_end, int mode, EventStat
         ABIE_CUDA(cudaEventCreate(&e1));
         ABIE_CUDA(cudaEventRecord(e0, st));
         int grid = 0;
-        rc = dispatch_engine(mode, js, a, g_sim.num_sms, st, &grid);
+        rc = dispatch_engine(mode, js, block, a, g_sim.num_sms, st, &grid);
         if (rc) return rc;
         ABIE_CUDA(cudaEventRecord(e1, st));
         ABIE_CUDA(cudaEventSynchronize(e1));
@@ -868,6 +1033,15 @@ int radau_run(const SystemView &sys, double t, double t_end, int mode, EventStat
 using namespace abie;
 
 extern "C" {
+
+void abie_debug_engine_shape(int lanes_per_body, int block)
+{
+    const bool ok_js = lanes_per_body == 0 || lanes_per_body == 1 || lanes_per_body == 4 ||
+                       lanes_per_body == 8 || lanes_per_body == 16 || lanes_per_body == 32;
+    const bool ok_block = block == 0 || (block >= 32 && block <= 256 && block % 32 == 0);
+    g_engine_js = ok_js ? lanes_per_body : 0;
+    g_engine_block = ok_block ? block : 0;
+}
 
 int integrator_gr(double t, double t_end, double dt)
 {

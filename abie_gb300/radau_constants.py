@@ -64,6 +64,39 @@ def tables():
     return h, rs, cs
 
 
+def fast_tables():
+    """Tables of the reassociated (fast) sweep, each entry rounded once.
+
+    * ``rsp[i][j] = prod_{l=j..i-1} rs[i][l]``: the divided-difference chain
+      g_{i-1} = (((F_i - F_0) rs[i][0] - g_0) rs[i][1] - ...) rs[i][i-1]
+      expanded into (F_i - F_0) rsp[i][0] - sum_{j<i-1} g_j rsp[i][j+1].
+    * ``wpos[i][k] = s_i**(k+1) / ((k+2)(k+3)/2)``, s_i = h_i for i < 8 and
+      s_8 = 1: the weights of b_k in the predicted position at spacing s_i.
+    * ``wg[i][j] = sum_{k<=j} cs[j][k] wpos[i][k]``: the same weights on the
+      Newton-form coefficients g_j, and ``vg[j] = sum_{k<=j} cs[j][k]/(k+2)``
+      those of the predicted velocity at spacing 1.
+    """
+    h, rs, cs = tables()
+    rsp = [[mpmath.mpf(0)] * NH for _ in range(NH)]
+    for i in range(1, NH):
+        for j in range(i):
+            p = mpmath.mpf(1)
+            for l in range(j, i):
+                p *= rs[i][l]
+            rsp[i][j] = p
+    wpos = []
+    for s in list(h) + [mpmath.mpf(1)]:
+        wpos.append([s ** (k + 1) / ((k + 2) * (k + 3) / 2) for k in range(7)])
+    # the same polynomials on the Newton-form coefficients g (b = C g):
+    # sum_k b_k w_k = sum_j g_j sum_{k<=j} cs[j][k] w_k
+    wg = [[sum(cs[j][k] * row[k] for k in range(j + 1)) for j in range(7)] for row in wpos]
+    vg = [sum(cs[j][k] / (k + 2) for k in range(j + 1)) for j in range(7)]
+    return ([[to_double(v) for v in row] for row in rsp],
+            [[to_double(v) for v in row] for row in wpos],
+            [[to_double(v) for v in row] for row in wg],
+            [to_double(v) for v in vg])
+
+
 def to_double(v):
     return float(mpmath.mpf(v))
 
@@ -77,6 +110,7 @@ def double_tables():
 
 def emit_header(path):
     h, rs, cs = double_tables()
+    rsp, wpos, wg, vg = fast_tables()
 
     def row(vals):
         return "{" + ", ".join(float.hex(v) for v in vals) + "}"
@@ -89,6 +123,10 @@ def emit_header(path):
         "#define ABIE_RADAU_HS_INIT " + row(h),
         "#define ABIE_RADAU_RS_INIT {" + ", ".join(row(r) for r in rs) + "}",
         "#define ABIE_RADAU_CS_INIT {" + ", ".join(row(c) for c in cs) + "}",
+        "#define ABIE_RADAU_RSP_INIT {" + ", ".join(row(r) for r in rsp) + "}",
+        "#define ABIE_RADAU_WPOS_INIT {" + ", ".join(row(w) for w in wpos) + "}",
+        "#define ABIE_RADAU_WG_INIT {" + ", ".join(row(w) for w in wg) + "}",
+        "#define ABIE_RADAU_VG_INIT " + row(vg),
         "#endif",
         "",
     ]

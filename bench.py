@@ -64,7 +64,7 @@ def parse():
     ap.add_argument("--no-extras", action="store_true", help="only the headline force line")
     ap.add_argument("--extras", default="ensemble,wh,radau",
                     help="comma list of sub-measurements: ensemble, wh, radau")
-    ap.add_argument("--ensemble-forms", default="plain_fp64,fp64,fp64_consistent,learned",
+    ap.add_argument("--ensemble-forms", default="plain_fp64,fp64,learned",
                     help="comma list of ensemble forms to time")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
@@ -353,10 +353,11 @@ def run_ensemble(lib, args, rank, dev):
     time.  Every rank draws its own systems (weak scaling).
 
     Forms: plain_fp64 = the reference's FP64 operations and predictor in the
-    batched kernel (the comparator); fp64 = 13-instruction pair terms, FMA
-    sweep; fp64_consistent = the same with g made consistent with the
-    predicted b; learned = that plus the BF16 network, trained online on
-    samples the ensemble records on a separate set of systems."""
+    batched kernel (the comparator); fp64 = 13-instruction pair terms and
+    the corrector on the Newton-form coefficients, each step starting from
+    g consistent with the reference's plain guess; learned = that with the
+    BF16 network's guess, trained online on samples the ensemble records on
+    a separate set of systems."""
     import time as _t
 
     from abie_gb300.learned import collect_samples, train_predictor
@@ -373,8 +374,7 @@ def run_ensemble(lib, args, rank, dev):
         out["training"] = {"systems": 2048, "years": 1.0, "samples": info["samples"],
                            "seconds": _t.perf_counter() - t0, "holdout_loss": info["holdout_loss"],
                            "holdout_loss_plain_guess": info["holdout_loss_plain"]}
-    forms = (("plain_fp64", "exact", {}), ("fp64", "fp64", {}),
-             ("fp64_consistent", "fp64", {"consistent": True}), ("learned", "fp64", {"learned": True}))
+    forms = (("plain_fp64", "exact", {}), ("fp64", "fp64", {}), ("learned", "fp64", {"learned": True}))
     for label, mode, kw in forms:
         if label not in wanted:
             continue
@@ -388,10 +388,13 @@ def run_ensemble(lib, args, rank, dev):
         out[label] = {"system_steps": int(steps), "seconds": secs, "system_steps_per_s": rate,
                       "corrector_iterations_per_attempt": c["iterations"] / max(c["attempts"], 1),
                       "max_abs_dE_over_E": _energy_errors(lib, P, V, res["pos"], res["vel"], M, offs),
-                      "failed_systems": int((res["status"] != 0).sum())}
+                      "failed_systems": int((res["status"] != 0).sum()),
+                      "max_steps_one_system": int(res["steps"].max())}
+        if label == "learned":
+            out[label]["attempts_redone_from_plain_guess"] = int(c["learned_fallbacks"])
     lib.mlp_enable(False)
     base = out.get("plain_fp64", {}).get("system_steps_per_s")
-    for label in ("fp64", "fp64_consistent", "learned"):
+    for label in ("fp64", "learned"):
         if base and label in out and out[label]["system_steps_per_s"]:
             out[label]["speedup_vs_plain_fp64"] = out[label]["system_steps_per_s"] / base
     return out

@@ -184,6 +184,10 @@ int abie_mlp_train(int steps, int batch, double lr, int seed, double *last_loss)
  * picks a default length. */
 int abie_measure_fp64_peak(int iters, double *tflops);
 int abie_measure_fp32_peak(int iters, double *tflops);
+/* The FP64 probe with only the first active_lanes (1..32) lanes of each warp
+ * working, its rate counted over all 32 lanes: shows what a partly idle warp
+ * costs the FP64 pipe. */
+int abie_measure_fp64_issue(int active_lanes, double *tflops);
 /* No counterpart in the reference.  The fast FP64 all-pairs force on device
  * pointers, like abie_force_device with mode ABIE_FORCE_FP64, for callers
  * that cannot allocate GPU memory (inside a stream capture that must hold
@@ -202,6 +206,10 @@ int abie_force_device_noalloc(const double *d_pos, const double *d_m, size_t N,
  * {1, 8, 32} and the number of source chunks; (0, 0) restores the
  * automatic choice.  For tests and the autotuner. */
 void abie_debug_force_shape(int lanes_per_sink, int chunks);
+/* Fixes the Radau15 engine's launch shape: lanes per body in {1, 4, 8, 16,
+ * 32} (the exact form takes 1 or 4) and threads per block (a multiple of 32
+ * up to 256); 0 keeps the automatic choice.  For tests and tuning. */
+void abie_debug_engine_shape(int lanes_per_body, int block);
 
 #ifdef __cplusplus
 }

@@ -1,9 +1,10 @@
 """Learned Radau15 predictor inside the batched ensemble.
 
-* An untrained network (zero output layer) reproduces the consistent-g
-  plain predictor bit for bit (the guess is E + s tau * 0, g = C^-1 E).
-* The consistent g alone lowers corrector iterations per attempt against
-  the reference's predictor (which keeps the previous step's g).
+* An untrained network (zero output layer) reproduces the fast form's plain
+  predictor bit for bit (the guess is E + s tau * 0, g = C^-1 E).
+* Consistent g (the fast form always; the exact form with the flag) lowers
+  corrector iterations per attempt against the reference's predictor, which
+  keeps the previous step's g.
 * Samples collected from the ensemble's own runs train a network whose
   held-out loss beats the plain guess; with it the corrector needs fewer
   iterations per attempt than with the reference's predictor on systems it
@@ -45,31 +46,33 @@ def test_collect_train_and_fewer_iterations(clib, oracle):
     assert info["holdout_loss"] < 0.8 * info["holdout_loss_plain"]
     # unseen systems
     P2, V2, M2, offs2 = ics.ensemble(n_systems=512, seed0=40000)
-    clib.mlp_enable(False)
-    clib.reset_counters()
-    plain = clib.gr_ensemble(P2, V2, M2, offs2, G, 0.0, 0.5)
-    cp = clib.counters()
-    clib.mlp_enable(True)
-    clib.reset_counters()
-    learned = clib.gr_ensemble(P2, V2, M2, offs2, G, 0.0, 0.5, learned=True)
-    cl = clib.counters()
-    clib.mlp_enable(False)
-    clib.reset_counters()
-    cons = clib.gr_ensemble(P2, V2, M2, offs2, G, 0.0, 0.5, consistent=True)
-    cc = clib.counters()
-    it_plain = cp["iterations"] / cp["attempts"]
-    it_cons = cc["iterations"] / cc["attempts"]
-    it_learned = cl["iterations"] / cl["attempts"]
-    print("iterations per attempt: reference predictor %.3f consistent g %.3f learned %.3f; "
-          "attempts redone from the plain guess: %d" % (it_plain, it_cons, it_learned,
-                                                          cl["learned_fallbacks"]))
-    for r in (plain, learned, cons):
+
+    def run(mode, **kw):
+        old = clib.set_force_mode(mode)
+        clib.mlp_enable(bool(kw.get("learned")))
+        clib.reset_counters()
+        try:
+            r = clib.gr_ensemble(P2, V2, M2, offs2, G, 0.0, 0.5, **kw)
+        finally:
+            clib.set_force_mode(old)
+            clib.mlp_enable(False)
+        c = clib.counters()
+        return r, c["iterations"] / c["attempts"], c
+
+    ref, it_ref, _ = run("exact")                       # the reference's predictor
+    cons, it_cons, _ = run("exact", consistent=True)    # same arithmetic, consistent g
+    fast, it_fast, _ = run("fp64")                      # fast form (consistent g)
+    learned, it_learned, cl = run("fp64", learned=True)
+    print("iterations per attempt: reference predictor %.3f consistent g %.3f fast form %.3f "
+          "learned %.3f; attempts redone from the plain guess: %d"
+          % (it_ref, it_cons, it_fast, it_learned, cl["learned_fallbacks"]))
+    for r in (ref, cons, fast, learned):
         assert (r["status"] == 0).all() and (r["t"] >= 0.5).all()
-    assert it_cons < it_plain and it_learned < it_plain
+    assert it_cons < it_ref and it_fast < it_ref and it_learned < it_ref
     for s in range(0, 512, 37):
         a, b = offs2[s], offs2[s + 1]
-        tp, tl = plain["t"][s], learned["t"][s]
+        tp, tl = ref["t"][s], learned["t"][s]
         assert abs(tp - tl) <= TIME_TOL_FAST * tp
         p, v = at_time(learned["pos"][3 * a:3 * b], learned["vel"][3 * a:3 * b], M2[a:b], tl, tp,
                        oracle)
-        assert rel_err_per_body(p, plain["pos"][3 * a:3 * b]) <= TOL
+        assert rel_err_per_body(p, ref["pos"][3 * a:3 * b]) <= TOL
