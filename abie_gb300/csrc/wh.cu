@@ -32,6 +32,7 @@ struct WhShared {
     double ind[3];        // indirect term
     double a2[3];         // accel2 carried past the head
     double gm_tail;       // Kepler parameter of a massless body
+    double gm_tail_k[3];  // sqrt(gm_tail), 1/gm_tail, 1/sqrt(gm_tail)
     unsigned long long kepler_failures;
 };
 
@@ -138,8 +139,140 @@ __device__ int kepler_drift(double r0v[3], double v0v[3], double gm, double dt)
     return failed;
 }
 
+// Stumpff functions by their series, c2 = sum_k (-psi)^k / (2k+2)!,
+// c3 = sum_k (-psi)^k / (2k+3)!, for |psi| <= 0.5 (nine terms each; the
+// first omitted term is below 1e-18).  More accurate there than the
+// closed forms, whose 1 - cos(sqrt(psi)) cancels, and free of sqrt and
+// sincos.
+__device__ __forceinline__ void stumpff_series(double psi, double &c2, double &c3)
+{
+    const double x = -psi;
+    double a = 1.0 / 6402373705728000.0;   // 1/18!
+    a = fma(a, x, 1.0 / 20922789888000.0); // 1/16!
+    a = fma(a, x, 1.0 / 87178291200.0);    // 1/14!
+    a = fma(a, x, 1.0 / 479001600.0);      // 1/12!
+    a = fma(a, x, 1.0 / 3628800.0);        // 1/10!
+    a = fma(a, x, 1.0 / 40320.0);          // 1/8!
+    a = fma(a, x, 1.0 / 720.0);            // 1/6!
+    a = fma(a, x, 1.0 / 24.0);             // 1/4!
+    c2 = fma(a, x, 0.5);                   // 1/2!
+    double b = 1.0 / 121645100408832000.0; // 1/19!
+    b = fma(b, x, 1.0 / 355687428096000.0);  // 1/17!
+    b = fma(b, x, 1.0 / 1307674368000.0);    // 1/15!
+    b = fma(b, x, 1.0 / 6227020800.0);       // 1/13!
+    b = fma(b, x, 1.0 / 39916800.0);         // 1/11!
+    b = fma(b, x, 1.0 / 362880.0);           // 1/9!
+    b = fma(b, x, 1.0 / 5040.0);             // 1/7!
+    b = fma(b, x, 1.0 / 120.0);              // 1/5!
+    c3 = fma(b, x, 1.0 / 6.0);               // 1/3!
+}
+
+// Fast form of kepler_drift: the same universal-variable Newton iteration,
+// convergence test (|dchi| < 1e-12) and f, g functions, with
+//  * a starting value from the Taylor series of chi(t) (dchi/dt = sqrt(gm)/r)
+//    to third order when the step covers a small arc (psi_0 < 0.1), so one
+//    or two Newton steps suffice instead of three or four;
+//  * the series Stumpff functions for |psi| <= 0.5 where the reference uses
+//    the closed forms (its constants 1/2, 1/6 in -1e-6 <= psi <= 1e-10 and
+//    the closed forms beyond |psi| = 0.5 are kept);
+//  * 1/r and 1/sqrt from rcp_fast / inv_sqrt_fast instead of divisions and
+//    sqrt, and sqrt(gm), 1/gm, 1/sqrt(gm) precomputed (k[0..2]).
+// The converged chi is the same root; the state agrees with the reference
+// form to rounding.  Distances must lie within the FP32 exponent range.
+__device__ int kepler_drift_fast(double r0v[3], double v0v[3], double gm, const double k[3],
+                                 double dt)
+{
+    const double sqrtgm = k[0], igm = k[1], isqrtgm = k[2];
+    const double r02 = fma(r0v[2], r0v[2], fma(r0v[1], r0v[1], r0v[0] * r0v[0]));
+    const double v02 = fma(v0v[2], v0v[2], fma(v0v[1], v0v[1], v0v[0] * v0v[0]));
+    const double ir0 = inv_sqrt_fast(r02);
+    const double r0 = r02 * ir0;
+    const double xi = fma(0.5, v02, -gm * ir0);
+    const double alpha = -2.0 * xi * igm;
+    const double rv = fma(r0v[2], v0v[2], fma(r0v[1], v0v[1], r0v[0] * v0v[0]));
+    double chi0;
+    const double w1 = sqrtgm * dt * ir0;  // first-order arc
+    if (alpha > TOL_ENERGY && w1 * w1 * alpha < 0.1) {
+        const double ir02 = ir0 * ir0;
+        const double u = rv * ir02;                       // rdot / r
+        const double w2 = -0.5 * u * dt;                  // second-order factor
+        const double w3 = (v02 - gm * ir0) * ir02 - 3.0 * u * u;
+        chi0 = w1 * fma(dt * dt / 6.0, -w3, 1.0 + w2);
+    } else if (alpha > TOL_ENERGY) {
+        chi0 = sqrtgm * dt * alpha;
+    } else if (alpha < TOL_ENERGY) {
+        const double sma = 1.0 / alpha;
+        double sg = (double)((dt > 0) - (dt < 0));
+        chi0 = sg * (sqrt(-sma) * log(-2.0 * gm * alpha * dt / (rv + sqrt(-gm * sma) * (1.0 - r0 * alpha))));
+    } else {
+        double c0 = r0v[1] * v0v[2] - r0v[2] * v0v[1];
+        double c1 = r0v[2] * v0v[0] - r0v[0] * v0v[2];
+        double c2_ = r0v[0] * v0v[1] - r0v[1] * v0v[0];
+        double cn = sqrt(c0 * c0 + c1 * c1 + c2_ * c2_);
+        double p = cn * cn / gm;
+        double s = 0.5 * atan(1.0 / (3.0 * sqrt(gm / cube_cr(p)) * dt));
+        double w = atan(pow(tan(s), 1.0 / 3.0));
+        chi0 = sqrt(p) * 2 / tan(2 * w);
+    }
+    double chi = 0.0, r = 0.0, c2 = 0.0, c3 = 0.0, psi = 0.0;
+    const double rvs = rv * isqrtgm;
+    const double sgdt = sqrtgm * dt;
+    for (int it = 0; it < KEPLER_MAX_IT; it++) {
+        const double chi2 = chi0 * chi0;
+        psi = chi2 * alpha;
+        if (psi > 1.e-10 || psi < -1.e-6) {
+            if (fabs(psi) <= 0.5) stumpff_series(psi, c2, c3);
+            else stumpff(psi, c2, c3);
+        } else {
+            c2 = 0.5;
+            c3 = 1.0 / 6.0;
+        }
+        const double s3 = fma(-psi, c3, 1.0), s2 = fma(-psi, c2, 1.0);
+        r = fma(chi2, c2, fma(rvs * chi0, s3, r0 * s2));
+        const double num = sgdt - chi2 * chi0 * c3 - rvs * chi2 * c2 - r0 * chi0 * s3;
+        chi = fma(num, rcp_fast(r), chi0);
+        if (fabs(chi - chi0) < KEPLER_TOL) break;
+        chi0 = chi;
+    }
+    int failed = fabs(chi - chi0) > KEPLER_TOL;
+    const double chi2 = chi * chi;
+    const double f = fma(-chi2 * ir0, c2, 1.0);
+    const double g = fma(-chi2 * chi * isqrtgm, c3, dt);
+    const double ir = rcp_fast(r);
+    const double dg = fma(-chi2 * ir, c2, 1.0);
+    const double df = sqrtgm * ir * ir0 * chi * fma(psi, c3, -1.0);
+    double nr[3], nv[3];
+    for (int c = 0; c < 3; c++) {
+        nr[c] = fma(f, r0v[c], g * v0v[c]);
+        nv[c] = fma(df, r0v[c], dg * v0v[c]);
+    }
+    for (int c = 0; c < 3; c++) {
+        r0v[c] = nr[c];
+        v0v[c] = nv[c];
+    }
+    return failed;
+}
+
 // One block.  init != 0: only Jacobi coordinates and accelerations (the
 // set-up at the start of integrator_wh, :524-525); otherwise a full step.
+// MODE as for the tail: the fast form divides by multiplying with
+// rcp_fast, drifts with kepler_drift_fast and takes r^-3 from gm_inv_r3.
+// The head is latency-bound (a few bodies, sequential prefixes), so its
+// time is its FP64 instruction count on one warp.
+template <int MODE>
+__device__ __forceinline__ double wdiv(double x, double y)
+{
+    return MODE == ABIE_FORCE_EXACT ? x / y : x * rcp_fast(y);
+}
+
+template <int MODE>
+__device__ __forceinline__ double wh_ir3(double x, double y, double z)
+{
+    if (MODE == ABIE_FORCE_EXACT) return 1.0 / cube_cr(norm3(x, y, z));
+    return gm_inv_r3(fma(z, z, fma(y, y, x * x)), 1.0);
+}
+
+template <int MODE>
 __global__ void __launch_bounds__(256) wh_head_kernel(WhArgs a, int init)
 {
     const int H = a.head, n = a.n;
@@ -162,7 +295,11 @@ __global__ void __launch_bounds__(256) wh_head_kernel(WhArgs a, int init)
         }
         {
             double eta = eta0 + 0.0;
-            sh->gm_tail = a.G * m[0] * eta / eta0;
+            const double gmt = a.G * m[0] * eta / eta0;
+            sh->gm_tail = gmt;
+            sh->gm_tail_k[0] = sqrt(gmt);
+            sh->gm_tail_k[1] = 1.0 / gmt;
+            sh->gm_tail_k[2] = 1.0 / sqrt(gmt);
         }
         // helio -> Jacobi for the head (:221-280)
         double *jp = a.jpos, *jv = a.jvel;
@@ -176,8 +313,8 @@ __global__ void __launch_bounds__(256) wh_head_kernel(WhArgs a, int init)
         for (int c = 0; c < 3; c++) {
             aR[c] = m[1] * a.pos[3 + c];
             aV[c] = m[1] * a.vel[3 + c];
-            R[c] = aR[c] / a.eta[1];
-            V[c] = aV[c] / a.eta[1];
+            R[c] = wdiv<MODE>(aR[c], a.eta[1]);
+            V[c] = wdiv<MODE>(aV[c], a.eta[1]);
         }
         for (int i = 2; i < H; i++) {
             for (int c = 0; c < 3; c++) {
@@ -188,8 +325,8 @@ __global__ void __launch_bounds__(256) wh_head_kernel(WhArgs a, int init)
                 for (int c = 0; c < 3; c++) {
                     aR[c] += (m[i] * a.pos[3 * i + c]);
                     aV[c] += (m[i] * a.vel[3 * i + c]);
-                    R[c] = aR[c] / a.eta[i];
-                    V[c] = aV[c] / a.eta[i];
+                    R[c] = wdiv<MODE>(aR[c], a.eta[i]);
+                    V[c] = wdiv<MODE>(aV[c], a.eta[i]);
                 }
             }
         }
@@ -204,7 +341,15 @@ __global__ void __launch_bounds__(256) wh_head_kernel(WhArgs a, int init)
         for (int i = 1 + threadIdx.x; i < H; i += blockDim.x) {
             double r[3] = {a.jpos[3 * i], a.jpos[3 * i + 1], a.jpos[3 * i + 2]};
             double v[3] = {a.jvel[3 * i], a.jvel[3 * i + 1], a.jvel[3 * i + 2]};
-            if (kepler_drift(r, v, a.gm[i], dt)) atomicAdd(&sh->kepler_failures, 1ull);
+            int failed;
+            if (MODE == ABIE_FORCE_EXACT) {
+                failed = kepler_drift(r, v, a.gm[i], dt);
+            } else {
+                const double sg = sqrt(a.gm[i]);
+                const double k[3] = {sg, 1.0 / a.gm[i], 1.0 / sg};
+                failed = kepler_drift_fast(r, v, a.gm[i], k, dt);
+            }
+            if (failed) atomicAdd(&sh->kepler_failures, 1ull);
             for (int c = 0; c < 3; c++) {
                 a.jpos[3 * i + c] = r[c];
                 a.jvel[3 * i + c] = v[c];
@@ -222,8 +367,8 @@ __global__ void __launch_bounds__(256) wh_head_kernel(WhArgs a, int init)
             }
             double R[3], V[3];
             for (int c = 0; c < 3; c++) {
-                R[c] = m[1] * jp[3 + c] / a.eta[1];
-                V[c] = m[1] * jv[3 + c] / a.eta[1];
+                R[c] = wdiv<MODE>(m[1] * jp[3 + c], a.eta[1]);
+                V[c] = wdiv<MODE>(m[1] * jv[3 + c], a.eta[1]);
             }
             for (int i = 2; i < H; i++) {
                 for (int c = 0; c < 3; c++) {
@@ -232,8 +377,8 @@ __global__ void __launch_bounds__(256) wh_head_kernel(WhArgs a, int init)
                 }
                 if (i < n - 1) {
                     for (int c = 0; c < 3; c++) {
-                        R[c] += m[i] * jp[3 * i + c] / a.eta[i];
-                        V[c] += m[i] * jv[3 * i + c] / a.eta[i];
+                        R[c] += wdiv<MODE>(m[i] * jp[3 * i + c], a.eta[i]);
+                        V[c] += wdiv<MODE>(m[i] * jv[3 * i + c], a.eta[i]);
                     }
                 }
             }
@@ -248,8 +393,13 @@ __global__ void __launch_bounds__(256) wh_head_kernel(WhArgs a, int init)
     for (int i = threadIdx.x; i < H; i += blockDim.x) {
         double h = 0.0, j = 0.0;
         if (i >= 2) {
-            h = cube_cr(1.0 / norm3(a.pos[3 * i], a.pos[3 * i + 1], a.pos[3 * i + 2]));
-            j = cube_cr(1.0 / norm3(a.jpos[3 * i], a.jpos[3 * i + 1], a.jpos[3 * i + 2]));
+            if (MODE == ABIE_FORCE_EXACT) {
+                h = cube_cr(1.0 / norm3(a.pos[3 * i], a.pos[3 * i + 1], a.pos[3 * i + 2]));
+                j = cube_cr(1.0 / norm3(a.jpos[3 * i], a.jpos[3 * i + 1], a.jpos[3 * i + 2]));
+            } else {
+                h = wh_ir3<MODE>(a.pos[3 * i], a.pos[3 * i + 1], a.pos[3 * i + 2]);
+                j = wh_ir3<MODE>(a.jpos[3 * i], a.jpos[3 * i + 1], a.jpos[3 * i + 2]);
+            }
         }
         a.ir3h[i] = h;
         a.ir3j[i] = j;
@@ -264,7 +414,7 @@ __global__ void __launch_bounds__(256) wh_head_kernel(WhArgs a, int init)
         for (int i = 2; i < H; i++) {
             etai += m[i - 1];
             for (int c = 0; c < 3; c++)
-                a2[c] = a2[c] + a.G * m[i] * m[0] * a.ir3j[i] / etai * a.jpos[3 * i + c];
+                a2[c] = a2[c] + wdiv<MODE>(a.G * m[i] * m[0] * a.ir3j[i], etai) * a.jpos[3 * i + c];
             for (int c = 0; c < 3; c++) a.acc[3 * i + c] = a2[c];  // temporarily: accel2[i]
         }
         for (int c = 0; c < 3; c++) {
@@ -284,14 +434,14 @@ __global__ void __launch_bounds__(256) wh_head_kernel(WhArgs a, int init)
                 if (m[i] == 0.0) continue;
                 double d[3];
                 for (int c = 0; c < 3; c++) d[c] = a.pos[3 * j + c] - a.pos[3 * i + c];
-                double aux = 1.0 / cube_cr(norm3(d[0], d[1], d[2]));
+                double aux = wh_ir3<MODE>(d[0], d[1], d[2]);
                 for (int c = 0; c < 3; c++) a3[c] -= a.G * m[i] * aux * d[c];
             }
             for (int k = j + 1; k < H; k++) {
                 if (m[k] == 0.0) continue;
                 double d[3];
                 for (int c = 0; c < 3; c++) d[c] = a.pos[3 * k + c] - a.pos[3 * j + c];
-                double aux = 1.0 / cube_cr(norm3(d[0], d[1], d[2]));
+                double aux = wh_ir3<MODE>(d[0], d[1], d[2]);
                 for (int c = 0; c < 3; c++) a3[c] += a.G * m[k] * aux * d[c];
             }
         }
@@ -313,6 +463,10 @@ __global__ void __launch_bounds__(256) wh_head_kernel(WhArgs a, int init)
 
 // One thread per tail body: the whole step (kick, Jacobi shift, drift, shift
 // back, acceleration, kick) with the head's published quantities.
+// MODE: ABIE_FORCE_EXACT keeps the reference's expressions (sqrt, divisions,
+// correctly rounded cubes, closed-form Stumpff functions); the fast form
+// uses kepler_drift_fast and the 13-instruction r^-3 of the force kernels.
+template <int MODE>
 __global__ void __launch_bounds__(256) wh_tail_kernel(WhArgs a, int init)
 {
     extern __shared__ double hs[];  // 4 doubles per massive head body: x y z G*m
@@ -344,20 +498,32 @@ __global__ void __launch_bounds__(256) wh_tail_kernel(WhArgs a, int init)
         jv[c] = v[c] - sh->V[c];
     }
     if (!init) {
-        if (kepler_drift(jp, jv, sh->gm_tail, a.dt)) atomicAdd(&a.sh->kepler_failures, 1ull);
+        const int failed = MODE == ABIE_FORCE_EXACT ? kepler_drift(jp, jv, sh->gm_tail, a.dt)
+                                                    : kepler_drift_fast(jp, jv, sh->gm_tail, sh->gm_tail_k, a.dt);
+        if (failed) atomicAdd(&a.sh->kepler_failures, 1ull);
         for (int c = 0; c < 3; c++) {
             p[c] = jp[c] + sh->Rp[c];
             v[c] = jv[c] + sh->Vp[c];
         }
     }
-    double ir3h = cube_cr(1.0 / norm3(p[0], p[1], p[2]));
-    double ir3j = cube_cr(1.0 / norm3(jp[0], jp[1], jp[2]));
+    double ir3h, ir3j;
     double a3[3] = {0.0, 0.0, 0.0};
-    for (int q = 0; q < n_src; q++) {
-        double d[3];
-        for (int c = 0; c < 3; c++) d[c] = p[c] - hs[4 * q + c];
-        double aux = 1.0 / cube_cr(norm3(d[0], d[1], d[2]));
-        for (int c = 0; c < 3; c++) a3[c] -= hs[4 * q + 3] * aux * d[c];
+    if (MODE == ABIE_FORCE_EXACT) {
+        ir3h = cube_cr(1.0 / norm3(p[0], p[1], p[2]));
+        ir3j = cube_cr(1.0 / norm3(jp[0], jp[1], jp[2]));
+        for (int q = 0; q < n_src; q++) {
+            double d[3];
+            for (int c = 0; c < 3; c++) d[c] = p[c] - hs[4 * q + c];
+            double aux = 1.0 / cube_cr(norm3(d[0], d[1], d[2]));
+            for (int c = 0; c < 3; c++) a3[c] -= hs[4 * q + 3] * aux * d[c];
+        }
+    } else {
+        ir3h = gm_inv_r3(fma(p[2], p[2], fma(p[1], p[1], p[0] * p[0])), 1.0);
+        ir3j = gm_inv_r3(fma(jp[2], jp[2], fma(jp[1], jp[1], jp[0] * jp[0])), 1.0);
+        for (int q = 0; q < n_src; q++) {
+            Src sq{hs[4 * q], hs[4 * q + 1], hs[4 * q + 2], hs[4 * q + 3]};
+            pair_fast(p[0], p[1], p[2], sq, a3[0], a3[1], a3[2]);
+        }
     }
     const double Gm0 = a.G * a.m[0];
     for (int c = 0; c < 3; c++) {
@@ -385,13 +551,16 @@ void free_wh_buffers()
     g_wh = WhBuffers();
 }
 
-static int wh_launch_step(const WhArgs &a, int init, int n_src, cudaStream_t st)
+static int wh_launch_step(const WhArgs &a, int init, int n_src, int mode, cudaStream_t st)
 {
-    wh_head_kernel<<<1, 256, 0, st>>>(a, init);
+    if (mode == ABIE_FORCE_EXACT) wh_head_kernel<ABIE_FORCE_EXACT><<<1, 256, 0, st>>>(a, init);
+    else wh_head_kernel<ABIE_FORCE_FP64><<<1, 256, 0, st>>>(a, init);
     long long tail = (long long)a.n - a.head;
     if (tail > 0) {
         unsigned blocks = (unsigned)((tail + 255) / 256);
-        wh_tail_kernel<<<blocks, 256, 4 * sizeof(double) * (size_t)std::max(n_src, 1), st>>>(a, init);
+        size_t smem = 4 * sizeof(double) * (size_t)std::max(n_src, 1);
+        if (mode == ABIE_FORCE_EXACT) wh_tail_kernel<ABIE_FORCE_EXACT><<<blocks, 256, smem, st>>>(a, init);
+        else wh_tail_kernel<ABIE_FORCE_FP64><<<blocks, 256, smem, st>>>(a, init);
     }
     return 0;
 }
@@ -444,11 +613,15 @@ int wh_run(const SystemView &sys, double t, double t_end, double dt, double *t_o
         tt += dt;
         steps++;
     }
+    const int mode = g_sim.force_mode == ABIE_FORCE_EXACT ? ABIE_FORCE_EXACT : ABIE_FORCE_FP64;
     size_t smem = 4 * sizeof(double) * (size_t)std::max(n_src, 1);
-    if (smem > 48 * 1024)
-        ABIE_CUDA(cudaFuncSetAttribute(wh_tail_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem));
-    rc = wh_launch_step(a, 1, n_src, st);
+    if (smem > 48 * 1024) {
+        ABIE_CUDA(cudaFuncSetAttribute(wh_tail_kernel<ABIE_FORCE_EXACT>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        ABIE_CUDA(cudaFuncSetAttribute(wh_tail_kernel<ABIE_FORCE_FP64>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    }
+    rc = wh_launch_step(a, 1, n_src, mode, st);
     ABIE_CUDA(cudaGetLastError());
     if (steps > 0) {
         const int CH = 32;
@@ -457,12 +630,12 @@ int wh_run(const SystemView &sys, double t, double t_end, double dt, double *t_o
         long long full = steps / CH;
         if (full > 0) {
             ABIE_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-            for (int k = 0; k < CH; k++) wh_launch_step(a, 0, n_src, st);
+            for (int k = 0; k < CH; k++) wh_launch_step(a, 0, n_src, mode, st);
             ABIE_CUDA(cudaStreamEndCapture(st, &graph));
             ABIE_CUDA(cudaGraphInstantiate(&exec, graph, 0));
             for (long long k = 0; k < full; k++) ABIE_CUDA(cudaGraphLaunch(exec, st));
         }
-        for (long long k = full * CH; k < steps; k++) wh_launch_step(a, 0, n_src, st);
+        for (long long k = full * CH; k < steps; k++) wh_launch_step(a, 0, n_src, mode, st);
         ABIE_CUDA(cudaGetLastError());
         if (exec) cudaGraphExecDestroy(exec);
         if (graph) cudaGraphDestroy(graph);

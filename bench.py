@@ -59,7 +59,7 @@ def parse():
     ap.add_argument("--n", type=int, default=16384, help="planetesimals (plus one star)")
     ap.add_argument("--ensemble-systems", type=int, default=4096)
     ap.add_argument("--ensemble-years", type=float, default=1.0)
-    ap.add_argument("--wh-steps", type=int, default=20)
+    ap.add_argument("--wh-steps", type=int, default=64)
     ap.add_argument("--gr-years", type=float, default=1.0)
     ap.add_argument("--no-extras", action="store_true", help="only the headline force line")
     ap.add_argument("--extras", default="ensemble,wh,radau",

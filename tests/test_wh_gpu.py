@@ -1,7 +1,10 @@
 """Wisdom-Holman on the device against the reference's golden run and the
-oracle.  The Kepler solver uses the device's transcendental functions, which
-differ from the host libm in the last bits, so states are compared to 1e-10
-relative (max over bodies); the step count and final time are exact."""
+oracle, in both forms: exact (the reference's expressions, the device's
+transcendental functions, which differ from the host libm in the last bits)
+and fast (series Stumpff functions, a third-order starting value for the
+Kepler iteration, reciprocals and r^-3 without divisions).  States are
+compared to 1e-10 relative (max over bodies); the step count and final time
+are exact."""
 import numpy as np
 import pytest
 
@@ -13,6 +16,13 @@ G = ics.G_SOLAR
 TOL = 1e-10
 
 
+@pytest.fixture(params=["fp64", "exact"])
+def wh_mode(sim, request):
+    old = sim.set_force_mode(request.param)
+    yield request.param
+    sim.set_force_mode(old)
+
+
 def _wh(sim, p, v, m, t0, t1, dt):
     sim.set_state(p, v, m, np.zeros(m.size), m.size, G, 0.0)
     sim.integrator_wh(t0, t1, dt)
@@ -21,7 +31,7 @@ def _wh(sim, p, v, m, t0, t1, dt):
     return pos, vel, sim.get_model_time()
 
 
-def test_golden_wh(sim, golden):
+def test_golden_wh(sim, golden, wh_mode):
     t0, t1, dt = golden["wh_span"]
     pos, vel, t = _wh(sim, golden["wh_in_pos"], golden["wh_in_vel"], golden["wh_m"], t0, t1, dt)
     assert t == golden["wh_t"][0]
@@ -29,7 +39,7 @@ def test_golden_wh(sim, golden):
     assert rel_err_per_body(vel, golden["wh_vel"]) <= TOL
 
 
-def test_wh_massive_bodies_only(sim, oracle):
+def test_wh_massive_bodies_only(sim, oracle, wh_mode):
     """No tail: every body goes through the head kernel."""
     p, v, m, r = ics.planetary_system(seed=61, n_planets=7, n_tp=0)
     p, v = ics.to_heliocentric(p, v)
@@ -39,7 +49,7 @@ def test_wh_massive_bodies_only(sim, oracle):
     assert rel_err_per_body(pos, ref["pos"]) <= TOL and rel_err_per_body(vel, ref["vel"]) <= TOL
 
 
-def test_wh_interleaved_massless(sim, oracle):
+def test_wh_interleaved_massless(sim, oracle, wh_mode):
     """A massless body between massive ones stays in the head."""
     p, v, m, r = ics.test_particle_swarm(seed=62, n_tp=50, n_planets=4)
     m = m.copy()
@@ -50,7 +60,7 @@ def test_wh_interleaved_massless(sim, oracle):
     assert rel_err_per_body(pos, ref["pos"]) <= TOL and rel_err_per_body(vel, ref["vel"]) <= TOL
 
 
-def test_wh_swarm_64k_vs_oracle(sim, oracle):
+def test_wh_swarm_64k_vs_oracle(sim, oracle, wh_mode):
     p, v, m, r = ics.test_particle_swarm(seed=63, n_tp=65536)
     p, v = ics.to_heliocentric(p, v)
     ref = oracle.wh(p, v, m, G, 0.0, 0.1, 0.01, sparse=True)
@@ -59,7 +69,7 @@ def test_wh_swarm_64k_vs_oracle(sim, oracle):
     assert rel_err_per_body(pos, ref["pos"]) <= TOL and rel_err_per_body(vel, ref["vel"]) <= TOL
 
 
-def test_wh_full_swarm_steps(sim, oracle):
+def test_wh_full_swarm_steps(sim, oracle, wh_mode):
     """The 1,048,581-body workload, three steps, against the oracle's O(N N_m)
     restatement (bit-identical to the reference's O(N^2) loop)."""
     p, v, m, r = ics.test_particle_swarm()
