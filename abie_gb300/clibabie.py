@@ -106,6 +106,23 @@ class CLibABIE(object):
         ext_acc = _f64(ext_acc)
         self.lib.set_additional_forces(_c.c_int(len(ext_acc) // 3), _vp(ext_acc))
 
+    # The reference's wrappers of the direct entry points (abie/clibabie.py:112-146)
+    # omit r_vec; these pass the full argument list (radii are unused by all
+    # three) and update pos / vel in place.
+    def _direct(self, fn, pos, vel, masses, N, G, t, t_end, dt):
+        radii = np.zeros(N)
+        fn(_vp(pos), _vp(vel), _vp(masses), _vp(radii), _c.c_size_t(N), _c.c_double(G),
+           _c.c_double(t), _c.c_double(t_end), _c.c_double(dt))
+
+    def integrator_runge_kutta(self, pos, vel, masses, N, G, t, t_end, dt):
+        self._direct(self.lib.integrator_runge_kutta, pos, vel, masses, N, G, t, t_end, dt)
+
+    def integrator_gauss_radau15(self, pos, vel, masses, N, G, t, t_end, dt):
+        self._direct(self.lib.integrator_gauss_radau15, pos, vel, masses, N, G, t, t_end, dt)
+
+    def integrator_wisdom_holman(self, pos, vel, masses, N, G, t, t_end, dt):
+        self._direct(self.lib.integrator_wisdom_holman, pos, vel, masses, N, G, t, t_end, dt)
+
     def integrator_gr(self, t, t_end, dt):
         ret = self.lib.integrator_gr(_c.c_double(t), _c.c_double(t_end), _c.c_double(dt))
         if ret == 1:

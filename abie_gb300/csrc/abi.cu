@@ -218,6 +218,7 @@ int finalize_code(void)
     force_scratch_free(s.fs);
     free_engine_buffers();
     free_wh_buffers();
+    free_rk_buffers();
     // like the reference, a finalized library is not re-initialized in the
     // same process (src/common.c:506-522 leaves code_inited set)
     return 0;
@@ -408,15 +409,6 @@ int abie_force_device(const double *d_pos, const double *d_m, size_t N, double G
     rc = launch_force(mode, d_pos, d_m, (int)lo32(N), G, g_sim.fs, d_acc, st);
     if (!rc) g_sim.ctr.force_calls++;
     return rc;
-}
-
-int integrator_rk(double t, double t_end, double dt)
-{
-    (void)t;
-    (void)t_end;
-    (void)dt;
-    set_error(ABIE_ERR_UNSUPPORTED, "Runge-Kutta (src/integrator_runge_kutta.c) is not on the GPU path");
-    return ABIE_ERR_UNSUPPORTED;
 }
 
 }  // extern "C"

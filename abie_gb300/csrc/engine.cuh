@@ -36,4 +36,9 @@ int wh_run(const SystemView &sys, double t, double t_end, double dt, double *t_o
            abie_counters *ctr, cudaStream_t st);
 void free_wh_buffers();
 
+// Runge-Kutta 4 (rk.cu) on device arrays, in the current force form.
+int rk_run(double *pos, double *vel, const double *m, int n, double G, double t, double t_end,
+           double dt, double *t_out, cudaStream_t st);
+void free_rk_buffers();
+
 }  // namespace abie

@@ -465,7 +465,7 @@ __global__ void __launch_bounds__(256) wh_head_kernel(WhArgs a, int init)
 // back, acceleration, kick) with the head's published quantities.
 // MODE: ABIE_FORCE_EXACT keeps the reference's expressions (sqrt, divisions,
 // correctly rounded cubes, closed-form Stumpff functions); the fast form
-// uses kepler_drift_fast and the 13-instruction r^-3 of the force kernels.
+// uses kepler_drift_fast and the one-instruction r^-3 of the force kernels.
 template <int MODE>
 __global__ void __launch_bounds__(256) wh_tail_kernel(WhArgs a, int init)
 {

@@ -77,8 +77,10 @@ int integrator_gr(double t, double t_end, double dt);
 /* src/common.c:534-537 -> src/integrator_wisdom_holman.c:513-537.
  * Fixed-step Wisdom-Holman on a heliocentric state. */
 int integrator_wh(double t, double t_end, double dt);
-/* src/common.c:529-532.  Runge-Kutta is not part of the GPU path:
- * returns ABIE_ERR_UNSUPPORTED. */
+/* src/common.c:529-532 -> src/integrator_runge_kutta.c:6-50.  Classical
+ * RK4 on the device-resident state in the current force form (the exact
+ * form reproduces the reference's doubles for non-negative masses); like
+ * the reference, it leaves the model time unchanged. */
 int integrator_rk(double t, double t_end, double dt);
 /* src/common.c:464-481.  Total energy of the stored state (FP64). */
 double calculate_energy(void);
@@ -98,6 +100,10 @@ size_t calculate_accelerations(const double *pos, const double *vel, size_t N,
 size_t integrator_gauss_radau15(double *pos, double *vel, double *m_vec,
                                 double *r_vec, size_t N, double G, double t,
                                 double t_end, double dt);
+/* src/integrator_runge_kutta.c:52-60 on caller arrays. */
+void integrator_runge_kutta(double *pos, double *vel, double *m_vec,
+                            double *r_vec, size_t N, double G, double t,
+                            double t_end, double dt);
 /* src/integrator_wisdom_holman.c:513 on caller arrays. */
 void integrator_wisdom_holman(double *pos, double *vel, double *m_vec,
                               double *r_vec, size_t N, double G, double t,

@@ -137,6 +137,15 @@ class Oracle:
                                  ctypes.c_double(dt), ctypes.byref(t_out), ctypes.c_int(int(sparse)))
         return {"pos": pos, "vel": vel, "t": t_out.value, "kepler_failures": failed}
 
+    def rk(self, pos, vel, m, G, t, t_end, dt):
+        """src/integrator_runge_kutta.c:6-50 (orc_rk)."""
+        pos, vel, m = _f64(pos).copy(), _f64(vel).copy(), _f64(m)
+        t_out = ctypes.c_double(t)
+        self.lib.orc_rk(_ptr(pos), _ptr(vel), _ptr(m), ctypes.c_size_t(m.size), ctypes.c_double(G),
+                        ctypes.c_double(t), ctypes.c_double(t_end), ctypes.c_double(dt),
+                        ctypes.byref(t_out))
+        return {"pos": pos, "vel": vel, "t": t_out.value}
+
     def wh_accel(self, pos, jpos, m, G, sparse=True):
         pos, jpos, m = _f64(pos), _f64(jpos), _f64(m)
         acc = np.zeros(3 * m.size)
@@ -270,6 +279,16 @@ class Reference:
             ctypes.c_double(t), ctypes.c_double(t_end), ctypes.c_double(dt)))
         p, v = self._state(m.size)
         return {"pos": p, "vel": v, "t": self.lib.get_model_time()}
+
+
+    def rk(self, pos, vel, m, G, t, t_end, dt):
+        """integrator_rk on the stored state (it leaves the model time alone)."""
+        pos, vel, m = _f64(pos), _f64(vel), _f64(m)
+        self._load(pos, vel, m, np.zeros(m.size), G)
+        _run_big_stack(lambda: self.lib.integrator_rk(
+            ctypes.c_double(t), ctypes.c_double(t_end), ctypes.c_double(dt)))
+        p, v = self._state(m.size)
+        return {"pos": p, "vel": v}
 
 
 def reference_available():

@@ -645,3 +645,62 @@ long orc_wh(double *pos, double *vel, const double *m, size_t n, double G,
     free(jpos); free(jvel); free(acc);
     return failed;
 }
+
+/* ------------------------------------------------------------------ */
+/* Runge-Kutta 4: src/integrator_runge_kutta.c                          */
+
+/* src/common.c:3-36.  Sources are the bodies with nonzero mass (negative
+ * masses included, unlike ode_n_body_second_order); every body is a sink. */
+void orc_first_order(const double *vec, size_t n, double G, const double *m, double *dxdt)
+{
+    for (size_t i = 0; i < 3 * n; i++) dxdt[i] = vec[3 * n + i];
+    for (size_t j = 0; j < n; j++) {
+        double x = vec[j * 3], y = vec[j * 3 + 1], z = vec[j * 3 + 2];
+        double ax = 0.0, ay = 0.0, az = 0.0;
+        for (size_t k = 0; k < n; k++) {
+            if ((j == k) || (m[k] == 0)) continue;
+            double GM = G * m[k];
+            double dx = x - vec[k * 3];
+            double dy = y - vec[k * 3 + 1];
+            double dz = z - vec[k * 3 + 2];
+            double r2 = dx * dx + dy * dy + dz * dz;
+            double r3 = sqrt(r2) * r2;
+            ax -= (GM * dx / r3);
+            ay -= (GM * dy / r3);
+            az -= (GM * dz / r3);
+        }
+        dxdt[(n + j) * 3] = ax;
+        dxdt[(n + j) * 3 + 1] = ay;
+        dxdt[(n + j) * 3 + 2] = az;
+    }
+}
+
+/* src/integrator_runge_kutta.c:6-50 */
+void orc_rk(double *pos, double *vel, const double *m, size_t n, double G, double t,
+            double t_end, double dt, double *t_out)
+{
+    size_t d = 6 * n;
+    double *k1 = (double *)malloc(d * sizeof(double));
+    double *k2 = (double *)malloc(d * sizeof(double));
+    double *k3 = (double *)malloc(d * sizeof(double));
+    double *k4 = (double *)malloc(d * sizeof(double));
+    double *tmp = (double *)malloc(d * sizeof(double));
+    double *vec = (double *)malloc(d * sizeof(double));
+    for (size_t i = 0; i < 3 * n; i++) vec[i] = pos[i];
+    for (size_t i = 3 * n; i < d; i++) vec[i] = vel[i - 3 * n];
+    while (t < t_end) {
+        orc_first_order(vec, n, G, m, k1);
+        for (size_t i = 0; i < d; i++) tmp[i] = vec[i] + 0.5 * dt * k1[i];
+        orc_first_order(tmp, n, G, m, k2);
+        for (size_t i = 0; i < d; i++) tmp[i] = vec[i] + 0.5 * dt * k2[i];
+        orc_first_order(tmp, n, G, m, k3);
+        for (size_t i = 0; i < d; i++) tmp[i] = vec[i] + dt * k3[i];
+        orc_first_order(tmp, n, G, m, k4);
+        for (size_t i = 0; i < d; i++) vec[i] += (dt * (k1[i] + 2 * k2[i] + 2 * k3[i] + k4[i]) / 6.0);
+        t += dt;
+    }
+    if (t_out) *t_out = t;
+    for (size_t i = 0; i < 3 * n; i++) pos[i] = vec[i];
+    for (size_t i = 3 * n; i < d; i++) vel[i - 3 * n] = vec[i];
+    free(k1); free(k2); free(k3); free(k4); free(tmp); free(vec);
+}

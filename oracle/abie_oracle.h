@@ -71,6 +71,12 @@ void orc_jacobi2helio(const double *jpos, const double *jvel, const double *m,
                       size_t n, double *pos, double *vel);
 /* src/integrator_wisdom_holman.c:66-147; returns 1 when not converged. */
 int orc_kepler(double *jpos, double *jvel, double gm, double dt, size_t id);
+/* src/common.c:3-36: derivative of the first-order state vec = (pos, vel). */
+void orc_first_order(const double *vec, size_t n, double G, const double *m, double *dxdt);
+/* src/integrator_runge_kutta.c:6-50: classical RK4 from t while t < t_end
+ * in steps of dt; pos/vel updated in place, *t_out the accumulated time. */
+void orc_rk(double *pos, double *vel, const double *m, size_t n, double G, double t,
+            double t_end, double dt, double *t_out);
 
 #ifdef __cplusplus
 }

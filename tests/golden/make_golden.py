@@ -5,7 +5,7 @@ Run in a container where the reference sources exist:
     oracle/build_ref.sh && python tests/golden/make_golden.py
 
 Every output array below comes from the reference's own entry points
-(ode_n_body_second_order, calculate_energy, integrator_gr, integrator_wh,
+(ode_n_body_second_order, calculate_energy, integrator_gr, integrator_wh, integrator_rk,
 the event buffers) driven through ctypes by ``oracle.Reference``.  The
 inputs are the package's seeded generators.  The resulting ``golden.npz``
 is small, committed, and travels with the tests; nothing at test time reads
@@ -95,6 +95,13 @@ def main(out=os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden.np
     gold["wh_span"] = np.array([0.0, 1.0, 0.01])
     gold["wh_pos"], gold["wh_vel"], gold["wh_t"] = out_["pos"], out_["vel"], np.array([out_["t"]])
     gold["wh_energy0"] = np.array([R.energy(p, v, m, G)])
+
+    # -- Runge-Kutta 4 (src/integrator_runge_kutta.c) ---------------------------------
+    p, v, m, r = ics.planetary_system(seed=71, n_planets=6, n_tp=10)
+    out_ = R.rk(p, v, m, G, 0.0, 0.5, 0.005)
+    gold["rk_in_pos"], gold["rk_in_vel"], gold["rk_m"] = p, v, m
+    gold["rk_span"] = np.array([0.0, 0.5, 0.005])
+    gold["rk_pos"], gold["rk_vel"] = out_["pos"], out_["vel"]
 
     np.savez_compressed(out, **gold)
     print("wrote", out, os.path.getsize(out), "bytes,", len(gold), "arrays")

@@ -61,6 +61,20 @@ def test_wh_golden(oracle, golden, sparse):
     assert out["t"] == golden["wh_t"][0]
 
 
+def test_rk_golden(oracle, golden):
+    t0, t1, dt = golden["rk_span"]
+    out = oracle.rk(golden["rk_in_pos"], golden["rk_in_vel"], golden["rk_m"], G, t0, t1, dt)
+    assert np.array_equal(out["pos"], golden["rk_pos"])
+    assert np.array_equal(out["vel"], golden["rk_vel"])
+
+
+def test_live_rk(oracle, reference):
+    p, v, m, r = ics.planetary_system(seed=401, n_planets=5, n_tp=20)
+    a = oracle.rk(p, v, m, G, 0.0, 0.2, 0.003)
+    b = reference.rk(p, v, m, G, 0.0, 0.2, 0.003)
+    assert np.array_equal(a["pos"], b["pos"]) and np.array_equal(a["vel"], b["vel"])
+
+
 @pytest.mark.parametrize("seed", [101, 102, 103])
 def test_live_force_energy(oracle, reference, seed):
     p, v, m, r = ics.planetary_system(seed=seed, n_planets=6, n_tp=50)
