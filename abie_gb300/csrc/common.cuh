@@ -29,26 +29,25 @@ int cuda_fail(cudaError_t e, const char *what);
         if (_e != cudaSuccess) return ::abie::cuda_fail(_e, #call);       \
     } while (0)
 
-// Device pair term for the fast FP64 form: G m / r^3 from r^2, with ONE
-// FP64 instruction.
+// Device pair term for the fast FP64 form: G m / r^3 from r^2 with no FP64
+// instruction at all.
 //
 // Seed: r2 truncated to 23 mantissa bits as a float, its single-precision
 // reciprocal square root y truncated to a 21-bit significand m, so that
-// y = m 2^E.  Then y^2 = m^2 2^2E (m^2 < 2^42) is exact in a double
-// (assembled by integer instructions) and y^3 = m^3 2^3E (m^3 < 2^63) exact
-// in a 64-bit integer.  The FP64 pipe computes only e = 1 - r2 y^2
-// (|e| < 2^-18); then
-//     r2^(-3/2) = y^3 (1 - e)^(-3/2) = y^3 (1 + k),  k = 3/2 e + 15/8 e^2 + 35/16 e^3 + O(e^4),
-// with e^2, e^3 in FP32, and everything after e is integer arithmetic:
-// e and the FP32 terms as fixed-point numbers with 62 fractional bits,
-// F = (1 + k) 2^62, the 126-bit product m^3 F (its high word), the product
-// with the 53-bit significand of G m (high word again), and the result
-// assembled as a double.  Every step truncates, so the result sits at most
-// ~2 ulp below the exact value (a C restatement of these operations over
-// 4 million random r2 in [1e-13, 1e13] and G m in [1e-13, 1e4], with the
-// FP32 seed perturbed by 2^-22: at most 2.02 ulp, mean 0.73).  r2 = 0 (a
-// body and itself) gives a finite value, so the caller's 0 * w is exactly
-// zero.  r2 must lie within the FP32 exponent range.
+// y = m 2^E, y^2 = m^2 2^2E (m^2 < 2^42) and y^3 = m^3 2^3E (m^3 < 2^63)
+// exactly, in 64-bit integers.  With e = 1 - r2 y^2 (|e| < 2^-18),
+//     r2^(-3/2) = y^3 (1 - e)^(-3/2) = y^3 (1 + k),  k = 3/2 e + 15/8 e^2 + 35/16 e^3 + O(e^4).
+// Everything is integer arithmetic on fixed-point numbers with 62
+// fractional bits: e from the high word of the product of r2's 53-bit
+// significand and m^2, e^2 and e^3 in FP32, F = (1 + k) 2^62, the high word
+// of m^3 F, the high word of its product with the significand of G m, and
+// the result assembled as a double.  Every step truncates, so the result
+// sits at most ~2 ulp below the exact value (a C restatement of these
+// operations over 4 million random r2 in [1e-13, 1e13] and G m in
+// [1e-13, 1e4], with the FP32 seed perturbed by 2^-22: at most 2.02 ulp,
+// mean 0.73).  r2 = 0 (a body and itself) gives a finite value, so the
+// caller's 0 * w is exactly zero.  r2 must lie within the FP32 exponent
+// range.  The FP64 pipe is left to the separations, r2 and the sums.
 __device__ __forceinline__ int clamp_exp_f32(int hi_rebased)
 {
     // keep the single-precision exponent in [1, 254]
@@ -94,20 +93,22 @@ __device__ __forceinline__ double gm_inv_r3(double r2, double gm)
     const ull m = (ull)(((yb & 0x7FFFFFu) | 0x800000u) >> 3);
     const int E = (int)(yb >> 23) - 147;  // y = m 2^E
     const ull m2 = m * m;                 // [2^40, 2^42)
-    const int p2 = 40 + (int)(m2 >> 41);
-    const double t = __longlong_as_double((long long)(
-        ((ull)(long long)(p2 + 2 * E + 1023) << 52) | ((m2 << (52 - p2)) & 0xFFFFFFFFFFFFFull)));
-    const double e = fma(-r2, t, 1.0);  // the one FP64 instruction
-    // e as a fixed-point number, 62 fractional bits (truncated)
-    const ull eb = (ull)__double_as_longlong(e);
-    const int ex = (int)((eb >> 52) & 0x7FF);
-    const ull mt = (eb & 0xFFFFFFFFFFFFFull) | (1ull << 52);
-    const int sh = max(1013 - ex, 0);
-    const ull ea = sh < 64 ? (mt >> sh) : 0ull;
-    const long long eh = (eb >> 63) ? -(long long)ea : (long long)ea;
-    // 15/8 e^2 + 35/16 e^3 in FP32 (non-negative), to the same fixed point
-    float ef = f64_to_f32_trunc23(e);
-    ef = (eb >> 63) ? -ef : ef;
+    // e 2^62 = 2^62 - r2 m^2 2^(2E + 62), r2 = Mr 2^(er - 1075): the high
+    // word of (Mr 2^11)(m^2 2^22) is Mr m^2 / 2^31, about 2^T
+    const ull rb = (ull)__double_as_longlong(r2);
+    const int er = (int)((rb >> 52) & 0x7FF);
+    const ull Mr = (rb & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+    const ull Phi = __umul64hi(Mr << 11, m2 << 22);
+    const int s2 = 1044 - er - 2 * E - 62;  // 0..2 for r2 in range
+    long long eh = 0;                        // r2 = 0: any finite value
+    if (s2 >= 0 && s2 < 64) eh = (long long)((1ull << 62) - (Phi >> s2));
+    else if (s2 < 0 && s2 > -3) eh = (long long)((1ull << 62) - (Phi << (-s2)));
+    // e as a float (truncated) for the FP32 terms
+    const ull ae = (ull)(eh < 0 ? -eh : eh);
+    const int lze = __clzll((long long)ae);
+    const unsigned fb = ae ? (((unsigned)(128 - lze) << 23) | (unsigned)(((ae << lze) >> 40) & 0x7FFFFFull)) : 0u;
+    const float ef = __uint_as_float(fb | (eh < 0 ? 0x80000000u : 0u));
+    // 15/8 e^2 + 35/16 e^3 (non-negative) to the same fixed point
     const float q = ef * ef * fmaf(2.1875f, ef, 1.875f);
     const unsigned qb = __float_as_uint(q);
     const int eq = (int)(qb >> 23);
@@ -198,8 +199,8 @@ __device__ __forceinline__ void pair_exact(double xj, double yj, double zj, cons
     az -= s.gm * dz / r3;
 }
 
-// Fast FP64 pair contribution (13 FP64 operations: 3 differences, 3 for r^2,
-// 4 for G m r^-3, 3 accumulations).
+// Fast FP64 pair contribution (9 FP64 operations: 3 differences, 3 for r^2,
+// 3 accumulations; G m r^-3 takes none).
 __device__ __forceinline__ void pair_fast(double xj, double yj, double zj, const Src &s,
                                           double &ax, double &ay, double &az)
 {

@@ -353,7 +353,7 @@ def run_ensemble(lib, args, rank, dev):
     time.  Every rank draws its own systems (weak scaling).
 
     Forms: plain_fp64 = the reference's FP64 operations and predictor in the
-    batched kernel (the comparator); fp64 = 10-instruction pair terms and
+    batched kernel (the comparator); fp64 = 9-instruction pair terms and
     the corrector on the Newton-form coefficients, each step starting from
     g consistent with the reference's plain guess; learned = that with the
     BF16 network's guess, trained online on samples the ensemble records on
