@@ -85,24 +85,27 @@ __device__ __forceinline__ double f32_to_f64_signed(float f)
     return __hiloint2double((int)(((b >> 3) + ((1023 - 127) << 20)) | sgn), (int)(b << 29));
 }
 
-__device__ __forceinline__ double gm_inv_r3(double r2, double gm)
+// The core on r2 = Mr 2^Er, Mr a 64-bit significand with its top bit set
+// (or 0 for r2 = 0).
+__device__ __forceinline__ double gm_inv_r3_int(unsigned long long Mr, int Er, double gm)
 {
     typedef unsigned long long ull;
-    const float yf = rsqrtf(f64_to_f32_trunc23(r2));
+    // seed: r2 truncated to 24 bits as a float, its rsqrtf cut to 21 bits
+    const int fe = min(max(Er + 63 + 127, 1), 254);
+    const float r2f = __uint_as_float(Mr ? (((unsigned)fe << 23) | (unsigned)((Mr >> 40) & 0x7FFFFFull))
+                                         : (1u << 23));
+    const float yf = rsqrtf(r2f);
     const unsigned yb = __float_as_uint(yf);
     const ull m = (ull)(((yb & 0x7FFFFFu) | 0x800000u) >> 3);
     const int E = (int)(yb >> 23) - 147;  // y = m 2^E
     const ull m2 = m * m;                 // [2^40, 2^42)
-    // e 2^62 = 2^62 - r2 m^2 2^(2E + 62), r2 = Mr 2^(er - 1075): the high
-    // word of (Mr 2^11)(m^2 2^22) is Mr m^2 / 2^31, about 2^T
-    const ull rb = (ull)__double_as_longlong(r2);
-    const int er = (int)((rb >> 52) & 0x7FF);
-    const ull Mr = (rb & 0xFFFFFFFFFFFFFull) | (1ull << 52);
-    const ull Phi = __umul64hi(Mr << 11, m2 << 22);
-    const int s2 = 1044 - er - 2 * E - 62;  // 0..2 for r2 in range
-    long long eh = 0;                        // r2 = 0: any finite value
-    if (s2 >= 0 && s2 < 64) eh = (long long)((1ull << 62) - (Phi >> s2));
-    else if (s2 < 0 && s2 > -3) eh = (long long)((1ull << 62) - (Phi << (-s2)));
+    // e 2^62 = 2^62 - r2 m^2 2^(2E + 62); the high word of Mr (m^2 2^22)
+    // is Mr m^2 / 2^42
+    const ull Phi = __umul64hi(Mr, m2 << 22);
+    const int s2 = -(104 + Er + 2 * E);  // 0..2 for r2 in range
+    long long eh = 0;                    // r2 = 0: any finite value
+    if (Mr && s2 >= 0 && s2 < 64) eh = (long long)((1ull << 62) - (Phi >> s2));
+    else if (Mr && s2 < 0 && s2 > -3) eh = (long long)((1ull << 62) - (Phi << (-s2)));
     // e as a float (truncated) for the FP32 terms
     const ull ae = (ull)(eh < 0 ? -eh : eh);
     const int lze = __clzll((long long)ae);
@@ -129,6 +132,49 @@ __device__ __forceinline__ double gm_inv_r3(double r2, double gm)
     const ull Zn = Z << lz2;
     const int be = min(max(eg + 3 * E - lz - lz2 + 66, 1), 2046);
     return __longlong_as_double((long long)(((ull)be << 52) | ((Zn >> 11) & 0xFFFFFFFFFFFFFull)));
+}
+
+__device__ __forceinline__ double gm_inv_r3(double r2, double gm)
+{
+    typedef unsigned long long ull;
+    const ull rb = (ull)__double_as_longlong(r2);
+    const int er = (int)((rb >> 52) & 0x7FF);
+    const ull Mr = er ? (((rb & 0xFFFFFFFFFFFFFull) | (1ull << 52)) << 11) : 0ull;
+    return gm_inv_r3_int(Mr, er - 1075 - 11, gm);
+}
+
+// d^2 for a double d as S 2^e2, S = the high word of (M 2^11)^2 (top bit set)
+// for d's 53-bit significand M; S = 0 for d = 0 (or subnormal).
+__device__ __forceinline__ void square_int(double d, unsigned long long &S, int &e2)
+{
+    typedef unsigned long long ull;
+    const ull b = (ull)__double_as_longlong(d);
+    const int ex = (int)((b >> 52) & 0x7FF);
+    const ull M = ((b & 0xFFFFFFFFFFFFFull) | (1ull << 52)) << 11;
+    S = ex ? __umul64hi(M, M) : 0ull;
+    e2 = ex ? 2 * (ex - 1075) + 42 : -100000;
+}
+
+// r2 = dx^2 + dy^2 + dz^2 as Mr 2^Er (64-bit significand, top bit set, or
+// 0), all integer: the three squares' high words aligned to the largest
+// exponent and added (truncating; about 2^-61 relative).
+__device__ __forceinline__ void r2_int(double dx, double dy, double dz, unsigned long long &Mr,
+                                       int &Er)
+{
+    typedef unsigned long long ull;
+    ull Sx, Sy, Sz;
+    int ex, ey, ez;
+    square_int(dx, Sx, ex);
+    square_int(dy, Sy, ey);
+    square_int(dz, Sz, ez);
+    const int K = max(ex, max(ey, ez));
+    const int hx = K - ex, hy = K - ey, hz = K - ez;
+    ull T = (hx < 64 ? (Sx >> hx) : 0ull) >> 2;
+    T += (hy < 64 ? (Sy >> hy) : 0ull) >> 2;
+    T += (hz < 64 ? (Sz >> hz) : 0ull) >> 2;
+    const int lz = __clzll((long long)T);
+    Mr = T ? (T << lz) : 0ull;
+    Er = K + 2 - lz;
 }
 
 // 1/sqrt(x) and 1/x for positive normal x within the single-precision
@@ -199,16 +245,20 @@ __device__ __forceinline__ void pair_exact(double xj, double yj, double zj, cons
     az -= s.gm * dz / r3;
 }
 
-// Fast FP64 pair contribution (9 FP64 operations: 3 differences, 3 for r^2,
-// 3 accumulations; G m r^-3 takes none).
+// Fast FP64 pair contribution: 6 FP64 instructions (3 separations, 3
+// accumulations); r2 and G m r^-3 are integer arithmetic (r2_int,
+// gm_inv_r3_int; a C restatement of the whole term over 4 million random
+// separations and masses: at most 2.02 ulp from the exact G m r^-3).
 __device__ __forceinline__ void pair_fast(double xj, double yj, double zj, const Src &s,
                                           double &ax, double &ay, double &az)
 {
-    double dx = xj - s.x;
-    double dy = yj - s.y;
-    double dz = zj - s.z;
-    double r2 = fma(dz, dz, fma(dy, dy, dx * dx));
-    double w = gm_inv_r3(r2, s.gm);
+    const double dx = xj - s.x;
+    const double dy = yj - s.y;
+    const double dz = zj - s.z;
+    unsigned long long Mr;
+    int Er;
+    r2_int(dx, dy, dz, Mr, Er);
+    const double w = gm_inv_r3_int(Mr, Er, s.gm);
     ax = fma(-w, dx, ax);
     ay = fma(-w, dy, ay);
     az = fma(-w, dz, az);

@@ -6,7 +6,7 @@
 //   fp64  : the production FP64 form.  A group of 1, 8 or 32 lanes shares a
 //           sink and splits its sources; partial sums meet in a fixed
 //           butterfly of warp shuffles, so results are deterministic.  The
-//           pair term is gm_inv_r3() (9 FP64 operations per interaction).
+//           pair term is pair_fast() (6 FP64 operations per interaction).
 //           Sinks are handed out to lane groups from an atomic counter, so
 //           the grid has no tail of idle SMs.
 //           Sources can also be split into chunks whose partial sums are

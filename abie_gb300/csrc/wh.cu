@@ -269,7 +269,10 @@ template <int MODE>
 __device__ __forceinline__ double wh_ir3(double x, double y, double z)
 {
     if (MODE == ABIE_FORCE_EXACT) return 1.0 / cube_cr(norm3(x, y, z));
-    return gm_inv_r3(fma(z, z, fma(y, y, x * x)), 1.0);
+    unsigned long long Mr;
+    int Er;
+    r2_int(x, y, z, Mr, Er);
+    return gm_inv_r3_int(Mr, Er, 1.0);
 }
 
 template <int MODE>
@@ -518,8 +521,8 @@ __global__ void __launch_bounds__(256) wh_tail_kernel(WhArgs a, int init)
             for (int c = 0; c < 3; c++) a3[c] -= hs[4 * q + 3] * aux * d[c];
         }
     } else {
-        ir3h = gm_inv_r3(fma(p[2], p[2], fma(p[1], p[1], p[0] * p[0])), 1.0);
-        ir3j = gm_inv_r3(fma(jp[2], jp[2], fma(jp[1], jp[1], jp[0] * jp[0])), 1.0);
+        ir3h = wh_ir3<MODE>(p[0], p[1], p[2]);
+        ir3j = wh_ir3<MODE>(jp[0], jp[1], jp[2]);
         for (int q = 0; q < n_src; q++) {
             Src sq{hs[4 * q], hs[4 * q + 1], hs[4 * q + 2], hs[4 * q + 3]};
             pair_fast(p[0], p[1], p[2], sq, a3[0], a3[1], a3[2]);

@@ -47,6 +47,10 @@ from abie_gb300 import ics  # noqa: E402
 
 G = ics.G_SOLAR
 FLOP_PER_INTERACTION = 20  # the convention of the reference's tiled kernel comments
+FP64_INSTR_PER_INTERACTION = 6  # the fast form's pair term (abie_gb300/csrc/common.cuh pair_fast)
+# dram__bytes_read.sum + dram__bytes_write.sum of one force-kernel launch,
+# from the ncu capture summarised in profiles/force_fp64_disk16385.md.
+DRAM_BYTES_PER_LAUNCH = {("fp64", 16385): 1074688}
 
 
 def parse():
@@ -284,10 +288,18 @@ def run_ours(args):
             "unit": "TFLOP/s", "frac": ach / peak if peak else None, "traffic": None,
             "peak_source": "measured FMA throughput (abie_measure_fp64_peak) on this GPU",
             "flop_per_interaction": FLOP_PER_INTERACTION}
-    prof = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.isfile(prof):
-        with open(prof) as fh:
-            roof["traffic"] = json.load(fh).get("force_%s_%d" % (args.mode, m.size))
+    if args.mode == "fp64":
+        # The fast form executes 6 FP64 instructions per interaction (3
+        # separations, 3 sums); r^2 and G m r^-3 are integer arithmetic, so the
+        # 20-flop convention reads above the FMA peak.  The FP64 pipe's own
+        # utilisation: executed FP64 instructions / (FMA peak / 2 flop).
+        roof["fp64_instructions_per_interaction"] = FP64_INSTR_PER_INTERACTION
+        roof["fp64_pipe_frac"] = (FP64_INSTR_PER_INTERACTION * inter / (ms_step * 1e-3)
+                                  / (peak * 1e12 / 2) if peak else None)
+        roof["note"] = ("frac uses the 20-flop convention against the FMA peak; the kernel does "
+                        "r^2 and G m r^-3 in integer arithmetic (6 FP64 instructions per "
+                        "interaction), so frac > 1 and fp64_pipe_frac is the FP64 pipe's use")
+    roof["traffic"] = DRAM_BYTES_PER_LAUNCH.get((args.mode, int(m.size)))
 
     extra = {}
     if not args.no_extras:
@@ -353,7 +365,7 @@ def run_ensemble(lib, args, rank, dev):
     time.  Every rank draws its own systems (weak scaling).
 
     Forms: plain_fp64 = the reference's FP64 operations and predictor in the
-    batched kernel (the comparator); fp64 = 9-instruction pair terms and
+    batched kernel (the comparator); fp64 = 6-instruction pair terms and
     the corrector on the Newton-form coefficients, each step starting from
     g consistent with the reference's plain guess; learned = that with the
     BF16 network's guess, trained online on samples the ensemble records on
