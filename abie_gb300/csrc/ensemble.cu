@@ -50,12 +50,6 @@ static constexpr double H_MIN = 1.e-13;
 static constexpr int ENS_MAX_BODIES = 21;  // 3N <= 64: two components per lane
 static constexpr int WARPS = 4;            // warps per block
 static constexpr int STATE_PER_COMP = 18;  // y0 dy0 F1 b[7] g[7] b6p
-#ifndef ENS_BLOCKS_NC1
-#define ENS_BLOCKS_NC1 4  // blocks per SM the plain one-component variant is built for
-#endif
-#ifndef ENS_BLOCKS_NC2
-#define ENS_BLOCKS_NC2 2
-#endif
 
 struct EnsScalars {
     double t, h;
@@ -305,47 +299,6 @@ __device__ __forceinline__ double absmax_or_none(double v)
     return (a == a) ? a : -1.7976931348623157e308;
 }
 
-// Accelerations of the n bodies whose predicted positions and G m are in
-// sp[k] = {x, y, z, Gm}; the result of sink i goes to sa[i].
-template <int MODE>
-__device__ __forceinline__ void warp_force(int n, const double (*sp)[4], double (*sa)[3], int lane,
-                                           int L)
-{
-    const int g = lane / L, hh = lane % L;
-    double ax = 0.0, ay = 0.0, az = 0.0;
-    if (g < n) {
-        const double xi = sp[g][0], yi = sp[g][1], zi = sp[g][2];
-        for (int k = hh; k < n; k += L) {
-            double gm = sp[k][3];
-            if (k == g || !(gm > 0.0)) continue;
-            Src s{sp[k][0], sp[k][1], sp[k][2], gm};
-            if (MODE == ABIE_FORCE_EXACT) pair_exact(xi, yi, zi, s, ax, ay, az);
-            else pair_fast(xi, yi, zi, s, ax, ay, az);
-        }
-    }
-    // partial sums of the lanes of one sink that hold work (the first
-    // min(L, n)), added as a fixed tree: lane hh takes lane hh + o
-    const int W = L < n ? L : n;
-    for (int o = 1; o < W; o <<= 1) {
-        int src = lane + o;
-        src = src < 32 ? src : 31;
-        double ox = __shfl_sync(0xffffffffu, ax, src);
-        double oy = __shfl_sync(0xffffffffu, ay, src);
-        double oz = __shfl_sync(0xffffffffu, az, src);
-        if (hh + o < W) {
-            ax += ox;
-            ay += oy;
-            az += oz;
-        }
-    }
-    if (g < n && hh == 0) {
-        sa[g][0] = ax;
-        sa[g][1] = ay;
-        sa[g][2] = az;
-    }
-    __syncwarp();
-}
-
 // g = C^-1 b for one component: back-substitution through the triangular
 // change of basis b_k = sum_{j>=k} cs[j][k] g_j, so that the corrector's
 // first sweep starts from the polynomial the guess describes.  (The
@@ -362,79 +315,136 @@ __device__ __forceinline__ void consistent_g(Comp &c)
     }
 }
 
+// A system's thread group: W warps (32 W threads, one component each).
+// W = 1 syncs with __syncwarp and reduces with shuffles; W = 2 syncs with a
+// named barrier per group and meets the warps' partial reductions in shared
+// memory (two alternating slots, so a slot is rewritten only after a barrier
+// that every reader of its previous value has passed).
+template <int W>
+struct Group {
+    int gl;    // lane in the group, 0 .. 32 W - 1
+    int lane;  // lane in the warp
+    int wig;   // warp in the group
+    int gidx;  // group in the block
+    double *red;
+    int *flg;
+    int tog;
+    __device__ __forceinline__ void sync() const
+    {
+        if (W == 1) __syncwarp();
+        else asm volatile("bar.sync %0, %1;" ::"r"(1 + gidx), "r"(32 * W) : "memory");
+    }
+    __device__ __forceinline__ double maxd(double v)
+    {
+        v = warp_maxd(v);
+        if (W == 1) return v;
+        if (lane == 0) red[tog * W + wig] = v;
+        sync();
+        double r = red[tog * W];
+#pragma unroll
+        for (int k = 1; k < W; k++) r = fmax(r, red[tog * W + k]);
+        tog ^= 1;
+        return r;
+    }
+    __device__ __forceinline__ bool any(bool b)
+    {
+        b = __any_sync(0xffffffffu, b);
+        if (W == 1) return b;
+        if (lane == 0) flg[tog * W + wig] = b ? 1 : 0;
+        sync();
+        int r = 0;
+#pragma unroll
+        for (int k = 0; k < W; k++) r |= flg[tog * W + k];
+        tog ^= 1;
+        return r != 0;
+    }
+    // the value group lane 0 holds, in every lane (one slot: the next write
+    // comes many barriers later)
+    __device__ __forceinline__ long long bcast0(long long v)
+    {
+        if (W == 1) return __shfl_sync(0xffffffffu, v, 0);
+        long long *slot = reinterpret_cast<long long *>(red + 2 * W);
+        if (gl == 0) *slot = v;
+        sync();
+        const long long r = *slot;
+        sync();
+        return r;
+    }
+};
+
 // At an accepted step (not the last): emit the pending training sample
 // when this step was reached by a single attempt after the previous accept,
 // then replace refine_bs's plain guess E_k by E_k + s_k tau_k out_k (network
 // output) when a network is active, and remember this step's features and
 // E.  Scales s_k are per coefficient order: the largest |b_k| of the body.
-__device__ __forceinline__ void learned_refine(const EnsArgs &a, LearnSmem &L, Comp C[2], int n,
-                                               int lane, bool has0, bool has1, double q, double h,
+template <int W>
+__device__ __forceinline__ void learned_refine(const EnsArgs &a, LearnSmem &L, Group<W> &grp,
+                                               Comp &X, int n, bool has, double q, double h,
                                                double dtreq, const double *m, bool &pend_valid,
                                                bool first_attempt, bool &net_guess,
                                                bool make_consistent)
 {
+    constexpr int GS = 32 * W;
+    const int gl = grp.gl;
     double h_next = (dtreq / h > 1.0 / FAC) ? h / FAC : ((dtreq < 1.e-12) ? h * FAC : dtreq);
     if (h_next < H_MIN) h_next = H_MIN;
     // converged b of this step, per body row (7 per component)
+    if (has) {
+        const int i = gl / 3, d = gl % 3;
 #pragma unroll
-    for (int u = 0; u < 2; u++) {
-        if (!(u == 0 ? has0 : has1)) continue;
-        int c = lane + 32 * u, i = c / 3, d = c % 3;
-        #pragma unroll
-        for (int k = 0; k < 7; k++) L.row[i][7 * d + k] = (float)C[u].b[k];
+        for (int k = 0; k < 7; k++) L.row[i][7 * d + k] = (float)X.b[k];
     }
-    __syncwarp();
-    for (int e = lane; e < n * 7; e += 32) {
+    grp.sync();
+    for (int e = gl; e < n * 7; e += GS) {
         int i = e / 7, k = e % 7;
         float sc = fmaxf(fmaxf(fabsf(L.row[i][k]), fabsf(L.row[i][7 + k])), fabsf(L.row[i][14 + k]));
         L.scale[i][k] = (sc > 0.0f && isfinite(sc)) ? sc : 1.0f;
     }
-    __syncwarp();
+    grp.sync();
     // the pending sample: features of the previous accept, target from this b
     if (a.samples && pend_valid && first_attempt) {
         unsigned long long base = 0;
-        if (lane == 0) base = atomicAdd(a.sample_count, (unsigned long long)n);
-        base = __shfl_sync(0xffffffffu, base, 0);
+        if (gl == 0) base = atomicAdd(a.sample_count, (unsigned long long)n);
+        base = (unsigned long long)grp.bcast0((long long)base);
         if (base + (unsigned long long)n <= (unsigned long long)a.sample_cap) {
-            for (int e = lane; e < n * MLP_IN; e += 32) {
+            for (int e = gl; e < n * MLP_IN; e += GS) {
                 int i = e / MLP_IN, k = e % MLP_IN;
                 a.samples[(base + i) * MLP_SAMPLE + k] = k < MLP_FEAT ? L.pfeat[i][k] : 0.0f;
             }
-            for (int e = lane; e < n * (MLP_OUT_PAD - MLP_OUT); e += 32) {
+            for (int e = gl; e < n * (MLP_OUT_PAD - MLP_OUT); e += GS) {
                 int i = e / (MLP_OUT_PAD - MLP_OUT), k = MLP_OUT + e % (MLP_OUT_PAD - MLP_OUT);
                 a.samples[(base + i) * MLP_SAMPLE + MLP_IN + k] = 0.0f;
             }
+            if (has) {
+                const int i = gl / 3, d = gl % 3;
 #pragma unroll
-            for (int u = 0; u < 2; u++) {
-                if (!(u == 0 ? has0 : has1)) continue;
-                int c = lane + 32 * u, i = c / 3, d = c % 3;
-                #pragma unroll
                 for (int k = 0; k < 7; k++) {
-                    float tgt = ((float)(C[u].b[k] / (double)L.ps[i][k]) - L.pE[i][7 * d + k]) / a.tau[k];
+                    float tgt = ((float)(X.b[k] / (double)L.ps[i][k]) - L.pE[i][7 * d + k]) / a.tau[k];
                     a.samples[(base + i) * MLP_SAMPLE + MLP_IN + 7 * d + k] = tgt;
                 }
             }
         }
     }
     // features of this step (into xh2 as bf16, ld 40) and the plain guess E
-    __syncwarp();
+    grp.sync();
     float lq = fminf(fmaxf(log2f((float)q), -8.0f), 8.0f) * 0.25f;
     float lh = fminf(fmaxf(log2f((float)(h_next / h)), -8.0f), 8.0f) * 0.25f;
+    if (has) {
+        const int i = gl / 3, d = gl % 3;
 #pragma unroll
-    for (int u = 0; u < 2; u++) {
-        if (!(u == 0 ? has0 : has1)) continue;
-        int c = lane + 32 * u, i = c / 3, d = c % 3;
-        #pragma unroll
         for (int k = 0; k < 7; k++) {
             float f = L.row[i][7 * d + k] / L.scale[i][k];
             L.xh2[i][7 * d + k] = __float2bfloat16_rn(f);
             L.pfeat[i][7 * d + k] = f;
         }
-        e_refine(C[u], q);
-        #pragma unroll
-        for (int k = 0; k < 7; k++) L.pE[i][7 * d + k] = (float)(C[u].b[k] / (double)L.scale[i][k]);
     }
-    for (int e = lane; e < LP_ROWS * 40; e += 32) {
+    e_refine(X, q);
+    if (has) {
+        const int i = gl / 3, d = gl % 3;
+#pragma unroll
+        for (int k = 0; k < 7; k++) L.pE[i][7 * d + k] = (float)(X.b[k] / (double)L.scale[i][k]);
+    }
+    for (int e = gl; e < LP_ROWS * 40; e += GS) {
         int i = e / 40, k = e % 40;
         if (i < n && k < MLP_OUT) continue;
         float f = 0.0f;
@@ -448,167 +458,192 @@ __device__ __forceinline__ void learned_refine(const EnsArgs &a, LearnSmem &L, C
         L.xh2[i][k] = __float2bfloat16_rn(f);
         if (i < n && k < MLP_FEAT) L.pfeat[i][k] = f;
     }
-    for (int e = lane; e < n * 7; e += 32) L.ps[e / 7][e % 7] = L.scale[e / 7][e % 7];
+    for (int e = gl; e < n * 7; e += GS) L.ps[e / 7][e % 7] = L.scale[e / 7][e % 7];
     pend_valid = a.samples != nullptr;
-    __syncwarp();
+    grp.sync();
     if (a.mlp) {
-        mlp_warp_forward(a.mlp, L);
+        if (grp.wig == 0) mlp_warp_forward(a.mlp, L);
+        grp.sync();
+        if (has) {
+            const int i = gl / 3, d = gl % 3;
 #pragma unroll
-        for (int u = 0; u < 2; u++) {
-            if (!(u == 0 ? has0 : has1)) continue;
-            int c = lane + 32 * u, i = c / 3, d = c % 3;
-            #pragma unroll
-            for (int k = 0; k < 7; k++) L.plain[c][k] = C[u].b[k];
-            L.plain[c][7] = C[u].b6p;
-            #pragma unroll
+            for (int k = 0; k < 7; k++) L.plain[gl][k] = X.b[k];
+            L.plain[gl][7] = X.b6p;
+#pragma unroll
             for (int k = 0; k < 7; k++) {
                 // outside the training range (|target| <= 20) or non-finite:
                 // keep the plain guess for this coefficient
                 float o = L.row[i][7 * d + k];
                 o = (isfinite(o) && fabsf(o) <= 20.0f) ? o : 0.0f;
-                C[u].b[k] += (double)L.scale[i][k] * (double)a.tau[k] * (double)o;
+                X.b[k] += (double)L.scale[i][k] * (double)a.tau[k] * (double)o;
             }
         }
-        __syncwarp();
+        grp.sync();
         net_guess = true;
     }
-    if (make_consistent) {
-        if (has0) consistent_g(C[0]);
-        if (has1) consistent_g(C[1]);
-    }
+    if (make_consistent && has) consistent_g(X);
 }
 
 // Back to the plain guess (consistent g) that learned_refine kept.
-__device__ __forceinline__ void restore_plain_guess(LearnSmem &L, Comp C[2], int lane, bool has0,
-                                                 bool has1)
+__device__ __forceinline__ void restore_plain_guess(LearnSmem &L, Comp &X, int gl, bool has)
 {
+    if (!has) return;
 #pragma unroll
-    for (int u = 0; u < 2; u++) {
-        if (!(u == 0 ? has0 : has1)) continue;
-        const int c = lane + 32 * u;
-#pragma unroll
-        for (int k = 0; k < 7; k++) C[u].b[k] = L.plain[c][k];
-        C[u].b6p = L.plain[c][7];
-        consistent_g(C[u]);
+    for (int k = 0; k < 7; k++) X.b[k] = L.plain[gl][k];
+    X.b6p = L.plain[gl][7];
+    consistent_g(X);
+}
+
+// Accelerations of the n bodies whose predicted positions and G m are in
+// sp[k] = {x, y, z, Gm}; the result of sink i goes to sa[i].  Warp w of the
+// group takes sinks w spw .. (w + 1) spw - 1, spw = ceil(n / W), with
+// L = 32 / spw lanes per sink (1 in the exact form), each summing every
+// L-th source; the partial sums of the lanes holding work meet in a fixed
+// tree of shuffles (a sink's lanes never straddle warps).
+template <int MODE, int W>
+__device__ __forceinline__ void group_force(const Group<W> &grp, int n, const double (*sp)[4],
+                                            double (*sa)[3])
+{
+    const int spw = (n + W - 1) / W;
+    const int L = MODE == ABIE_FORCE_EXACT ? 1 : max(1, 32 / max(spw, 1));
+    const int lane = grp.lane;
+    const int gw = lane / L, hh = lane % L;
+    const int g = grp.wig * spw + gw;
+    const bool sink = gw < spw && g < n;
+    double ax = 0.0, ay = 0.0, az = 0.0;
+    if (sink) {
+        const double xi = sp[g][0], yi = sp[g][1], zi = sp[g][2];
+        for (int k = hh; k < n; k += L) {
+            double gm = sp[k][3];
+            if (k == g || !(gm > 0.0)) continue;
+            Src s{sp[k][0], sp[k][1], sp[k][2], gm};
+            if (MODE == ABIE_FORCE_EXACT) pair_exact(xi, yi, zi, s, ax, ay, az);
+            else pair_fast(xi, yi, zi, s, ax, ay, az);
+        }
     }
+    const int Wt = L < n ? L : n;
+    for (int o = 1; o < Wt; o <<= 1) {
+        int src = lane + o;
+        src = src < 32 ? src : 31;
+        double ox = __shfl_sync(0xffffffffu, ax, src);
+        double oy = __shfl_sync(0xffffffffu, ay, src);
+        double oz = __shfl_sync(0xffffffffu, az, src);
+        if (hh + o < Wt) {
+            ax += ox;
+            ay += oy;
+            az += oz;
+        }
+    }
+    if (sink && hh == 0) {
+        sa[g][0] = ax;
+        sa[g][1] = ay;
+        sa[g][2] = az;
+    }
+    grp.sync();
 }
 
 // Blocks per SM the register budget is sized for, per variant.
-template <int NC, bool LEARN>
+template <int W, bool LEARN>
 struct EnsOccupancy {
-    static constexpr int value = LEARN ? (NC == 1 ? 4 : 2) : (NC == 1 ? ENS_BLOCKS_NC1 : ENS_BLOCKS_NC2);
+    static constexpr int value = LEARN ? 3 : 4;
 };
 
-template <int MODE, int NC, bool LEARN>
-__global__ void __launch_bounds__(32 * WARPS, (EnsOccupancy<NC, LEARN>::value)) ensemble_kernel(EnsArgs a)
+template <int MODE, int W, bool LEARN>
+__global__ void __launch_bounds__(32 * WARPS, (EnsOccupancy<W, LEARN>::value)) ensemble_kernel(EnsArgs a)
 {
-    __shared__ double s_pos[WARPS][32][4];
-    __shared__ double s_acc[WARPS][32][3];
+    constexpr int GROUPS = WARPS / W;
+    __shared__ double s_pos[GROUPS][32][4];
+    __shared__ double s_acc[GROUPS][32][3];
+    __shared__ double s_red[GROUPS][2 * W + 1];
+    __shared__ int s_flg[GROUPS][2 * W];
     extern __shared__ __align__(16) unsigned char ens_dyn[];  // learned path only
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    LearnSmem &LS = reinterpret_cast<LearnSmem *>(ens_dyn)[w];
-    double(*sp)[4] = s_pos[w];
-    double(*sa)[3] = s_acc[w];
+    Group<W> grp;
+    {
+        const int w = threadIdx.x >> 5;
+        grp.lane = threadIdx.x & 31;
+        grp.wig = w % W;
+        grp.gidx = w / W;
+        grp.gl = grp.wig * 32 + grp.lane;
+        grp.red = s_red[grp.gidx];
+        grp.flg = s_flg[grp.gidx];
+        grp.tog = 0;
+    }
+    const int gl = grp.gl;
+    LearnSmem &LS = reinterpret_cast<LearnSmem *>(ens_dyn)[grp.gidx];
+    double(*sp)[4] = s_pos[grp.gidx];
+    double(*sa)[3] = s_acc[grp.gidx];
     const unsigned long long deadline = ens_timer() + a.budget_ns;
 
     for (;;) {
         int qi = 0;
-        if (lane == 0) qi = atomicAdd(a.queue, 1);
-        qi = __shfl_sync(0xffffffffu, qi, 0);
+        if (gl == 0) qi = atomicAdd(a.queue, 1);
+        qi = (int)grp.bcast0(qi);
         if (qi >= a.n_active) break;
         const int sid = a.active[qi];
         const long long off = a.offsets[sid];
         const int n = (int)(a.offsets[sid + 1] - off);
         const int dim = 3 * n;
-        const int L = MODE == ABIE_FORCE_EXACT ? 1 : max(1, 32 / max(n, 1));
         const double *m = a.m + off;
         EnsScalars S = a.sc[sid];
-        // lane's components c0 = lane, c1 = lane + 32
-        // NC = 1: systems of at most 10 bodies, one component per lane; the
-        // second component's state is then compiled out
-        const bool has0 = lane < dim, has1 = (NC > 1) && (lane + 32 < dim);
-        Comp C[2];
+        const bool has = gl < dim;  // this thread's component c = gl
+        Comp X;
         double *st = a.state + (size_t)STATE_PER_COMP * 3 * off;
-        auto slot = [&](int c, int k) -> double & { return st[(size_t)k * dim + c]; };
+        auto slot = [&](int k) -> double & { return st[(size_t)k * dim + gl]; };
+        if (!has || S.phase == 0) {
+            X.y0 = has ? a.pos[3 * off + gl] : 0.0;
+            X.dy0 = has ? a.vel[3 * off + gl] : 0.0;
+            X.F1 = X.b6p = 0.0;
 #pragma unroll
-        for (int u = 0; u < 2; u++) {
-            const int c = lane + 32 * u;
-            const bool has = u == 0 ? has0 : has1;
-            Comp &X = C[u];
-            if (!has) {
-                X.y0 = X.dy0 = X.F1 = X.b6p = 0.0;
-                #pragma unroll
-                for (int k = 0; k < 7; k++) X.b[k] = X.g[k] = 0.0;
-                continue;
-            }
-            if (S.phase == 0) {
-                X.y0 = a.pos[3 * off + c];
-                X.dy0 = a.vel[3 * off + c];
-                X.F1 = 0.0;
-                X.b6p = 0.0;
-                #pragma unroll
-                for (int k = 0; k < 7; k++) X.b[k] = X.g[k] = 0.0;
-            } else {
-                X.y0 = slot(c, 0);
-                X.dy0 = slot(c, 1);
-                X.F1 = slot(c, 2);
-                #pragma unroll
-                for (int k = 0; k < 7; k++) X.b[k] = slot(c, 3 + k);
-                #pragma unroll
-                for (int k = 0; k < 7; k++) X.g[k] = slot(c, 10 + k);
-                X.b6p = slot(c, 17);
-            }
+            for (int k = 0; k < 7; k++) X.b[k] = X.g[k] = 0.0;
+        } else {
+            X.y0 = slot(0);
+            X.dy0 = slot(1);
+            X.F1 = slot(2);
+#pragma unroll
+            for (int k = 0; k < 7; k++) X.b[k] = slot(3 + k);
+#pragma unroll
+            for (int k = 0; k < 7; k++) X.g[k] = slot(10 + k);
+            X.b6p = slot(17);
         }
         const double G = a.G;
         // publish a predicted position for every body (components of a
         // body may sit on different lanes, so go through shared memory)
-        auto publish = [&](double p0, double p1) {
-            if (has0) sp[lane / 3][lane % 3] = p0;
-            if (has1) sp[(lane + 32) / 3][(lane + 32) % 3] = p1;
-            if (lane < n) sp[lane][3] = m[lane] > 0.0 ? G * m[lane] : 0.0;
-            __syncwarp();
+        auto publish = [&](double p) {
+            if (has) sp[gl / 3][gl % 3] = p;
+            if (gl < n) sp[gl][3] = m[gl] > 0.0 ? G * m[gl] : 0.0;
+            grp.sync();
         };
-        auto force_of = [&](int u) -> double {
-            int c = lane + 32 * u;
-            int i = c / 3;
-            return (m[i] >= 0.0) ? sa[i][c % 3] : 0.0;
-        };
+        auto force_here = [&]() -> double { return (has && m[gl / 3] >= 0.0) ? sa[gl / 3][gl % 3] : 0.0; };
 
         if (S.phase == 0) {
             // F1 = f(y0), then initial_time_step (:75-120)
-            publish(C[0].y0, C[1].y0);
-            warp_force<MODE>(n, sp, sa, lane, L);
-            if (has0) C[0].F1 = force_of(0);
-            if (has1) C[1].F1 = force_of(1);
+            publish(X.y0);
+            group_force<MODE, W>(grp, n, sp, sa);
+            if (has) X.F1 = force_here();
             S.force_calls++;
             // d0, d1 over the first n of the 3n entries, as the reference does
             double d0 = -1.7976931348623157e308, d1 = d0;
-            if (lane < n) {
-                d0 = absmax_or_none(C[0].y0);
-                d1 = absmax_or_none(C[0].F1);
+            if (gl < n) {
+                d0 = absmax_or_none(X.y0);
+                d1 = absmax_or_none(X.F1);
             }
-            if (lane + 32 < n) {
-                d0 = fmax(d0, absmax_or_none(C[1].y0));
-                d1 = fmax(d1, absmax_or_none(C[1].F1));
-            }
-            d0 = warp_maxd(d0);
-            d1 = warp_maxd(d1);
+            d0 = grp.maxd(d0);
+            d1 = grp.maxd(d1);
             double dt0 = (d0 < 1e-5 || d1 < 1e-5) ? 1e-6 : 0.01 * (d0 / d1);
-            __syncwarp();
-            publish(C[0].y0 + dt0 * C[0].dy0, C[1].y0 + dt0 * C[1].dy0);
-            warp_force<MODE>(n, sp, sa, lane, L);
+            grp.sync();
+            publish(X.y0 + dt0 * X.dy0);
+            group_force<MODE, W>(grp, n, sp, sa);
             S.force_calls++;
             double d2 = -1.7976931348623157e308;
-            if (has0) d2 = absmax_or_none(force_of(0) - C[0].F1);
-            if (has1) d2 = fmax(d2, absmax_or_none(force_of(1) - C[1].F1));
-            d2 = warp_maxd(d2) / dt0;
+            if (has) d2 = absmax_or_none(force_here() - X.F1);
+            d2 = grp.maxd(d2) / dt0;
             double dt1;
             if (fmax(d1, d2) <= 1e-15) dt1 = fmax(1e-6, dt0 * 1e-3);
             else dt1 = pow(0.01 / fmax(d1, d2), (1.0 / (15 + 1)));
             S.h = fmin(100 * dt0, dt1);
             S.loop_count = 0;
             S.phase = 1;
-            __syncwarp();
+            grp.sync();
         }
 
         double t = S.t, h = S.h;
@@ -619,53 +654,48 @@ __global__ void __launch_bounds__(32 * WARPS, (EnsOccupancy<NC, LEARN>::value)) 
         bool pend_valid = false, first_attempt = false;
         bool net_guess = false;  // this attempt started from the network's guess
         while (!done) {
-            if (ens_timer() > deadline) break;
+            if (grp.any(ens_timer() > deadline)) break;
             int iters = 0;
             for (int ipc = 0; ipc < 12; ipc++) {
                 iters++;
                 double f8 = -1.7976931348623157e308, db6 = f8;
                 for (int ih = 1; ih < 8; ih++) {
-                    __syncwarp();
+                    grp.sync();
                     const double sh = e_hs[ih], ds = h * sh, hh = 0.5 * ds * ds;
-                    publish(e_pred_pos<MODE>(C[0], ih, sh, h, ds, hh),
-                            e_pred_pos<MODE>(C[1], ih, sh, h, ds, hh));
-                    warp_force<MODE>(n, sp, sa, lane, L);
-#pragma unroll
-                    for (int u = 0; u < 2; u++) {
-                        if (!(u == 0 ? has0 : has1)) continue;
-                        double F = force_of(u);
-                        e_gb_update<MODE>(C[u], ih, F);
+                    publish(e_pred_pos<MODE>(X, ih, sh, h, ds, hh));
+                    group_force<MODE, W>(grp, n, sp, sa);
+                    if (has) {
+                        const double F = force_here();
+                        e_gb_update<MODE>(X, ih, F);
                         if (ih == 7) {
-                            f8 = fmax(f8, absmax_or_none(F));
-                            db6 = fmax(db6, absmax_or_none(e_b6<MODE>(C[u]) - C[u].b6p));
+                            f8 = absmax_or_none(F);
+                            db6 = absmax_or_none(e_b6<MODE>(X) - X.b6p);
                         }
                     }
                 }
                 S.force_calls += 7;
-                f8 = warp_maxd(f8);
-                db6 = warp_maxd(db6);
+                f8 = grp.maxd(f8);
+                db6 = grp.maxd(db6);
                 if (db6 / f8 < TOLPC) break;
-#pragma unroll
-                for (int u = 0; u < 2; u++) C[u].b6p = e_b6<MODE>(C[u]);
+                X.b6p = e_b6<MODE>(X);
             }
             S.iterations += iters;
             S.attempts++;
             // advance
-            __syncwarp();
+            grp.sync();
             const double hh1 = 0.5 * h * h;
-            double ya0 = e_pred_pos<MODE>(C[0], 8, 1.0, h, h, hh1),
-                   ya1 = e_pred_pos<MODE>(C[1], 8, 1.0, h, h, hh1);
-            double va0 = e_pred_vel<MODE>(C[0], h), va1 = e_pred_vel<MODE>(C[1], h);
-            publish(ya0, ya1);
-            warp_force<MODE>(n, sp, sa, lane, L);
+            const double ya = e_pred_pos<MODE>(X, 8, 1.0, h, h, hh1);
+            const double va = e_pred_vel<MODE>(X, h);
+            publish(ya);
+            group_force<MODE, W>(grp, n, sp, sa);
             S.force_calls++;
-            double dd0 = has0 ? force_of(0) : 0.0, dd1 = has1 ? force_of(1) : 0.0;
-            bool bad = (has0 && !isfinite(ya0 + dd0 + va0)) || (has1 && !isfinite(ya1 + dd1 + va1));
-            if (__any_sync(0xffffffffu, bad)) {
+            const double dd = has ? force_here() : 0.0;
+            const bool bad = has && !isfinite(ya + dd + va);
+            if (grp.any(bad)) {
                 if (net_guess) {
                     // the network's guess led the corrector astray: redo the
                     // attempt from the plain guess
-                    restore_plain_guess(LS, C, lane, has0, has1);
+                    restore_plain_guess(LS, X, gl, has);
                     net_guess = false;
                     S.fallbacks++;
                     continue;
@@ -675,22 +705,18 @@ __global__ void __launch_bounds__(32 * WARPS, (EnsOccupancy<NC, LEARN>::value)) 
                 break;
             }
             double mb6 = -1.7976931348623157e308, mdd = mb6;
-            if (has0) {
-                mb6 = absmax_or_none(e_b6<MODE>(C[0]));
-                mdd = absmax_or_none(dd0);
+            if (has) {
+                mb6 = absmax_or_none(e_b6<MODE>(X));
+                mdd = absmax_or_none(dd);
             }
-            if (has1) {
-                mb6 = fmax(mb6, absmax_or_none(e_b6<MODE>(C[1])));
-                mdd = fmax(mdd, absmax_or_none(dd1));
-            }
-            mb6 = warp_maxd(mb6);
-            mdd = warp_maxd(mdd);
+            mb6 = grp.maxd(mb6);
+            mdd = grp.maxd(mdd);
             double estim_b6 = mb6 / mdd;
             double err = pow(estim_b6 / EPSB, 1. / 7);
             double dtreq = h / err;
             if (!(err == err)) {  // NaN step control: the state is not finite
                 if (net_guess) {
-                    restore_plain_guess(LS, C, lane, has0, has1);
+                    restore_plain_guess(LS, X, gl, has);
                     net_guess = false;
                     S.fallbacks++;
                     continue;
@@ -710,30 +736,19 @@ __global__ void __launch_bounds__(32 * WARPS, (EnsOccupancy<NC, LEARN>::value)) 
                     stop = true;
                 }
                 double q = dtreq / h;
-                if (MODE != ABIE_FORCE_EXACT) {  // the fast form carries g only
-                    e_b_from_g(C[0]);
-                    e_b_from_g(C[1]);
-                }
-                C[0].y0 = ya0;
-                C[0].dy0 = va0;
-                C[0].F1 = dd0;
-                C[0].b6p = C[0].b[6];
-                C[1].y0 = ya1;
-                C[1].dy0 = va1;
-                C[1].F1 = dd1;
-                C[1].b6p = C[1].b[6];
+                if (MODE != ABIE_FORCE_EXACT) e_b_from_g(X);  // the fast form carries g only
+                X.y0 = ya;
+                X.dy0 = va;
+                X.F1 = dd;
+                X.b6p = X.b[6];
                 // the fast form always continues from g consistent with the guess
                 const bool make_consistent = a.consistent_g || MODE != ABIE_FORCE_EXACT;
                 if (!stop && learn) {
-                    learned_refine(a, LS, C, n, lane, has0, has1, q, h, dtreq, m, pend_valid,
-                                   first_attempt, net_guess, make_consistent);
+                    learned_refine<W>(a, LS, grp, X, n, has, q, h, dtreq, m, pend_valid,
+                                      first_attempt, net_guess, make_consistent);
                 } else if (!stop) {
-                    e_refine(C[0], q);
-                    e_refine(C[1], q);
-                    if (make_consistent) {
-                        consistent_g(C[0]);
-                        consistent_g(C[1]);
-                    }
+                    e_refine(X, q);
+                    if (make_consistent) consistent_g(X);
                 }
                 first_attempt = true;
                 if (stop) {
@@ -753,60 +768,53 @@ __global__ void __launch_bounds__(32 * WARPS, (EnsOccupancy<NC, LEARN>::value)) 
         S.h = h;
         S.loop_count = loop_count;
         if (done) S.phase = 2;
-#pragma unroll
-        for (int u = 0; u < 2; u++) {
-            const int c = lane + 32 * u;
-            if (!(u == 0 ? has0 : has1)) continue;
-            const Comp &X = C[u];
+        if (has) {
             if (done) {
-                a.pos[3 * off + c] = X.y0;
-                a.vel[3 * off + c] = X.dy0;
+                a.pos[3 * off + gl] = X.y0;
+                a.vel[3 * off + gl] = X.dy0;
             } else {
-                slot(c, 0) = X.y0;
-                slot(c, 1) = X.dy0;
-                slot(c, 2) = X.F1;
-                #pragma unroll
-                for (int k = 0; k < 7; k++) slot(c, 3 + k) = X.b[k];
-                #pragma unroll
-                for (int k = 0; k < 7; k++) slot(c, 10 + k) = X.g[k];
-                slot(c, 17) = X.b6p;
+                slot(0) = X.y0;
+                slot(1) = X.dy0;
+                slot(2) = X.F1;
+#pragma unroll
+                for (int k = 0; k < 7; k++) slot(3 + k) = X.b[k];
+#pragma unroll
+                for (int k = 0; k < 7; k++) slot(10 + k) = X.g[k];
+                slot(17) = X.b6p;
             }
         }
-        if (lane == 0) a.sc[sid] = S;
-        __syncwarp();
+        if (gl == 0) a.sc[sid] = S;
+        grp.sync();
     }
 }
 
 static double g_last_seconds = 0.0;
 
-static size_t learn_smem(const EnsArgs &a)
-{
-    return (a.mlp || a.samples) ? WARPS * sizeof(LearnSmem) : 0;
-}
-
 template <int MODE, bool LEARN>
-static const void *ensemble_fn_l(int nc)
+static const void *ensemble_fn_l(int w)
 {
-    return nc == 1 ? (const void *)ensemble_kernel<MODE, 1, LEARN>
-                   : (const void *)ensemble_kernel<MODE, 2, LEARN>;
+    return w == 1 ? (const void *)ensemble_kernel<MODE, 1, LEARN>
+                  : (const void *)ensemble_kernel<MODE, 2, LEARN>;
 }
 
-// The kernel for a force form, components per lane and whether the learned
+// The kernel for a force form, warps per system and whether the learned
 // predictor (or sample collection) is in use: without it the variant leaves
-// the predictor's code out and fits more warps per SM.
-static const void *ensemble_fn(int mode, int nc, bool learn)
+// the predictor's code out.
+static const void *ensemble_fn(int mode, int w, bool learn)
 {
     if (mode == ABIE_FORCE_EXACT)
-        return learn ? ensemble_fn_l<ABIE_FORCE_EXACT, true>(nc) : ensemble_fn_l<ABIE_FORCE_EXACT, false>(nc);
-    return learn ? ensemble_fn_l<ABIE_FORCE_FP64, true>(nc) : ensemble_fn_l<ABIE_FORCE_FP64, false>(nc);
+        return learn ? ensemble_fn_l<ABIE_FORCE_EXACT, true>(w) : ensemble_fn_l<ABIE_FORCE_EXACT, false>(w);
+    return learn ? ensemble_fn_l<ABIE_FORCE_FP64, true>(w) : ensemble_fn_l<ABIE_FORCE_FP64, false>(w);
 }
 
-static int launch_ensemble(int mode, int nc, int blocks, const EnsArgs &a, cudaStream_t st)
+static size_t learn_smem(int w) { return (size_t)(WARPS / w) * sizeof(LearnSmem); }
+
+static int launch_ensemble(int mode, int w, int blocks, const EnsArgs &a, cudaStream_t st)
 {
     const bool learn = a.mlp || a.samples;
-    size_t dyn = learn ? WARPS * sizeof(LearnSmem) : 0;
+    size_t dyn = learn ? learn_smem(w) : 0;
     void *args[] = {const_cast<EnsArgs *>(&a)};
-    ABIE_CUDA(cudaLaunchKernel(ensemble_fn(mode, nc, learn), dim3(blocks), dim3(32 * WARPS), args, dyn, st));
+    ABIE_CUDA(cudaLaunchKernel(ensemble_fn(mode, w, learn), dim3(blocks), dim3(32 * WARPS), args, dyn, st));
     return 0;
 }
 
@@ -876,13 +884,12 @@ int ensemble_run(double *pos, double *vel, const double *m, const long long *off
     ABIE_CUDA(cudaStreamSynchronize(st));
 
     const bool learning = mlp || (learn_io && learn_io->samples);
-    const size_t dyn = learning ? WARPS * sizeof(LearnSmem) : 0;
     int bps[2] = {1, 1};
     for (int k = 0; k < 2; k++) {
         const void *fn = ensemble_fn(mode, k + 1, learning);
+        const size_t dyn = learning ? learn_smem(k + 1) : 0;
         if (learning)
-            ABIE_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)(WARPS * sizeof(LearnSmem))));
+            ABIE_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
         ABIE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps[k], fn, 32 * WARPS, dyn));
         bps[k] = std::max(bps[k], 1);
     }
@@ -932,7 +939,9 @@ int ensemble_run(double *pos, double *vel, const double *m, const long long *off
             ak.active = d_active + (k == 0 ? 0 : n_small);
             ak.n_active = cnt;
             ak.queue = d_queue + k;
-            int blocks = (int)std::min<long long>((long long)bps[k] * g_sim.num_sms, (cnt + WARPS - 1) / WARPS);
+            const int per_block = WARPS / (k + 1);  // systems per block
+            int blocks = (int)std::min<long long>((long long)bps[k] * g_sim.num_sms,
+                                                  (cnt + per_block - 1) / per_block);
             blocks = std::max(blocks, 1);
             int lrc = launch_ensemble(mode, k + 1, blocks, ak, k == 0 ? st : g_ens_stream2);
             if (lrc) return lrc;
