@@ -26,6 +26,7 @@
 
 #include "abi_state.cuh"
 #include "engine.cuh"
+#include "radau_comp.cuh"
 #include "radau_constants.h"
 
 namespace abie {
@@ -37,10 +38,7 @@ __constant__ double c_rsp[8][8] = ABIE_RADAU_RSP_INIT;  // fast form: expanded g
 __constant__ double c_wg[9][7] = ABIE_RADAU_WG_INIT;    // fast form: position weights on g
 __constant__ double c_vg[7] = ABIE_RADAU_VG_INIT;       // fast form: velocity weights on g at spacing 1
 
-static constexpr double EPSB = 1.e-4;    // src/integrator_gauss_radau15.h:58
-static constexpr double FAC = 0.25;      // :59
-static constexpr double TOLPC = 1.e-16;  // :63
-static constexpr double H_MIN = 1.e-13;  // :17
+// EPSB, FAC, TOLPC, H_MIN (src/integrator_gauss_radau15.h:17-63): radau_comp.cuh
 
 struct EventRec {
     int j, k, kind;  // kind 0: close encounter, 1: collision
@@ -71,6 +69,8 @@ struct EngineArgs {
     int n, dim, n_src;
     const int *src_body;  // [n_src] body index of each massive body, ascending
     const int *src_slot;  // [n] slot in the source list or -1
+    const int *tp_body;   // [n_tp] bodies without positive mass, ascending (split engine)
+    int n_tp;
     const double *m, *r, *ext;
     double G;
     double *y0, *dy0, *F1, *b, *g, *b6p, *ddy, *dyp;
@@ -412,14 +412,20 @@ __device__ __forceinline__ void ring_put(double *buf, unsigned long long count, 
 
 // Pairs j < k closer than the event thresholds (src/common.c:240-282).  A
 // pair passes the prefilter r2 <= thr2 before the reference's exact test.
+// One warp per body j (grid-stride over warps), its lanes over k > j, so a
+// check costs about N / 32 pair tests per warp instead of N per thread
+// (the order of the records does not matter: commit_events sorts them).
 __device__ void scan_events(const EngineArgs &a, double t, int tid, int nthreads)
 {
+    (void)t;
     EngineCtl *ctl = a.ctl;
-    for (int j = tid; j < a.n; j += nthreads) {
-        double xj = __ldcg(a.ypa + 3 * j), yj = __ldcg(a.ypa + 3 * j + 1),
-               zj = __ldcg(a.ypa + 3 * j + 2);
-        double rj = a.r[j];
-        for (int k = j + 1; k < a.n; k++) {
+    const int lane = tid & 31;
+    const int warp = tid >> 5, nwarps = nthreads >> 5;
+    for (int j = warp; j < a.n; j += nwarps) {
+        const double xj = __ldcg(a.ypa + 3 * j), yj = __ldcg(a.ypa + 3 * j + 1),
+                     zj = __ldcg(a.ypa + 3 * j + 2);
+        const double rj = a.r[j];
+        for (int k = j + 1 + lane; k < a.n; k += 32) {
             double dx = xj - __ldcg(a.ypa + 3 * k);
             double dy = yj - __ldcg(a.ypa + 3 * k + 1);
             double dz = zj - __ldcg(a.ypa + 3 * k + 2);
@@ -742,6 +748,285 @@ __global__ void __launch_bounds__(256) radau_engine(EngineArgs a)
     }
 }
 
+// ---------------------------------------------------------------------------
+// Split engine: systems whose massive bodies fit one warp (3 n_src <= 32),
+// such as a star, planets and many test particles.  Massless bodies never
+// act on the massive ones, so every block integrates a private replica of
+// the massive subsystem (warp 0, one component per lane, bitwise the same in
+// every block) next to its own test particles (warp 1, SPLIT_TPW particles
+// of 4 lanes: lanes 0..2 own x, y, z and the 4 lanes split the sources).
+// All state stays in registers; a substep needs only a block barrier, and
+// the grid meets once per corrector iteration (the convergence test) and
+// per step attempt (the step control, the event check), instead of once per
+// substep.  The per-component arithmetic is radau_comp.cuh's, so the exact
+// form repeats the reference's expressions and the results equal the
+// single-system engine's.
+constexpr int SPLIT_TPW = 8;  // test particles per block
+
+template <int MODE>
+__device__ __forceinline__ void split_tp_force(const EngineArgs &a, const double (*sp)[4], int n_m,
+                                               double p, int lane, double &fx, double &fy,
+                                               double &fz)
+{
+    // the particle's position from its component lanes
+    const double x = __shfl_sync(0xffffffffu, p, 0, 4);
+    const double y = __shfl_sync(0xffffffffu, p, 1, 4);
+    const double z = __shfl_sync(0xffffffffu, p, 2, 4);
+    const int q0 = lane & 3;
+    double ax = 0.0, ay = 0.0, az = 0.0;
+    if (MODE == ABIE_FORCE_EXACT) {
+        if (q0 == 0)
+            for (int k = 0; k < n_m; k++) {
+                Src s{sp[k][0], sp[k][1], sp[k][2], sp[k][3]};
+                pair_exact(x, y, z, s, ax, ay, az);
+            }
+        fx = __shfl_sync(0xffffffffu, ax, 0, 4);
+        fy = __shfl_sync(0xffffffffu, ay, 0, 4);
+        fz = __shfl_sync(0xffffffffu, az, 0, 4);
+    } else {
+        for (int k = q0; k < n_m; k += 4) {
+            Src s{sp[k][0], sp[k][1], sp[k][2], sp[k][3]};
+            pair_fast(x, y, z, s, ax, ay, az);
+        }
+#pragma unroll
+        for (int o = 2; o > 0; o >>= 1) {
+            ax += __shfl_xor_sync(0xffffffffu, ax, o, 4);
+            ay += __shfl_xor_sync(0xffffffffu, ay, o, 4);
+            az += __shfl_xor_sync(0xffffffffu, az, o, 4);
+        }
+        fx = ax;
+        fy = ay;
+        fz = az;
+    }
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(64) radau_split(EngineArgs a)
+{
+    __shared__ double s_sp[2][32][4];  // massive predicted positions, G m (two buffers)
+    __shared__ double s_sa[32][3];     // massive accelerations
+    EngineCtl *ctl = a.ctl;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x, nthreads = gridDim.x * blockDim.x;
+    const bool leader = (blockIdx.x == 0 && threadIdx.x == 0);
+    const long long T = a.timeout_ns;
+    const int n_m = a.n_src;
+    // this thread's component
+    int gi = -1;        // global component index
+    bool alive = true;  // m >= 0
+    bool writer = true; // owns the component's copy in global memory
+    if (warp == 0) {
+        if (lane < 3 * n_m) gi = 3 * a.src_body[lane / 3] + lane % 3;
+        writer = blockIdx.x == 0;
+    } else {
+        const int tpi = blockIdx.x * SPLIT_TPW + lane / 4;
+        if ((lane & 3) < 3 && tpi < a.n_tp) {
+            const int body = a.tp_body[tpi];
+            gi = 3 * body + (lane & 3);
+            alive = a.m[body] >= 0.0;
+        }
+    }
+    const bool has = gi >= 0;
+    const double ext = (has && a.ext) ? a.ext[gi] : 0.0;
+    Group<1> mg;  // the massive warp as a group
+    mg.gl = lane;
+    mg.lane = lane;
+    mg.wig = 0;
+    mg.gidx = 0;
+    mg.red = nullptr;
+    mg.flg = nullptr;
+    mg.tog = 0;
+    if (threadIdx.x < n_m) {
+        const double gm = a.G * a.m[a.src_body[threadIdx.x]];
+        s_sp[0][threadIdx.x][3] = gm;
+        s_sp[1][threadIdx.x][3] = gm;
+    }
+    Comp X;
+    X.y0 = has ? a.y0[gi] : 0.0;
+    X.dy0 = has ? a.dy0[gi] : 0.0;
+    if (ctl->phase == 0 || !has) {
+        X.F1 = X.b6p = 0.0;
+#pragma unroll
+        for (int k = 0; k < 7; k++) X.b[k] = X.g[k] = 0.0;
+    } else {
+        X.F1 = a.F1[gi];
+        X.b6p = a.b6p[gi];
+#pragma unroll
+        for (int k = 0; k < 7; k++) X.b[k] = a.b[k * a.dim + gi];
+#pragma unroll
+        for (int k = 0; k < 7; k++) X.g[k] = a.g[k * a.dim + gi];
+    }
+    int ib = 0;
+    // forces at this thread's position p (one per component): publish the
+    // massive positions, one block barrier, then the massive warp's group
+    // force or the particle's sum over the massive sources
+    auto forces = [&](double p) -> double {
+        if (warp == 0 && has) s_sp[ib][lane / 3][lane % 3] = p;
+        __syncthreads();
+        double F = 0.0;
+        if (warp == 0) {
+            group_force<MODE, 1>(mg, n_m, s_sp[ib], s_sa);
+            if (has) F = s_sa[lane / 3][lane % 3];
+        } else {
+            double fx, fy, fz;
+            split_tp_force<MODE>(a, s_sp[ib], n_m, p, lane, fx, fy, fz);
+            const int c = lane & 3;
+            F = c == 0 ? fx : (c == 1 ? fy : fz);
+        }
+        ib ^= 1;
+        return has ? ((alive ? F : 0.0) + ext) : 0.0;
+    };
+
+    double t, h;
+    int loop_count, red_idx;
+    long long my_attempts = 0;
+    if (ctl->phase == 0) {
+        // F1 = f(y0), then initial_time_step (src/integrator_gauss_radau15.c:75-120)
+        X.F1 = forces(X.y0);
+        if (leader) ctl->force_calls++;
+        unsigned long long k0 = 0, k1 = 0;
+        if (has && gi < a.n && writer) {  // the reference scans the first n of 3n entries
+            k0 = absmax_key(X.y0);
+            k1 = absmax_key(X.F1);
+        }
+        red_idx = 0;
+        reduce2(ctl, red_idx, k0, k1);
+        if (!grid_sync(ctl, T)) return;
+        double d0, d1;
+        read2(ctl, red_idx++, d0, d1);
+        const double dt0 = (d0 < 1e-5 || d1 < 1e-5) ? 1e-6 : 0.01 * (d0 / d1);
+        const double f1 = forces(X.y0 + dt0 * X.dy0);
+        if (leader) ctl->force_calls++;
+        const unsigned long long k2 = (has && writer) ? absmax_key(f1 - X.F1) : 0ull;
+        reduce2(ctl, red_idx, k2, 0ull);
+        if (!grid_sync(ctl, T)) return;
+        double d2, unused;
+        read2(ctl, red_idx++, d2, unused);
+        d2 = d2 / dt0;
+        double dt1;
+        if (fmax(d1, d2) <= 1e-15) dt1 = fmax(1e-6, dt0 * 1e-3);
+        else dt1 = pow(0.01 / fmax(d1, d2), (1.0 / (15 + 1)));
+        h = fmin(100 * dt0, dt1);
+        t = ctl->t;
+        loop_count = 0;
+    } else {
+        t = ctl->t;
+        h = ctl->h;
+        loop_count = ctl->loop_count;
+        red_idx = ctl->red_idx;
+    }
+
+    bool done = false;
+    while (!done && my_attempts < a.attempt_budget) {
+        int iters = 0;
+        for (int ipc = 0; ipc < 12; ipc++) {
+            iters++;
+            unsigned long long kdb = 0, kf8 = 0;
+            for (int ih = 1; ih < 8; ih++) {
+                const double sh = e_hs[ih], ds = h * sh, hh = 0.5 * ds * ds;
+                const double F = forces(has ? e_pred_pos<MODE>(X, ih, sh, h, ds, hh) : 0.0);
+                if (has) {
+                    e_gb_update<MODE>(X, ih, F);
+                    if (ih == 7 && writer) {
+                        kdb = absmax_key(e_b6<MODE>(X) - X.b6p);
+                        kf8 = absmax_key(F);
+                    }
+                }
+            }
+            if (leader) ctl->force_calls += 7;
+            reduce2(ctl, red_idx, kdb, kf8);
+            if (!grid_sync(ctl, T)) return;
+            double db6, f8;
+            read2(ctl, red_idx++, db6, f8);
+            if (db6 / f8 < TOLPC) break;  // src/integrator_gauss_radau15.c:366
+            X.b6p = e_b6<MODE>(X);
+        }
+        // advance (spacing 1)
+        const double hh1 = 0.5 * h * h;
+        const double ya = has ? e_pred_pos<MODE>(X, 8, 1.0, h, h, hh1) : 0.0;
+        const double va = has ? e_pred_vel<MODE>(X, h) : 0.0;
+        const double dd = forces(ya);
+        unsigned long long kb6 = 0, kdd = 0;
+        if (has && writer) {
+            a.ypa[gi] = ya;
+            if (!isfinite(dd + ya + va)) atomicCAS(&ctl->err, 0, ABIE_ERR_NUMERICS);
+            kb6 = absmax_key(e_b6<MODE>(X));
+            kdd = absmax_key(dd);
+        }
+        reduce2(ctl, red_idx, kb6, kdd);
+        if (!grid_sync(ctl, T)) return;
+        if (leader) {
+            ctl->force_calls += 1;
+            ctl->iterations += iters;
+            ctl->attempts += 1;
+        }
+        double mb6, mdd;
+        read2(ctl, red_idx++, mb6, mdd);
+        // step control (src/integrator_gauss_radau15.c:379-433)
+        const double estim_b6 = mb6 / mdd;
+        const double err = pow(estim_b6 / EPSB, 1. / 7);
+        const double dtreq = h / err;
+        const bool accepted = (err <= 1 || loop_count > 100);
+        bool stop = false;
+        if (accepted) {
+            t += h;
+            loop_count = 0;
+            if (t > a.t_end) {
+                h = a.t_end - t;
+                stop = true;
+            }
+            const double q = dtreq / h;
+            if (MODE != ABIE_FORCE_EXACT) e_b_from_g(X);  // the fast form carries g only
+            X.y0 = ya;
+            X.dy0 = va;
+            X.F1 = dd;
+            X.b6p = X.b[6];
+            e_refine(X, q);
+            if (MODE != ABIE_FORCE_EXACT) consistent_g(X);
+            scan_events(a, t, tid, nthreads);
+            if (leader) ctl->accepts++;
+        } else {
+            loop_count += 1;
+            if (leader) ctl->rejects++;
+        }
+        if (!stop) {
+            if (dtreq / h > 1.0 / FAC) h /= FAC;
+            else if (dtreq < 1.e-12) h *= FAC;
+            else h = dtreq;
+            if (h < H_MIN) h = H_MIN;
+        }
+        if (!grid_sync(ctl, T)) return;
+        if (accepted && *(volatile int *)&ctl->n_ev > 0) {
+            if (leader) commit_events(a, t);
+            if (!grid_sync(ctl, T)) return;
+            if (*(volatile int *)&ctl->flag > 0) stop = true;
+        }
+        my_attempts++;
+        if (accepted && leader) ctl->t = t;
+        done = stop;
+    }
+    // state back to global memory (one writer per component)
+    if (has && writer) {
+        a.y0[gi] = X.y0;
+        a.dy0[gi] = X.dy0;
+        a.F1[gi] = X.F1;
+        a.b6p[gi] = X.b6p;
+#pragma unroll
+        for (int k = 0; k < 7; k++) a.b[k * a.dim + gi] = X.b[k];
+#pragma unroll
+        for (int k = 0; k < 7; k++) a.g[k * a.dim + gi] = X.g[k];
+    }
+    if (leader) {
+        ctl->t = t;
+        ctl->h = h;
+        ctl->loop_count = loop_count;
+        ctl->red_idx = red_idx;
+        ctl->phase = done ? 2 : 1;
+        ctl->attempts_done += my_attempts;
+        __threadfence();
+    }
+}
+
 }  // namespace abie
 
 namespace abie {
@@ -750,7 +1035,7 @@ struct EngineBuffers {
     double *slab = nullptr;
     size_t slab_n = 0;  // bodies the slab holds
     Src *srcs = nullptr;
-    int *src_body = nullptr, *src_slot = nullptr;
+    int *src_body = nullptr, *src_slot = nullptr, *tp_body = nullptr;
     size_t src_n = 0;
     EngineCtl *ctl = nullptr;
     EventRec *ev = nullptr;
@@ -768,6 +1053,7 @@ void free_engine_buffers()
     if (e.srcs) cudaFree(e.srcs);
     if (e.src_body) cudaFree(e.src_body);
     if (e.src_slot) cudaFree(e.src_slot);
+    if (e.tp_body) cudaFree(e.tp_body);
     if (e.ctl) cudaFree(e.ctl);
     if (e.ev) cudaFree(e.ev);
     if (e.d_ce) cudaFree(e.d_ce);
@@ -783,12 +1069,14 @@ static int engine_reserve(size_t n, size_t max_ce, size_t max_coll)
         if (e.srcs) cudaFree(e.srcs);
         if (e.src_body) cudaFree(e.src_body);
         if (e.src_slot) cudaFree(e.src_slot);
+        if (e.tp_body) cudaFree(e.tp_body);
         e.slab = nullptr;
         size_t c = n < 64 ? 64 : n;
         ABIE_CUDA(cudaMalloc(&e.slab, c * SLAB_PER_BODY * sizeof(double)));
         ABIE_CUDA(cudaMalloc(&e.srcs, 3 * c * sizeof(Src)));
         ABIE_CUDA(cudaMalloc(&e.src_body, c * sizeof(int)));
         ABIE_CUDA(cudaMalloc(&e.src_slot, c * sizeof(int)));
+        ABIE_CUDA(cudaMalloc(&e.tp_body, c * sizeof(int)));
         e.slab_n = c;
     }
     if (!e.ctl) ABIE_CUDA(cudaMalloc(&e.ctl, sizeof(EngineCtl)));
@@ -910,6 +1198,11 @@ int radau_run(const SystemView &sys, double t, double t_end, int mode, EventStat
     }
     int n_src = (int)body.size();
     if (n_src) ABIE_CUDA(cudaMemcpyAsync(e.src_body, body.data(), n_src * sizeof(int), cudaMemcpyHostToDevice, st));
+    std::vector<int> tps;
+    for (int j = 0; j < n; j++)
+        if (!(sys.h_m[j] > 0.0)) tps.push_back(j);
+    const int n_tp = (int)tps.size();
+    if (n_tp) ABIE_CUDA(cudaMemcpyAsync(e.tp_body, tps.data(), n_tp * sizeof(int), cudaMemcpyHostToDevice, st));
     ABIE_CUDA(cudaMemcpyAsync(e.src_slot, slot.data(), n * sizeof(int), cudaMemcpyHostToDevice, st));
 
     ABIE_CUDA(cudaMemsetAsync(e.slab, 0, (size_t)n * SLAB_PER_BODY * sizeof(double), st));
@@ -918,6 +1211,8 @@ int radau_run(const SystemView &sys, double t, double t_end, int mode, EventStat
     a.dim = (int)d;
     a.n_src = n_src;
     a.src_body = e.src_body;
+    a.tp_body = e.tp_body;
+    a.n_tp = n_tp;
     a.src_slot = e.src_slot;
     a.m = sys.m;
     a.r = sys.r;
@@ -970,6 +1265,18 @@ int radau_run(const SystemView &sys, double t, double t_end, int mode, EventStat
 
     int js = 1, block = 256;
     engine_shape(mode, n, n_src, g_sim.num_sms, &js, &block);
+    // few massive bodies: the split engine (a replica of them per block),
+    // unless a launch shape is forced or the particles exceed one
+    // resident wave
+    bool split = false;
+    if (n_src <= 10 && g_engine_js == 0) {
+        int bps = 0;
+        ABIE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &bps, mode == ABIE_FORCE_EXACT ? (const void *)radau_split<ABIE_FORCE_EXACT>
+                                           : (const void *)radau_split<ABIE_FORCE_FP64>, 64, 0));
+        split = (long long)std::max(1, (n_tp + SPLIT_TPW - 1) / SPLIT_TPW) <=
+                (long long)bps * g_sim.num_sms;
+    }
     EngineCtl c;
     long long budget = 4;
     for (;;) {
@@ -979,7 +1286,17 @@ int radau_run(const SystemView &sys, double t, double t_end, int mode, EventStat
         ABIE_CUDA(cudaEventCreate(&e1));
         ABIE_CUDA(cudaEventRecord(e0, st));
         int grid = 0;
-        rc = dispatch_engine(mode, js, block, a, g_sim.num_sms, st, &grid);
+        if (split) {
+            EngineArgs args = a;
+            void *params[] = {&args};
+            grid = std::max(1, (n_tp + SPLIT_TPW - 1) / SPLIT_TPW);
+            const void *fn = mode == ABIE_FORCE_EXACT ? (const void *)radau_split<ABIE_FORCE_EXACT>
+                                                      : (const void *)radau_split<ABIE_FORCE_FP64>;
+            ABIE_CUDA(cudaLaunchCooperativeKernel(fn, dim3((unsigned)grid), dim3(64), params, 0, st));
+            rc = 0;
+        } else {
+            rc = dispatch_engine(mode, js, block, a, g_sim.num_sms, st, &grid);
+        }
         if (rc) return rc;
         ABIE_CUDA(cudaEventRecord(e1, st));
         ABIE_CUDA(cudaEventSynchronize(e1));

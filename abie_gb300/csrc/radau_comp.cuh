@@ -1,0 +1,318 @@
+// Radau15 on one component per thread (src/integrator_gauss_radau15.c:56-284),
+// shared by the batched ensemble (ensemble.cu) and the split engine for
+// systems with few massive bodies (radau_split.cu).  Each thread keeps its
+// component's state -- y0, dy0, F1, b[7], g[7], previous b6 -- in
+// registers.  MODE ABIE_FORCE_EXACT repeats the reference's expressions in
+// its order (built with --fmad=false); the fast form runs the corrector on
+// the Newton-form coefficients g with tabulated weights.
+#pragma once
+#include "common.cuh"
+#include "radau_constants.h"
+
+namespace abie {
+
+static __constant__ double e_hs[8] = ABIE_RADAU_HS_INIT;
+static __constant__ double e_rs[8][8] = ABIE_RADAU_RS_INIT;
+static __constant__ double e_cs[8][8] = ABIE_RADAU_CS_INIT;
+static __constant__ double e_rsp[8][8] = ABIE_RADAU_RSP_INIT;  // fast sweep: expanded g recurrence
+static __constant__ double e_wg[9][7] = ABIE_RADAU_WG_INIT;    // fast sweep: position weights on g, row 8 = spacing 1
+static __constant__ double e_vg[7] = ABIE_RADAU_VG_INIT;       // fast sweep: velocity weights on g at spacing 1
+
+
+static constexpr double EPSB = 1.e-4;
+static constexpr double FAC = 0.25;
+static constexpr double TOLPC = 1.e-16;
+static constexpr double H_MIN = 1.e-13;
+
+__device__ __forceinline__ unsigned long long ens_timer()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Component state of one lane.
+struct Comp {
+    double y0, dy0, F1, b[7], g[7], b6p;
+};
+
+// Predicted position at spacing s = e_hs[row] (row 8: s = 1) of a step dt.
+// Exact form: the reference's Horner polynomial in b with its divisions.
+// Fast form: the same polynomial written on the Newton-form coefficients
+// g (b = C g), y0 + ds dy0 + hh (F1 + sum_j g_j W_j(s)) with the weights
+// W_j(s) = sum_{k<=j} cs[j][k] s^(k+1) / ((k+2)(k+3)/2) tabulated, and
+// ds = dt s, hh = ds^2 / 2 once per substep: 10 FP64 instructions, and b
+// is never needed inside the corrector.
+template <int MODE>
+__device__ __forceinline__ double e_pred_pos(const Comp &c, int row, double s, double dt, double ds,
+                                             double hh)
+{
+    const double *b = c.b;
+    if (MODE == ABIE_FORCE_EXACT)
+        return c.y0 + dt * s * (c.dy0 + dt * s * (c.F1 + s * (b[0] / 0.3e1 + s * (b[1] / 0.6e1 + s * (b[2] / 0.10e2 + s * (b[3] / 0.15e2 + s * (b[4] / 0.21e2 + s * (b[5] / 0.28e2 + s * b[6] / 0.36e2))))))) / 0.2e1);
+    const double *w = e_wg[row];
+    const double *g = c.g;
+    double u = g[6] * w[6];
+    u = fma(g[5], w[5], u);
+    u = fma(g[4], w[4], u);
+    u = fma(g[3], w[3], u);
+    u = fma(g[2], w[2], u);
+    u = fma(g[1], w[1], u);
+    u = fma(g[0], w[0], u);
+    return fma(hh, c.F1 + u, fma(ds, c.dy0, c.y0));
+}
+
+// Predicted velocity at spacing 1 (the advance).
+template <int MODE>
+__device__ __forceinline__ double e_pred_vel(const Comp &c, double dt)
+{
+    const double *b = c.b;
+    if (MODE == ABIE_FORCE_EXACT) {
+        const double s = 1.0;
+        return c.dy0 + dt * s * (c.F1 + s * (b[0] / 0.2e1 + s * (b[1] / 0.3e1 + s * (b[2] / 0.4e1 + s * (b[3] / 0.5e1 + s * (b[4] / 0.6e1 + s * (b[5] / 0.7e1 + s * b[6] / 0.8e1)))))));
+    }
+    const double *g = c.g;
+    double u = g[6] * e_vg[6];
+    u = fma(g[5], e_vg[5], u);
+    u = fma(g[4], e_vg[4], u);
+    u = fma(g[3], e_vg[3], u);
+    u = fma(g[2], e_vg[2], u);
+    u = fma(g[1], e_vg[1], u);
+    u = fma(g[0], e_vg[0], u);
+    return fma(dt, c.F1 + u, c.dy0);
+}
+
+// b6 of the corrector: b_6 = cs[6][6] g_6 = g_6, read from g in the fast form.
+template <int MODE>
+__device__ __forceinline__ double e_b6(const Comp &c)
+{
+    return MODE == ABIE_FORCE_EXACT ? c.b[6] : c.g[6];
+}
+
+// g and b after the force F of substep IH (src/integrator_gauss_radau15.c:136-241);
+// one fully static variant per substep keeps the coefficients in registers.
+template <int MODE, int IH>
+__device__ __forceinline__ void e_gb_update_ih(Comp &c, double F)
+{
+    double v = (F - c.F1) * e_rs[IH][0];
+#pragma unroll
+    for (int l = 1; l < IH; l++) v = (v - c.g[l - 1]) * e_rs[IH][l];
+    c.g[IH - 1] = v;
+#pragma unroll
+    for (int k = 0; k < IH; k++) {
+        double s = e_cs[k][k] * c.g[k];
+#pragma unroll
+        for (int jj = k + 1; jj < 7; jj++) {
+            if (MODE == ABIE_FORCE_EXACT) s = s + e_cs[jj][k] * c.g[jj];  // reference roundings
+            else s = fma(e_cs[jj][k], c.g[jj], s);
+        }
+        c.b[k] = s;
+    }
+}
+
+// Fast form: only the new Newton coefficient, g_{IH-1} from the expanded
+// recurrence (F - F1) rsp[IH][0] - sum_{l<IH-1} g_l rsp[IH][l+1]; b is
+// formed from g once per accepted step (e_b_from_g).
+template <int IH>
+__device__ __forceinline__ void e_g_update_ih(Comp &c, double F)
+{
+    double v = (F - c.F1) * e_rsp[IH][0];
+#pragma unroll
+    for (int l = 1; l < IH; l++) v = fma(-c.g[l - 1], e_rsp[IH][l], v);
+    c.g[IH - 1] = v;
+}
+
+template <int MODE>
+__device__ __forceinline__ void e_gb_update(Comp &c, int ih, double F)
+{
+    if (MODE == ABIE_FORCE_EXACT) {
+        switch (ih) {
+        case 1: e_gb_update_ih<MODE, 1>(c, F); break;
+        case 2: e_gb_update_ih<MODE, 2>(c, F); break;
+        case 3: e_gb_update_ih<MODE, 3>(c, F); break;
+        case 4: e_gb_update_ih<MODE, 4>(c, F); break;
+        case 5: e_gb_update_ih<MODE, 5>(c, F); break;
+        case 6: e_gb_update_ih<MODE, 6>(c, F); break;
+        default: e_gb_update_ih<MODE, 7>(c, F); break;
+        }
+        return;
+    }
+    switch (ih) {
+    case 1: e_g_update_ih<1>(c, F); break;
+    case 2: e_g_update_ih<2>(c, F); break;
+    case 3: e_g_update_ih<3>(c, F); break;
+    case 4: e_g_update_ih<4>(c, F); break;
+    case 5: e_g_update_ih<5>(c, F); break;
+    case 6: e_g_update_ih<6>(c, F); break;
+    default: e_g_update_ih<7>(c, F); break;
+    }
+}
+
+// b_k = sum_{j>=k} cs[j][k] g_j for every k (fast form, at an accept).
+__device__ __forceinline__ void e_b_from_g(Comp &c)
+{
+#pragma unroll
+    for (int k = 0; k < 7; k++) {
+        double s = c.g[k];  // cs[k][k] = 1
+#pragma unroll
+        for (int j = k + 1; j < 7; j++) s = fma(e_cs[j][k], c.g[j], s);
+        c.b[k] = s;
+    }
+}
+
+__device__ __forceinline__ void e_refine(Comp &c, double q)
+{
+    double *b = c.b;
+    double q2 = q * q, q3 = q2 * q, q4 = q2 * q2, q5 = q2 * q3, q6 = q3 * q3, q7 = q2 * q5;
+    double e0 = q * (b[6] * 7.0 + b[5] * 6.0 + b[4] * 5.0 + b[3] * 4.0 + b[2] * 3.0 + b[1] * 2.0 + b[0]);
+    double e1 = q2 * (b[6] * 21.0 + b[5] * 15.0 + b[4] * 10.0 + b[3] * 6.0 + b[2] * 3.0 + b[1]);
+    double e2 = q3 * (b[6] * 35.0 + b[5] * 20.0 + b[4] * 10.0 + b[3] * 4.0 + b[2]);
+    double e3 = q4 * (b[6] * 35.0 + b[5] * 15.0 + b[4] * 5.0 + b[3]);
+    double e4 = q5 * (b[6] * 21.0 + b[5] * 6.0 + b[4]);
+    double e5 = q6 * (b[6] * 7.0 + b[5]);
+    double e6 = q7 * b[6];
+    b[0] = e0 + 0.0;
+    b[1] = e1 + 0.0;
+    b[2] = e2 + 0.0;
+    b[3] = e3 + 0.0;
+    b[4] = e4 + 0.0;
+    b[5] = e5 + 0.0;
+    b[6] = e6 + 0.0;
+}
+
+__device__ __forceinline__ double warp_maxd(double v)
+{
+    // the values are non-negative magnitudes or -DBL_MAX; plain max is exact
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+__device__ __forceinline__ double absmax_or_none(double v)
+{
+    double a = fabs(v);
+    return (a == a) ? a : -1.7976931348623157e308;
+}
+
+// g = C^-1 b for one component: back-substitution through the triangular
+// change of basis b_k = sum_{j>=k} cs[j][k] g_j, so that the corrector's
+// first sweep starts from the polynomial the guess describes.  (The
+// reference keeps the previous step's g, which the first sweep mixes into
+// every b it rebuilds, src/integrator_gauss_radau15.c:189-241.)
+__device__ __forceinline__ void consistent_g(Comp &c)
+{
+#pragma unroll
+    for (int k = 6; k >= 0; k--) {
+        double v = c.b[k];
+#pragma unroll
+        for (int j = k + 1; j < 7; j++) v -= e_cs[j][k] * c.g[j];
+        c.g[k] = v;
+    }
+}
+
+// A system's thread group: W warps (32 W threads, one component each).
+// W = 1 syncs with __syncwarp and reduces with shuffles; W = 2 syncs with a
+// named barrier per group and meets the warps' partial reductions in shared
+// memory (two alternating slots, so a slot is rewritten only after a barrier
+// that every reader of its previous value has passed).
+template <int W>
+struct Group {
+    int gl;    // lane in the group, 0 .. 32 W - 1
+    int lane;  // lane in the warp
+    int wig;   // warp in the group
+    int gidx;  // group in the block
+    double *red;
+    int *flg;
+    int tog;
+    __device__ __forceinline__ void sync() const
+    {
+        if (W == 1) __syncwarp();
+        else asm volatile("bar.sync %0, %1;" ::"r"(1 + gidx), "r"(32 * W) : "memory");
+    }
+    __device__ __forceinline__ double maxd(double v)
+    {
+        v = warp_maxd(v);
+        if (W == 1) return v;
+        if (lane == 0) red[tog * W + wig] = v;
+        sync();
+        double r = red[tog * W];
+#pragma unroll
+        for (int k = 1; k < W; k++) r = fmax(r, red[tog * W + k]);
+        tog ^= 1;
+        return r;
+    }
+    __device__ __forceinline__ bool any(bool b)
+    {
+        b = __any_sync(0xffffffffu, b);
+        if (W == 1) return b;
+        if (lane == 0) flg[tog * W + wig] = b ? 1 : 0;
+        sync();
+        int r = 0;
+#pragma unroll
+        for (int k = 0; k < W; k++) r |= flg[tog * W + k];
+        tog ^= 1;
+        return r != 0;
+    }
+    // the value group lane 0 holds, in every lane (one slot: the next write
+    // comes many barriers later)
+    __device__ __forceinline__ long long bcast0(long long v)
+    {
+        if (W == 1) return __shfl_sync(0xffffffffu, v, 0);
+        long long *slot = reinterpret_cast<long long *>(red + 2 * W);
+        if (gl == 0) *slot = v;
+        sync();
+        const long long r = *slot;
+        sync();
+        return r;
+    }
+};
+
+// Accelerations of the n bodies whose predicted positions and G m are in
+// sp[k] = {x, y, z, Gm}; the result of sink i goes to sa[i].  Warp w of the
+// group takes sinks w spw .. (w + 1) spw - 1, spw = ceil(n / W), with
+// L = 32 / spw lanes per sink (1 in the exact form), each summing every
+// L-th source; the partial sums of the lanes holding work meet in a fixed
+// tree of shuffles (a sink's lanes never straddle warps).
+template <int MODE, int W>
+__device__ __forceinline__ void group_force(const Group<W> &grp, int n, const double (*sp)[4],
+                                            double (*sa)[3])
+{
+    const int spw = (n + W - 1) / W;
+    const int L = MODE == ABIE_FORCE_EXACT ? 1 : max(1, 32 / max(spw, 1));
+    const int lane = grp.lane;
+    const int gw = lane / L, hh = lane % L;
+    const int g = grp.wig * spw + gw;
+    const bool sink = gw < spw && g < n;
+    double ax = 0.0, ay = 0.0, az = 0.0;
+    if (sink) {
+        const double xi = sp[g][0], yi = sp[g][1], zi = sp[g][2];
+        for (int k = hh; k < n; k += L) {
+            double gm = sp[k][3];
+            if (k == g || !(gm > 0.0)) continue;
+            Src s{sp[k][0], sp[k][1], sp[k][2], gm};
+            if (MODE == ABIE_FORCE_EXACT) pair_exact(xi, yi, zi, s, ax, ay, az);
+            else pair_fast(xi, yi, zi, s, ax, ay, az);
+        }
+    }
+    const int Wt = L < n ? L : n;
+    for (int o = 1; o < Wt; o <<= 1) {
+        int src = lane + o;
+        src = src < 32 ? src : 31;
+        double ox = __shfl_sync(0xffffffffu, ax, src);
+        double oy = __shfl_sync(0xffffffffu, ay, src);
+        double oz = __shfl_sync(0xffffffffu, az, src);
+        if (hh + o < Wt) {
+            ax += ox;
+            ay += oy;
+            az += oz;
+        }
+    }
+    if (sink && hh == 0) {
+        sa[g][0] = ax;
+        sa[g][1] = ay;
+        sa[g][2] = az;
+    }
+    grp.sync();
+}
+
+
+}  // namespace abie
