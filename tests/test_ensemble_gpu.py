@@ -90,3 +90,29 @@ def test_rejects_oversized_system(clib):
     P, V, M, offs = ics.ensemble(n_systems=1, seed0=1, n_planets=(25, 25))
     with pytest.raises(AbieError):
         clib.gr_ensemble(P, V, M, offs, G, 0.0, 0.1)
+
+
+@pytest.mark.parametrize("mode", ["exact", "fp64"])
+def test_edge_sizes_vs_oracle(clib, oracle, mode):
+    """Systems of 2, 3, 10, 11 (the first two-warp size) and 21 bodies (the
+    largest), each against the oracle.  (A lone body is no case: with zero
+    force the reference's step control divides 0 by 0 and never ends.)"""
+    systems = []
+    for k, n in enumerate([2, 3, 10, 11, 21]):
+        p, v, m, r = ics.planetary_system(seed=900 + k, n_planets=n - 1, n_tp=0)
+        systems.append((p, v, m))
+    P, V, M, offs = _pack(systems)
+    old = clib.set_force_mode(mode)
+    try:
+        out = clib.gr_ensemble(P, V, M, offs, G, 0.0, 0.3)
+    finally:
+        clib.set_force_mode(old)
+    assert (out["status"] == 0).all()
+    for s in range(len(systems)):
+        sv, sm = _sl(offs, s)
+        ref = oracle.radau15(P[sv], V[sv], M[sm], np.zeros(M[sm].size), G, 0.0, 0.3)
+        tol_t = TIME_TOL if mode == "exact" else TIME_TOL_FAST
+        assert abs(out["t"][s] - ref["t"]) <= tol_t * ref["t"]
+        p, v = at_time(out["pos"][sv], out["vel"][sv], M[sm], out["t"][s], ref["t"], oracle)
+        assert rel_err_per_body(p, ref["pos"]) <= TOL
+        assert rel_err_per_body(v, ref["vel"]) <= TOL

@@ -168,3 +168,36 @@ def test_counters_reported(clib):
     c = clib.counters()
     assert c["accepts"] > 0 and c["attempts"] == c["accepts"] + c["rejects"]
     assert c["force_calls"] >= 7 * c["iterations"] + c["attempts"]
+
+
+@pytest.mark.parametrize("n_planets,n_tp", [(9, 40), (10, 40), (3, 0), (0, 30)])
+def test_split_and_general_engines_vs_oracle(clib, oracle, n_planets, n_tp):
+    """Systems at and beyond the split engine's limit (10 massive bodies),
+    without test particles, and without massive bodies but the star (a
+    lone star plus massless bodies), in both forms, against the oracle."""
+    p, v, m, r = ics.planetary_system(seed=77 + n_planets, n_planets=n_planets, n_tp=n_tp)
+    ref = oracle.radau15(p, v, m, r, G, 0.0, 0.4)
+    for mode, tol_t in (("exact", TIME_TOL), ("fp64", TIME_TOL_FAST)):
+        rc, p1, v1, t = _direct(clib, p, v, m, r, 0.0, 0.4, mode)
+        assert rc == 0
+        assert abs(t - ref["t"]) <= tol_t * ref["t"]
+        p1, v1 = at_time(p1, v1, m, t, ref["t"], oracle)
+        assert rel_err_per_body(p1, ref["pos"]) <= TOL
+        assert rel_err_per_body(v1, ref["vel"]) <= TOL
+
+
+def test_split_engine_matches_general_engine(clib, oracle):
+    """The same 1,009-body run on the split engine and, with a forced launch
+    shape, on the general engine: equal at a common time."""
+    import ctypes as C
+    p, v, m, r = ics.planetary_system()
+    rc, p1, v1, t1 = _direct(clib, p, v, m, r, 0.0, 0.3, "fp64")
+    clib.lib.abie_debug_engine_shape(C.c_int(16), C.c_int(128))
+    try:
+        rc2, p2, v2, t2 = _direct(clib, p, v, m, r, 0.0, 0.3, "fp64")
+    finally:
+        clib.lib.abie_debug_engine_shape(C.c_int(0), C.c_int(0))
+    assert rc == 0 and rc2 == 0
+    assert abs(t1 - t2) <= TIME_TOL_FAST * t2
+    p1, v1 = at_time(p1, v1, m, t1, t2, oracle)
+    assert rel_err_per_body(p1, p2) <= TOL and rel_err_per_body(v1, v2) <= TOL
