@@ -14,6 +14,7 @@
 
 #include "abi_state.cuh"
 #include "engine.cuh"
+#include "pn.cuh"
 #include "force.cuh"
 
 namespace abie {
@@ -101,7 +102,7 @@ static void free_dev(double *&p)
 // abie_force_host).  For sinks with m < 0 the caller's acc entries are kept,
 // as the reference leaves them untouched.
 static int host_force(const double *pos, const double *m, size_t n, double G, double *acc,
-                      int mode)
+                      int mode, const double *vel = nullptr, double C = 0.0)
 {
     int rc = ensure_device(-1);
     if (rc) return rc;
@@ -119,6 +120,12 @@ static int host_force(const double *pos, const double *m, size_t n, double G, do
                                   s.st));
     rc = launch_force(mode, s.tmp_pos, s.tmp_m, (int)n, G, s.fs, s.tmp_acc, s.st);
     if (rc) return rc;
+    if (vel && C > 0.0) {  // src/common.c:101-107 -> src/additional_forces.c:14-121
+        if ((rc = reserve(&s.tmp_vel, &s.tmp_vel_cap, 3 * n))) return rc;
+        ABIE_CUDA(cudaMemcpyAsync(s.tmp_vel, vel, 3 * n * sizeof(double), cudaMemcpyHostToDevice, s.st));
+        rc = launch_post_newtonian(s.tmp_pos, s.tmp_vel, s.tmp_m, (int)n, G, C, s.tmp_acc, s.st);
+        if (rc) return rc;
+    }
     ABIE_CUDA(cudaMemcpyAsync(acc, s.tmp_acc, 3 * n * sizeof(double), cudaMemcpyDeviceToHost, s.st));
     ABIE_CUDA(cudaStreamSynchronize(s.st));
     s.ctr.force_calls++;
@@ -212,9 +219,10 @@ int finalize_code(void)
     free_dev(s.tmp_pos);
     free_dev(s.tmp_m);
     free_dev(s.tmp_acc);
+    free_dev(s.tmp_vel);
     free_dev(s.energy_partials);
     s.pos_cap = s.vel_cap = s.m_cap = s.r_cap = s.ext_cap = 0;
-    s.tmp_pos_cap = s.tmp_m_cap = s.tmp_acc_cap = s.energy_cap = 0;
+    s.tmp_pos_cap = s.tmp_m_cap = s.tmp_acc_cap = s.tmp_vel_cap = s.energy_cap = 0;
     force_scratch_free(s.fs);
     free_engine_buffers();
     free_wh_buffers();
@@ -366,16 +374,12 @@ size_t ode_n_body_second_order(const double *pos, size_t N, double G, const doub
 size_t calculate_accelerations(const double *pos, const double *vel, size_t N, double G,
                                const double *masses, const double *radii, double *acc)
 {
-    (void)vel;
     (void)radii;
     Sim &s = g_sim;
     N = lo32(N);
-    if (s.C > 0.0) {
-        set_error(ABIE_ERR_UNSUPPORTED,
-                  "post-Newtonian terms (C > 0, src/additional_forces.c) are not on the GPU path");
-        return (size_t)(long long)ABIE_ERR_UNSUPPORTED;
-    }
-    int rc = host_force(pos, masses, N, G, acc, s.force_mode);
+    // Newton, then the post-Newtonian terms when the stored C is positive
+    // (src/common.c:82-114), then the external accelerations
+    int rc = host_force(pos, masses, N, G, acc, s.force_mode, vel, s.C);
     if (rc) return (size_t)(long long)rc;
     if (s.ext_enabled && s.inited && N <= s.n_max) {
         std::vector<double> ext(3 * N);

@@ -24,8 +24,8 @@ struct Sim {
     size_t pos_cap = 0, vel_cap = 0, m_cap = 0, r_cap = 0, ext_cap = 0;
     bool ext_enabled = false;
     // staging for the stateless host-array entry points
-    double *tmp_pos = nullptr, *tmp_m = nullptr, *tmp_acc = nullptr;
-    size_t tmp_pos_cap = 0, tmp_m_cap = 0, tmp_acc_cap = 0;
+    double *tmp_pos = nullptr, *tmp_m = nullptr, *tmp_acc = nullptr, *tmp_vel = nullptr;
+    size_t tmp_pos_cap = 0, tmp_m_cap = 0, tmp_acc_cap = 0, tmp_vel_cap = 0;
     double *energy_partials = nullptr;
     size_t energy_cap = 0;
     ForceScratch fs;

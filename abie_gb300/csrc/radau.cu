@@ -26,6 +26,7 @@
 
 #include "abi_state.cuh"
 #include "engine.cuh"
+#include "pn.cuh"
 #include "radau_comp.cuh"
 #include "radau_constants.h"
 
@@ -71,6 +72,8 @@ struct EngineArgs {
     const int *src_slot;  // [n] slot in the source list or -1
     const int *tp_body;   // [n_tp] bodies without positive mass, ascending (split engine)
     int n_tp;
+    double C;             // speed of light: post-Newtonian terms when > 0 (split engine)
+    PnConst pn;
     const double *m, *r, *ext;
     double G;
     double *y0, *dy0, *F1, *b, *g, *b6p, *ddy, *dyp;
@@ -800,10 +803,11 @@ __device__ __forceinline__ void split_tp_force(const EngineArgs &a, const double
     }
 }
 
-template <int MODE>
+template <int MODE, bool PN>
 __global__ void __launch_bounds__(64) radau_split(EngineArgs a)
 {
     __shared__ double s_sp[2][32][4];  // massive predicted positions, G m (two buffers)
+    __shared__ double s_sv[2][32][4];  // massive predicted velocities, m (post-Newtonian only)
     __shared__ double s_sa[32][3];     // massive accelerations
     EngineCtl *ctl = a.ctl;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -836,10 +840,15 @@ __global__ void __launch_bounds__(64) radau_split(EngineArgs a)
     mg.red = nullptr;
     mg.flg = nullptr;
     mg.tog = 0;
+    constexpr bool pn = PN;  // post-Newtonian terms (src/common.c:101-107), a.C > 0
+    const double my_m = has ? a.m[gi / 3] : 0.0;
     if (threadIdx.x < n_m) {
-        const double gm = a.G * a.m[a.src_body[threadIdx.x]];
+        const double mm = a.m[a.src_body[threadIdx.x]];
+        const double gm = a.G * mm;
         s_sp[0][threadIdx.x][3] = gm;
         s_sp[1][threadIdx.x][3] = gm;
+        s_sv[0][threadIdx.x][3] = mm;
+        s_sv[1][threadIdx.x][3] = mm;
     }
     Comp X;
     X.y0 = has ? a.y0[gi] : 0.0;
@@ -857,19 +866,61 @@ __global__ void __launch_bounds__(64) radau_split(EngineArgs a)
         for (int k = 0; k < 7; k++) X.g[k] = a.g[k * a.dim + gi];
     }
     int ib = 0;
-    // forces at this thread's position p (one per component): publish the
-    // massive positions, one block barrier, then the massive warp's group
-    // force or the particle's sum over the massive sources
-    auto forces = [&](double p) -> double {
-        if (warp == 0 && has) s_sp[ib][lane / 3][lane % 3] = p;
+    // forces at this thread's position p and velocity v (one component
+    // each): publish the massive positions (and velocities for the
+    // post-Newtonian terms), one block barrier, then the massive warp's
+    // group force or the particle's sum over the massive sources.  Newton,
+    // then the post-Newtonian sum, then the external acceleration, as
+    // src/common.c:82-114 adds them.
+    auto forces = [&](double p, double v) -> double {
+        if (warp == 0 && has) {
+            s_sp[ib][lane / 3][lane % 3] = p;
+            if (pn) s_sv[ib][lane / 3][lane % 3] = v;
+        }
         __syncthreads();
         double F = 0.0;
         if (warp == 0) {
             group_force<MODE, 1>(mg, n_m, s_sp[ib], s_sa);
+            if (pn) {
+                if (lane < n_m) {
+                    const double(*P)[4] = s_sp[ib];
+                    const double(*V)[4] = s_sv[ib];
+                    double ax = 0.0, ay = 0.0, az = 0.0;
+                    for (int k = 0; k < n_m; k++) {
+                        if (k == lane) continue;
+                        pn_pair(a.pn, P[lane][0], P[lane][1], P[lane][2], V[lane][0], V[lane][1],
+                                V[lane][2], V[lane][3], P[k][0], P[k][1], P[k][2], V[k][0], V[k][1],
+                                V[k][2], V[k][3], ax, ay, az);
+                    }
+                    s_sa[lane][0] += ax;
+                    s_sa[lane][1] += ay;
+                    s_sa[lane][2] += az;
+                }
+                __syncwarp();
+            }
             if (has) F = s_sa[lane / 3][lane % 3];
         } else {
             double fx, fy, fz;
             split_tp_force<MODE>(a, s_sp[ib], n_m, p, lane, fx, fy, fz);
+            if (pn) {
+                const double x = __shfl_sync(0xffffffffu, p, 0, 4);
+                const double y = __shfl_sync(0xffffffffu, p, 1, 4);
+                const double z = __shfl_sync(0xffffffffu, p, 2, 4);
+                const double vx = __shfl_sync(0xffffffffu, v, 0, 4);
+                const double vy = __shfl_sync(0xffffffffu, v, 1, 4);
+                const double vz = __shfl_sync(0xffffffffu, v, 2, 4);
+                double ax = 0.0, ay = 0.0, az = 0.0;
+                if ((lane & 3) == 0) {
+                    const double(*P)[4] = s_sp[ib];
+                    const double(*V)[4] = s_sv[ib];
+                    for (int k = 0; k < n_m; k++)
+                        pn_pair(a.pn, x, y, z, vx, vy, vz, my_m, P[k][0], P[k][1], P[k][2],
+                                V[k][0], V[k][1], V[k][2], V[k][3], ax, ay, az);
+                }
+                fx += __shfl_sync(0xffffffffu, ax, 0, 4);
+                fy += __shfl_sync(0xffffffffu, ay, 0, 4);
+                fz += __shfl_sync(0xffffffffu, az, 0, 4);
+            }
             const int c = lane & 3;
             F = c == 0 ? fx : (c == 1 ? fy : fz);
         }
@@ -882,7 +933,7 @@ __global__ void __launch_bounds__(64) radau_split(EngineArgs a)
     long long my_attempts = 0;
     if (ctl->phase == 0) {
         // F1 = f(y0), then initial_time_step (src/integrator_gauss_radau15.c:75-120)
-        X.F1 = forces(X.y0);
+        X.F1 = forces(X.y0, X.dy0);
         if (leader) ctl->force_calls++;
         unsigned long long k0 = 0, k1 = 0;
         if (has && gi < a.n && writer) {  // the reference scans the first n of 3n entries
@@ -895,7 +946,7 @@ __global__ void __launch_bounds__(64) radau_split(EngineArgs a)
         double d0, d1;
         read2(ctl, red_idx++, d0, d1);
         const double dt0 = (d0 < 1e-5 || d1 < 1e-5) ? 1e-6 : 0.01 * (d0 / d1);
-        const double f1 = forces(X.y0 + dt0 * X.dy0);
+        const double f1 = forces(X.y0 + dt0 * X.dy0, X.dy0 + dt0 * X.F1);
         if (leader) ctl->force_calls++;
         const unsigned long long k2 = (has && writer) ? absmax_key(f1 - X.F1) : 0ull;
         reduce2(ctl, red_idx, k2, 0ull);
@@ -924,7 +975,8 @@ __global__ void __launch_bounds__(64) radau_split(EngineArgs a)
             unsigned long long kdb = 0, kf8 = 0;
             for (int ih = 1; ih < 8; ih++) {
                 const double sh = e_hs[ih], ds = h * sh, hh = 0.5 * ds * ds;
-                const double F = forces(has ? e_pred_pos<MODE>(X, ih, sh, h, ds, hh) : 0.0);
+                const double F = forces(has ? e_pred_pos<MODE>(X, ih, sh, h, ds, hh) : 0.0,
+                                        (has && pn) ? e_pred_vel_at<MODE>(X, ih, sh, h) : 0.0);
                 if (has) {
                     e_gb_update<MODE>(X, ih, F);
                     if (ih == 7 && writer) {
@@ -945,7 +997,7 @@ __global__ void __launch_bounds__(64) radau_split(EngineArgs a)
         const double hh1 = 0.5 * h * h;
         const double ya = has ? e_pred_pos<MODE>(X, 8, 1.0, h, h, hh1) : 0.0;
         const double va = has ? e_pred_vel<MODE>(X, h) : 0.0;
-        const double dd = forces(ya);
+        const double dd = forces(ya, va);
         unsigned long long kb6 = 0, kdd = 0;
         if (has && writer) {
             a.ypa[gi] = ya;
@@ -1132,6 +1184,15 @@ static int dispatch_engine(int mode, int js, int block, const EngineArgs &a, int
 
 static int g_engine_js = 0, g_engine_block = 0;  // debug override (0: automatic)
 
+static const void *split_fn(int mode, bool pn)
+{
+    if (mode == ABIE_FORCE_EXACT)
+        return pn ? (const void *)radau_split<ABIE_FORCE_EXACT, true>
+                  : (const void *)radau_split<ABIE_FORCE_EXACT, false>;
+    return pn ? (const void *)radau_split<ABIE_FORCE_FP64, true>
+              : (const void *)radau_split<ABIE_FORCE_FP64, false>;
+}
+
 // Launch shape.  Each FP64 warp instruction occupies an SM sub-partition's
 // FP64 pipe for about 64 cycles however many lanes are active, so the time
 // of a substep is about (warps per sub-partition) x (FP64 instructions per
@@ -1234,6 +1295,8 @@ int radau_run(const SystemView &sys, double t, double t_end, int mode, EventStat
     a.src[1] = e.srcs + n;
     a.srca = e.srcs + 2 * n;
     a.t_end = t_end;
+    a.C = g_sim.C;  // the stored speed of light, as src/common.c:101-107 reads it
+    a.pn = pn_const(sys.G, a.C > 0.0 ? a.C : 1.0);
     double ce = evs ? evs->ce_dist : 0.0;
     a.ce_dist = ce;
     double thr = std::max(ce, 2.0 * rmax);
@@ -1271,11 +1334,16 @@ int radau_run(const SystemView &sys, double t, double t_end, int mode, EventStat
     bool split = false;
     if (n_src <= 10 && g_engine_js == 0) {
         int bps = 0;
-        ABIE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &bps, mode == ABIE_FORCE_EXACT ? (const void *)radau_split<ABIE_FORCE_EXACT>
-                                           : (const void *)radau_split<ABIE_FORCE_FP64>, 64, 0));
+        ABIE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, split_fn(mode, a.C > 0.0), 64, 0));
         split = (long long)std::max(1, (n_tp + SPLIT_TPW - 1) / SPLIT_TPW) <=
                 (long long)bps * g_sim.num_sms;
+    }
+    if (a.C > 0.0 && !split) {
+        set_error(ABIE_ERR_UNSUPPORTED,
+                  "post-Newtonian terms (C > 0) run on the split Radau15 engine only: at most 10 "
+                  "massive bodies (this system has %d) and one resident wave of test particles",
+                  n_src);
+        return ABIE_ERR_UNSUPPORTED;
     }
     EngineCtl c;
     long long budget = 4;
@@ -1290,9 +1358,8 @@ int radau_run(const SystemView &sys, double t, double t_end, int mode, EventStat
             EngineArgs args = a;
             void *params[] = {&args};
             grid = std::max(1, (n_tp + SPLIT_TPW - 1) / SPLIT_TPW);
-            const void *fn = mode == ABIE_FORCE_EXACT ? (const void *)radau_split<ABIE_FORCE_EXACT>
-                                                      : (const void *)radau_split<ABIE_FORCE_FP64>;
-            ABIE_CUDA(cudaLaunchCooperativeKernel(fn, dim3((unsigned)grid), dim3(64), params, 0, st));
+            ABIE_CUDA(cudaLaunchCooperativeKernel(split_fn(mode, a.C > 0.0), dim3((unsigned)grid), dim3(64),
+                                                  params, 0, st));
             rc = 0;
         } else {
             rc = dispatch_engine(mode, js, block, a, g_sim.num_sms, st, &grid);
@@ -1367,11 +1434,6 @@ int integrator_gr(double t, double t_end, double dt)
     if (!s.inited) {
         set_error(ABIE_ERR_NOT_INITIALIZED, "integrator_gr before initialize_code");
         return ABIE_ERR_NOT_INITIALIZED;
-    }
-    if (s.C > 0.0) {
-        set_error(ABIE_ERR_UNSUPPORTED,
-                  "post-Newtonian terms (C > 0, src/additional_forces.c) are not on the GPU path");
-        return ABIE_ERR_UNSUPPORTED;
     }
     SystemView v{s.pos, s.vel, s.m, s.r, s.ext_enabled ? s.ext_acc : nullptr,
                  s.h_m.data(), s.h_r.data(), (int)s.n, s.G};

@@ -17,6 +17,7 @@ static __constant__ double e_cs[8][8] = ABIE_RADAU_CS_INIT;
 static __constant__ double e_rsp[8][8] = ABIE_RADAU_RSP_INIT;  // fast sweep: expanded g recurrence
 static __constant__ double e_wg[9][7] = ABIE_RADAU_WG_INIT;    // fast sweep: position weights on g, row 8 = spacing 1
 static __constant__ double e_vg[7] = ABIE_RADAU_VG_INIT;       // fast sweep: velocity weights on g at spacing 1
+static __constant__ double e_vgs[9][7] = ABIE_RADAU_VGS_INIT;  // velocity weights on g at every spacing
 
 
 static constexpr double EPSB = 1.e-4;
@@ -80,6 +81,26 @@ __device__ __forceinline__ double e_pred_vel(const Comp &c, double dt)
     u = fma(g[1], e_vg[1], u);
     u = fma(g[0], e_vg[0], u);
     return fma(dt, c.F1 + u, c.dy0);
+}
+
+// Predicted velocity at spacing s = e_hs[row] (row 8: s = 1), needed only
+// by velocity-dependent forces (src/integrator_gauss_radau15.c:129-134).
+template <int MODE>
+__device__ __forceinline__ double e_pred_vel_at(const Comp &c, int row, double s, double dt)
+{
+    const double *b = c.b;
+    if (MODE == ABIE_FORCE_EXACT)
+        return c.dy0 + dt * s * (c.F1 + s * (b[0] / 0.2e1 + s * (b[1] / 0.3e1 + s * (b[2] / 0.4e1 + s * (b[3] / 0.5e1 + s * (b[4] / 0.6e1 + s * (b[5] / 0.7e1 + s * b[6] / 0.8e1)))))));
+    const double *w = e_vgs[row];
+    const double *g = c.g;
+    double u = g[6] * w[6];
+    u = fma(g[5], w[5], u);
+    u = fma(g[4], w[4], u);
+    u = fma(g[3], w[3], u);
+    u = fma(g[2], w[2], u);
+    u = fma(g[1], w[1], u);
+    u = fma(g[0], w[0], u);
+    return fma(dt * s, c.F1 + u, c.dy0);
 }
 
 // b6 of the corrector: b_6 = cs[6][6] g_6 = g_6, read from g in the fast form.

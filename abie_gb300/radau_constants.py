@@ -74,7 +74,8 @@ def fast_tables():
       s_8 = 1: the weights of b_k in the predicted position at spacing s_i.
     * ``wg[i][j] = sum_{k<=j} cs[j][k] wpos[i][k]``: the same weights on the
       Newton-form coefficients g_j, and ``vg[j] = sum_{k<=j} cs[j][k]/(k+2)``
-      those of the predicted velocity at spacing 1.
+      those of the predicted velocity at spacing 1; ``vgs[i][j]`` the
+      velocity weights at every spacing s_i (row 8: s = 1).
     """
     h, rs, cs = tables()
     rsp = [[mpmath.mpf(0)] * NH for _ in range(NH)]
@@ -91,10 +92,14 @@ def fast_tables():
     # sum_k b_k w_k = sum_j g_j sum_{k<=j} cs[j][k] w_k
     wg = [[sum(cs[j][k] * row[k] for k in range(j + 1)) for j in range(7)] for row in wpos]
     vg = [sum(cs[j][k] / (k + 2) for k in range(j + 1)) for j in range(7)]
+    # velocity weights at every spacing: sum_k b_k s^(k+1) / (k+2) on g
+    vgs = [[sum(cs[j][k] * s ** (k + 1) / (k + 2) for k in range(j + 1)) for j in range(7)]
+           for s in list(h) + [mpmath.mpf(1)]]
     return ([[to_double(v) for v in row] for row in rsp],
             [[to_double(v) for v in row] for row in wpos],
             [[to_double(v) for v in row] for row in wg],
-            [to_double(v) for v in vg])
+            [to_double(v) for v in vg],
+            [[to_double(v) for v in row] for row in vgs])
 
 
 def to_double(v):
@@ -110,7 +115,7 @@ def double_tables():
 
 def emit_header(path):
     h, rs, cs = double_tables()
-    rsp, wpos, wg, vg = fast_tables()
+    rsp, wpos, wg, vg, vgs = fast_tables()
 
     def row(vals):
         return "{" + ", ".join(float.hex(v) for v in vals) + "}"
@@ -127,6 +132,7 @@ def emit_header(path):
         "#define ABIE_RADAU_WPOS_INIT {" + ", ".join(row(w) for w in wpos) + "}",
         "#define ABIE_RADAU_WG_INIT {" + ", ".join(row(w) for w in wg) + "}",
         "#define ABIE_RADAU_VG_INIT " + row(vg),
+        "#define ABIE_RADAU_VGS_INIT {" + ", ".join(row(w) for w in vgs) + "}",
         "#endif",
         "",
     ]

@@ -72,7 +72,10 @@ void reset_collision_buffer(void);
 size_t set_additional_forces(size_t N, double *ext_acc);
 /* src/common.c:524-527 -> src/integrator_gauss_radau15.c:287-446.
  * Gauss-Radau 15 from t to the first accepted time past t_end, on the
- * device-resident state; dt is ignored as in the reference. */
+ * device-resident state; dt is ignored as in the reference.  With a stored
+ * C > 0 the accelerations include the post-Newtonian terms
+ * (src/additional_forces.c), for systems of at most 10 massive bodies;
+ * more massive bodies with C > 0 return ABIE_ERR_UNSUPPORTED. */
 int integrator_gr(double t, double t_end, double dt);
 /* src/common.c:534-537 -> src/integrator_wisdom_holman.c:513-537.
  * Fixed-step Wisdom-Holman on a heliocentric state. */
@@ -90,8 +93,10 @@ double calculate_energy(void);
 size_t ode_n_body_second_order(const double *pos, size_t N, double G,
                                const double *masses, const double *radii,
                                double *acc);
-/* src/common.c:206-238: ode_n_body_second_order plus the external
- * accelerations set by set_additional_forces. */
+/* src/common.c:206-238: ode_n_body_second_order, the post-Newtonian terms
+ * when the stored C is positive (src/additional_forces.c:14-121, in the
+ * reference's operations), then the external accelerations set by
+ * set_additional_forces. */
 size_t calculate_accelerations(const double *pos, const double *vel, size_t N,
                                double G, const double *masses,
                                const double *radii, double *acc);

@@ -108,8 +108,16 @@ class Oracle:
         return self.lib.orc_energy(_ptr(pos), _ptr(vel), _ptr(m), ctypes.c_size_t(m.size),
                                    ctypes.c_double(G))
 
+    def post_newtonian(self, pos, vel, m, G, C, acc=None):
+        """src/additional_forces.c:14-121 added to acc (zeros by default)."""
+        pos, vel, m = _f64(pos), _f64(vel), _f64(m)
+        acc = np.zeros(pos.size) if acc is None else _f64(acc).copy()
+        self.lib.orc_post_newtonian(_ptr(pos), _ptr(vel), ctypes.c_size_t(m.size),
+                                    ctypes.c_double(G), ctypes.c_double(C), _ptr(m), _ptr(acc))
+        return acc
+
     def radau15(self, pos, vel, m, r, G, t, t_end, ce_dist=0.0, max_ce=1, max_coll=1,
-                events=True):
+                events=True, C=0.0):
         pos, vel, m, r = (_f64(pos).copy(), _f64(vel).copy(), _f64(m), _f64(r))
         ev = _Events()
         buf_ce = np.zeros(4 * max(max_ce, 1))
@@ -120,11 +128,15 @@ class Oracle:
         ev.buf_coll = _ptr(buf_coll) if max_coll > 0 else None
         st = RadauStats()
         t_out = ctypes.c_double(t)
-        flag = self.lib.orc_radau15(_ptr(pos), _ptr(vel), _ptr(m), _ptr(r),
-                                    ctypes.c_size_t(m.size), ctypes.c_double(G),
-                                    ctypes.c_double(t), ctypes.c_double(t_end),
-                                    ctypes.byref(ev) if events else None,
-                                    ctypes.byref(t_out), ctypes.byref(st))
+        self.lib.orc_set_pn(ctypes.c_double(C))
+        try:
+            flag = self.lib.orc_radau15(_ptr(pos), _ptr(vel), _ptr(m), _ptr(r),
+                                        ctypes.c_size_t(m.size), ctypes.c_double(G),
+                                        ctypes.c_double(t), ctypes.c_double(t_end),
+                                        ctypes.byref(ev) if events else None,
+                                        ctypes.byref(t_out), ctypes.byref(st))
+        finally:
+            self.lib.orc_set_pn(ctypes.c_double(0.0))
         return {"pos": pos, "vel": vel, "t": t_out.value, "flag": flag,
                 "stats": st.as_dict(), "n_ce": ev.n_ce, "n_coll": ev.n_coll,
                 "buf_ce": buf_ce, "buf_coll": buf_coll}
@@ -256,9 +268,19 @@ class Reference:
         self._load(pos, vel, m, np.zeros(m.size), G)
         return self.lib.calculate_energy()
 
-    def radau15(self, pos, vel, m, r, G, t, t_end, ce_dist=0.0, max_ce=1, max_coll=1):
+    def accelerations(self, pos, vel, m, G, C):
+        """calculate_accelerations (Newton, then post-Newtonian terms for C > 0)."""
+        pos, vel, m = _f64(pos), _f64(vel), _f64(m)
+        self._load(pos, vel, m, np.zeros(m.size), G, C=C)
+        acc = np.zeros(pos.size)
+        self.lib.calculate_accelerations(_ptr(pos), _ptr(vel), ctypes.c_size_t(m.size),
+                                         ctypes.c_double(G), _ptr(m), _ptr(np.zeros(m.size)),
+                                         _ptr(acc))
+        return acc
+
+    def radau15(self, pos, vel, m, r, G, t, t_end, ce_dist=0.0, max_ce=1, max_coll=1, C=0.0):
         pos, vel, m, r = _f64(pos), _f64(vel), _f64(m), _f64(r)
-        self._load(pos, vel, m, r, G, max_ce=max_ce, max_coll=max_coll, ce_dist=ce_dist)
+        self._load(pos, vel, m, r, G, C=C, max_ce=max_ce, max_coll=max_coll, ce_dist=ce_dist)
         flag = _run_big_stack(lambda: self.lib.integrator_gr(
             ctypes.c_double(t), ctypes.c_double(t_end), ctypes.c_double(1.0)))
         p, v = self._state(m.size)

@@ -204,15 +204,87 @@ static const double TOLPC = 1.e-16;      /* .h:63 */
 static const double H_MIN = 1.e-13;      /* .h:17 */
 #define EXPONENT (1. / 7)                /* .h:61 */
 
-static void force_counted(const double *y, size_t n, double G, const double *m,
-                          double *acc, orc_radau_stats *st)
+/* src/additional_forces.c:14-121: adds the 1PN, 2PN and 2.5PN terms of
+ * every pair to acc (the pair loop runs over all k != j, massless bodies
+ * included). */
+void orc_post_newtonian(const double *pos, const double *vel, size_t n, double G, double C,
+                        const double *m, double *acc)
+{
+    double CM1 = 1.0 / C;
+    double CM2 = CM1 * CM1;
+    double CM4 = CM2 * CM2;
+    double CM5 = CM1 * CM4;
+    double c8div5 = (8.0 / 5.0);
+    double c17div3 = (17.0 / 3.0);
+    for (size_t j = 0; j < n; j++) {
+        double x = pos[j * 3], y = pos[j * 3 + 1], z = pos[j * 3 + 2];
+        double vx = vel[j * 3], vy = vel[j * 3 + 1], vz = vel[j * 3 + 2];
+        double M_j = m[j];
+        double ax = 0.0, ay = 0.0, az = 0.0;
+        for (size_t k = 0; k < n; k++) {
+            if (j == k) continue;
+            double M_k = m[k];
+            double GM = G * M_k;
+            double GM_C_PM2 = GM * CM2;
+            double GM_P2_C_PM2 = GM * GM_C_PM2;
+            double dx = x - pos[k * 3], dy = y - pos[k * 3 + 1], dz = z - pos[k * 3 + 2];
+            double dvx = vx - vel[k * 3], dvy = vy - vel[k * 3 + 1], dvz = vz - vel[k * 3 + 2];
+            double r_dot_v = dx * dvx + dy * dvy + dz * dvz;
+            double v_dot_v = dvx * dvx + dvy * dvy + dvz * dvz;
+            double rel_sep2 = dx * dx + dy * dy + dz * dz;
+            double rel_sep1 = sqrt(rel_sep2);
+            double d1 = 1.0 / rel_sep1;
+            double d2 = d1 * d1;
+            double d3 = d1 * d2;
+            double d4 = d1 * d3;
+            /* 1PN */
+            double F0 = 4.0 * GM_C_PM2 * r_dot_v * d3;
+            double F1 = 4.0 * GM_P2_C_PM2 * d4;
+            double F2 = -GM_C_PM2 * v_dot_v * d3;
+            ax += F0 * dvx + F1 * dx + F2 * dx;
+            ay += F0 * dvy + F1 * dy + F2 * dy;
+            az += F0 * dvz + F1 * dz + F2 * dz;
+            /* 2PN */
+            double GM_P2_RC_PM4 = GM_P2_C_PM2 * CM2 * d4;
+            double G0 = 2.0 * r_dot_v * r_dot_v * d2;
+            double G1 = -9.0 * GM * d1;
+            double G2 = -2.0 * r_dot_v;
+            ax += GM_P2_RC_PM4 * (G0 * dx + G1 * dx + G2 * dvx);
+            ay += GM_P2_RC_PM4 * (G0 * dy + G1 * dy + G2 * dvy);
+            az += GM_P2_RC_PM4 * (G0 * dz + G1 * dz + G2 * dvz);
+            /* 2.5PN */
+            double M_tot = M_j + M_k;
+            double nu = M_j * M_k / (M_tot * M_tot);
+            double GM_tot = G * M_tot;
+            double H0 = -c8div5 * GM_tot * GM_tot * nu * CM5 * d3;
+            double H1 = v_dot_v + 3.0 * GM_tot * d1;
+            double H2 = -(3.0 * v_dot_v + c17div3 * GM_tot * d1) * r_dot_v * d2;
+            ax += H0 * (H1 * dvx + H2 * dx);
+            ay += H0 * (H1 * dvy + H2 * dy);
+            az += H0 * (H1 * dvz + H2 * dz);
+        }
+        acc[j * 3] += ax;
+        acc[j * 3 + 1] += ay;
+        acc[j * 3 + 2] += az;
+    }
+}
+
+/* src/common.c:82-114 without external accelerations: Newton, then the
+ * post-Newtonian terms when C > 0. */
+static double g_orc_C = 0.0;
+static void force_counted_v(const double *y, const double *dy, size_t n, double G, const double *m,
+                            double *acc, orc_radau_stats *st)
 {
     /* sinks with negative mass keep a zero acceleration (see DESIGN notes on
      * the reference leaving them untouched in malloc'd buffers) */
     memset(acc, 0, 3 * n * sizeof(double));
     orc_force(y, n, G, m, acc, 0, n);
+    if (g_orc_C > 0.0) orc_post_newtonian(y, dy, n, G, g_orc_C, m, acc);
     if (st) st->force_calls++;
 }
+
+/* Speed of light for the oracle's Radau15 (0: no post-Newtonian terms). */
+void orc_set_pn(double C) { g_orc_C = C; }
 
 /* :75-120 */
 static double initial_step(const double *y0, const double *dy0, double G,
@@ -225,7 +297,7 @@ static double initial_step(const double *y0, const double *dy0, double G,
     double *y1 = (double *)malloc(dim * sizeof(double));
     double *dy1 = (double *)malloc(dim * sizeof(double));
     double dt0, dt1;
-    force_counted(y0, n, G, m, f0, st);
+    force_counted_v(y0, dy0, n, G, m, f0, st);
     double d0 = max_abs(y0, n); /* the reference scans n (not 3n) entries (:89-90) */
     double d1 = max_abs(f0, n);
     if (d0 < 1e-5 || d1 < 1e-5) dt0 = 1e-6;
@@ -234,7 +306,7 @@ static double initial_step(const double *y0, const double *dy0, double G,
         y1[i] = y0[i] + dt0 * dy0[i];
         dy1[i] = dy0[i] + dt0 * f0[i];
     }
-    force_counted(y1, n, G, m, f1, st);
+    force_counted_v(y1, dy1, n, G, m, f1, st);
     double d2 = -DBL_MAX;
     for (size_t i = 0; i < dim; i++) {
         double a = fabs(f1[i] - f0[i]);
@@ -335,7 +407,7 @@ int orc_radau15(double *pos, double *vel, const double *m, const double *r,
     memcpy(y0, pos, dim * sizeof(double));
     memcpy(dy0, vel, dim * sizeof(double));
     int flag = 0;
-    force_counted(y0, n, G, m, ddy0, st);                 /* :336 */
+    force_counted_v(y0, dy0, n, G, m, ddy0, st);         /* :336 */
     double h = initial_step(y0, dy0, G, m, n, st);        /* :339 */
 
     int running = 1, rejects_in_row = 0;
@@ -347,7 +419,7 @@ int orc_radau15(double *pos, double *vel, const double *m, const double *r,
             for (int ih = 0; ih < 8; ih++) {
                 predict_pos(y0, dy0, ddy0, HS[ih], b, dim, h, y);
                 predict_vel(dy0, ddy0, HS[ih], b, dim, h, dy);
-                force_counted(y, n, G, m, F[ih], st);
+                force_counted_v(y, dy, n, G, m, F[ih], st);
                 update_g(F, ih, dim, g);
                 update_b(g, ih, dim, b);
             }
@@ -362,7 +434,7 @@ int orc_radau15(double *pos, double *vel, const double *m, const double *r,
         }
         predict_pos(y0, dy0, ddy0, 1., b, dim, h, y);        /* :375 */
         predict_vel(dy0, ddy0, 1., b, dim, h, dy);
-        force_counted(y, n, G, m, ddy, st);
+        force_counted_v(y, dy, n, G, m, ddy, st);
         double estim_b6 = max_abs(b[6], dim) / max_abs(ddy, dim);
         double err = pow(estim_b6 / EPSB, EXPONENT);
         double dtreq = h / err;

@@ -71,6 +71,11 @@ void orc_jacobi2helio(const double *jpos, const double *jvel, const double *m,
                       size_t n, double *pos, double *vel);
 /* src/integrator_wisdom_holman.c:66-147; returns 1 when not converged. */
 int orc_kepler(double *jpos, double *jvel, double gm, double dt, size_t id);
+/* src/additional_forces.c:14-121: adds the post-Newtonian pair terms to acc. */
+void orc_post_newtonian(const double *pos, const double *vel, size_t n, double G, double C,
+                        const double *m, double *acc);
+/* Speed of light used by orc_radau15's accelerations (0: Newtonian only). */
+void orc_set_pn(double C);
 /* src/common.c:3-36: derivative of the first-order state vec = (pos, vel). */
 void orc_first_order(const double *vec, size_t n, double G, const double *m, double *dxdt);
 /* src/integrator_runge_kutta.c:6-50: classical RK4 from t while t < t_end

@@ -5,7 +5,8 @@ Run in a container where the reference sources exist:
     oracle/build_ref.sh && python tests/golden/make_golden.py
 
 Every output array below comes from the reference's own entry points
-(ode_n_body_second_order, calculate_energy, integrator_gr, integrator_wh, integrator_rk,
+(ode_n_body_second_order, calculate_accelerations, calculate_energy, integrator_gr,
+integrator_wh, integrator_rk,
 the event buffers) driven through ctypes by ``oracle.Reference``.  The
 inputs are the package's seeded generators.  The resulting ``golden.npz``
 is small, committed, and travels with the tests; nothing at test time reads
@@ -102,6 +103,14 @@ def main(out=os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden.np
     gold["rk_in_pos"], gold["rk_in_vel"], gold["rk_m"] = p, v, m
     gold["rk_span"] = np.array([0.0, 0.5, 0.005])
     gold["rk_pos"], gold["rk_vel"] = out_["pos"], out_["vel"]
+
+    # -- post-Newtonian terms (src/additional_forces.c), C = speed of light in au/yr --
+    C = 63239.7263
+    p, v, m, r = ics.planetary_system(seed=81, n_planets=5, n_tp=0)
+    gold["pn_in_pos"], gold["pn_in_vel"], gold["pn_m"], gold["pn_C"] = p, v, m, np.array([C])
+    gold["pn_acc"] = R.accelerations(p, v, m, G, C)
+    out_ = R.radau15(p, v, m, r, G, 0.0, 2.0, C=C)
+    gold["pn_gr_pos"], gold["pn_gr_vel"], gold["pn_gr_t"] = out_["pos"], out_["vel"], np.array([out_["t"]])
 
     np.savez_compressed(out, **gold)
     print("wrote", out, os.path.getsize(out), "bytes,", len(gold), "arrays")

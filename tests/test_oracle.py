@@ -61,6 +61,23 @@ def test_wh_golden(oracle, golden, sparse):
     assert out["t"] == golden["wh_t"][0]
 
 
+def test_post_newtonian_golden(oracle, golden):
+    p, v, m, C = golden["pn_in_pos"], golden["pn_in_vel"], golden["pn_m"], golden["pn_C"][0]
+    acc = oracle.post_newtonian(p, v, m, G, C, acc=oracle.force(p, m, G))
+    assert np.array_equal(acc, golden["pn_acc"])
+    out = oracle.radau15(p, v, m, np.zeros(m.size), G, 0.0, 2.0, C=C)
+    assert np.array_equal(out["pos"], golden["pn_gr_pos"])
+    assert np.array_equal(out["vel"], golden["pn_gr_vel"])
+    assert out["t"] == golden["pn_gr_t"][0]
+
+
+def test_live_post_newtonian(oracle, reference):
+    p, v, m, r = ics.planetary_system(seed=411, n_planets=6, n_tp=0)
+    C = 63239.7263
+    a = oracle.post_newtonian(p, v, m, G, C, acc=oracle.force(p, m, G))
+    assert np.array_equal(a, reference.accelerations(p, v, m, G, C))
+
+
 def test_rk_golden(oracle, golden):
     t0, t1, dt = golden["rk_span"]
     out = oracle.rk(golden["rk_in_pos"], golden["rk_in_vel"], golden["rk_m"], G, t0, t1, dt)
