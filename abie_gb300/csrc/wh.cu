@@ -44,7 +44,8 @@ struct WhArgs {
     double *jpos, *jvel;      // head Jacobi state (3 * head)
     double *eta, *gm;         // head interior masses and Kepler parameters
     double *ir3h, *ir3j;      // head inverse cubes
-    WhShared *sh;
+    WhShared *sh;             // two sets, by step parity
+    double *hsrc;             // two sets of the massive head bodies: x y z G m (4 per body)
 };
 
 // x^3 rounded once: x*x with its exact error (fma), times x (Dekker-style
@@ -276,12 +277,12 @@ __device__ __forceinline__ double wh_ir3(double x, double y, double z)
 }
 
 template <int MODE>
-__global__ void __launch_bounds__(256) wh_head_kernel(WhArgs a, int init)
+__global__ void __launch_bounds__(256) wh_head_kernel(WhArgs a, int init, int parity)
 {
     const int H = a.head, n = a.n;
     const double dt = a.dt, half = dt / 2;
     const double *m = a.m;
-    WhShared *sh = a.sh;
+    WhShared *sh = a.sh + parity;
     if (!init)
         for (int i = 1 + threadIdx.x; i < H; i += blockDim.x)
             for (int c = 0; c < 3; c++) a.vel[3 * i + c] += a.acc[3 * i + c] * half;
@@ -392,6 +393,20 @@ __global__ void __launch_bounds__(256) wh_head_kernel(WhArgs a, int init)
         }
         __syncthreads();
     }
+    // the massive head bodies' positions of this step for the tail kernel
+    // (its own copy, so the next step's head can run beside this tail)
+    if (threadIdx.x == 0) {
+        double *hs = a.hsrc + parity * 4 * WH_HEAD_MAX;
+        int q = 0;
+        for (int i = 1; i < H; i++) {
+            if (m[i] == 0.0) continue;
+            hs[4 * q] = a.pos[3 * i];
+            hs[4 * q + 1] = a.pos[3 * i + 1];
+            hs[4 * q + 2] = a.pos[3 * i + 2];
+            hs[4 * q + 3] = a.G * m[i];
+            q++;
+        }
+    }
     // accelerations of the head (:364-451)
     for (int i = threadIdx.x; i < H; i += blockDim.x) {
         double h = 0.0, j = 0.0;
@@ -470,27 +485,16 @@ __global__ void __launch_bounds__(256) wh_head_kernel(WhArgs a, int init)
 // correctly rounded cubes, closed-form Stumpff functions); the fast form
 // uses kepler_drift_fast and the one-instruction r^-3 of the force kernels.
 template <int MODE>
-__global__ void __launch_bounds__(256) wh_tail_kernel(WhArgs a, int init)
+__global__ void __launch_bounds__(256) wh_tail_kernel(WhArgs a, int init, int parity, int n_src)
 {
     extern __shared__ double hs[];  // 4 doubles per massive head body: x y z G*m
-    __shared__ int n_src;
     const int H = a.head;
-    if (threadIdx.x == 0) {
-        int q = 0;
-        for (int i = 1; i < H; i++) {
-            if (a.m[i] == 0.0) continue;
-            hs[4 * q] = a.pos[3 * i];
-            hs[4 * q + 1] = a.pos[3 * i + 1];
-            hs[4 * q + 2] = a.pos[3 * i + 2];
-            hs[4 * q + 3] = a.G * a.m[i];
-            q++;
-        }
-        n_src = q;
-    }
+    const double *hsrc = a.hsrc + parity * 4 * WH_HEAD_MAX;
+    for (int e = threadIdx.x; e < 4 * n_src; e += blockDim.x) hs[e] = hsrc[e];
     __syncthreads();
     const long long i = (long long)H + (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
-    const WhShared *sh = a.sh;
+    const WhShared *sh = a.sh + parity;
     const double half = a.dt / 2;
     double p[3], v[3], jp[3], jv[3];
     for (int c = 0; c < 3; c++) {
@@ -503,7 +507,7 @@ __global__ void __launch_bounds__(256) wh_tail_kernel(WhArgs a, int init)
     if (!init) {
         const int failed = MODE == ABIE_FORCE_EXACT ? kepler_drift(jp, jv, sh->gm_tail, a.dt)
                                                     : kepler_drift_fast(jp, jv, sh->gm_tail, sh->gm_tail_k, a.dt);
-        if (failed) atomicAdd(&a.sh->kepler_failures, 1ull);
+        if (failed) atomicAdd(&a.sh[parity].kepler_failures, 1ull);
         for (int c = 0; c < 3; c++) {
             p[c] = jp[c] + sh->Rp[c];
             v[c] = jv[c] + sh->Vp[c];
@@ -542,7 +546,9 @@ __global__ void __launch_bounds__(256) wh_tail_kernel(WhArgs a, int init)
 struct WhBuffers {
     double *acc = nullptr, *scratch = nullptr;
     size_t acc_n = 0;
-    WhShared *sh = nullptr;
+    WhShared *sh = nullptr;  // two sets
+    cudaStream_t tail_stream = nullptr;
+    cudaEvent_t ev_head = nullptr, ev_tail[2] = {nullptr, nullptr};
 };
 static WhBuffers g_wh;
 
@@ -551,20 +557,48 @@ void free_wh_buffers()
     if (g_wh.acc) cudaFree(g_wh.acc);
     if (g_wh.scratch) cudaFree(g_wh.scratch);
     if (g_wh.sh) cudaFree(g_wh.sh);
+    if (g_wh.ev_head) cudaEventDestroy(g_wh.ev_head);
+    for (int k = 0; k < 2; k++)
+        if (g_wh.ev_tail[k]) cudaEventDestroy(g_wh.ev_tail[k]);
+    if (g_wh.tail_stream) cudaStreamDestroy(g_wh.tail_stream);
     g_wh = WhBuffers();
 }
 
-static int wh_launch_step(const WhArgs &a, int init, int n_src, int mode, cudaStream_t st)
+static void wh_launch_head(const WhArgs &a, int init, int parity, int mode, cudaStream_t st)
 {
-    if (mode == ABIE_FORCE_EXACT) wh_head_kernel<ABIE_FORCE_EXACT><<<1, 256, 0, st>>>(a, init);
-    else wh_head_kernel<ABIE_FORCE_FP64><<<1, 256, 0, st>>>(a, init);
+    if (mode == ABIE_FORCE_EXACT) wh_head_kernel<ABIE_FORCE_EXACT><<<1, 256, 0, st>>>(a, init, parity);
+    else wh_head_kernel<ABIE_FORCE_FP64><<<1, 256, 0, st>>>(a, init, parity);
+}
+
+static void wh_launch_tail(const WhArgs &a, int init, int parity, int n_src, int mode, cudaStream_t st)
+{
     long long tail = (long long)a.n - a.head;
-    if (tail > 0) {
-        unsigned blocks = (unsigned)((tail + 255) / 256);
-        size_t smem = 4 * sizeof(double) * (size_t)std::max(n_src, 1);
-        if (mode == ABIE_FORCE_EXACT) wh_tail_kernel<ABIE_FORCE_EXACT><<<blocks, 256, smem, st>>>(a, init);
-        else wh_tail_kernel<ABIE_FORCE_FP64><<<blocks, 256, smem, st>>>(a, init);
+    if (tail <= 0) return;
+    unsigned blocks = (unsigned)((tail + 255) / 256);
+    size_t smem = 4 * sizeof(double) * (size_t)std::max(n_src, 1);
+    if (mode == ABIE_FORCE_EXACT)
+        wh_tail_kernel<ABIE_FORCE_EXACT><<<blocks, 256, smem, st>>>(a, init, parity, n_src);
+    else
+        wh_tail_kernel<ABIE_FORCE_FP64><<<blocks, 256, smem, st>>>(a, init, parity, n_src);
+}
+
+// count steps: heads on st, tails on the tail stream.  The massive bodies
+// never feel the test particles, so head k+1 runs beside tail k; step
+// parity selects the published set, and head k waits for tail k-2, the
+// last reader of its set.  Ends with st waiting for the last tail.
+static int wh_launch_steps(const WhArgs &a, int count, int n_src, int mode, cudaStream_t st)
+{
+    cudaStream_t st2 = g_wh.tail_stream;
+    for (int k = 0; k < count; k++) {
+        const int par = k & 1;
+        if (k >= 2) ABIE_CUDA(cudaStreamWaitEvent(st, g_wh.ev_tail[par], 0));
+        wh_launch_head(a, 0, par, mode, st);
+        ABIE_CUDA(cudaEventRecord(g_wh.ev_head, st));
+        ABIE_CUDA(cudaStreamWaitEvent(st2, g_wh.ev_head, 0));
+        wh_launch_tail(a, 0, par, n_src, mode, st2);
+        ABIE_CUDA(cudaEventRecord(g_wh.ev_tail[par], st2));
     }
+    if (count > 0) ABIE_CUDA(cudaStreamWaitEvent(st, g_wh.ev_tail[(count - 1) & 1], 0));
     return 0;
 }
 
@@ -589,9 +623,14 @@ int wh_run(const SystemView &sys, double t, double t_end, double dt, double *t_o
     for (int i = 1; i < H; i++) n_src += (sys.h_m[i] != 0.0);
     int rc;
     if ((rc = reserve(&g_wh.acc, &g_wh.acc_n, 3 * (size_t)n))) return rc;
-    if (!g_wh.scratch) ABIE_CUDA(cudaMalloc(&g_wh.scratch, (size_t)WH_HEAD_MAX * 10 * sizeof(double)));
-    if (!g_wh.sh) ABIE_CUDA(cudaMalloc(&g_wh.sh, sizeof(WhShared)));
-    ABIE_CUDA(cudaMemsetAsync(g_wh.sh, 0, sizeof(WhShared), st));
+    if (!g_wh.scratch) ABIE_CUDA(cudaMalloc(&g_wh.scratch, (size_t)WH_HEAD_MAX * 18 * sizeof(double)));
+    if (!g_wh.sh) ABIE_CUDA(cudaMalloc(&g_wh.sh, 2 * sizeof(WhShared)));
+    if (!g_wh.tail_stream) {
+        ABIE_CUDA(cudaStreamCreateWithFlags(&g_wh.tail_stream, cudaStreamNonBlocking));
+        ABIE_CUDA(cudaEventCreateWithFlags(&g_wh.ev_head, cudaEventDisableTiming));
+        for (int k = 0; k < 2; k++) ABIE_CUDA(cudaEventCreateWithFlags(&g_wh.ev_tail[k], cudaEventDisableTiming));
+    }
+    ABIE_CUDA(cudaMemsetAsync(g_wh.sh, 0, 2 * sizeof(WhShared), st));
     WhArgs a;
     a.n = n;
     a.head = H;
@@ -609,6 +648,7 @@ int wh_run(const SystemView &sys, double t, double t_end, double dt, double *t_o
     a.ir3h = s + 8 * WH_HEAD_MAX;
     a.ir3j = s + 9 * WH_HEAD_MAX;
     a.sh = g_wh.sh;
+    a.hsrc = s + 10 * WH_HEAD_MAX;  // 2 x 4 x WH_HEAD_MAX
 
     long long steps = 0;
     double tt = t;
@@ -618,36 +658,44 @@ int wh_run(const SystemView &sys, double t, double t_end, double dt, double *t_o
     }
     const int mode = g_sim.force_mode == ABIE_FORCE_EXACT ? ABIE_FORCE_EXACT : ABIE_FORCE_FP64;
     size_t smem = 4 * sizeof(double) * (size_t)std::max(n_src, 1);
-    if (smem > 48 * 1024) {
+    if (smem > 48 * 1024) {  // up to WH_HEAD_MAX massive head bodies
         ABIE_CUDA(cudaFuncSetAttribute(wh_tail_kernel<ABIE_FORCE_EXACT>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         ABIE_CUDA(cudaFuncSetAttribute(wh_tail_kernel<ABIE_FORCE_FP64>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     }
-    rc = wh_launch_step(a, 1, n_src, mode, st);
+    // set-up (:524-525): Jacobi coordinates and accelerations, in order
+    wh_launch_head(a, 1, 0, mode, st);
+    wh_launch_tail(a, 1, 0, n_src, mode, st);
     ABIE_CUDA(cudaGetLastError());
     if (steps > 0) {
-        const int CH = 32;
+        const int CH = 32;  // steps per captured graph (even: parities line up)
         cudaGraph_t graph = nullptr;
         cudaGraphExec_t exec = nullptr;
         long long full = steps / CH;
         if (full > 0) {
             ABIE_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-            for (int k = 0; k < CH; k++) wh_launch_step(a, 0, n_src, mode, st);
-            ABIE_CUDA(cudaStreamEndCapture(st, &graph));
+            rc = wh_launch_steps(a, CH, n_src, mode, st);
+            cudaError_t ce = cudaStreamEndCapture(st, &graph);
+            if (rc) {
+                if (graph) cudaGraphDestroy(graph);
+                return rc;
+            }
+            ABIE_CUDA(ce);
             ABIE_CUDA(cudaGraphInstantiate(&exec, graph, 0));
             for (long long k = 0; k < full; k++) ABIE_CUDA(cudaGraphLaunch(exec, st));
         }
-        for (long long k = full * CH; k < steps; k++) wh_launch_step(a, 0, n_src, mode, st);
+        rc = wh_launch_steps(a, (int)(steps - full * CH), n_src, mode, st);
+        if (rc) return rc;
         ABIE_CUDA(cudaGetLastError());
         if (exec) cudaGraphExecDestroy(exec);
         if (graph) cudaGraphDestroy(graph);
     }
-    WhShared h;
-    ABIE_CUDA(cudaMemcpyAsync(&h, g_wh.sh, sizeof h, cudaMemcpyDeviceToHost, st));
+    WhShared h[2];
+    ABIE_CUDA(cudaMemcpyAsync(h, g_wh.sh, sizeof h, cudaMemcpyDeviceToHost, st));
     ABIE_CUDA(cudaStreamSynchronize(st));
     if (ctr) {
-        ctr->kepler_failures += (long long)h.kepler_failures;
+        ctr->kepler_failures += (long long)(h[0].kepler_failures + h[1].kepler_failures);
         ctr->wh_steps += steps;
     }
     *t_out = tt;
