@@ -1,13 +1,15 @@
 // Batched Gauss-Radau 15 over many independent small systems.
 //
-// One warp integrates one system (at most 21 bodies) from a work queue; a
-// finished warp takes the next system, so systems of uneven size and
-// difficulty do not wait for each other.  Each lane owns up to two of the
-// system's 3N components and keeps their Radau state (y0, dy0, F1, b[7],
-// g[7], previous b6) in registers.  For the force, the predicted positions
-// go to shared memory and the pairs spread over the lanes: L = 32/N lanes
-// per sink, each summing every L-th source, partial sums added as a fixed
-// tree (L = 1 and the reference's operations in the exact form).  The
+// A group of threads integrates one system (at most 21 bodies) from a work
+// queue -- one warp for up to 10 bodies, two warps (a named barrier each)
+// for 11-21 -- and a finished group takes the next system, so systems of
+// uneven size and difficulty do not wait for each other.  Each thread owns
+// one of the system's 3N components and keeps its Radau state (y0, dy0,
+// F1, b[7], g[7], previous b6) in registers.  For the force, the predicted
+// positions go to shared memory and the pairs spread over the lanes: each
+// warp takes ceil(N / warps) sinks with L = 32 / that lanes per sink, each
+// summing every L-th source, partial sums added as a fixed tree (L = 1 and
+// the reference's operations in the exact form).  The
 // sweep itself -- predictor, g/b updates, convergence test, step control,
 // refine_bs -- is the reference's (src/integrator_gauss_radau15.c:287-446)
 // component by component, as in the single-system engine.  The fast form
@@ -36,7 +38,7 @@
 
 namespace abie {
 
-static constexpr int ENS_MAX_BODIES = 21;  // 3N <= 64: two components per lane
+static constexpr int ENS_MAX_BODIES = 21;  // 3N <= 64: one component per thread of two warps
 static constexpr int WARPS = 4;            // warps per block
 static constexpr int STATE_PER_COMP = 18;  // y0 dy0 F1 b[7] g[7] b6p
 
@@ -305,14 +307,16 @@ __global__ void __launch_bounds__(32 * WARPS, (EnsOccupancy<W, LEARN>::value)) e
             X.b6p = slot(17);
         }
         const double G = a.G;
+        // G m of every body once per system; alive: this component's body has m >= 0
+        if (gl < n) sp[gl][3] = m[gl] > 0.0 ? G * m[gl] : 0.0;
+        const bool alive = has && m[gl / 3] >= 0.0;
         // publish a predicted position for every body (components of a
         // body may sit on different lanes, so go through shared memory)
         auto publish = [&](double p) {
             if (has) sp[gl / 3][gl % 3] = p;
-            if (gl < n) sp[gl][3] = m[gl] > 0.0 ? G * m[gl] : 0.0;
             grp.sync();
         };
-        auto force_here = [&]() -> double { return (has && m[gl / 3] >= 0.0) ? sa[gl / 3][gl % 3] : 0.0; };
+        auto force_here = [&]() -> double { return alive ? sa[gl / 3][gl % 3] : 0.0; };
 
         if (S.phase == 0) {
             // F1 = f(y0), then initial_time_step (:75-120)
