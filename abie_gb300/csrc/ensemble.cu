@@ -497,7 +497,8 @@ template <int MODE, bool LEARN>
 static const void *ensemble_fn_l(int w)
 {
     return w == 1 ? (const void *)ensemble_kernel<MODE, 1, LEARN>
-                  : (const void *)ensemble_kernel<MODE, 2, LEARN>;
+                  : (w == 2 ? (const void *)ensemble_kernel<MODE, 2, LEARN>
+                            : (const void *)ensemble_kernel<MODE, 4, LEARN>);
 }
 
 // The kernel for a force form, warps per system and whether the learned
@@ -521,7 +522,7 @@ static int launch_ensemble(int mode, int w, int blocks, const EnsArgs &a, cudaSt
     return 0;
 }
 
-static cudaStream_t g_ens_stream2 = nullptr;
+static cudaStream_t g_ens_stream[2] = {nullptr, nullptr};  // besides the caller's stream
 
 int ensemble_run(double *pos, double *vel, const double *m, const long long *offsets, int ns,
                  double G, double t0, double t_end, double *t_out, int *status, long long *steps,
@@ -550,7 +551,7 @@ int ensemble_run(double *pos, double *vel, const double *m, const long long *off
     ABIE_CUDA(cudaMalloc(&d_off, (ns + 1) * sizeof(long long)));
     ABIE_CUDA(cudaMalloc(&d_sc, ns * sizeof(EnsScalars)));
     ABIE_CUDA(cudaMalloc(&d_active, ns * sizeof(int)));
-    ABIE_CUDA(cudaMalloc(&d_queue, 2 * sizeof(int)));
+    ABIE_CUDA(cudaMalloc(&d_queue, 3 * sizeof(int)));
     std::vector<EnsScalars> sc(ns);
     for (int s = 0; s < ns; s++) {
         memset(&sc[s], 0, sizeof(EnsScalars));
@@ -587,16 +588,29 @@ int ensemble_run(double *pos, double *vel, const double *m, const long long *off
     ABIE_CUDA(cudaStreamSynchronize(st));
 
     const bool learning = mlp || (learn_io && learn_io->samples);
-    int bps[2] = {1, 1};
-    for (int k = 0; k < 2; k++) {
-        const void *fn = ensemble_fn(mode, k + 1, learning);
-        const size_t dyn = learning ? learn_smem(k + 1) : 0;
+    // three classes of system: up to 10 bodies on one warp, 11-21 on two,
+    // and the slowest few (longest-first order) on four warps, which cuts
+    // their per-substep latency -- the batch ends with its slowest system
+    const int WC[3] = {1, 2, 4};
+    int bps[3] = {1, 1, 1};
+    for (int k = 0; k < 3; k++) {
+        const void *fn = ensemble_fn(mode, WC[k], learning);
+        const size_t dyn = learning ? learn_smem(WC[k]) : 0;
         if (learning)
             ABIE_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
         ABIE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps[k], fn, 32 * WARPS, dyn));
         bps[k] = std::max(bps[k], 1);
     }
-    if (!g_ens_stream2) ABIE_CUDA(cudaStreamCreateWithFlags(&g_ens_stream2, cudaStreamNonBlocking));
+    std::vector<unsigned char> cls(ns);
+    {
+        const int heavy = std::min(ns, std::max(1, ns / 256));
+        for (int q = 0; q < ns; q++) {
+            const int s2 = active[q];
+            cls[s2] = q < heavy ? 2 : (3 * (offsets[s2 + 1] - offsets[s2]) <= 32 ? 0 : 1);
+        }
+    }
+    for (int k = 0; k < 2; k++)
+        if (!g_ens_stream[k]) ABIE_CUDA(cudaStreamCreateWithFlags(&g_ens_stream[k], cudaStreamNonBlocking));
     cudaEvent_t e0, e1, ej;
     ABIE_CUDA(cudaEventCreate(&e0));
     ABIE_CUDA(cudaEventCreate(&e1));
@@ -606,16 +620,20 @@ int ensemble_run(double *pos, double *vel, const double *m, const long long *off
     int n_active = ns;
     std::vector<int> part(ns);
     while (n_active > 0) {
-        // small systems (3n <= 32) first, then the rest
-        int n_small = 0;
-        for (int q = 0; q < n_active; q++)
-            if (3 * (offsets[active[q] + 1] - offsets[active[q]]) <= 32) part[n_small++] = active[q];
-        int k2 = n_small;
-        for (int q = 0; q < n_active; q++)
-            if (3 * (offsets[active[q] + 1] - offsets[active[q]]) > 32) part[k2++] = active[q];
+        // the classes' lists, each in longest-first order
+        int first[4] = {0, 0, 0, 0};
+        {
+            int k2 = 0;
+            for (int c = 0; c < 3; c++) {
+                first[c] = k2;
+                for (int q = 0; q < n_active; q++)
+                    if (cls[active[q]] == c) part[k2++] = active[q];
+            }
+            first[3] = k2;
+        }
         ABIE_CUDA(cudaMemcpyAsync(d_active, part.data(), n_active * sizeof(int),
                                   cudaMemcpyHostToDevice, st));
-        ABIE_CUDA(cudaMemsetAsync(d_queue, 0, 2 * sizeof(int), st));
+        ABIE_CUDA(cudaMemsetAsync(d_queue, 0, 3 * sizeof(int), st));
         EnsArgs a;
         a.offsets = d_off;
         a.m = d_m;
@@ -634,23 +652,25 @@ int ensemble_run(double *pos, double *vel, const double *m, const long long *off
         a.budget_ns = 2000000000ull;  // each launch yields after about two seconds
         ABIE_CUDA(cudaEventRecord(e0, st));
         ABIE_CUDA(cudaEventRecord(ej, st));
-        ABIE_CUDA(cudaStreamWaitEvent(g_ens_stream2, ej, 0));
-        for (int k = 0; k < 2; k++) {
-            int cnt = k == 0 ? n_small : n_active - n_small;
+        for (int k = 0; k < 2; k++) ABIE_CUDA(cudaStreamWaitEvent(g_ens_stream[k], ej, 0));
+        for (int k = 0; k < 3; k++) {
+            const int cnt = first[k + 1] - first[k];
             if (cnt == 0) continue;
             EnsArgs ak = a;
-            ak.active = d_active + (k == 0 ? 0 : n_small);
+            ak.active = d_active + first[k];
             ak.n_active = cnt;
             ak.queue = d_queue + k;
-            const int per_block = WARPS / (k + 1);  // systems per block
+            const int per_block = WARPS / WC[k];  // systems per block
             int blocks = (int)std::min<long long>((long long)bps[k] * g_sim.num_sms,
                                                   (cnt + per_block - 1) / per_block);
             blocks = std::max(blocks, 1);
-            int lrc = launch_ensemble(mode, k + 1, blocks, ak, k == 0 ? st : g_ens_stream2);
+            int lrc = launch_ensemble(mode, WC[k], blocks, ak, k == 0 ? st : g_ens_stream[k - 1]);
             if (lrc) return lrc;
         }
-        ABIE_CUDA(cudaEventRecord(ej, g_ens_stream2));
-        ABIE_CUDA(cudaStreamWaitEvent(st, ej, 0));
+        for (int k = 0; k < 2; k++) {
+            ABIE_CUDA(cudaEventRecord(ej, g_ens_stream[k]));
+            ABIE_CUDA(cudaStreamWaitEvent(st, ej, 0));
+        }
         ABIE_CUDA(cudaEventRecord(e1, st));
         ABIE_CUDA(cudaEventSynchronize(e1));
         float ms = 0.f;
