@@ -78,6 +78,7 @@ struct EngineArgs {
     double G;
     double *y0, *dy0, *F1, *b, *g, *b6p, *ddy, *dyp;
     double *yp[2], *ypa;
+    float2 *ypf;  // [3n] accepted positions as {float, bound on its error} for the event prefilter
     Src *src[2], *srca;
     double t_end;
     double ce_dist, thr2;
@@ -251,6 +252,14 @@ __device__ __forceinline__ double b6_at(const EngineArgs &a, int i)
     return MODE == ABIE_FORCE_EXACT ? a.b[6 * a.dim + i] : a.g[6 * a.dim + i];
 }
 
+// The accepted coordinate p as the nearest float and an upper bound on the
+// rounding error, for the event scan's single-precision prefilter.
+__device__ __forceinline__ void put_prefilter(const EngineArgs &a, int i, double p)
+{
+    const float f = __double2float_rn(p);
+    a.ypf[i] = make_float2(f, __double2float_ru(fabs(p - (double)f)));
+}
+
 // Predicted component c of body j into yp, and into the source list when j
 // is massive (lane of component 0 also writes G m).
 template <int MODE>
@@ -260,6 +269,7 @@ __device__ __forceinline__ void publish_comp(const EngineArgs &a, int j, int c, 
     const int i = 3 * j + c;
     const double p = pred_pos<MODE>(a, i, row, s, dt, ds, hh);
     yp[i] = p;
+    if (row == 8) put_prefilter(a, i, p);
     const int slot = a.src_slot[j];
     if (slot >= 0) {
         double *rec = reinterpret_cast<double *>(src + slot);
@@ -413,22 +423,41 @@ __device__ __forceinline__ void ring_put(double *buf, unsigned long long count, 
     buf[(4ull * count + 3) % w] = d;
 }
 
-// Pairs j < k closer than the event thresholds (src/common.c:240-282).  A
-// pair passes the prefilter r2 <= thr2 before the reference's exact test.
+// Pairs j < k closer than the event thresholds (src/common.c:116-158).
 // One warp per body j (grid-stride over warps), its lanes over k > j, so a
 // check costs about N / 32 pair tests per warp instead of N per thread
 // (the order of the records does not matter: commit_events sorts them).
+//
+// Single-precision prefilter: with each coordinate held as a float f and a
+// bound e >= |x - f| (put_prefilter), a pair whose floats differ in some
+// coordinate by more than (T + e_j + e_k)(1 + 2^-21) is farther apart than
+// T >= sqrt(thr2) (1 + 2^-20) in exact arithmetic -- the factor covers the
+// float roundings of the test -- so its FP64 r2 exceeds thr2 and the
+// reference's test cannot fire.  Every other pair (NaN or infinite
+// coordinates included: their comparisons are false) takes the FP64 test
+// r2 <= thr2, then the reference's comparisons.  The FP64 pipe sees only
+// pairs within about the threshold of each other.
 __device__ void scan_events(const EngineArgs &a, double t, int tid, int nthreads)
 {
     (void)t;
     EngineCtl *ctl = a.ctl;
     const int lane = tid & 31;
     const int warp = tid >> 5, nwarps = nthreads >> 5;
+    const float T = __double2float_ru(sqrt(a.thr2) * (1.0 + 0x1p-20));
+    const float widen = 1.0f + 0x1p-21f;
     for (int j = warp; j < a.n; j += nwarps) {
-        const double xj = __ldcg(a.ypa + 3 * j), yj = __ldcg(a.ypa + 3 * j + 1),
-                     zj = __ldcg(a.ypa + 3 * j + 2);
+        const float2 fx = __ldcg(a.ypf + 3 * j), fy = __ldcg(a.ypf + 3 * j + 1),
+                     fz = __ldcg(a.ypf + 3 * j + 2);
+        const float tx = T + fx.y, ty = T + fy.y, tz = T + fz.y;
         const double rj = a.r[j];
         for (int k = j + 1 + lane; k < a.n; k += 32) {
+            const float2 gx = __ldcg(a.ypf + 3 * k), gy = __ldcg(a.ypf + 3 * k + 1),
+                         gz = __ldcg(a.ypf + 3 * k + 2);
+            if (fabsf(fx.x - gx.x) > (tx + gx.y) * widen || fabsf(fy.x - gy.x) > (ty + gy.y) * widen ||
+                fabsf(fz.x - gz.x) > (tz + gz.y) * widen)
+                continue;
+            const double xj = __ldcg(a.ypa + 3 * j), yj = __ldcg(a.ypa + 3 * j + 1),
+                         zj = __ldcg(a.ypa + 3 * j + 2);
             double dx = xj - __ldcg(a.ypa + 3 * k);
             double dy = yj - __ldcg(a.ypa + 3 * k + 1);
             double dz = zj - __ldcg(a.ypa + 3 * k + 2);
@@ -1001,6 +1030,7 @@ __global__ void __launch_bounds__(64) radau_split(EngineArgs a)
         unsigned long long kb6 = 0, kdd = 0;
         if (has && writer) {
             a.ypa[gi] = ya;
+            put_prefilter(a, gi, ya);
             if (!isfinite(dd + ya + va)) atomicCAS(&ctl->err, 0, ABIE_ERR_NUMERICS);
             kb6 = absmax_key(e_b6<MODE>(X));
             kdd = absmax_key(dd);
@@ -1096,7 +1126,8 @@ struct EngineBuffers {
 };
 static EngineBuffers g_eb;
 static const int EV_CAP = 4096;
-static const int SLAB_PER_BODY = 3 * (3 + 7 + 7 + 1 + 1 + 1 + 2 + 1);  // y0 dy0 F1 b g b6p ddy dyp yp[2] ypa
+// y0 dy0 F1 b g b6p ddy dyp yp[2] ypa, and ypf (a float2 per component)
+static const int SLAB_PER_BODY = 3 * (3 + 7 + 7 + 1 + 1 + 1 + 2 + 1 + 1);
 
 void free_engine_buffers()
 {
@@ -1291,6 +1322,7 @@ int radau_run(const SystemView &sys, double t, double t_end, int mode, EventStat
     a.yp[0] = p; p += d;
     a.yp[1] = p; p += d;
     a.ypa = p; p += d;
+    a.ypf = reinterpret_cast<float2 *>(p); p += d;
     a.src[0] = e.srcs;
     a.src[1] = e.srcs + n;
     a.srca = e.srcs + 2 * n;

@@ -201,3 +201,62 @@ def test_split_engine_matches_general_engine(clib, oracle):
     assert abs(t1 - t2) <= TIME_TOL_FAST * t2
     p1, v1 = at_time(p1, v1, m, t1, t2, oracle)
     assert rel_err_per_body(p1, p2) <= TOL and rel_err_per_body(v1, v2) <= TOL
+
+
+def _threshold_pairs(ce):
+    """planetary_system(seed=5, 3 planets, 300 test particles) plus four
+    test-particle pairs at 30 au, each pair the same orbit offset out of the
+    plane: two pairs 1e-4 inside the close-encounter distance ce and two
+    1e-4 outside it (over a step the offsets change by ~1e-6)."""
+    p, v, m, r = ics.planetary_system(seed=5, n_planets=3, n_tp=300)
+    extra_p, extra_v = [], []
+    vc = np.sqrt(G * m[0] / 30.0)
+    for q, scale in enumerate((1 - 1e-4, 1 + 1e-4, 1 - 1e-4, 1 + 1e-4)):
+        ang = 0.5 * np.pi * q + 0.3
+        x = np.array([30.0 * np.cos(ang), 30.0 * np.sin(ang), 0.0])
+        u = np.array([-vc * np.sin(ang), vc * np.cos(ang), 0.0])
+        extra_p += [x, x + np.array([0.0, 0.0, ce * scale])]
+        extra_v += [u, u]
+    p = np.concatenate([p, np.concatenate(extra_p)])
+    v = np.concatenate([v, np.concatenate(extra_v)])
+    m = np.concatenate([m, np.zeros(8)])
+    r = np.concatenate([r, np.zeros(8)])
+    return p, v, m, r
+
+
+@pytest.mark.parametrize("engine", ["split", "general"])
+def test_event_prefilter_at_threshold(sim, oracle, engine):
+    """Pairs 1e-4 inside and outside the close-encounter distance, among
+    hundreds of far-apart bodies that the single-precision prefilter skips:
+    the inside pairs are recorded, the outside ones are not, on both
+    engines; the flag, ring buffer and stop time equal the oracle's."""
+    import ctypes as C
+    ce = 0.01
+    p, v, m, r = _threshold_pairs(ce)
+    ref = oracle.radau15(p, v, m, r, G, 0.0, 10.0, ce_dist=ce, max_ce=3, max_coll=2)
+    assert ref["flag"] == 1 and ref["n_ce"] == 4  # two pairs in each of two steps
+    n0 = m.size - 8
+    gold = ref["buf_ce"].reshape(-1, 4)
+    assert sorted(set(map(int, gold[:, 1]))) == [n0, n0 + 4]
+    old = sim.set_force_mode("exact")
+    sim.set_close_encounter_distance(ce)
+    sim.reset_close_encounter_buffer()
+    sim.reset_collision_buffer()
+    if engine == "general":
+        sim.lib.abie_debug_engine_shape(C.c_int(16), C.c_int(128))
+    try:
+        sim.set_state(p, v, m, r, m.size, G, 0.0)
+        with pytest.raises(CloseEncounterException):
+            sim.integrator_gr(0.0, 10.0, 1.0)
+        buf = sim.get_close_encounter_data()
+        t = sim.get_model_time()
+    finally:
+        sim.lib.abie_debug_engine_shape(C.c_int(0), C.c_int(0))
+        sim.set_force_mode(old)
+        sim.set_close_encounter_distance(0.0)
+        sim.reset_close_encounter_buffer()
+        sim.reset_collision_buffer()
+    assert np.array_equal(buf[:, 1:3], gold[:, 1:3])
+    assert np.allclose(buf[:, 0], gold[:, 0], rtol=TIME_TOL, atol=0)
+    assert np.allclose(buf[:, 3], gold[:, 3], rtol=1e-12, atol=0)
+    assert abs(t - ref["t"]) <= TIME_TOL * ref["t"]
