@@ -72,12 +72,13 @@ struct EngineArgs {
     const int *src_slot;  // [n] slot in the source list or -1
     const int *tp_body;   // [n_tp] bodies without positive mass, ascending (split engine)
     int n_tp;
-    double C;             // speed of light: post-Newtonian terms when > 0 (split engine)
+    double C;             // speed of light: post-Newtonian terms when > 0
     PnConst pn;
     const double *m, *r, *ext;
     double G;
     double *y0, *dy0, *F1, *b, *g, *b6p, *ddy, *dyp;
     double *yp[2], *ypa;
+    double *vp[2];  // predicted velocities of the published substeps (post-Newtonian terms only)
     float2 *ypf;  // [3n] accepted positions as {float, bound on its error} for the event prefilter
     Src *src[2], *srca;
     double t_end;
@@ -183,6 +184,64 @@ __device__ __forceinline__ void sink_accel(const EngineArgs &a, int j, const Src
     }
 }
 
+// Post-Newtonian sum of the massive sources on sink j (src/additional_forces.c:14-121):
+// source positions from the list src, velocities from vel (3n, the same
+// evaluation's), masses from m.  The exact form sums in source order on lane
+// 0, as the reference's loop over k; the fast form spreads the sources over
+// the JS lanes.
+template <int MODE, int JS>
+__device__ __noinline__ void sink_pn(const EngineArgs &a, int j, const Src *src, const double *vel,
+                                     double xj, double yj, double zj, int lane, double &ax,
+                                     double &ay, double &az)
+{
+    ax = 0.0;
+    ay = 0.0;
+    az = 0.0;
+    const double vxj = vel[3 * j], vyj = vel[3 * j + 1], vzj = vel[3 * j + 2], mj = a.m[j];
+    const int q0 = MODE == ABIE_FORCE_EXACT ? 0 : lane;
+    const int qs = MODE == ABIE_FORCE_EXACT ? 1 : JS;
+    if (MODE != ABIE_FORCE_EXACT || lane == 0) {
+        for (int q = q0; q < a.n_src; q += qs) {
+            const int k = a.src_body[q];
+            if (k == j) continue;
+            const Src sk = load_src(src + q);
+            pn_pair(a.pn, xj, yj, zj, vxj, vyj, vzj, mj, sk.x, sk.y, sk.z, vel[3 * k],
+                    vel[3 * k + 1], vel[3 * k + 2], a.m[k], ax, ay, az);
+        }
+    }
+    if (JS > 1) {
+        if (MODE == ABIE_FORCE_EXACT) {
+            ax = __shfl_sync(0xffffffffu, ax, 0, JS);
+            ay = __shfl_sync(0xffffffffu, ay, 0, JS);
+            az = __shfl_sync(0xffffffffu, az, 0, JS);
+        } else {
+#pragma unroll
+            for (int o = JS / 2; o > 0; o >>= 1) {
+                ax += __shfl_xor_sync(0xffffffffu, ax, o, JS);
+                ay += __shfl_xor_sync(0xffffffffu, ay, o, JS);
+                az += __shfl_xor_sync(0xffffffffu, az, o, JS);
+            }
+        }
+    }
+}
+
+// Newton, plus the post-Newtonian sum when C > 0 (velocities vel), as
+// src/common.c:82-114 adds them; the caller adds the external acceleration.
+template <int MODE, int JS, bool PN>
+__device__ __forceinline__ void sink_force(const EngineArgs &a, int j, const Src *src,
+                                           const double *vel, double xj, double yj, double zj,
+                                           int lane, double f[3])
+{
+    sink_accel<MODE, JS>(a, j, src, xj, yj, zj, lane, f[0], f[1], f[2]);
+    if (PN) {
+        double px, py, pz;
+        sink_pn<MODE, JS>(a, j, src, vel, xj, yj, zj, lane, px, py, pz);
+        f[0] += px;
+        f[1] += py;
+        f[2] += pz;
+    }
+}
+
 // f[c] without a dynamically indexed local array.
 __device__ __forceinline__ double pick3(const double f[3], int c)
 {
@@ -245,6 +304,29 @@ __device__ __forceinline__ double pred_vel(const EngineArgs &a, int i, double dt
     return fma(dt, a.F1[i] + u, a.dy0[i]);
 }
 
+// Predicted velocity at spacing s = c_hs[row] (src/integrator_gauss_radau15.c:63-68),
+// needed only by the post-Newtonian terms.  Fast form: from g with the
+// tabulated weights of that spacing.
+template <int MODE>
+__device__ __forceinline__ double pred_vel_at(const EngineArgs &a, int i, int row, double s, double dt)
+{
+    const int d = a.dim;
+    if (MODE == ABIE_FORCE_EXACT) {
+        const double *b = a.b;
+        return a.dy0[i] + dt * s * (a.F1[i] + s * (b[i] / 0.2e1 + s * (b[d + i] / 0.3e1 + s * (b[2 * d + i] / 0.4e1 + s * (b[3 * d + i] / 0.5e1 + s * (b[4 * d + i] / 0.6e1 + s * (b[5 * d + i] / 0.7e1 + s * b[6 * d + i] / 0.8e1)))))));
+    }
+    const double *g = a.g;
+    const double *w = e_vgs[row];
+    double u = g[6 * d + i] * w[6];
+    u = fma(g[5 * d + i], w[5], u);
+    u = fma(g[4 * d + i], w[4], u);
+    u = fma(g[3 * d + i], w[3], u);
+    u = fma(g[2 * d + i], w[2], u);
+    u = fma(g[d + i], w[1], u);
+    u = fma(g[i], w[0], u);
+    return fma(dt * s, a.F1[i] + u, a.dy0[i]);
+}
+
 // The corrector's b6 (b_6 = cs[6][6] g_6 = g_6: read from g in the fast form).
 template <int MODE>
 __device__ __forceinline__ double b6_at(const EngineArgs &a, int i)
@@ -264,11 +346,13 @@ __device__ __forceinline__ void put_prefilter(const EngineArgs &a, int i, double
 // is massive (lane of component 0 also writes G m).
 template <int MODE>
 __device__ __forceinline__ void publish_comp(const EngineArgs &a, int j, int c, int row, double s,
-                                             double dt, double ds, double hh, double *yp, Src *src)
+                                             double dt, double ds, double hh, double *yp, Src *src,
+                                             double *vp = nullptr)
 {
     const int i = 3 * j + c;
     const double p = pred_pos<MODE>(a, i, row, s, dt, ds, hh);
     yp[i] = p;
+    if (vp) vp[i] = pred_vel_at<MODE>(a, i, row, s, dt);
     if (row == 8) put_prefilter(a, i, p);
     const int slot = a.src_slot[j];
     if (slot >= 0) {
@@ -517,7 +601,7 @@ __device__ void commit_events(const EngineArgs &a, double t)
     __threadfence();
 }
 
-template <int MODE, int JS>
+template <int MODE, int JS, bool PN>
 __global__ void __launch_bounds__(256) radau_engine(EngineArgs a)
 {
     EngineCtl *ctl = a.ctl;
@@ -549,8 +633,8 @@ __global__ void __launch_bounds__(256) radau_engine(EngineArgs a)
             const bool live = jj < n;
             const int j = live ? jj : n - 1;
             double f[3];
-            sink_accel<MODE, JS>(a, j, a.src[0], a.y0[3 * j], a.y0[3 * j + 1], a.y0[3 * j + 2],
-                                 lane, f[0], f[1], f[2]);
+            sink_force<MODE, JS, PN>(a, j, a.src[0], a.dy0, a.y0[3 * j], a.y0[3 * j + 1],
+                                 a.y0[3 * j + 2], lane, f);
             if (!live) continue;
             const bool alive = a.m[j] >= 0.0;
             for (int c = c0; c < c1; c++)
@@ -572,12 +656,14 @@ __global__ void __launch_bounds__(256) radau_engine(EngineArgs a)
         double d0, d1;
         read2(ctl, red_idx++, d0, d1);
         double dt0 = (d0 < 1e-5 || d1 < 1e-5) ? 1e-6 : 0.01 * (d0 / d1);
-        // Euler probe y1 = y0 + dt0 dy0 into yp[1] / src[1]
+        // Euler probe y1 = y0 + dt0 dy0 into yp[1] / src[1] (and, for the
+        // post-Newtonian terms, dy1 = dy0 + dt0 f0 into vp[1])
         for (int j = gid; j < n; j += ngroups) {
             const int slot = a.src_slot[j];
             for (int c = c0; c < c1; c++) {
                 const double p = a.y0[3 * j + c] + dt0 * a.dy0[3 * j + c];
                 a.yp[1][3 * j + c] = p;
+                if (PN) a.vp[1][3 * j + c] = a.dy0[3 * j + c] + dt0 * __ldcg(a.F1 + 3 * j + c);
                 if (slot >= 0) {
                     double *rec = reinterpret_cast<double *>(a.src[1] + slot);
                     rec[c] = p;
@@ -591,8 +677,8 @@ __global__ void __launch_bounds__(256) radau_engine(EngineArgs a)
             const bool live = jj < n;
             const int j = live ? jj : n - 1;
             double f[3];
-            sink_accel<MODE, JS>(a, j, a.src[1], a.yp[1][3 * j], a.yp[1][3 * j + 1],
-                                 a.yp[1][3 * j + 2], lane, f[0], f[1], f[2]);
+            sink_force<MODE, JS, PN>(a, j, a.src[1], a.vp[1], a.yp[1][3 * j], a.yp[1][3 * j + 1],
+                                 a.yp[1][3 * j + 2], lane, f);
             if (!live) continue;
             const bool alive = a.m[j] >= 0.0;
             for (int c = c0; c < c1; c++) {
@@ -619,7 +705,8 @@ __global__ void __launch_bounds__(256) radau_engine(EngineArgs a)
             const double ds = h * c_hs[1], hh = 0.5 * ds * ds;
             for (int j = gid; j < n; j += ngroups)
                 for (int c = c0; c < c1; c++)
-                    publish_comp<MODE>(a, j, c, 1, c_hs[1], h, ds, hh, a.yp[pc & 1], a.src[pc & 1]);
+                    publish_comp<MODE>(a, j, c, 1, c_hs[1], h, ds, hh, a.yp[pc & 1], a.src[pc & 1],
+                                       PN ? a.vp[pc & 1] : nullptr);
         }
         if (!grid_sync(ctl, T)) return;
     } else {
@@ -649,8 +736,8 @@ __global__ void __launch_bounds__(256) radau_engine(EngineArgs a)
                     const bool live = jj < n;
                     const int j = live ? jj : n - 1;
                     double f[3];
-                    sink_accel<MODE, JS>(a, j, src, yp[3 * j], yp[3 * j + 1], yp[3 * j + 2], lane,
-                                         f[0], f[1], f[2]);
+                    sink_force<MODE, JS, PN>(a, j, src, a.vp[pc & 1], yp[3 * j], yp[3 * j + 1],
+                                         yp[3 * j + 2], lane, f);
                     if (!live) continue;
                     const bool alive = a.m[j] >= 0.0;
                     for (int c = c0; c < c1; c++) {
@@ -664,7 +751,8 @@ __global__ void __launch_bounds__(256) radau_engine(EngineArgs a)
                             kf8 = w > kf8 ? w : kf8;
                         }
                         publish_comp<MODE>(a, j, c, nrow, ns, h, nds, nhh, a.yp[(pc + 1) & 1],
-                                           a.src[(pc + 1) & 1]);
+                                           a.src[(pc + 1) & 1],
+                                           PN ? a.vp[(pc + 1) & 1] : nullptr);
                         if (ih == 7) {
                             // speculative advance (spacing 1)
                             publish_comp<MODE>(a, j, c, 8, 1.0, h, h, hh1, a.ypa, a.srca);
@@ -689,8 +777,8 @@ __global__ void __launch_bounds__(256) radau_engine(EngineArgs a)
             const bool live = jj < n;
             const int j = live ? jj : n - 1;
             double f[3];
-            sink_accel<MODE, JS>(a, j, a.srca, a.ypa[3 * j], a.ypa[3 * j + 1], a.ypa[3 * j + 2],
-                                 lane, f[0], f[1], f[2]);
+            sink_force<MODE, JS, PN>(a, j, a.srca, a.dyp, a.ypa[3 * j], a.ypa[3 * j + 1],
+                                 a.ypa[3 * j + 2], lane, f);
             if (!live) continue;
             const bool alive = a.m[j] >= 0.0;
             for (int c = c0; c < c1; c++) {
@@ -756,7 +844,8 @@ __global__ void __launch_bounds__(256) radau_engine(EngineArgs a)
             const double ds = h * c_hs[1], hh = 0.5 * ds * ds;
             for (int j = gid; j < n; j += ngroups)
                 for (int c = c0; c < c1; c++)
-                    publish_comp<MODE>(a, j, c, 1, c_hs[1], h, ds, hh, a.yp[pc & 1], a.src[pc & 1]);
+                    publish_comp<MODE>(a, j, c, 1, c_hs[1], h, ds, hh, a.yp[pc & 1], a.src[pc & 1],
+                                       PN ? a.vp[pc & 1] : nullptr);
         }
         if (!grid_sync(ctl, T)) return;
         if (accepted && *(volatile int *)&ctl->n_ev > 0) {
@@ -1126,8 +1215,8 @@ struct EngineBuffers {
 };
 static EngineBuffers g_eb;
 static const int EV_CAP = 4096;
-// y0 dy0 F1 b g b6p ddy dyp yp[2] ypa, and ypf (a float2 per component)
-static const int SLAB_PER_BODY = 3 * (3 + 7 + 7 + 1 + 1 + 1 + 2 + 1 + 1);
+// y0 dy0 F1 b g b6p ddy dyp yp[2] ypa vp[2], and ypf (a float2 per component)
+static const int SLAB_PER_BODY = 3 * (3 + 7 + 7 + 1 + 1 + 1 + 2 + 1 + 2 + 1);
 
 void free_engine_buffers()
 {
@@ -1177,11 +1266,11 @@ static int engine_reserve(size_t n, size_t max_ce, size_t max_coll)
     return 0;
 }
 
-template <int MODE, int JS>
+template <int MODE, int JS, bool PN = false>
 static int launch_engine(const EngineArgs &a, int num_sms, int block, cudaStream_t st, int *grid_out)
 {
     int bps = 0;
-    ABIE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, radau_engine<MODE, JS>, block, 0));
+    ABIE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, radau_engine<MODE, JS, PN>, block, 0));
     if (bps < 1) {
         set_error(ABIE_ERR_CUDA, "radau engine does not fit on an SM");
         return ABIE_ERR_CUDA;
@@ -1191,7 +1280,7 @@ static int launch_engine(const EngineArgs &a, int num_sms, int block, cudaStream
     long long grid = std::min<long long>((long long)bps * num_sms, std::max<long long>(want, 1));
     EngineArgs args = a;
     void *params[] = {&args};
-    ABIE_CUDA(cudaLaunchCooperativeKernel((const void *)radau_engine<MODE, JS>, dim3((unsigned)grid),
+    ABIE_CUDA(cudaLaunchCooperativeKernel((const void *)radau_engine<MODE, JS, PN>, dim3((unsigned)grid),
                                           dim3(block), params, 0, st));
     *grid_out = (int)grid;
     return 0;
@@ -1200,6 +1289,13 @@ static int launch_engine(const EngineArgs &a, int num_sms, int block, cudaStream
 static int dispatch_engine(int mode, int js, int block, const EngineArgs &a, int num_sms,
                            cudaStream_t st, int *grid)
 {
+    if (a.C > 0.0) {  // post-Newtonian variants: one or four lanes per body
+        if (mode == ABIE_FORCE_EXACT)
+            return js >= 4 ? launch_engine<ABIE_FORCE_EXACT, 4, true>(a, num_sms, block, st, grid)
+                           : launch_engine<ABIE_FORCE_EXACT, 1, true>(a, num_sms, block, st, grid);
+        return js >= 4 ? launch_engine<ABIE_FORCE_FP64, 4, true>(a, num_sms, block, st, grid)
+                       : launch_engine<ABIE_FORCE_FP64, 1, true>(a, num_sms, block, st, grid);
+    }
     if (mode == ABIE_FORCE_EXACT) {
         if (js == 4) return launch_engine<ABIE_FORCE_EXACT, 4>(a, num_sms, block, st, grid);
         return launch_engine<ABIE_FORCE_EXACT, 1>(a, num_sms, block, st, grid);
@@ -1322,6 +1418,8 @@ int radau_run(const SystemView &sys, double t, double t_end, int mode, EventStat
     a.yp[0] = p; p += d;
     a.yp[1] = p; p += d;
     a.ypa = p; p += d;
+    a.vp[0] = p; p += d;
+    a.vp[1] = p; p += d;
     a.ypf = reinterpret_cast<float2 *>(p); p += d;
     a.src[0] = e.srcs;
     a.src[1] = e.srcs + n;
@@ -1340,7 +1438,8 @@ int radau_run(const SystemView &sys, double t, double t_end, int mode, EventStat
     a.ev = e.ev;
     a.ev_cap = EV_CAP;
     a.ctl = e.ctl;
-    a.timeout_ns = 2000000000ll + 12ll * (long long)n * (long long)std::max(n_src, 1);
+    // a phase's work bounds its barrier wait (post-Newtonian pairs cost ~20x more)
+    a.timeout_ns = 2000000000ll + (a.C > 0.0 ? 240ll : 12ll) * (long long)n * (long long)std::max(n_src, 1);
 
     ABIE_CUDA(cudaMemcpyAsync(a.y0, sys.pos, d * sizeof(double), cudaMemcpyDeviceToDevice, st));
     ABIE_CUDA(cudaMemcpyAsync(a.dy0, sys.vel, d * sizeof(double), cudaMemcpyDeviceToDevice, st));
@@ -1369,13 +1468,6 @@ int radau_run(const SystemView &sys, double t, double t_end, int mode, EventStat
         ABIE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, split_fn(mode, a.C > 0.0), 64, 0));
         split = (long long)std::max(1, (n_tp + SPLIT_TPW - 1) / SPLIT_TPW) <=
                 (long long)bps * g_sim.num_sms;
-    }
-    if (a.C > 0.0 && !split) {
-        set_error(ABIE_ERR_UNSUPPORTED,
-                  "post-Newtonian terms (C > 0) run on the split Radau15 engine only: at most 10 "
-                  "massive bodies (this system has %d) and one resident wave of test particles",
-                  n_src);
-        return ABIE_ERR_UNSUPPORTED;
     }
     EngineCtl c;
     long long budget = 4;

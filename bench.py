@@ -441,6 +441,9 @@ def run_radau_single(lib, args):
     out = {"bodies": int(m.size), "years": args.gr_years}
     for mode in ("fp64", "exact"):
         old = lib.set_force_mode(mode)
+        # warm-up: loads the engine kernels and sizes the buffers
+        lib.set_state(p, v, m, r, m.size, G, 0.0)
+        lib.integrator_gr(0.0, 0.01, 1.0)
         lib.set_state(p, v, m, r, m.size, G, 0.0)
         lib.reset_counters()
         t0 = _t.perf_counter()

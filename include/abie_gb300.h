@@ -74,8 +74,7 @@ size_t set_additional_forces(size_t N, double *ext_acc);
  * Gauss-Radau 15 from t to the first accepted time past t_end, on the
  * device-resident state; dt is ignored as in the reference.  With a stored
  * C > 0 the accelerations include the post-Newtonian terms
- * (src/additional_forces.c), for systems of at most 10 massive bodies;
- * more massive bodies with C > 0 return ABIE_ERR_UNSUPPORTED. */
+ * (src/additional_forces.c) of the massive bodies. */
 int integrator_gr(double t, double t_end, double dt);
 /* src/common.c:534-537 -> src/integrator_wisdom_holman.c:513-537.
  * Fixed-step Wisdom-Holman on a heliocentric state. */

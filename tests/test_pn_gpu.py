@@ -4,13 +4,12 @@ calculate_accelerations adds them when the stored speed of light C is
 positive (src/common.c:101-107), and Radau15 then integrates with them:
 bit-identical accelerations in the exact form, trajectories at a common
 time to 1e-10, against the reference's golden vectors and the oracle.
-The split engine carries them (at most 10 massive bodies); a system with
-more massive bodies and C > 0 is refused with an error."""
+Both Radau15 engines carry them: the split engine (at most 10 massive
+bodies) and the general one."""
 import numpy as np
 import pytest
 
 from abie_gb300 import ics
-from abie_gb300.events import AbieError
 from conftest import rel_err_per_body
 from test_radau_gpu import TIME_TOL, TIME_TOL_FAST, TOL, at_time
 
@@ -88,11 +87,28 @@ def test_pn_radau_with_test_particle_vs_oracle(sim, oracle):
     assert rel_err_per_body(pos, ref["pos"]) <= TOL and rel_err_per_body(vel, ref["vel"]) <= TOL
 
 
-def test_pn_needs_split_engine(sim):
-    p, v, m, r = ics.planetary_system(seed=86, n_planets=12, n_tp=0)
-    sim.set_state(p, v, m, r, m.size, G, 63239.7263)
+@pytest.mark.parametrize("mode,tol_t", [("exact", TIME_TOL), ("fp64", TIME_TOL_FAST)])
+def test_pn_general_engine_vs_oracle(sim, oracle, mode, tol_t):
+    """Twelve planets (13 massive bodies: beyond the split engine) and
+    one test particle (the reference turns a second massless body into
+    0/0), post-Newtonian terms on the general engine."""
+    p, v, m, r = ics.planetary_system(seed=86, n_planets=12, n_tp=1)
+    Cl = 63239.7263
+    ref = oracle.radau15(p, v, m, r, G, 0.0, 0.3, C=Cl)
+    newton = oracle.radau15(p, v, m, r, G, 0.0, 0.3)
+    old = sim.set_force_mode(mode)
     try:
-        with pytest.raises(AbieError):
-            sim.integrator_gr(0.0, 0.1, 1.0)
+        sim.set_state(p, v, m, r, m.size, G, Cl)
+        sim.integrator_gr(0.0, 0.3, 1.0)
+        pos, vel = np.zeros(p.size), np.zeros(p.size)
+        sim.get_state(pos, vel, np.zeros(m.size), np.zeros(m.size))
+        t = sim.get_model_time()
     finally:
+        sim.set_force_mode(old)
         sim.set_state(p, v, m, r, m.size, G, 0.0)
+    assert abs(t - ref["t"]) <= tol_t * ref["t"]
+    pos, vel = at_time(pos, vel, m, t, ref["t"], oracle)
+    assert rel_err_per_body(pos, ref["pos"]) <= TOL and rel_err_per_body(vel, ref["vel"]) <= TOL
+    # the terms matter at this tolerance (about 3e-7 here)
+    npos, nvel = at_time(newton["pos"], newton["vel"], m, newton["t"], ref["t"], oracle)
+    assert rel_err_per_body(nvel, ref["vel"]) > 100 * TOL
