@@ -47,6 +47,7 @@ class CLibABIE(object):
         self.lib = load(path)
         self.max_close_encounter_events = 1
         self.max_collision_events = 1
+        self.N = 0  # bodies of the last set_state
 
     # -- helpers ------------------------------------------------------------
     def _check(self, rc, what):
@@ -70,6 +71,7 @@ class CLibABIE(object):
 
     def set_state(self, pos, vel, masses, radii, N, G, C):
         pos, vel, masses, radii = _f64(pos), _f64(vel), _f64(masses), _f64(radii)
+        self.N = int(N)
         self.lib.set_state(_vp(pos), _vp(vel), _vp(masses), _vp(radii), _c.c_int(N),
                            _c.c_double(G), _c.c_double(C))
 
@@ -201,6 +203,34 @@ class CLibABIE(object):
         self._check(rc, "abie_gr_ensemble")
         return {"pos": pos, "vel": vel, "t": t_out, "status": status, "steps": steps,
                 "seconds": self.lib.abie_last_ensemble_seconds()}
+
+    def integrate_snapshots(self, t, t_end, store_dt, integrator="gr", h=0.0, primary="#COM#",
+                            max_snaps=None):
+        """Integrate the stored state from t to t_end, keeping a snapshot after
+        every chunk of store_dt on the GPU (abie/integrator.py:158-204 with
+        store_state): times, positions, velocities, a/e/i about the primary
+        ("#COM#", "#M_MAX#", "#M_MIN#" or a body index) and energies.
+        Returns a dict of arrays and the return code ("flag": 0, or the event
+        flag 1 / 2 at which the run stopped)."""
+        modes = {"#COM#": -1, "#M_MAX#": -2, "#M_MIN#": -3}
+        prim = modes[primary] if isinstance(primary, str) else int(primary)
+        n = self.N
+        if max_snaps is None:
+            max_snaps = int(np.ceil((t_end - t) / min(store_dt, max(t_end - t, 1e-300)))) + 2
+        max_snaps = max(int(max_snaps), 0)
+        st = np.zeros(max_snaps)
+        sp, sv, sa = (np.zeros((max_snaps, 3 * n)) for _ in range(3))
+        se = np.zeros(max_snaps)
+        k = _c.c_int(0)
+        rc = self.lib.abie_integrate_snapshots(
+            _c.c_int({"gr": 0, "wh": 1}[integrator]), _c.c_double(t), _c.c_double(t_end),
+            _c.c_double(store_dt), _c.c_double(h), _c.c_int(prim), _c.c_int(max_snaps),
+            _vp(st), _vp(sp), _vp(sv), _vp(sa), _vp(se), _c.byref(k))
+        if rc < 0:
+            self._check(rc, "abie_integrate_snapshots")
+        k = k.value
+        return {"t": st[:k], "pos": sp[:k], "vel": sv[:k], "aei": sa[:k].reshape(k, n, 3),
+                "energy": se[:k], "flag": rc}
 
     def measure_fp64_issue(self, active_lanes):
         """FP64 FMA rate counted over whole warps with only active_lanes lanes working."""

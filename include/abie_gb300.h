@@ -164,6 +164,27 @@ int abie_gr_ensemble(double *pos, double *vel, const double *m,
 /* Seconds of GPU time spent in the last abie_gr_ensemble call. */
 double abie_last_ensemble_seconds(void);
 
+/* Device snapshots, replacing abie/integrator.py:158-204 with store_state
+ * (:233-252) and Particles.calculate_aei (abie/particles.py:352-376): the
+ * stored state is integrated from t to t_end in chunks of store_dt, with
+ * integrate()'s schedule (next_t = t + dt - ((t + dt) % dt), dt =
+ * min(store_dt, t_end - t)), by integrator_gr (integrator 0) or
+ * integrator_wh with step h (integrator 1).  After each chunk the GPU keeps
+ * the model time, positions, velocities, a/e/i of every body about the
+ * primary (ABIE_PRIMARY_* or a body index; NaN for the primary itself) and
+ * the energy; they reach the caller's arrays (max_snaps rows of 1, 3N, 3N,
+ * 3N and 1 doubles, any may be NULL) once, at the end.  *n_snaps = rows
+ * written.  Returns 0; an event flag 1 / 2 after storing the snapshot at the
+ * event (the run stops there so that the caller can handle it); a negative
+ * error, ABIE_ERR_CAPACITY when more than max_snaps chunks are needed. */
+#define ABIE_PRIMARY_COM (-1)    /* "#COM#": centre of mass, total mass */
+#define ABIE_PRIMARY_M_MAX (-2)  /* "#M_MAX#": the most massive body */
+#define ABIE_PRIMARY_M_MIN (-3)  /* "#M_MIN#": the least massive body */
+int abie_integrate_snapshots(int integrator, double t, double t_end, double store_dt, double h,
+                             int primary, int max_snaps, double *snap_t, double *snap_pos,
+                             double *snap_vel, double *snap_aei, double *snap_energy,
+                             int *n_snaps);
+
 /* Learned Radau15 predictor (BF16 MLP 30 -> 128 -> 128 -> 21; see
  * abie_gb300/csrc/mlp.cuh for features and targets).  abie_gr_ensemble
  * flags: bit 0 starts every step from the network's guess, with the g

@@ -10,7 +10,9 @@ integrator_wh, integrator_rk,
 the event buffers) driven through ctypes by ``oracle.Reference``.  The
 inputs are the package's seeded generators.  The resulting ``golden.npz``
 is small, committed, and travels with the tests; nothing at test time reads
-the reference sources.
+the reference sources.  ``golden_aei.npz`` (``make_golden.py aei``) holds
+orbital elements from the reference's own Python (abie/particles.py,
+abie/tools.py), imported from its source tree.
 """
 import os
 import sys
@@ -116,5 +118,43 @@ def main(out=os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden.np
     print("wrote", out, os.path.getsize(out), "bytes,", len(gold), "arrays")
 
 
+def _reference_python(ref_root="/root/reference"):
+    """The reference's abie.particles and abie.tools, imported from its
+    source tree without running abie/__init__.py (which needs h5py/toml)."""
+    import types
+    if "abie" not in sys.modules:
+        pkg = types.ModuleType("abie")
+        pkg.__path__ = [os.path.join(ref_root, "abie")]
+        sys.modules["abie"] = pkg
+    import abie.particles  # noqa: E402
+    return abie.particles.Particles
+
+
+def main_aei(out=os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden_aei.npz")):
+    """a, e, i of every body about the primary, from the reference's own
+    Particles.calculate_aei (abie/particles.py:352-376), for the global
+    primary modes the device snapshots support.  The reference's "#M_MAX#"
+    and "#M_MIN#" modes fail there (np.argmax's integer is not an ``int`` to
+    Particles.__getitem__, which returns None), so the most massive body is
+    pinned through its index, the mode's evident meaning."""
+    Particles = _reference_python()
+    gold = {}
+    p, v, m, r = ics.planetary_system(seed=91, n_planets=8, n_tp=40)
+    gold["aei_pos"], gold["aei_vel"], gold["aei_m"] = p, v, m
+    for key, prim in (("com", "#COM#"), ("mmax", int(np.argmax(m))), ("body3", 3)):
+        P = Particles(G)
+        for k in range(m.size):
+            P.add(pos=p[3 * k:3 * k + 3].copy(), vel=v[3 * k:3 * k + 3].copy(), mass=float(m[k]))
+        P.primary = prim
+        with np.errstate(divide="ignore", invalid="ignore"):
+            gold["aei_" + key] = np.asarray(P.calculate_aei())
+    np.savez_compressed(out, **gold)
+    print("wrote", out, os.path.getsize(out), "bytes,", len(gold), "arrays")
+
+
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["aei"]:
+        main_aei()
+    else:
+        main()
+        main_aei()
