@@ -31,6 +31,7 @@ struct WhShared {
     double Rp[3], Vp[3];  // Jacobi -> helio shift after the drift
     double ind[3];        // indirect term
     double a2[3];         // accel2 carried past the head
+    double ind_a2[3];     // ind + a2 (the fast form adds them once)
     double gm_tail;       // Kepler parameter of a massless body
     double gm_tail_k[3];  // sqrt(gm_tail), 1/gm_tail, 1/sqrt(gm_tail)
     unsigned long long kepler_failures;
@@ -39,6 +40,7 @@ struct WhShared {
 struct WhArgs {
     int n, head;        // bodies, head size (head_end + 1)
     double G, dt;
+    double dt2_6;       // dt * dt / 6 (the fast Kepler start)
     double *pos, *vel, *acc;  // heliocentric state and last acceleration (3n)
     const double *m;
     double *jpos, *jvel;      // head Jacobi state (3 * head)
@@ -168,20 +170,38 @@ __device__ __forceinline__ void stumpff_series(double psi, double &c2, double &c
     c3 = fma(b, x, 1.0 / 6.0);               // 1/3!
 }
 
+// The same series to five terms each, for |psi| <= 0.01: the first omitted
+// terms, psi^5 / 12! and psi^5 / 13!, are below 3e-19 of c2 and c3.
+__device__ __forceinline__ void stumpff_series_short(double psi, double &c2, double &c3)
+{
+    const double x = -psi;
+    double a = 1.0 / 3628800.0;        // 1/10!
+    a = fma(a, x, 1.0 / 40320.0);      // 1/8!
+    a = fma(a, x, 1.0 / 720.0);        // 1/6!
+    a = fma(a, x, 1.0 / 24.0);         // 1/4!
+    c2 = fma(a, x, 0.5);               // 1/2!
+    double b = 1.0 / 39916800.0;       // 1/11!
+    b = fma(b, x, 1.0 / 362880.0);     // 1/9!
+    b = fma(b, x, 1.0 / 5040.0);       // 1/7!
+    b = fma(b, x, 1.0 / 120.0);        // 1/5!
+    c3 = fma(b, x, 1.0 / 6.0);         // 1/3!
+}
+
 // Fast form of kepler_drift: the same universal-variable Newton iteration,
 // convergence test (|dchi| < 1e-12) and f, g functions, with
 //  * a starting value from the Taylor series of chi(t) (dchi/dt = sqrt(gm)/r)
 //    to third order when the step covers a small arc (psi_0 < 0.1), so one
 //    or two Newton steps suffice instead of three or four;
 //  * the series Stumpff functions for |psi| <= 0.5 where the reference uses
-//    the closed forms (its constants 1/2, 1/6 in -1e-6 <= psi <= 1e-10 and
-//    the closed forms beyond |psi| = 0.5 are kept);
+//    the closed forms (five terms each up to |psi| = 0.01, nine beyond; its
+//    constants 1/2, 1/6 in -1e-6 <= psi <= 1e-10 and the closed forms
+//    beyond |psi| = 0.5 are kept);
 //  * 1/r and 1/sqrt from rcp_fast / inv_sqrt_fast instead of divisions and
 //    sqrt, and sqrt(gm), 1/gm, 1/sqrt(gm) precomputed (k[0..2]).
 // The converged chi is the same root; the state agrees with the reference
 // form to rounding.  Distances must lie within the FP32 exponent range.
 __device__ int kepler_drift_fast(double r0v[3], double v0v[3], double gm, const double k[3],
-                                 double dt)
+                                 double dt, double dt2_6)
 {
     const double sqrtgm = k[0], igm = k[1], isqrtgm = k[2];
     const double r02 = fma(r0v[2], r0v[2], fma(r0v[1], r0v[1], r0v[0] * r0v[0]));
@@ -198,7 +218,7 @@ __device__ int kepler_drift_fast(double r0v[3], double v0v[3], double gm, const 
         const double u = rv * ir02;                       // rdot / r
         const double w2 = -0.5 * u * dt;                  // second-order factor
         const double w3 = (v02 - gm * ir0) * ir02 - 3.0 * u * u;
-        chi0 = w1 * fma(dt * dt / 6.0, -w3, 1.0 + w2);
+        chi0 = w1 * fma(dt2_6, -w3, 1.0 + w2);
     } else if (alpha > TOL_ENERGY) {
         chi0 = sqrtgm * dt * alpha;
     } else if (alpha < TOL_ENERGY) {
@@ -222,7 +242,8 @@ __device__ int kepler_drift_fast(double r0v[3], double v0v[3], double gm, const 
         const double chi2 = chi0 * chi0;
         psi = chi2 * alpha;
         if (psi > 1.e-10 || psi < -1.e-6) {
-            if (fabs(psi) <= 0.5) stumpff_series(psi, c2, c3);
+            if (fabs(psi) <= 0.01) stumpff_series_short(psi, c2, c3);
+            else if (fabs(psi) <= 0.5) stumpff_series(psi, c2, c3);
             else stumpff(psi, c2, c3);
         } else {
             c2 = 0.5;
@@ -351,7 +372,7 @@ __global__ void __launch_bounds__(256) wh_head_kernel(WhArgs a, int init, int pa
             } else {
                 const double sg = sqrt(a.gm[i]);
                 const double k[3] = {sg, 1.0 / a.gm[i], 1.0 / sg};
-                failed = kepler_drift_fast(r, v, a.gm[i], k, dt);
+                failed = kepler_drift_fast(r, v, a.gm[i], k, dt, a.dt2_6);
             }
             if (failed) atomicAdd(&sh->kepler_failures, 1ull);
             for (int c = 0; c < 3; c++) {
@@ -438,6 +459,7 @@ __global__ void __launch_bounds__(256) wh_head_kernel(WhArgs a, int init, int pa
         for (int c = 0; c < 3; c++) {
             sh->ind[c] = ind[c];
             sh->a2[c] = a2[c];
+            sh->ind_a2[c] = ind[c] + a2[c];
             a.acc[c] = 0.0;
             a.acc[3 + c] = 0.0;
         }
@@ -500,13 +522,16 @@ __global__ void __launch_bounds__(256) wh_tail_kernel(WhArgs a, int init, int pa
     for (int c = 0; c < 3; c++) {
         p[c] = a.pos[3 * i + c];
         v[c] = a.vel[3 * i + c];
-        if (!init) v[c] += a.acc[3 * i + c] * half;
+        if (!init) {
+            if (MODE == ABIE_FORCE_EXACT) v[c] += a.acc[3 * i + c] * half;
+            else v[c] = fma(a.acc[3 * i + c], half, v[c]);
+        }
         jp[c] = p[c] - sh->R[c];
         jv[c] = v[c] - sh->V[c];
     }
     if (!init) {
         const int failed = MODE == ABIE_FORCE_EXACT ? kepler_drift(jp, jv, sh->gm_tail, a.dt)
-                                                    : kepler_drift_fast(jp, jv, sh->gm_tail, sh->gm_tail_k, a.dt);
+                                                    : kepler_drift_fast(jp, jv, sh->gm_tail, sh->gm_tail_k, a.dt, a.dt2_6);
         if (failed) atomicAdd(&a.sh[parity].kepler_failures, 1ull);
         for (int c = 0; c < 3; c++) {
             p[c] = jp[c] + sh->Rp[c];
@@ -534,10 +559,19 @@ __global__ void __launch_bounds__(256) wh_tail_kernel(WhArgs a, int init, int pa
     }
     const double Gm0 = a.G * a.m[0];
     for (int c = 0; c < 3; c++) {
-        double cent = Gm0 * (jp[c] * ir3j - p[c] * ir3h);
-        double acc = sh->ind[c] + cent + sh->a2[c] + a3[c];
+        double acc;
+        if (MODE == ABIE_FORCE_EXACT) {
+            const double cent = Gm0 * (jp[c] * ir3j - p[c] * ir3h);
+            acc = sh->ind[c] + cent + sh->a2[c] + a3[c];
+        } else {
+            const double cent = Gm0 * fma(jp[c], ir3j, -p[c] * ir3h);
+            acc = sh->ind_a2[c] + cent + a3[c];
+        }
         a.acc[3 * i + c] = acc;
-        if (!init) v[c] += acc * half;
+        if (!init) {
+            if (MODE == ABIE_FORCE_EXACT) v[c] += acc * half;
+            else v[c] = fma(acc, half, v[c]);
+        }
         a.pos[3 * i + c] = p[c];
         a.vel[3 * i + c] = v[c];
     }
@@ -636,6 +670,7 @@ int wh_run(const SystemView &sys, double t, double t_end, double dt, double *t_o
     a.head = H;
     a.G = sys.G;
     a.dt = dt;
+    a.dt2_6 = dt * dt / 6.0;
     a.pos = sys.pos;
     a.vel = sys.vel;
     a.acc = g_wh.acc;
