@@ -212,7 +212,8 @@ __device__ int kepler_drift_fast(double r0v[3], double v0v[3], double gm, const 
     const double alpha = -2.0 * xi * igm;
     const double rv = fma(r0v[2], v0v[2], fma(r0v[1], v0v[1], r0v[0] * v0v[0]));
     double chi0;
-    const double w1 = sqrtgm * dt * ir0;  // first-order arc
+    const double sgdt = sqrtgm * dt;
+    const double w1 = sgdt * ir0;  // first-order arc
     if (alpha > TOL_ENERGY && w1 * w1 * alpha < 0.1) {
         const double ir02 = ir0 * ir0;
         const double u = rv * ir02;                       // rdot / r
@@ -237,7 +238,6 @@ __device__ int kepler_drift_fast(double r0v[3], double v0v[3], double gm, const 
     }
     double chi = 0.0, r = 0.0, c2 = 0.0, c3 = 0.0, psi = 0.0;
     const double rvs = rv * isqrtgm;
-    const double sgdt = sqrtgm * dt;
     for (int it = 0; it < KEPLER_MAX_IT; it++) {
         const double chi2 = chi0 * chi0;
         psi = chi2 * alpha;
@@ -251,7 +251,8 @@ __device__ int kepler_drift_fast(double r0v[3], double v0v[3], double gm, const 
         }
         const double s3 = fma(-psi, c3, 1.0), s2 = fma(-psi, c2, 1.0);
         r = fma(chi2, c2, fma(rvs * chi0, s3, r0 * s2));
-        const double num = sgdt - chi2 * chi0 * c3 - rvs * chi2 * c2 - r0 * chi0 * s3;
+        // sgdt - chi^3 c3 - rvs chi^2 c2 - r0 chi s3, nested
+        const double num = fma(-chi0, fma(chi0, fma(chi0, c3, rvs * c2), r0 * s3), sgdt);
         chi = fma(num, rcp_fast(r), chi0);
         if (fabs(chi - chi0) < KEPLER_TOL) break;
         chi0 = chi;
@@ -285,6 +286,15 @@ template <int MODE>
 __device__ __forceinline__ double wdiv(double x, double y)
 {
     return MODE == ABIE_FORCE_EXACT ? x / y : x * rcp_fast(y);
+}
+
+// G m |(x, y, z)|^-3 in integer arithmetic (the fast form's pair term core).
+__device__ __forceinline__ double wh_gm_ir3(double x, double y, double z, double gm)
+{
+    unsigned long long Mr;
+    int Er;
+    r2_int(x, y, z, Mr, Er);
+    return gm_inv_r3_int(Mr, Er, gm);
 }
 
 template <int MODE>
@@ -550,8 +560,11 @@ __global__ void __launch_bounds__(256) wh_tail_kernel(WhArgs a, int init, int pa
             for (int c = 0; c < 3; c++) a3[c] -= hs[4 * q + 3] * aux * d[c];
         }
     } else {
-        ir3h = wh_ir3<MODE>(p[0], p[1], p[2]);
-        ir3j = wh_ir3<MODE>(jp[0], jp[1], jp[2]);
+        // G m0 folded into the inverse cubes; the planets' sum starts from
+        // the indirect and accel2 terms
+        ir3h = wh_gm_ir3(p[0], p[1], p[2], a.G * a.m[0]);
+        ir3j = wh_gm_ir3(jp[0], jp[1], jp[2], a.G * a.m[0]);
+        for (int c = 0; c < 3; c++) a3[c] = sh->ind_a2[c];
         for (int q = 0; q < n_src; q++) {
             Src sq{hs[4 * q], hs[4 * q + 1], hs[4 * q + 2], hs[4 * q + 3]};
             pair_fast(p[0], p[1], p[2], sq, a3[0], a3[1], a3[2]);
@@ -564,8 +577,7 @@ __global__ void __launch_bounds__(256) wh_tail_kernel(WhArgs a, int init, int pa
             const double cent = Gm0 * (jp[c] * ir3j - p[c] * ir3h);
             acc = sh->ind[c] + cent + sh->a2[c] + a3[c];
         } else {
-            const double cent = Gm0 * fma(jp[c], ir3j, -p[c] * ir3h);
-            acc = sh->ind_a2[c] + cent + a3[c];
+            acc = a3[c] + fma(jp[c], ir3j, -p[c] * ir3h);
         }
         a.acc[3 * i + c] = acc;
         if (!init) {
