@@ -65,9 +65,10 @@ def parse():
     ap.add_argument("--ensemble-years", type=float, default=1.0)
     ap.add_argument("--wh-steps", type=int, default=64)
     ap.add_argument("--gr-years", type=float, default=1.0)
+    ap.add_argument("--disk-years", type=float, default=1.0)
     ap.add_argument("--no-extras", action="store_true", help="only the headline force line")
-    ap.add_argument("--extras", default="ensemble,wh,radau",
-                    help="comma list of sub-measurements: ensemble, wh, radau")
+    ap.add_argument("--extras", default="ensemble,wh,radau,disk",
+                    help="comma list of sub-measurements: ensemble, wh, radau, disk")
     ap.add_argument("--ensemble-forms", default="plain_fp64,fp64,learned",
                     help="comma list of ensemble forms to time")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -310,6 +311,8 @@ def run_ours(args):
             extra["wh"] = run_wh(lib, args)
         if args.gr_years > 0 and "radau" in which:
             extra["radau_1009"] = run_radau_single(lib, args)
+        if args.disk_years > 0 and "disk" in which:
+            extra["radau_disk"] = run_radau_disk(lib, args)
 
     if rank == 0:
         cpu = None
@@ -428,8 +431,11 @@ def run_wh(lib, args):
     dt = _t.perf_counter() - t0
     c = lib.counters()
     steps = c["wh_steps"]
+    n_m = int(np.count_nonzero(m > 0))
+    kick = (n - n_m) * n_m + n_m * (n_m - 1)  # particle-massive and massive pairs per step
     return {"bodies": int(n), "steps": int(steps), "seconds": dt, "steps_per_s": steps / dt,
-            "kepler_solves_per_s": steps * (n - 1) / dt, "kepler_failures": c["kepler_failures"],
+            "kepler_solves_per_s": steps * (n - 1) / dt, "kick_interactions_per_step": int(kick),
+            "kick_gint_per_s": steps * kick / dt / 1e9, "kepler_failures": c["kepler_failures"],
             "timing": "wall clock around integrator_wh (device-resident state)"}
 
 
@@ -445,16 +451,48 @@ def run_radau_single(lib, args):
         lib.set_state(p, v, m, r, m.size, G, 0.0)
         lib.integrator_gr(0.0, 0.01, 1.0)
         lib.set_state(p, v, m, r, m.size, G, 0.0)
+        e0 = lib.get_total_energy()
         lib.reset_counters()
         t0 = _t.perf_counter()
         lib.integrator_gr(0.0, args.gr_years, 1.0)
         dt = _t.perf_counter() - t0
         c = lib.counters()
+        e1 = lib.get_total_energy()
         lib.set_force_mode(old)
-        out[mode] = {"seconds": dt, "accepts": c["accepts"], "attempts": c["attempts"],
-                     "ms_per_attempt": 1e3 * dt / max(c["attempts"], 1),
-                     "force_calls": c["force_calls"]}
+        out[mode] = {"seconds": dt, "accepts": c["accepts"], "rejects": c["rejects"],
+                     "attempts": c["attempts"], "ms_per_attempt": 1e3 * dt / max(c["attempts"], 1),
+                     "force_calls": c["force_calls"], "abs_dE_over_E": abs((e1 - e0) / e0)}
     return out
+
+
+def run_radau_disk(lib, args):
+    """Radau15 (fast form) on the 16,385-body planetesimal disk, a bounded
+    slice of the reference's 10-yr run: every body massive, so each force
+    call is 268 M interactions inside the general engine."""
+    import time as _t
+    p, v, m, r = ics.planetesimal_disk()
+    n = m.size
+    lib.initialize_code(G, 0.0, 1 << 21, MAX_CE_EVENTS=3, MAX_COLLISION_EVENTS=2, deviceID=0)
+    old = lib.set_force_mode("fp64")
+    lib.set_state(p, v, m, r, n, G, 0.0)
+    lib.integrator_gr(0.0, 1e-3, 1.0)  # warm-up: kernels, buffers
+    lib.set_state(p, v, m, r, n, G, 0.0)
+    e0 = lib.get_total_energy()
+    lib.reset_counters()
+    t0 = _t.perf_counter()
+    lib.integrator_gr(0.0, args.disk_years, 1.0)
+    dt = _t.perf_counter() - t0
+    c = lib.counters()
+    e1 = lib.get_total_energy()
+    lib.set_force_mode(old)
+    inter = interactions(m)
+    return {"bodies": int(n), "years": args.disk_years, "t_reached": lib.get_model_time(),
+            "seconds": dt, "accepts": c["accepts"], "rejects": c["rejects"],
+            "attempts": c["attempts"], "force_calls": c["force_calls"],
+            "ms_per_attempt": 1e3 * dt / max(c["attempts"], 1),
+            "gint_per_s_in_engine": c["force_calls"] * inter / dt / 1e9,
+            "abs_dE_over_E": abs((e1 - e0) / e0),
+            "timing": "wall clock around integrator_gr (device-resident state)"}
 
 
 def main():
