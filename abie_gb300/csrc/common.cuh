@@ -269,8 +269,16 @@ __device__ __forceinline__ void pair_fast(double xj, double yj, double zj, const
 // NaN is skipped, like the reference's vector_max_abs (src/common.c:316-322).
 __device__ __forceinline__ unsigned long long absmax_key(double v)
 {
-    double a = fabs(v);
-    return (a == a) ? (unsigned long long)__double_as_longlong(a) + 1ull : 0ull;
+    // integer instructions only: |v|'s bits, NaN (above the infinity
+    // pattern) -> 0
+    const unsigned long long a = (unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFull;
+    return a <= 0x7FF0000000000000ull ? a + 1ull : 0ull;
+}
+
+// Finite test on the exponent bits (no FP64 instruction).
+__device__ __forceinline__ bool finite_bits(double v)
+{
+    return ((unsigned)__double2hiint(v) & 0x7FF00000u) != 0x7FF00000u;
 }
 
 __host__ __device__ inline double absmax_value(unsigned long long key)

@@ -325,21 +325,19 @@ __global__ void __launch_bounds__(32 * WARPS, (EnsOccupancy<W, LEARN>::value)) e
             if (has) X.F1 = force_here();
             S.force_calls++;
             // d0, d1 over the first n of the 3n entries, as the reference does
-            double d0 = -1.7976931348623157e308, d1 = d0;
+            unsigned long long k0 = 0, k1 = 0;
             if (gl < n) {
-                d0 = absmax_or_none(X.y0);
-                d1 = absmax_or_none(X.F1);
+                k0 = absmax_key(X.y0);
+                k1 = absmax_key(X.F1);
             }
-            d0 = grp.maxd(d0);
-            d1 = grp.maxd(d1);
+            const double d0 = grp.maxk(k0);
+            const double d1 = grp.maxk(k1);
             double dt0 = (d0 < 1e-5 || d1 < 1e-5) ? 1e-6 : 0.01 * (d0 / d1);
             grp.sync();
             publish(X.y0 + dt0 * X.dy0);
             group_force<MODE, W>(grp, n, sp, sa);
             S.force_calls++;
-            double d2 = -1.7976931348623157e308;
-            if (has) d2 = absmax_or_none(force_here() - X.F1);
-            d2 = grp.maxd(d2) / dt0;
+            const double d2 = grp.maxk(has ? absmax_key(force_here() - X.F1) : 0ull) / dt0;
             double dt1;
             if (fmax(d1, d2) <= 1e-15) dt1 = fmax(1e-6, dt0 * 1e-3);
             else dt1 = pow(0.01 / fmax(d1, d2), (1.0 / (15 + 1)));
@@ -361,7 +359,7 @@ __global__ void __launch_bounds__(32 * WARPS, (EnsOccupancy<W, LEARN>::value)) e
             int iters = 0;
             for (int ipc = 0; ipc < 12; ipc++) {
                 iters++;
-                double f8 = -1.7976931348623157e308, db6 = f8;
+                unsigned long long kf8 = 0, kdb6 = 0;
                 for (int ih = 1; ih < 8; ih++) {
                     grp.sync();
                     const double sh = e_hs[ih], ds = h * sh, hh = 0.5 * ds * ds;
@@ -371,15 +369,15 @@ __global__ void __launch_bounds__(32 * WARPS, (EnsOccupancy<W, LEARN>::value)) e
                         const double F = force_here();
                         e_gb_update<MODE>(X, ih, F);
                         if (ih == 7) {
-                            f8 = absmax_or_none(F);
-                            db6 = absmax_or_none(e_b6<MODE>(X) - X.b6p);
+                            kf8 = absmax_key(F);
+                            kdb6 = absmax_key(e_b6<MODE>(X) - X.b6p);
                         }
                     }
                 }
                 S.force_calls += 7;
-                f8 = grp.maxd(f8);
-                db6 = grp.maxd(db6);
-                if (db6 / f8 < TOLPC) break;
+                const double f8 = grp.maxk(kf8);
+                const double db6 = grp.maxk(kdb6);
+                if (corrector_converged<MODE>(db6, f8)) break;
                 X.b6p = e_b6<MODE>(X);
             }
             S.iterations += iters;
@@ -393,7 +391,7 @@ __global__ void __launch_bounds__(32 * WARPS, (EnsOccupancy<W, LEARN>::value)) e
             group_force<MODE, W>(grp, n, sp, sa);
             S.force_calls++;
             const double dd = has ? force_here() : 0.0;
-            const bool bad = has && !isfinite(ya + dd + va);
+            const bool bad = has && !(finite_bits(ya) && finite_bits(dd) && finite_bits(va));
             if (grp.any(bad)) {
                 if (net_guess) {
                     // the network's guess led the corrector astray: redo the
@@ -407,16 +405,11 @@ __global__ void __launch_bounds__(32 * WARPS, (EnsOccupancy<W, LEARN>::value)) e
                 done = true;
                 break;
             }
-            double mb6 = -1.7976931348623157e308, mdd = mb6;
-            if (has) {
-                mb6 = absmax_or_none(e_b6<MODE>(X));
-                mdd = absmax_or_none(dd);
-            }
-            mb6 = grp.maxd(mb6);
-            mdd = grp.maxd(mdd);
-            double estim_b6 = mb6 / mdd;
-            double err = pow(estim_b6 / EPSB, 1. / 7);
-            double dtreq = h / err;
+            const double mb6 = grp.maxk(has ? absmax_key(e_b6<MODE>(X)) : 0ull);
+            const double mdd = grp.maxk(has ? absmax_key(dd) : 0ull);
+            const double estim_b6 = mb6 / mdd;
+            double err, dtreq, rq;
+            step_size<MODE>(estim_b6, h, err, dtreq, rq);
             if (!(err == err)) {  // NaN step control: the state is not finite
                 if (net_guess) {
                     restore_plain_guess(LS, X, gl, has);
@@ -438,7 +431,7 @@ __global__ void __launch_bounds__(32 * WARPS, (EnsOccupancy<W, LEARN>::value)) e
                     h = a.t_end - t;
                     stop = true;
                 }
-                double q = dtreq / h;
+                const double q = MODE == ABIE_FORCE_EXACT ? dtreq / h : rq;
                 if (MODE != ABIE_FORCE_EXACT) e_b_from_g(X);  // the fast form carries g only
                 X.y0 = ya;
                 X.dy0 = va;
@@ -462,7 +455,7 @@ __global__ void __launch_bounds__(32 * WARPS, (EnsOccupancy<W, LEARN>::value)) e
                 loop_count += 1;
                 first_attempt = false;
             }
-            if (dtreq / h > 1.0 / FAC) h /= FAC;
+            if ((MODE == ABIE_FORCE_EXACT ? dtreq / h : rq) > 1.0 / FAC) h /= FAC;
             else if (dtreq < 1.e-12) h *= FAC;
             else h = dtreq;
             if (h < H_MIN) h = H_MIN;

@@ -767,7 +767,7 @@ __global__ void __launch_bounds__(256) radau_engine(EngineArgs a)
             if (leader) ctl->force_calls += 7;
             double db6, f8;
             read2(ctl, red_idx++, db6, f8);
-            if (db6 / f8 < TOLPC) break;  // src/integrator_gauss_radau15.c:366
+            if (corrector_converged<MODE>(db6, f8)) break;  // src/integrator_gauss_radau15.c:366
             for (int j = gid; j < n; j += ngroups)
                 for (int c = c0; c < c1; c++) a.b6p[3 * j + c] = b6_at<MODE>(a, 3 * j + c);
         }
@@ -785,7 +785,8 @@ __global__ void __launch_bounds__(256) radau_engine(EngineArgs a)
                 const int i = 3 * j + c;
                 const double fi = (alive ? pick3(f, c) : 0.0) + (a.ext ? a.ext[i] : 0.0);
                 a.ddy[i] = fi;
-                if (!isfinite(fi + a.ypa[i] + a.dyp[i])) atomicCAS(&ctl->err, 0, ABIE_ERR_NUMERICS);
+                if (!(finite_bits(fi) && finite_bits(a.ypa[i]) && finite_bits(a.dyp[i])))
+                    atomicCAS(&ctl->err, 0, ABIE_ERR_NUMERICS);
                 unsigned long long u = absmax_key(b6_at<MODE>(a, i));
                 unsigned long long w = absmax_key(fi);
                 kb6 = u > kb6 ? u : kb6;
@@ -803,8 +804,8 @@ __global__ void __launch_bounds__(256) radau_engine(EngineArgs a)
         read2(ctl, red_idx++, mb6, mdd);
         // ---------------- step control (src/integrator_gauss_radau15.c:379-433) ----------------
         double estim_b6 = mb6 / mdd;
-        double err = pow(estim_b6 / EPSB, 1. / 7);
-        double dtreq = h / err;
+        double err, dtreq, rq;
+        step_size<MODE>(estim_b6, h, err, dtreq, rq);
         bool accepted = (err <= 1 || loop_count > 100);
         bool stop = false;
         if (accepted) {
@@ -814,7 +815,7 @@ __global__ void __launch_bounds__(256) radau_engine(EngineArgs a)
                 h = a.t_end - t;
                 stop = true;
             }
-            double q = dtreq / h;
+            double q = MODE == ABIE_FORCE_EXACT ? dtreq / h : rq;
             for (int j = gid; j < n; j += ngroups) {
                 for (int c = c0; c < c1; c++) {
                     int i = 3 * j + c;
@@ -836,7 +837,7 @@ __global__ void __launch_bounds__(256) radau_engine(EngineArgs a)
             if (leader) ctl->rejects++;
         }
         if (!stop) {
-            if (dtreq / h > 1.0 / FAC) h /= FAC;
+            if ((MODE == ABIE_FORCE_EXACT ? dtreq / h : rq) > 1.0 / FAC) h /= FAC;
             else if (dtreq < 1.e-12) h *= FAC;
             else h = dtreq;
             if (h < H_MIN) h = H_MIN;
@@ -1108,7 +1109,7 @@ __global__ void __launch_bounds__(64) radau_split(EngineArgs a)
             if (!grid_sync(ctl, T)) return;
             double db6, f8;
             read2(ctl, red_idx++, db6, f8);
-            if (db6 / f8 < TOLPC) break;  // src/integrator_gauss_radau15.c:366
+            if (corrector_converged<MODE>(db6, f8)) break;  // src/integrator_gauss_radau15.c:366
             X.b6p = e_b6<MODE>(X);
         }
         // advance (spacing 1)
@@ -1120,7 +1121,8 @@ __global__ void __launch_bounds__(64) radau_split(EngineArgs a)
         if (has && writer) {
             a.ypa[gi] = ya;
             put_prefilter(a, gi, ya);
-            if (!isfinite(dd + ya + va)) atomicCAS(&ctl->err, 0, ABIE_ERR_NUMERICS);
+            if (!(finite_bits(dd) && finite_bits(ya) && finite_bits(va)))
+                atomicCAS(&ctl->err, 0, ABIE_ERR_NUMERICS);
             kb6 = absmax_key(e_b6<MODE>(X));
             kdd = absmax_key(dd);
         }
@@ -1135,8 +1137,8 @@ __global__ void __launch_bounds__(64) radau_split(EngineArgs a)
         read2(ctl, red_idx++, mb6, mdd);
         // step control (src/integrator_gauss_radau15.c:379-433)
         const double estim_b6 = mb6 / mdd;
-        const double err = pow(estim_b6 / EPSB, 1. / 7);
-        const double dtreq = h / err;
+        double err, dtreq, rq;
+        step_size<MODE>(estim_b6, h, err, dtreq, rq);
         const bool accepted = (err <= 1 || loop_count > 100);
         bool stop = false;
         if (accepted) {
@@ -1146,7 +1148,7 @@ __global__ void __launch_bounds__(64) radau_split(EngineArgs a)
                 h = a.t_end - t;
                 stop = true;
             }
-            const double q = dtreq / h;
+            const double q = MODE == ABIE_FORCE_EXACT ? dtreq / h : rq;
             if (MODE != ABIE_FORCE_EXACT) e_b_from_g(X);  // the fast form carries g only
             X.y0 = ya;
             X.dy0 = va;
@@ -1161,7 +1163,7 @@ __global__ void __launch_bounds__(64) radau_split(EngineArgs a)
             if (leader) ctl->rejects++;
         }
         if (!stop) {
-            if (dtreq / h > 1.0 / FAC) h /= FAC;
+            if ((MODE == ABIE_FORCE_EXACT ? dtreq / h : rq) > 1.0 / FAC) h /= FAC;
             else if (dtreq < 1.e-12) h *= FAC;
             else h = dtreq;
             if (h < H_MIN) h = H_MIN;

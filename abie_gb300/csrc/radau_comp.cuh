@@ -201,17 +201,58 @@ __device__ __forceinline__ void e_refine(Comp &c, double q)
     b[6] = e6 + 0.0;
 }
 
-__device__ __forceinline__ double warp_maxd(double v)
+// Max over the warp of absmax_key values (integer instructions only).
+__device__ __forceinline__ unsigned long long warp_maxk(unsigned long long v)
 {
-    // the values are non-negative magnitudes or -DBL_MAX; plain max is exact
-    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
+        v = w > v ? w : v;
+    }
     return v;
 }
 
-__device__ __forceinline__ double absmax_or_none(double v)
+// The corrector's convergence test (src/integrator_gauss_radau15.c:366),
+// db6 / f8 < tolpc.  The fast form multiplies instead of dividing.
+template <int MODE>
+__device__ __forceinline__ bool corrector_converged(double db6, double f8)
 {
-    double a = fabs(v);
-    return (a == a) ? a : -1.7976931348623157e308;
+    return MODE == ABIE_FORCE_EXACT ? db6 / f8 < TOLPC : db6 < TOLPC * f8;
+}
+
+// Step control (src/integrator_gauss_radau15.c:379-433): err =
+// (estim_b6 / epsb)^(1/7) and dtreq = h / err.  The fast form returns
+// rq = 1 / err as well (so dtreq = h rq, and the ratio dtreq / h the
+// controller tests is rq) and takes the seventh root in single precision
+// (log2 / exp2 of the ratio truncated to a float; NaN, infinite or negative
+// ratios take the reference's path): the step size only steers the
+// integrator.  The one visible difference: a retry after a rejection lands
+// at err = 1 within rounding, and the single-precision err accepts it where
+// the reference's last bits may reject it again (fewer attempts, about the
+// same accepted steps).  Whenever the float err exceeds 1 its reciprocal is
+// below 1, so a rejection always shrinks the step.
+template <int MODE>
+__device__ __forceinline__ void step_size(double estim_b6, double h, double &err, double &dtreq,
+                                          double &rq)
+{
+    if (MODE == ABIE_FORCE_EXACT) {  // the reference's operations
+        err = pow(estim_b6 / EPSB, 1. / 7);
+        dtreq = h / err;
+        rq = dtreq / h;
+        return;
+    }
+    const double x = estim_b6 * (1.0 / EPSB);
+    if (!finite_bits(x) || !(__double2hiint(x) >= 0)) {  // NaN, infinite or negative
+        err = pow(estim_b6 / EPSB, 1. / 7);
+        dtreq = h / err;
+        rq = dtreq / h;
+        return;
+    }
+    const float xf = f64_to_f32_trunc23(x);  // exponent clamped to the float range; 0 stays tiny
+    const float l7 = log2f(xf) * (1.0f / 7.0f);
+    const float ef = exp2f(l7), rf = exp2f(-l7);
+    err = f32_bits_to_f64(__float_as_int(ef));  // positive normal floats: exact
+    rq = f32_bits_to_f64(__float_as_int(rf));
+    dtreq = h * rq;
 }
 
 // g = C^-1 b for one component: back-substitution through the triangular
@@ -249,17 +290,20 @@ struct Group {
         if (W == 1) __syncwarp();
         else asm volatile("bar.sync %0, %1;" ::"r"(1 + gidx), "r"(32 * W) : "memory");
     }
-    __device__ __forceinline__ double maxd(double v)
+    // max over the group of absmax_key values, as the double absmax_value
+    // gives back (-DBL_MAX when every value was NaN or absent)
+    __device__ __forceinline__ double maxk(unsigned long long v)
     {
-        v = warp_maxd(v);
-        if (W == 1) return v;
-        if (lane == 0) red[tog * W + wig] = v;
+        v = warp_maxk(v);
+        if (W == 1) return absmax_value(v);
+        unsigned long long *slot = reinterpret_cast<unsigned long long *>(red);
+        if (lane == 0) slot[tog * W + wig] = v;
         sync();
-        double r = red[tog * W];
+        unsigned long long r = slot[tog * W];
 #pragma unroll
-        for (int k = 1; k < W; k++) r = fmax(r, red[tog * W + k]);
+        for (int k = 1; k < W; k++) r = slot[tog * W + k] > r ? slot[tog * W + k] : r;
         tog ^= 1;
-        return r;
+        return absmax_value(r);
     }
     __device__ __forceinline__ bool any(bool b)
     {
