@@ -2,8 +2,9 @@
 //
 // A group of threads integrates one system (at most 21 bodies) from a work
 // queue -- one warp for up to 10 bodies, two warps (a named barrier each)
-// for 11-21 -- and a finished group takes the next system, so systems of
-// uneven size and difficulty do not wait for each other.  Each thread owns
+// for 11-21, four warps for the slowest 1 in 256 systems, each class a
+// kernel on its own stream -- and a finished group takes the next system,
+// so systems of uneven size and difficulty do not wait for each other.  Each thread owns
 // one of the system's 3N components and keeps its Radau state (y0, dy0,
 // F1, b[7], g[7], previous b6) in registers.  For the force, the predicted
 // positions go to shared memory and the pairs spread over the lanes: each
@@ -20,7 +21,10 @@
 // substep (on this GPU each FP64 warp instruction holds the SM
 // sub-partition's FP64 pipe for ~64 cycles whatever the number of active
 // lanes, so the instruction count sets the time per substep), the same
-// converged solution, and fewer corrector iterations.
+// converged solution, and fewer corrector iterations.  The maxima behind
+// the convergence test and the step control are integer maxima of the
+// values' bit patterns, and the fast form's step-size root is taken in
+// single precision (radau_comp.cuh, step_size).
 //
 // Systems start longest first (shortest two-body time scale first), since
 // a batch lasts at least as long as its slowest system.
