@@ -31,6 +31,13 @@ int launch_compact_sources(const double *pos, const double *m, int n, double G, 
 int launch_force(int mode, const double *pos, const double *m, int n, double G,
                  ForceScratch &s, double *acc, cudaStream_t st);
 
+// Fast FP64 force of the n sinks at pos against a source list already built
+// (*n_src_dev records, e.g. the Radau15 engine's published substep), 32
+// lanes per sink with sinks handed out from the counter next (zeroed here):
+// the same sums, in the same order, as the engine's own 32-lane sink loop.
+int launch_force_published(const double *pos, const double *m, int n, const Src *src,
+                           const int *n_src_dev, double *acc, unsigned int *next, cudaStream_t st);
+
 // Fast FP64 force with caller-provided scratch (src / src_body sized for n
 // entries, n_src one int); allocates nothing.  Uses one source chunk.
 int launch_force_fp64_scratch(const double *pos, const double *m, int n, double G, Src *src,

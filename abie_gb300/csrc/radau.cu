@@ -64,6 +64,12 @@ struct EngineCtl {
     unsigned long long n_ce, n_coll;
     int ev_overflow;
     int hmin_warned;
+    // stepped engine (host-driven): source count, sink counter of the force
+    // kernel, and the step control's decision for the host
+    int n_src;
+    unsigned int next_sink;
+    int accepted, stop;
+    double q, dt0, d1;
 };
 
 struct EngineArgs {
@@ -1268,6 +1274,333 @@ static int engine_reserve(size_t n, size_t max_ce, size_t max_coll)
     return 0;
 }
 
+// ---------------------------------------------------------------------------
+// Stepped engine for large systems (fast form, no post-Newtonian terms): the
+// host drives radau_engine's sweep one phase per kernel, and every force
+// evaluation is the standalone force kernel on the published substep
+// (launch_force_published), which keeps 40 warps per SM busy on the FP64
+// pipe where the persistent engine, holding the whole sweep in registers,
+// keeps 16.  The per-component device functions, the force sums (32 lanes
+// per sink, in the engine's order) and the scalar step control (one
+// thread, the engine's expressions) are the persistent engine's, so both
+// give the same trajectory.  The host reads two maxima per corrector
+// iteration and the controller's decision per attempt.
+
+template <int MODE>
+__global__ void __launch_bounds__(256) st_publish_kernel(EngineArgs a, int row, double h, int buf)
+{
+    const double s = row == 8 ? 1.0 : c_hs[row], ds = h * s, hh = 0.5 * ds * ds;
+    double *yp = buf < 2 ? a.yp[buf] : a.ypa;
+    Src *src = buf < 2 ? a.src[buf] : a.srca;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.dim; i += gridDim.x * blockDim.x)
+        publish_comp<MODE>(a, i / 3, i % 3, row, row == 0 ? 0.0 : s, row == 0 ? 0.0 : h,
+                           row == 0 ? 0.0 : ds, row == 0 ? 0.0 : hh, yp, src);
+}
+
+__device__ __forceinline__ void st_keys(unsigned long long *keys, unsigned long long k0,
+                                        unsigned long long k1)
+{
+    k0 = warp_max_u64(k0);
+    k1 = warp_max_u64(k1);
+    if ((threadIdx.x & 31) == 0) {
+        if (k0) atomicMax(&keys[0], k0);
+        if (k1) atomicMax(&keys[1], k1);
+    }
+}
+
+__device__ __forceinline__ double st_force_at(const EngineArgs &a, const double *acc, int i)
+{
+    return (a.m[i / 3] >= 0.0 ? acc[i] : 0.0) + (a.ext ? a.ext[i] : 0.0);
+}
+
+// F1 = f(y0); maxima of |y0| and |F1| over the first n entries (as the
+// reference's initial_time_step scans them)
+__global__ void __launch_bounds__(256) st_f1_kernel(EngineArgs a, const double *acc)
+{
+    unsigned long long k0 = 0, k1 = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.dim; i += gridDim.x * blockDim.x) {
+        const double fi = st_force_at(a, acc, i);
+        a.F1[i] = fi;
+        if (i < a.n) {
+            const unsigned long long u = absmax_key(a.y0[i]), w = absmax_key(fi);
+            k0 = u > k0 ? u : k0;
+            k1 = w > k1 ? w : k1;
+        }
+    }
+    st_keys(&a.ctl->red[0][0], k0, k1);
+}
+
+// initial_time_step's dt0 (src/integrator_gauss_radau15.c:75-120), one thread
+__global__ void st_dt0_kernel(EngineArgs a)
+{
+    EngineCtl *ctl = a.ctl;
+    const double d0 = absmax_value(ctl->red[0][0]), d1 = absmax_value(ctl->red[0][1]);
+    ctl->dt0 = (d0 < 1e-5 || d1 < 1e-5) ? 1e-6 : 0.01 * (d0 / d1);
+    ctl->d1 = d1;
+    ctl->red[0][0] = ctl->red[0][1] = 0ull;
+}
+
+// the Euler probe y1 = y0 + dt0 dy0 into yp[1] / src[1]
+__global__ void __launch_bounds__(256) st_probe_kernel(EngineArgs a)
+{
+    const double dt0 = a.ctl->dt0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.dim; i += gridDim.x * blockDim.x) {
+        const int j = i / 3, c = i % 3;
+        const double p = a.y0[i] + dt0 * a.dy0[i];
+        a.yp[1][i] = p;
+        const int slot = a.src_slot[j];
+        if (slot >= 0) {
+            double *rec = reinterpret_cast<double *>(a.src[1] + slot);
+            rec[c] = p;
+            if (c == 0) rec[3] = a.G * a.m[j];
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) st_d2_kernel(EngineArgs a, const double *acc)
+{
+    unsigned long long k2 = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.dim; i += gridDim.x * blockDim.x) {
+        const unsigned long long u = absmax_key(st_force_at(a, acc, i) - a.F1[i]);
+        k2 = u > k2 ? u : k2;
+    }
+    st_keys(&a.ctl->red[0][0], k2, 0ull);
+}
+
+// the first step size, one thread
+__global__ void st_h0_kernel(EngineArgs a)
+{
+    EngineCtl *ctl = a.ctl;
+    const double dt0 = ctl->dt0, d1 = ctl->d1;
+    const double d2 = absmax_value(ctl->red[0][0]) / dt0;
+    double dt1;
+    if (fmax(d1, d2) <= 1e-15) dt1 = fmax(1e-6, dt0 * 1e-3);
+    else dt1 = pow(0.01 / fmax(d1, d2), (1.0 / (15 + 1)));
+    ctl->h = fmin(100 * dt0, dt1);
+    ctl->loop_count = 0;
+    ctl->red[0][0] = ctl->red[0][1] = 0ull;
+}
+
+// one substep after its forces: new g (b), the next publication, and at
+// the last substep the convergence maxima and the speculative advance
+template <int MODE>
+__global__ void __launch_bounds__(256) st_sweep_kernel(EngineArgs a, const double *acc, int ih,
+                                                       double h, int pc)
+{
+    const int nrow = ih < 7 ? ih + 1 : 1;
+    const double ns = c_hs[nrow], nds = h * ns, nhh = 0.5 * nds * nds;
+    const double hh1 = 0.5 * h * h;
+    unsigned long long kdb = 0, kf8 = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.dim; i += gridDim.x * blockDim.x) {
+        const int j = i / 3, c = i % 3;
+        const double fi = st_force_at(a, acc, i);
+        gb_update<MODE>(a, i, ih, fi);
+        if (ih == 7) {
+            const unsigned long long u = absmax_key(b6_at<MODE>(a, i) - a.b6p[i]);
+            const unsigned long long w = absmax_key(fi);
+            kdb = u > kdb ? u : kdb;
+            kf8 = w > kf8 ? w : kf8;
+        }
+        publish_comp<MODE>(a, j, c, nrow, ns, h, nds, nhh, a.yp[(pc + 1) & 1], a.src[(pc + 1) & 1]);
+        if (ih == 7) {
+            publish_comp<MODE>(a, j, c, 8, 1.0, h, h, hh1, a.ypa, a.srca);
+            a.dyp[i] = pred_vel<MODE>(a, i, h);
+        }
+    }
+    if (ih == 7) st_keys(&a.ctl->red[0][0], kdb, kf8);
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(256) st_b6p_kernel(EngineArgs a)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.dim; i += gridDim.x * blockDim.x)
+        a.b6p[i] = b6_at<MODE>(a, i);
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(256) st_advance_kernel(EngineArgs a, const double *acc)
+{
+    unsigned long long kb6 = 0, kdd = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.dim; i += gridDim.x * blockDim.x) {
+        const double fi = st_force_at(a, acc, i);
+        a.ddy[i] = fi;
+        if (!(finite_bits(fi) && finite_bits(a.ypa[i]) && finite_bits(a.dyp[i])))
+            atomicCAS(&a.ctl->err, 0, ABIE_ERR_NUMERICS);
+        const unsigned long long u = absmax_key(b6_at<MODE>(a, i)), w = absmax_key(fi);
+        kb6 = u > kb6 ? u : kb6;
+        kdd = w > kdd ? w : kdd;
+    }
+    st_keys(&a.ctl->red[0][0], kb6, kdd);
+}
+
+// step control (src/integrator_gauss_radau15.c:379-433) as radau_engine
+// runs it, one thread; the decision goes to the host through ctl
+template <int MODE>
+__global__ void st_control_kernel(EngineArgs a)
+{
+    EngineCtl *ctl = a.ctl;
+    const double mb6 = absmax_value(ctl->red[0][0]), mdd = absmax_value(ctl->red[0][1]);
+    ctl->red[0][0] = ctl->red[0][1] = 0ull;
+    double h = ctl->h, t = ctl->t;
+    int loop_count = ctl->loop_count;
+    const double estim_b6 = mb6 / mdd;
+    double err, dtreq, rq;
+    step_size<MODE>(estim_b6, h, err, dtreq, rq);
+    const bool accepted = (err <= 1 || loop_count > 100);
+    bool stop = false;
+    double q = 0.0;
+    if (accepted) {
+        t += h;
+        loop_count = 0;
+        if (t > a.t_end) {
+            h = a.t_end - t;
+            stop = true;
+        }
+        q = MODE == ABIE_FORCE_EXACT ? dtreq / h : rq;
+        ctl->accepts++;
+    } else {
+        loop_count += 1;
+        ctl->rejects++;
+    }
+    if (!stop) {
+        if ((MODE == ABIE_FORCE_EXACT ? dtreq / h : rq) > 1.0 / FAC) h /= FAC;
+        else if (dtreq < 1.e-12) h *= FAC;
+        else h = dtreq;
+        if (h < H_MIN) h = H_MIN;
+    }
+    ctl->t = t;
+    ctl->h = h;
+    ctl->loop_count = loop_count;
+    ctl->accepted = accepted ? 1 : 0;
+    ctl->stop = stop ? 1 : 0;
+    ctl->q = q;
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(256) st_accept_kernel(EngineArgs a)
+{
+    const double q = a.ctl->q;
+    const bool stop = a.ctl->stop != 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.dim; i += gridDim.x * blockDim.x) {
+        a.y0[i] = a.ypa[i];
+        a.dy0[i] = a.dyp[i];
+        a.F1[i] = a.ddy[i];
+        if (MODE == ABIE_FORCE_EXACT) {
+            a.b6p[i] = a.b[6 * a.dim + i];
+            refine_b(a, i, q);
+        } else {
+            refine_g(a, i, q, stop);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) st_scan_kernel(EngineArgs a)
+{
+    scan_events(a, a.ctl->t, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+}
+
+__global__ void st_commit_kernel(EngineArgs a)
+{
+    if (a.ctl->n_ev > 0) commit_events(a, a.ctl->t);
+}
+
+// The host loop; the state sits in the engine's buffers (phase 0 start).
+template <int MODE>
+static int stepped_run(const EngineArgs &a, int num_sms, cudaStream_t st, EngineCtl *out)
+{
+    EngineCtl *ctl = a.ctl;
+    double *acc = a.vp[0];  // force output (the velocity buffers serve post-Newtonian runs only)
+    const int threads = 256;
+    const int blocks = (int)std::max<long long>(1, std::min<long long>(((long long)a.dim + threads - 1) / threads,
+                                                                       (long long)num_sms * 8));
+    long long force_calls = 0, iterations = 0, attempts = 0;
+    auto force = [&](int buf) {
+        const double *pos = buf < 2 ? a.yp[buf] : a.ypa;
+        const Src *src = buf < 2 ? a.src[buf] : a.srca;
+        force_calls++;
+        return launch_force_published(pos, a.m, a.n, src, &ctl->n_src, acc, &ctl->next_sink, st);
+    };
+    unsigned long long hk[2];
+    auto read_keys = [&](double &v0, double &v1) -> int {
+        ABIE_CUDA(cudaMemcpyAsync(hk, &ctl->red[0][0], sizeof hk, cudaMemcpyDeviceToHost, st));
+        ABIE_CUDA(cudaMemsetAsync(&ctl->red[0][0], 0, sizeof hk, st));
+        ABIE_CUDA(cudaStreamSynchronize(st));
+        v0 = absmax_value(hk[0]);
+        v1 = absmax_value(hk[1]);
+        return 0;
+    };
+    EngineCtl c;
+    auto read_ctl = [&]() -> int {
+        ABIE_CUDA(cudaMemcpyAsync(&c, ctl, sizeof c, cudaMemcpyDeviceToHost, st));
+        ABIE_CUDA(cudaStreamSynchronize(st));
+        return 0;
+    };
+    int rc;
+    // F1 = f(y0), then initial_time_step
+    st_publish_kernel<MODE><<<blocks, threads, 0, st>>>(a, 0, 0.0, 0);
+    if ((rc = force(0))) return rc;
+    st_f1_kernel<<<blocks, threads, 0, st>>>(a, acc);
+    st_dt0_kernel<<<1, 1, 0, st>>>(a);
+    st_probe_kernel<<<blocks, threads, 0, st>>>(a);
+    if ((rc = force(1))) return rc;
+    st_d2_kernel<<<blocks, threads, 0, st>>>(a, acc);
+    st_h0_kernel<<<1, 1, 0, st>>>(a);
+    ABIE_CUDA(cudaGetLastError());
+    if ((rc = read_ctl())) return rc;
+    int pc = 0;
+    double h = c.h;
+    st_publish_kernel<MODE><<<blocks, threads, 0, st>>>(a, 1, h, pc & 1);
+    for (;;) {
+        int iters = 0;
+        for (int ipc = 0; ipc < 12; ipc++) {
+            iters++;
+            for (int ih = 1; ih < 8; ih++) {
+                if ((rc = force(pc & 1))) return rc;
+                st_sweep_kernel<MODE><<<blocks, threads, 0, st>>>(a, acc, ih, h, pc);
+                pc++;
+            }
+            double db6, f8;
+            if ((rc = read_keys(db6, f8))) return rc;
+            const bool conv = MODE == ABIE_FORCE_EXACT ? db6 / f8 < TOLPC : db6 < TOLPC * f8;
+            if (conv) break;
+            st_b6p_kernel<MODE><<<blocks, threads, 0, st>>>(a);
+        }
+        iterations += iters;
+        attempts++;
+        if ((rc = force(2))) return rc;
+        st_advance_kernel<MODE><<<blocks, threads, 0, st>>>(a, acc);
+        st_control_kernel<MODE><<<1, 1, 0, st>>>(a);
+        ABIE_CUDA(cudaGetLastError());
+        if ((rc = read_ctl())) return rc;
+        if (c.err) break;
+        bool stop = c.stop != 0;
+        if (c.accepted) {
+            st_accept_kernel<MODE><<<blocks, threads, 0, st>>>(a);
+            st_scan_kernel<<<blocks, threads, 0, st>>>(a);
+            st_commit_kernel<<<1, 1, 0, st>>>(a);
+            ABIE_CUDA(cudaGetLastError());
+        }
+        if (!stop) {
+            h = c.h;
+            st_publish_kernel<MODE><<<blocks, threads, 0, st>>>(a, 1, h, pc & 1);
+        }
+        if (c.accepted) {
+            if ((rc = read_ctl())) return rc;
+            if (c.flag > 0) stop = true;
+        }
+        if (stop) break;
+    }
+    if ((rc = read_ctl())) return rc;
+    c.force_calls = force_calls;
+    c.iterations = iterations;
+    c.attempts = attempts;
+    c.phase = 2;
+    *out = c;
+    return 0;
+}
+
+static int g_radau_path = 0;  // debug override: 0 automatic, 1 persistent engine, 2 stepped
+
 template <int MODE, int JS, bool PN = false>
 static int launch_engine(const EngineArgs &a, int num_sms, int block, cudaStream_t st, int *grid_out)
 {
@@ -1456,6 +1789,7 @@ int radau_run(const SystemView &sys, double t, double t_end, int mode, EventStat
     c0.t = t;
     c0.n_ce = evs ? *evs->n_ce : 0;
     c0.n_coll = evs ? *evs->n_coll : 0;
+    c0.n_src = n_src;
     ABIE_CUDA(cudaMemcpyAsync(e.ctl, &c0, sizeof c0, cudaMemcpyHostToDevice, st));
     ABIE_CUDA(cudaStreamSynchronize(st));
 
@@ -1472,8 +1806,22 @@ int radau_run(const SystemView &sys, double t, double t_end, int mode, EventStat
                 (long long)bps * g_sim.num_sms;
     }
     EngineCtl c;
+    // large systems in the fast form without post-Newtonian terms: the
+    // stepped engine (the standalone force kernel for every substep)
+    const bool stepped =
+        !split && a.C <= 0.0 && mode == ABIE_FORCE_FP64 &&
+        (g_radau_path == 2 ||
+         (g_radau_path == 0 && g_engine_js == 0 && (long long)n * (long long)n_src >= (1ll << 24)));
+    if (stepped) {
+        rc = stepped_run<ABIE_FORCE_FP64>(a, g_sim.num_sms, st, &c);
+        if (rc) return rc;
+        if (c.err) {
+            set_error(c.err, "radau engine stopped (code %d, t=%g)", c.err, c.t);
+            return c.err;
+        }
+    }
     long long budget = 4;
-    for (;;) {
+    for (; !stepped;) {
         a.attempt_budget = budget;
         cudaEvent_t e0, e1;
         ABIE_CUDA(cudaEventCreate(&e0));
@@ -1543,6 +1891,8 @@ int radau_run(const SystemView &sys, double t, double t_end, int mode, EventStat
 using namespace abie;
 
 extern "C" {
+
+void abie_debug_radau_path(int path) { g_radau_path = (path == 1 || path == 2) ? path : 0; }
 
 void abie_debug_engine_shape(int lanes_per_body, int block)
 {
