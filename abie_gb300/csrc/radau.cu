@@ -19,6 +19,13 @@
 // A call runs as a series of launches, each bounded to a number of step
 // attempts (sized from the measured time of the previous launch), so no
 // launch holds the GPU for long and every wait has a limit.
+//
+// Three paths share the per-component device functions: the split engine
+// (radau_split, at most 10 massive bodies: a replica of them per block, no
+// grid barrier per substep), the persistent engine (radau_engine), and for
+// systems of 2^24 or more interactions per force evaluation the stepped
+// engine (st_* kernels driven from the host, the standalone force kernel
+// for every substep), which gives the persistent engine's doubles.
 #include <stdio.h>
 
 #include <algorithm>
