@@ -309,17 +309,23 @@ ForceShape force_shape_default(int n_sink, int n_src)
 }
 
 int launch_force_published(const double *pos, const double *m, int n, const Src *src,
-                           const int *n_src_dev, double *acc, unsigned int *next, cudaStream_t st)
+                           const int *n_src_dev, int lanes, double *acc, unsigned int *next,
+                           cudaStream_t st)
 {
     if (n <= 0) return 0;
     int dev = 0, sms = 152, bps = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    ABIE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, force_fp64_dyn_kernel<32>, 256, 0));
-    const long long want = ((long long)n * 32 + 255) / 256;
+    const void *fn = lanes == 1 ? (const void *)force_fp64_dyn_kernel<1>
+                     : lanes == 8 ? (const void *)force_fp64_dyn_kernel<8>
+                                  : (const void *)force_fp64_dyn_kernel<32>;
+    ABIE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fn, 256, 0));
+    const long long want = ((long long)n * lanes + 255) / 256;
     const int blocks = (int)std::max<long long>(1, std::min<long long>((long long)sms * std::max(bps, 1), want));
     ABIE_CUDA(cudaMemsetAsync(next, 0, sizeof(unsigned int), st));
-    force_fp64_dyn_kernel<32><<<blocks, 256, 0, st>>>(pos, m, n, src, n_src_dev, acc, next);
+    if (lanes == 1) force_fp64_dyn_kernel<1><<<blocks, 256, 0, st>>>(pos, m, n, src, n_src_dev, acc, next);
+    else if (lanes == 8) force_fp64_dyn_kernel<8><<<blocks, 256, 0, st>>>(pos, m, n, src, n_src_dev, acc, next);
+    else force_fp64_dyn_kernel<32><<<blocks, 256, 0, st>>>(pos, m, n, src, n_src_dev, acc, next);
     ABIE_CUDA(cudaGetLastError());
     return 0;
 }

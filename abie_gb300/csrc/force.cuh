@@ -32,11 +32,13 @@ int launch_force(int mode, const double *pos, const double *m, int n, double G,
                  ForceScratch &s, double *acc, cudaStream_t st);
 
 // Fast FP64 force of the n sinks at pos against a source list already built
-// (*n_src_dev records, e.g. the Radau15 engine's published substep), 32
-// lanes per sink with sinks handed out from the counter next (zeroed here):
-// the same sums, in the same order, as the engine's own 32-lane sink loop.
+// (*n_src_dev records, e.g. the Radau15 engine's published substep), with
+// lanes (1, 8 or 32) per sink and sinks handed out from the counter next
+// (zeroed here): the same sums, in the same order, as the persistent
+// engine's sink loop with that many lanes per body.
 int launch_force_published(const double *pos, const double *m, int n, const Src *src,
-                           const int *n_src_dev, double *acc, unsigned int *next, cudaStream_t st);
+                           const int *n_src_dev, int lanes, double *acc, unsigned int *next,
+                           cudaStream_t st);
 
 // Fast FP64 force with caller-provided scratch (src / src_body sized for n
 // entries, n_src one int); allocates nothing.  Uses one source chunk.

@@ -22,10 +22,11 @@
 //
 // Three paths share the per-component device functions: the split engine
 // (radau_split, at most 10 massive bodies: a replica of them per block, no
-// grid barrier per substep), the persistent engine (radau_engine), and for
-// systems of 2^24 or more interactions per force evaluation the stepped
-// engine (st_* kernels driven from the host, the standalone force kernel
-// for every substep), which gives the persistent engine's doubles.
+// grid barrier per substep), the persistent engine (radau_engine), and,
+// from 2^20 interactions per force evaluation in the fast form without
+// post-Newtonian terms, the stepped engine (st_* kernels driven from the
+// host, the standalone force kernel for every substep), which gives the
+// persistent engine's doubles.
 #include <stdio.h>
 
 #include <algorithm>
@@ -1282,16 +1283,19 @@ static int engine_reserve(size_t n, size_t max_ce, size_t max_coll)
 }
 
 // ---------------------------------------------------------------------------
-// Stepped engine for large systems (fast form, no post-Newtonian terms): the
-// host drives radau_engine's sweep one phase per kernel, and every force
-// evaluation is the standalone force kernel on the published substep
-// (launch_force_published), which keeps 40 warps per SM busy on the FP64
-// pipe where the persistent engine, holding the whole sweep in registers,
-// keeps 16.  The per-component device functions, the force sums (32 lanes
-// per sink, in the engine's order) and the scalar step control (one
-// thread, the engine's expressions) are the persistent engine's, so both
-// give the same trajectory.  The host reads two maxima per corrector
-// iteration and the controller's decision per attempt.
+// Stepped engine for large systems (fast form, no post-Newtonian terms; from
+// 2^20 interactions per force evaluation, where it overtakes the persistent
+// engine: 45 against 50 us per force call at 1,025 bodies, 80 against 170
+// at 2,049, 795 against 988 at 8,193): the host drives radau_engine's sweep
+// one phase per kernel, and every force evaluation is the standalone force
+// kernel on the published substep (launch_force_published), which keeps 40
+// warps per SM busy on the FP64 pipe where the persistent engine, holding
+// the whole sweep in registers, keeps 16.  The per-component device
+// functions, the force sums (the engine's order for the same lanes per
+// body) and the scalar step control (one thread, the engine's expressions)
+// are the persistent engine's, so both give the same trajectory.  The host
+// reads two maxima per corrector iteration and the controller's decision
+// per attempt.
 
 template <int MODE>
 __global__ void __launch_bounds__(256) st_publish_kernel(EngineArgs a, int row, double h, int buf)
@@ -1521,11 +1525,13 @@ static int stepped_run(const EngineArgs &a, int num_sms, cudaStream_t st, Engine
     const int blocks = (int)std::max<long long>(1, std::min<long long>(((long long)a.dim + threads - 1) / threads,
                                                                        (long long)num_sms * 8));
     long long force_calls = 0, iterations = 0, attempts = 0;
+    // lanes per sink as the standalone force picks them (force_shape_default)
+    const int lanes = a.n_src <= 64 ? 1 : (a.n_src <= 1024 ? 8 : 32);
     auto force = [&](int buf) {
         const double *pos = buf < 2 ? a.yp[buf] : a.ypa;
         const Src *src = buf < 2 ? a.src[buf] : a.srca;
         force_calls++;
-        return launch_force_published(pos, a.m, a.n, src, &ctl->n_src, acc, &ctl->next_sink, st);
+        return launch_force_published(pos, a.m, a.n, src, &ctl->n_src, lanes, acc, &ctl->next_sink, st);
     };
     unsigned long long hk[2];
     auto read_keys = [&](double &v0, double &v1) -> int {
@@ -1818,7 +1824,7 @@ int radau_run(const SystemView &sys, double t, double t_end, int mode, EventStat
     const bool stepped =
         !split && a.C <= 0.0 && mode == ABIE_FORCE_FP64 &&
         (g_radau_path == 2 ||
-         (g_radau_path == 0 && g_engine_js == 0 && (long long)n * (long long)n_src >= (1ll << 24)));
+         (g_radau_path == 0 && g_engine_js == 0 && (long long)n * (long long)n_src >= (1ll << 20)));
     if (stepped) {
         rc = stepped_run<ABIE_FORCE_FP64>(a, g_sim.num_sms, st, &c);
         if (rc) return rc;

@@ -244,7 +244,7 @@ void abie_debug_engine_shape(int lanes_per_body, int block);
 /* Chooses the Radau15 path for systems beyond the split engine: 1 the
  * persistent engine, 2 the stepped engine (one kernel per phase, the
  * standalone force kernel for every substep; fast form without
- * post-Newtonian terms only), 0 automatic (stepped from 2^24 interactions
+ * post-Newtonian terms only), 0 automatic (stepped from 2^20 interactions
  * per force evaluation).  For tests and tuning. */
 void abie_debug_radau_path(int path);
 

@@ -264,7 +264,7 @@ def test_event_prefilter_at_threshold(sim, oracle, engine):
 
 def test_stepped_engine_matches_persistent_engine(clib):
     """The stepped engine (one kernel per phase, the standalone force kernel
-    for every substep; chosen automatically from 2^24 interactions per
+    for every substep; chosen automatically from 2^20 interactions per
     force evaluation) and the persistent engine with 32 lanes per body run
     the same arithmetic in the same order: a 2,049-body all-massive disk
     over 0.05 yr in the fast form gives the same doubles."""
