@@ -203,12 +203,12 @@ def test_split_engine_matches_general_engine(clib, oracle):
     assert rel_err_per_body(p1, p2) <= TOL and rel_err_per_body(v1, v2) <= TOL
 
 
-def _threshold_pairs(ce):
-    """planetary_system(seed=5, 3 planets, 300 test particles) plus four
+def _threshold_pairs(ce, n_planets=3):
+    """planetary_system(seed=5, n_planets, 300 test particles) plus four
     test-particle pairs at 30 au, each pair the same orbit offset out of the
     plane: two pairs 1e-4 inside the close-encounter distance ce and two
     1e-4 outside it (over a step the offsets change by ~1e-6)."""
-    p, v, m, r = ics.planetary_system(seed=5, n_planets=3, n_tp=300)
+    p, v, m, r = ics.planetary_system(seed=5, n_planets=n_planets, n_tp=300)
     extra_p, extra_v = [], []
     vc = np.sqrt(G * m[0] / 30.0)
     for q, scale in enumerate((1 - 1e-4, 1 + 1e-4, 1 - 1e-4, 1 + 1e-4)):
@@ -224,26 +224,30 @@ def _threshold_pairs(ce):
     return p, v, m, r
 
 
-@pytest.mark.parametrize("engine", ["split", "general"])
+@pytest.mark.parametrize("engine", ["split", "general", "stepped"])
 def test_event_prefilter_at_threshold(sim, oracle, engine):
     """Pairs 1e-4 inside and outside the close-encounter distance, among
     hundreds of far-apart bodies that the single-precision prefilter skips:
-    the inside pairs are recorded, the outside ones are not, on both
-    engines; the flag, ring buffer and stop time equal the oracle's."""
+    the inside pairs are recorded, the outside ones are not, on every
+    engine (the stepped one with 12 planets, beyond the split engine); the
+    flag, ring buffer and stop time equal the oracle's."""
     import ctypes as C
     ce = 0.01
-    p, v, m, r = _threshold_pairs(ce)
+    p, v, m, r = _threshold_pairs(ce, n_planets=12 if engine == "stepped" else 3)
     ref = oracle.radau15(p, v, m, r, G, 0.0, 10.0, ce_dist=ce, max_ce=3, max_coll=2)
     assert ref["flag"] == 1 and ref["n_ce"] == 4  # two pairs in each of two steps
     n0 = m.size - 8
     gold = ref["buf_ce"].reshape(-1, 4)
     assert sorted(set(map(int, gold[:, 1]))) == [n0, n0 + 4]
-    old = sim.set_force_mode("exact")
+    # the stepped engine runs the fast form; the others the exact one
+    old = sim.set_force_mode("fp64" if engine == "stepped" else "exact")
     sim.set_close_encounter_distance(ce)
     sim.reset_close_encounter_buffer()
     sim.reset_collision_buffer()
     if engine == "general":
         sim.lib.abie_debug_engine_shape(C.c_int(16), C.c_int(128))
+    if engine == "stepped":
+        sim.lib.abie_debug_radau_path(C.c_int(2))
     try:
         sim.set_state(p, v, m, r, m.size, G, 0.0)
         with pytest.raises(CloseEncounterException):
@@ -252,14 +256,16 @@ def test_event_prefilter_at_threshold(sim, oracle, engine):
         t = sim.get_model_time()
     finally:
         sim.lib.abie_debug_engine_shape(C.c_int(0), C.c_int(0))
+        sim.lib.abie_debug_radau_path(C.c_int(0))
         sim.set_force_mode(old)
         sim.set_close_encounter_distance(0.0)
         sim.reset_close_encounter_buffer()
         sim.reset_collision_buffer()
+    t_tol, sep_tol = (TIME_TOL_FAST, 1e-8) if engine == "stepped" else (TIME_TOL, 1e-12)
     assert np.array_equal(buf[:, 1:3], gold[:, 1:3])
-    assert np.allclose(buf[:, 0], gold[:, 0], rtol=TIME_TOL, atol=0)
-    assert np.allclose(buf[:, 3], gold[:, 3], rtol=1e-12, atol=0)
-    assert abs(t - ref["t"]) <= TIME_TOL * ref["t"]
+    assert np.allclose(buf[:, 0], gold[:, 0], rtol=t_tol, atol=0)
+    assert np.allclose(buf[:, 3], gold[:, 3], rtol=sep_tol, atol=0)
+    assert abs(t - ref["t"]) <= t_tol * ref["t"]
 
 
 def test_stepped_engine_matches_persistent_engine(clib):
