@@ -41,6 +41,7 @@ int force_scratch_reserve(ForceScratch &s, size_t n)
     ABIE_CUDA(cudaMalloc(&s.src_body, cap * sizeof(int)));
     ABIE_CUDA(cudaMalloc(&s.n_src, sizeof(int)));
     ABIE_CUDA(cudaMalloc(&s.next, sizeof(unsigned int)));
+    ABIE_CUDA(cudaMalloc(&s.counts, ((cap + 2047) / 2048) * sizeof(int)));
     s.cap = cap;
     return 0;
 }
@@ -53,6 +54,7 @@ void force_scratch_free(ForceScratch &s)
     if (s.partial) cudaFree(s.partial);
     if (s.gm_max) cudaFree(s.gm_max);
     if (s.next) cudaFree(s.next);
+    if (s.counts) cudaFree(s.counts);
     s = ForceScratch();
 }
 
@@ -104,6 +106,88 @@ int launch_compact_sources(const double *pos, const double *m, int n, double G, 
                            int *src_body, int *n_src, cudaStream_t st)
 {
     compact_sources_kernel<<<1, 1024, 0, st>>>(pos, m, n, G, src, src_body, n_src);
+    ABIE_CUDA(cudaGetLastError());
+    return 0;
+}
+
+// Parallel form: chunks of CCH bodies, one block each.  Pass 1 counts the
+// massive bodies of every chunk; pass 2 gives each block its offset (the
+// sum of the earlier chunks' counts) and compacts its chunk in order, so
+// the list equals compact_sources_kernel's.
+constexpr int CCH = 2048;
+
+__device__ __forceinline__ int block_sum_256(int v, int *ws)
+{
+    v = __reduce_add_sync(0xffffffffu, v);
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = v;
+    __syncthreads();
+    int t = 0;
+#pragma unroll
+    for (int w = 0; w < 8; w++) t += ws[w];
+    __syncthreads();
+    return t;
+}
+
+__global__ void __launch_bounds__(256) count_sources_kernel(const double *__restrict__ m, int n,
+                                                            int *__restrict__ counts)
+{
+    __shared__ int ws[8];
+    const int base = blockIdx.x * CCH, end = min(n, base + CCH);
+    int c = 0;
+    for (int i = base + threadIdx.x; i < end; i += 256) c += m[i] > 0.0 ? 1 : 0;
+    c = block_sum_256(c, ws);
+    if (threadIdx.x == 0) counts[blockIdx.x] = c;
+}
+
+__global__ void __launch_bounds__(256) scatter_sources_kernel(const double *__restrict__ pos,
+                                                              const double *__restrict__ m, int n,
+                                                              double G, const int *__restrict__ counts,
+                                                              Src *__restrict__ src,
+                                                              int *__restrict__ src_body,
+                                                              int *__restrict__ n_src)
+{
+    __shared__ int ws[8];
+    __shared__ int wc[8];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int part = 0;
+    for (int b = threadIdx.x; b < (int)blockIdx.x; b += 256) part += counts[b];
+    int base = block_sum_256(part, ws);
+    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) *n_src = base + counts[blockIdx.x];
+    const int start = blockIdx.x * CCH, end = min(n, start + CCH);
+    for (int off = start; off < end; off += 256) {
+        const int i = off + threadIdx.x;
+        const bool keep = i < end && m[i] > 0.0;
+        const unsigned ballot = __ballot_sync(0xffffffffu, keep);
+        if (lane == 0) wc[warp] = __popc(ballot);
+        __syncthreads();
+        int before = 0, tot = 0;
+#pragma unroll
+        for (int w = 0; w < 8; w++) {
+            before += w < warp ? wc[w] : 0;
+            tot += wc[w];
+        }
+        if (keep) {
+            const int slot = base + before + __popc(ballot & ((1u << lane) - 1u));
+            Src s;
+            s.x = pos[3 * i];
+            s.y = pos[3 * i + 1];
+            s.z = pos[3 * i + 2];
+            s.gm = G * m[i];
+            src[slot] = s;
+            src_body[slot] = i;
+        }
+        base += tot;
+        __syncthreads();
+    }
+}
+
+int launch_compact_sources_parallel(const double *pos, const double *m, int n, double G, Src *src,
+                                    int *src_body, int *n_src, int *counts, cudaStream_t st)
+{
+    if (n <= 4096 || !counts) return launch_compact_sources(pos, m, n, G, src, src_body, n_src, st);
+    const int nb = (n + CCH - 1) / CCH;
+    count_sources_kernel<<<nb, 256, 0, st>>>(m, n, counts);
+    scatter_sources_kernel<<<nb, 256, 0, st>>>(pos, m, n, G, counts, src, src_body, n_src);
     ABIE_CUDA(cudaGetLastError());
     return 0;
 }
@@ -341,7 +425,7 @@ int launch_force(int mode, const double *pos, const double *m, int n, double G, 
     }
     int rc = force_scratch_reserve(s, (size_t)n);
     if (rc) return rc;
-    rc = launch_compact_sources(pos, m, n, G, s.src, s.src_body, s.n_src, st);
+    rc = launch_compact_sources_parallel(pos, m, n, G, s.src, s.src_body, s.n_src, s.counts, st);
     if (rc) return rc;
     if (mode == ABIE_FORCE_EXACT) {
         force_exact_kernel<<<(n + 255) / 256, 256, 0, st>>>(pos, m, n, s.src, s.src_body, s.n_src,

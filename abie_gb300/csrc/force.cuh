@@ -14,6 +14,7 @@ struct ForceScratch {
     double *partial = nullptr;  // per (sink, source chunk) partial sums, 3 doubles each
     unsigned long long *gm_max = nullptr;  // mixed form: largest G m (as ordered bits)
     unsigned int *next = nullptr;          // fp64 form: next sink to hand out
+    int *counts = nullptr;      // parallel compaction: massive bodies per chunk
     size_t cap = 0;             // bodies
     size_t partial_cap = 0;     // doubles
 };
@@ -25,6 +26,10 @@ void force_scratch_free(ForceScratch &s);
 // only positive masses act as sources).
 int launch_compact_sources(const double *pos, const double *m, int n, double G, Src *src,
                            int *src_body, int *n_src, cudaStream_t st);
+// The same list built by many blocks (a count pass and a scatter pass),
+// for n above a few thousand bodies; counts holds one int per 2,048 bodies.
+int launch_compact_sources_parallel(const double *pos, const double *m, int n, double G, Src *src,
+                                    int *src_body, int *n_src, int *counts, cudaStream_t st);
 
 // acc[3j..3j+2] for every sink j in [0, n).  Sinks with m < 0 are skipped
 // (their entries are not written), as in src/common.c:173-176.
