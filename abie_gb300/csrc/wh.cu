@@ -33,7 +33,7 @@ struct WhShared {
     double a2[3];         // accel2 carried past the head
     double ind_a2[3];     // ind + a2 (the fast form adds them once)
     double gm_tail;       // Kepler parameter of a massless body
-    double gm_tail_k[3];  // sqrt(gm_tail), 1/gm_tail, 1/sqrt(gm_tail)
+    double gm_tail_k[4];  // sqrt(gm_tail), 1/gm_tail, 1/sqrt(gm_tail), sqrt(gm_tail) dt
     unsigned long long kepler_failures;
 };
 
@@ -200,25 +200,39 @@ __device__ __forceinline__ void stumpff_series_short(double psi, double &c2, dou
 //    sqrt, and sqrt(gm), 1/gm, 1/sqrt(gm) precomputed (k[0..2]).
 // The converged chi is the same root; the state agrees with the reference
 // form to rounding.  Distances must lie within the FP32 exponent range.
-__device__ int kepler_drift_fast(double r0v[3], double v0v[3], double gm, const double k[3],
+// Comparisons on the bit patterns of doubles, with integer instructions
+// (an FP64 compare holds the FP64 pipe like any FP64 instruction): |x| < t
+// and x > t for a positive threshold t, x < t for a negative one.  NaN
+// compares like a large magnitude; the callers' NaN states fail the
+// convergence test either way.
+__device__ __forceinline__ unsigned long long dmag(double x)
+{
+    return (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
+}
+__device__ __forceinline__ bool dneg(double x) { return __double_as_longlong(x) < 0; }
+__device__ __forceinline__ bool abs_lt(double x, double t) { return dmag(x) < dmag(t); }
+__device__ __forceinline__ bool abs_le(double x, double t) { return dmag(x) <= dmag(t); }
+__device__ __forceinline__ bool gt_pos(double x, double t) { return !dneg(x) && dmag(x) > dmag(t); }
+__device__ __forceinline__ bool lt_neg(double x, double t) { return dneg(x) && dmag(x) > dmag(t); }
+
+__device__ int kepler_drift_fast(double r0v[3], double v0v[3], double gm, const double k[4],
                                  double dt, double dt2_6)
 {
-    const double sqrtgm = k[0], igm = k[1], isqrtgm = k[2];
+    const double sqrtgm = k[0], igm = k[1], isqrtgm = k[2], sgdt = k[3];
     const double r02 = fma(r0v[2], r0v[2], fma(r0v[1], r0v[1], r0v[0] * r0v[0]));
     const double v02 = fma(v0v[2], v0v[2], fma(v0v[1], v0v[1], v0v[0] * v0v[0]));
     const double ir0 = inv_sqrt_fast(r02);
     const double r0 = r02 * ir0;
-    const double xi = fma(0.5, v02, -gm * ir0);
-    const double alpha = -2.0 * xi * igm;
+    const double gmir0 = gm * ir0;
+    const double alpha = fma(-v02, igm, ir0 + ir0);  // -2 xi / gm, xi = v0^2 / 2 - gm / r0
     const double rv = fma(r0v[2], v0v[2], fma(r0v[1], v0v[1], r0v[0] * v0v[0]));
     double chi0;
-    const double sgdt = sqrtgm * dt;
     const double w1 = sgdt * ir0;  // first-order arc
-    if (alpha > TOL_ENERGY && w1 * w1 * alpha < 0.1) {
+    if (gt_pos(alpha, 0.0) && abs_lt(w1 * w1 * alpha, 0.1)) {
         const double ir02 = ir0 * ir0;
         const double u = rv * ir02;                       // rdot / r
         const double w2 = -0.5 * u * dt;                  // second-order factor
-        const double w3 = (v02 - gm * ir0) * ir02 - 3.0 * u * u;
+        const double w3 = fma(v02 - gmir0, ir02, -3.0 * u * u);
         chi0 = w1 * fma(dt2_6, -w3, 1.0 + w2);
     } else if (alpha > TOL_ENERGY) {
         chi0 = sqrtgm * dt * alpha;
@@ -241,9 +255,9 @@ __device__ int kepler_drift_fast(double r0v[3], double v0v[3], double gm, const 
     for (int it = 0; it < KEPLER_MAX_IT; it++) {
         const double chi2 = chi0 * chi0;
         psi = chi2 * alpha;
-        if (psi > 1.e-10 || psi < -1.e-6) {
-            if (fabs(psi) <= 0.01) stumpff_series_short(psi, c2, c3);
-            else if (fabs(psi) <= 0.5) stumpff_series(psi, c2, c3);
+        if (gt_pos(psi, 1.e-10) || lt_neg(psi, -1.e-6)) {
+            if (abs_le(psi, 0.01)) stumpff_series_short(psi, c2, c3);
+            else if (abs_le(psi, 0.5)) stumpff_series(psi, c2, c3);
             else stumpff(psi, c2, c3);
         } else {
             c2 = 0.5;
@@ -254,10 +268,10 @@ __device__ int kepler_drift_fast(double r0v[3], double v0v[3], double gm, const 
         // sgdt - chi^3 c3 - rvs chi^2 c2 - r0 chi s3, nested
         const double num = fma(-chi0, fma(chi0, fma(chi0, c3, rvs * c2), r0 * s3), sgdt);
         chi = fma(num, rcp_fast(r), chi0);
-        if (fabs(chi - chi0) < KEPLER_TOL) break;
+        if (abs_lt(chi - chi0, KEPLER_TOL)) break;
         chi0 = chi;
     }
-    int failed = fabs(chi - chi0) > KEPLER_TOL;
+    int failed = !abs_le(chi - chi0, KEPLER_TOL);
     const double chi2 = chi * chi;
     const double f = fma(-chi2 * ir0, c2, 1.0);
     const double g = fma(-chi2 * chi * isqrtgm, c3, dt);
@@ -335,6 +349,7 @@ __global__ void __launch_bounds__(256) wh_head_kernel(WhArgs a, int init, int pa
             sh->gm_tail_k[0] = sqrt(gmt);
             sh->gm_tail_k[1] = 1.0 / gmt;
             sh->gm_tail_k[2] = 1.0 / sqrt(gmt);
+            sh->gm_tail_k[3] = sqrt(gmt) * a.dt;
         }
         // helio -> Jacobi for the head (:221-280)
         double *jp = a.jpos, *jv = a.jvel;
@@ -381,7 +396,7 @@ __global__ void __launch_bounds__(256) wh_head_kernel(WhArgs a, int init, int pa
                 failed = kepler_drift(r, v, a.gm[i], dt);
             } else {
                 const double sg = sqrt(a.gm[i]);
-                const double k[3] = {sg, 1.0 / a.gm[i], 1.0 / sg};
+                const double k[4] = {sg, 1.0 / a.gm[i], 1.0 / sg, sg * dt};
                 failed = kepler_drift_fast(r, v, a.gm[i], k, dt, a.dt2_6);
             }
             if (failed) atomicAdd(&sh->kepler_failures, 1ull);
