@@ -352,7 +352,9 @@ __device__ __forceinline__ void group_force(const Group<W> &grp, int n, const do
         const double xi = sp[g][0], yi = sp[g][1], zi = sp[g][2];
         for (int k = hh; k < n; k += L) {
             double gm = sp[k][3];
-            if (k == g || !(gm > 0.0)) continue;
+            // gm > 0 on its bit pattern (an FP64 compare would hold the
+            // FP64 pipe like a seventh instruction of the pair term)
+            if (k == g || __double_as_longlong(gm) <= 0) continue;
             Src s{sp[k][0], sp[k][1], sp[k][2], gm};
             if (MODE == ABIE_FORCE_EXACT) pair_exact(xi, yi, zi, s, ax, ay, az);
             else pair_fast(xi, yi, zi, s, ax, ay, az);
