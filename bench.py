@@ -162,6 +162,75 @@ def cpu_force_rate(p, m, threads, sinks=None, reps=1):
     return inter / dt / 1e9, dt, inter
 
 
+def _ensemble_cpu_chunk(job):
+    """Oracle Radau15 (the reference's algorithm and predictor) over systems
+    lo..hi-1 of the ensemble; returns accepted steps.  A spawn-pool worker."""
+    lo, hi, seed0, years = job
+    from oracle import Oracle
+    O = Oracle()
+    P, V, M, offs = ics.ensemble(n_systems=hi - lo, seed0=seed0 + lo)
+    steps = 0
+    for s in range(offs.size - 1):
+        a, b = offs[s], offs[s + 1]
+        res = O.radau15(P[3 * a:3 * b], V[3 * a:3 * b], M[a:b], np.zeros(b - a), G, 0.0, years)
+        steps += res["stats"]["accepts"]
+    return steps
+
+
+def cpu_baselines_extras(args, extra):
+    """The reference's algorithms (the oracle) on the host cores beside each
+    sub-measurement: bounded samples of the same workloads."""
+    import multiprocessing as mp
+    from oracle import Oracle
+    O = Oracle()
+    cores = os.cpu_count() or 1
+    if "ensemble" in extra:
+        ns, years = args.ensemble_systems, args.ensemble_years
+        seed0 = D.ensemble_seed0(10000, 0, ns)
+        per = max(1, (ns + 4 * cores - 1) // (4 * cores))
+        jobs = [(lo, min(ns, lo + per), seed0, years) for lo in range(0, ns, per)]
+        from concurrent.futures import ProcessPoolExecutor
+        try:
+            # spawned workers (this process has used the GPU); a worker that
+            # dies raises here instead of hanging the pool
+            with ProcessPoolExecutor(cores, mp_context=mp.get_context("spawn")) as pool:
+                list(pool.map(_ensemble_cpu_chunk, [(0, 1, seed0, 0.01)] * cores))  # start them
+                t0 = time.perf_counter()
+                steps = sum(pool.map(_ensemble_cpu_chunk, jobs))
+                dt = time.perf_counter() - t0
+            extra["ensemble"]["cpu_baseline"] = {
+                "value": steps / dt, "unit": "system-steps/s", "cores": cores, "kind": "port",
+                "sample": "all %d systems over %.2f yr, one process per core (oracle orc_radau15, "
+                          "the reference's operations and predictor)" % (ns, years),
+                "system_steps": int(steps), "seconds": dt}
+        except Exception as exc:  # reported, not fatal: the GPU figures stand alone
+            extra["ensemble"]["cpu_baseline"] = {"unavailable": "%s: %s" % (type(exc).__name__, exc)}
+    if "wh" in extra:
+        out = {}
+        for n_tp in (1024, 4096):
+            p, v, m, r = ics.test_particle_swarm(n_tp=n_tp)
+            p, v = ics.to_heliocentric(p, v)
+            steps = 10
+            t0 = time.perf_counter()
+            O.wh(p, v, m, G, 0.0, steps * 0.01 - 1e-9, 0.01, sparse=False)
+            out["ms_per_step_%d_particles" % n_tp] = 1e3 * (time.perf_counter() - t0) / steps
+        extra["wh"]["cpu_baseline"] = dict(out, cores=1, kind="port",
+                                           sample="10 steps of swarms of 1,024 and 4,096 "
+                                                  "particles from the same generator (the star and "
+                                                  "5 planets; oracle orc_wh with the reference's "
+                                                  "O(N^2) accelerations)")
+    if "radau_1009" in extra:
+        p, v, m, r = ics.planetary_system()
+        t0 = time.perf_counter()
+        res = O.radau15(p, v, m, r, G, 0.0, 0.2)
+        dt = time.perf_counter() - t0
+        att = res["stats"]["attempts"]
+        extra["radau_1009"]["cpu_baseline"] = {
+            "ms_per_attempt": 1e3 * dt / max(att, 1), "attempts": int(att), "seconds": dt,
+            "cores": 1, "kind": "port",
+            "sample": "0.2 yr of the same system (oracle orc_radau15, the reference's operations)"}
+
+
 def run_reference(args):
     rank, world, local = dist_env()
     if rank != 0:
@@ -343,6 +412,8 @@ def run_ours(args):
             "gpu_launches": 2 * args.steps,
             "peaks_measured": peaks,
         }
+        if not args.no_cpu_baseline and extra:
+            cpu_baselines_extras(args, extra)
         line.update(extra)
         print(json.dumps(line), flush=True)
     if world > 1:
