@@ -76,3 +76,24 @@ def test_snapshot_capacity_and_arguments(sim):
         sim.integrate_snapshots(0.0, 1.0, 0.1, primary=m.size)
     with pytest.raises(AbieError):
         sim.integrate_snapshots(0.0, 1.0, 0.1, integrator="wh", h=0.0)
+
+
+def test_snapshots_stop_at_an_event(sim):
+    """A close encounter ends the run after its chunk's snapshot, with the
+    integrator's flag (the caller handles the event, then continues)."""
+    from test_radau_gpu import _threshold_pairs
+    ce = 0.01
+    p, v, m, r = _threshold_pairs(ce)
+    sim.set_close_encounter_distance(ce)
+    sim.reset_close_encounter_buffer()
+    sim.reset_collision_buffer()
+    try:
+        sim.set_state(p, v, m, r, m.size, G, 0.0)
+        out = sim.integrate_snapshots(0.0, 1.0, 0.25)
+    finally:
+        sim.set_close_encounter_distance(0.0)
+        sim.reset_close_encounter_buffer()
+        sim.reset_collision_buffer()
+    assert out["flag"] == 1
+    assert len(out["t"]) == 1 and 0.0 < out["t"][0] < 0.25  # inside the first chunk
+    assert out["t"][0] == sim.get_model_time()
