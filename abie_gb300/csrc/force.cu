@@ -7,10 +7,11 @@
 //           sink and splits its sources; partial sums meet in a fixed
 //           butterfly of warp shuffles, so results are deterministic.  The
 //           pair term is pair_fast() (6 FP64 operations per interaction).
-//           Sinks are handed out to lane groups from an atomic counter, so
-//           the grid has no tail of idle SMs.
-//           Sources can also be split into chunks whose partial sums are
-//           added in chunk order by a second pass, to balance the grid.
+//           Below 8,192 sinks, sinks are handed out to lane groups from an
+//           atomic counter (force_fp64_dyn_kernel); from 8,192 sinks each
+//           sink's sources split into two chunks, one lane group per (sink,
+//           chunk) on a static grid (force_fp64_kernel), and a second pass
+//           adds the chunks' partial sums in chunk order.
 //   naive : one thread per sink over global memory with rsqrt, the
 //           semantics of the reference's GPU offload (src/gpuforce.cu:61-84):
 //           sources with m == 0 and coincident pairs are skipped, sinks and
@@ -220,8 +221,19 @@ __global__ void __launch_bounds__(256) force_exact_kernel(const double *__restri
 // ---------------------------------------------------------------------------
 // fp64
 // ---------------------------------------------------------------------------
+// Tuning knobs of the chunked form: blocks per SM the registers are sized
+// for, sources per loop iteration.  Measured on the 16,385- and 32,769-body
+// disks with 32 lanes per sink and 2 source chunks (Gint/s): (1, 4) 85.3 /
+// 86.7, (3, 2) 87.7 / 89.2, (4, 2) 90.5 / 92.1, (5, 2) 91.6 / 93.2, (4, 4)
+// 91.9 / 93.4 (kept: 64 registers, 32 warps per SM).
+#ifndef ABIE_FORCE_S_MINB
+#define ABIE_FORCE_S_MINB 4
+#endif
+#ifndef ABIE_FORCE_S_UNROLL
+#define ABIE_FORCE_S_UNROLL 4
+#endif
 template <int JS>
-__global__ void __launch_bounds__(256) force_fp64_kernel(const double *__restrict__ pos,
+__global__ void __launch_bounds__(256, ABIE_FORCE_S_MINB) force_fp64_kernel(const double *__restrict__ pos,
                                                          const double *__restrict__ m, int n,
                                                          const Src *__restrict__ src,
                                                          const int *__restrict__ n_src_p,
@@ -243,13 +255,14 @@ __global__ void __launch_bounds__(256) force_fp64_kernel(const double *__restric
     if (live) {
         const double xj = pos[3 * j], yj = pos[3 * j + 1], zj = pos[3 * j + 2];
         int q = q0 + lane;
+        constexpr int U = ABIE_FORCE_S_UNROLL;
 #pragma unroll 1
-        for (; q + 3 * JS < q1; q += 4 * JS) {
-            Src s0 = src[q], s1 = src[q + JS], s2 = src[q + 2 * JS], s3 = src[q + 3 * JS];
-            pair_fast(xj, yj, zj, s0, ax, ay, az);
-            pair_fast(xj, yj, zj, s1, ax, ay, az);
-            pair_fast(xj, yj, zj, s2, ax, ay, az);
-            pair_fast(xj, yj, zj, s3, ax, ay, az);
+        for (; q + (U - 1) * JS < q1; q += U * JS) {
+            Src sv[U];
+#pragma unroll
+            for (int u = 0; u < U; u++) sv[u] = src[q + u * JS];
+#pragma unroll
+            for (int u = 0; u < U; u++) pair_fast(xj, yj, zj, sv[u], ax, ay, az);
         }
         for (; q < q1; q += JS) pair_fast(xj, yj, zj, src[q], ax, ay, az);
     }
@@ -388,7 +401,12 @@ ForceShape force_shape_default(int n_sink, int n_src)
         return s;
     }
     s.lanes_per_sink = n_src <= 64 ? 1 : (n_src <= 1024 ? 8 : 32);
-    s.chunks = 1;
+    // from 8,192 sinks two source chunks per sink (partial sums added in
+    // chunk order): finer work items than the sink queue's and fewer idle
+    // SMs at the end; on the disks of 8,193 / 16,385 / 32,769 / 65,537
+    // bodies 85.3 / 91.7 / 93.2 / 94.0 Gint/s against 84.5 / 89.5 / 87.6 /
+    // 92.2 for one chunk from the sink queue
+    s.chunks = (s.lanes_per_sink == 32 && n_sink >= 8192) ? 2 : 1;
     return s;
 }
 

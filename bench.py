@@ -50,7 +50,16 @@ FLOP_PER_INTERACTION = 20  # the convention of the reference's tiled kernel comm
 FP64_INSTR_PER_INTERACTION = 6  # the fast form's pair term (abie_gb300/csrc/common.cuh pair_fast)
 # dram__bytes_read.sum + dram__bytes_write.sum of one force-kernel launch,
 # from the ncu capture summarised in profiles/force_fp64_disk16385.md.
-DRAM_BYTES_PER_LAUNCH = {("fp64", 16385): 1074688}
+DRAM_BYTES_PER_LAUNCH = {("fp64", 16385): 945920}
+
+
+def launches_per_force_call(m):
+    """Kernels of one fast FP64 force call (abie_gb300/csrc/force.cu): the
+    source compaction (one block, or a count and a scatter pass above 4,096
+    bodies), the force kernel, and from 8,192 sinks with more than 1,024
+    sources the pass that adds the two source chunks."""
+    n, n_src = int(m.size), int((m > 0).sum())
+    return (2 if n > 4096 else 1) + 1 + (1 if (n_src > 1024 and n >= 8192) else 0)
 
 
 def parse():
@@ -409,7 +418,7 @@ def run_ours(args):
                     "d2h_bytes_per_step": int(8 * p.size),
                     "entry_point": "ode_n_body_second_order (host arrays, pinned)"},
             "clocks": clk,
-            "gpu_launches": 2 * args.steps,
+            "gpu_launches": launches_per_force_call(m) * args.steps,
             "peaks_measured": peaks,
         }
         if not args.no_cpu_baseline and extra:
