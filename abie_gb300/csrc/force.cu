@@ -412,9 +412,18 @@ ForceShape force_shape_default(int n_sink, int n_src)
 
 int launch_force_published(const double *pos, const double *m, int n, const Src *src,
                            const int *n_src_dev, int lanes, double *acc, unsigned int *next,
-                           cudaStream_t st)
+                           cudaStream_t st, double *partial)
 {
     if (n <= 0) return 0;
+    if (partial && lanes == 32) {
+        // two source chunks per sink on a static grid, then the chunk sum
+        const long long groups = 2ll * n;
+        const int blocks = (int)((groups + 7) / 8);
+        force_fp64_kernel<32><<<blocks, 256, 0, st>>>(pos, m, n, src, n_src_dev, 2, acc, partial);
+        sum_chunks_kernel<<<(n + 255) / 256, 256, 0, st>>>(partial, m, n, 2, acc);
+        ABIE_CUDA(cudaGetLastError());
+        return 0;
+    }
     int dev = 0, sms = 152, bps = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);

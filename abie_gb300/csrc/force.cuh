@@ -40,10 +40,12 @@ int launch_force(int mode, const double *pos, const double *m, int n, double G,
 // (*n_src_dev records, e.g. the Radau15 engine's published substep), with
 // lanes (1, 8 or 32) per sink and sinks handed out from the counter next
 // (zeroed here): the same sums, in the same order, as the persistent
-// engine's sink loop with that many lanes per body.
+// engine's sink loop with that many lanes per body.  With 32 lanes and a
+// partial-sum buffer (6 n doubles) each sink's sources split in two chunks
+// instead (the standalone force's form from 8,192 sinks).
 int launch_force_published(const double *pos, const double *m, int n, const Src *src,
                            const int *n_src_dev, int lanes, double *acc, unsigned int *next,
-                           cudaStream_t st);
+                           cudaStream_t st, double *partial = nullptr);
 
 // Fast FP64 force with caller-provided scratch (src / src_body sized for n
 // entries, n_src one int); allocates nothing.  Uses one source chunk.

@@ -25,8 +25,8 @@
 // grid barrier per substep), the persistent engine (radau_engine), and,
 // from 2^20 interactions per force evaluation in the fast form without
 // post-Newtonian terms, the stepped engine (st_* kernels driven from the
-// host, the standalone force kernel for every substep), which gives the
-// persistent engine's doubles.
+// host, the standalone force kernel for every substep), which below 8,192
+// bodies gives the persistent engine's doubles.
 #include <stdio.h>
 
 #include <algorithm>
@@ -1226,6 +1226,8 @@ struct EngineBuffers {
     size_t src_n = 0;
     EngineCtl *ctl = nullptr;
     EventRec *ev = nullptr;
+    double *partial = nullptr;  // stepped engine: two source chunks' partial sums (6 per body)
+    size_t partial_n = 0;
     double *d_ce = nullptr, *d_coll = nullptr;
     size_t d_ce_n = 0, d_coll_n = 0;
 };
@@ -1246,6 +1248,7 @@ void free_engine_buffers()
     if (e.ev) cudaFree(e.ev);
     if (e.d_ce) cudaFree(e.d_ce);
     if (e.d_coll) cudaFree(e.d_coll);
+    if (e.partial) cudaFree(e.partial);
     e = EngineBuffers();
 }
 
@@ -1292,8 +1295,10 @@ static int engine_reserve(size_t n, size_t max_ce, size_t max_coll)
 // warps per SM busy on the FP64 pipe where the persistent engine, holding
 // the whole sweep in registers, keeps 16.  The per-component device
 // functions, the force sums (the engine's order for the same lanes per
-// body) and the scalar step control (one thread, the engine's expressions)
-// are the persistent engine's, so both give the same trajectory.  The host
+// body, below 8,192 bodies; two source chunks from there, as the
+// standalone force) and the scalar step control (one thread, the engine's
+// expressions) are the persistent engine's, so below 8,192 bodies both
+// give the same trajectory.  The host
 // reads two maxima per corrector iteration and the controller's decision
 // per attempt.
 
@@ -1525,13 +1530,28 @@ static int stepped_run(const EngineArgs &a, int num_sms, cudaStream_t st, Engine
     const int blocks = (int)std::max<long long>(1, std::min<long long>(((long long)a.dim + threads - 1) / threads,
                                                                        (long long)num_sms * 8));
     long long force_calls = 0, iterations = 0, attempts = 0;
-    // lanes per sink as the standalone force picks them (force_shape_default)
+    // lanes per sink and source chunks as the standalone force picks them
+    // (force_shape_default): from 8,192 sinks two chunks, whose order of
+    // sums differs from the persistent engine's
     const int lanes = a.n_src <= 64 ? 1 : (a.n_src <= 1024 ? 8 : 32);
+    double *partial = nullptr;
+    if (lanes == 32 && a.n >= 8192) {
+        EngineBuffers &e = g_eb;
+        if ((size_t)a.n > e.partial_n) {
+            if (e.partial) cudaFree(e.partial);
+            e.partial = nullptr;
+            e.partial_n = 0;
+            ABIE_CUDA(cudaMalloc(&e.partial, 6 * (size_t)a.n * sizeof(double)));
+            e.partial_n = (size_t)a.n;
+        }
+        partial = e.partial;
+    }
     auto force = [&](int buf) {
         const double *pos = buf < 2 ? a.yp[buf] : a.ypa;
         const Src *src = buf < 2 ? a.src[buf] : a.srca;
         force_calls++;
-        return launch_force_published(pos, a.m, a.n, src, &ctl->n_src, lanes, acc, &ctl->next_sink, st);
+        return launch_force_published(pos, a.m, a.n, src, &ctl->n_src, lanes, acc, &ctl->next_sink, st,
+                                      partial);
     };
     unsigned long long hk[2];
     auto read_keys = [&](double &v0, double &v1) -> int {
