@@ -86,8 +86,12 @@ __device__ __forceinline__ double f32_to_f64_signed(float f)
 }
 
 // The core on r2 = Mr 2^Er, Mr a 64-bit significand with its top bit set
-// (or 0 for r2 = 0).
-__device__ __forceinline__ double gm_inv_r3_int(unsigned long long Mr, int Er, double gm)
+// (or 0 for r2 = 0), in two parts: r^-3 as a normalised 64-bit significand
+// Wn (top bit set) with exponent eW, then its product with G m, so that a
+// pair evaluated for both of its bodies (the symmetric force) shares the
+// first part.
+__device__ __forceinline__ void inv_r3_core(unsigned long long Mr, int Er, unsigned long long &Wn,
+                                            int &eW)
 {
     typedef unsigned long long ull;
     // seed: r2 truncated to 24 bits as a float, its rsqrtf cut to 21 bits
@@ -123,15 +127,29 @@ __device__ __forceinline__ double gm_inv_r3_int(unsigned long long Mr, int Er, d
     const ull m3 = m2 * m;                                // [2^60, 2^63)
     const ull W = __umul64hi(m3, F);                      // m^3 (1 + k) 2^-2
     const int lz = __clzll((long long)W);
-    const ull Wn = W << lz;
+    Wn = W << lz;
+    eW = 3 * E - lz;
+}
+
+__device__ __forceinline__ double gm_times_inv_r3(unsigned long long Wn, int eW, double gm)
+{
+    typedef unsigned long long ull;
     const ull gb = (ull)__double_as_longlong(gm);
     const int eg = (int)((gb >> 52) & 0x7FF);
     const ull Mg = (gb & 0xFFFFFFFFFFFFFull) | (1ull << 52);
     const ull Z = __umul64hi(Mg << 11, Wn);
     const int lz2 = __clzll((long long)Z);
     const ull Zn = Z << lz2;
-    const int be = min(max(eg + 3 * E - lz - lz2 + 66, 1), 2046);
+    const int be = min(max(eg + eW - lz2 + 66, 1), 2046);
     return __longlong_as_double((long long)(((ull)be << 52) | ((Zn >> 11) & 0xFFFFFFFFFFFFFull)));
+}
+
+__device__ __forceinline__ double gm_inv_r3_int(unsigned long long Mr, int Er, double gm)
+{
+    unsigned long long Wn;
+    int eW;
+    inv_r3_core(Mr, Er, Wn, eW);
+    return gm_times_inv_r3(Wn, eW, gm);
 }
 
 __device__ __forceinline__ double gm_inv_r3(double r2, double gm)

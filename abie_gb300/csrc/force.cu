@@ -18,6 +18,7 @@
 //           sources with m < 0 are not.
 //   mixed : in mixed.cu.
 #include <algorithm>
+#include <vector>
 
 #include "force.cuh"
 #include "pn.cuh"
@@ -56,6 +57,10 @@ void force_scratch_free(ForceScratch &s)
     if (s.gm_max) cudaFree(s.gm_max);
     if (s.next) cudaFree(s.next);
     if (s.counts) cudaFree(s.counts);
+    if (s.sym_items) cudaFree(s.sym_items);
+    if (s.sym_row) cudaFree(s.sym_row);
+    if (s.sym_apart) cudaFree(s.sym_apart);
+    if (s.sym_bpart) cudaFree(s.sym_bpart);
     s = ForceScratch();
 }
 
@@ -238,8 +243,11 @@ __global__ void __launch_bounds__(256, ABIE_FORCE_S_MINB) force_fp64_kernel(cons
                                                          const Src *__restrict__ src,
                                                          const int *__restrict__ n_src_p,
                                                          int chunks, double *__restrict__ acc,
-                                                         double *__restrict__ partial)
+                                                         double *__restrict__ partial,
+                                                         bool sym_launched = false)
 {
+    // the symmetric form took this call (every body massive)
+    if (sym_launched && *n_src_p == n) return;
     const int groups_per_block = 256 / JS;
     const long long group = (long long)blockIdx.x * groups_per_block + threadIdx.x / JS;
     const int lane = threadIdx.x % JS;
@@ -347,9 +355,175 @@ __global__ void __launch_bounds__(256, ABIE_FORCE_MINB) force_fp64_dyn_kernel(co
     (void)gl;
 }
 
-__global__ void sum_chunks_kernel(const double *__restrict__ partial, const double *__restrict__ m,
-                                  int n, int chunks, double *__restrict__ acc)
+// ---------------------------------------------------------------------------
+// Symmetric form, for systems whose bodies are all massive (from 8,192
+// bodies): every unordered pair is evaluated once, for both of its bodies.
+// The separation, r^2 and r^-3 are shared; the two G m r^-3 factors differ
+// only in the mass (inv_r3_core once, gm_times_inv_r3 twice), so a pair
+// costs 3 separations and 6 accumulating FMAs: 4.5 FP64 instructions per
+// interaction against 6, and half the integer work.
+//
+// Bodies are tiled by 32.  A warp takes a work item -- tile I (its lanes'
+// sinks) and SYM_K source tiles J >= I -- from an atomic counter, stages
+// each source tile in shared memory and walks it as a ring: at step s lane
+// t pairs sink 32 I + t with body 32 J + (t + s) % 32, adds the sink's term
+// to its own sum and the body's to a ring sum that moves one lane down per
+// step, so after 32 steps lane t holds the sum for body 32 J + t.  The
+// diagonal tile (J = I) is summed one way only.  Each item writes its
+// sinks' partial sums and one partial sum per source tile; a second pass
+// adds, for every body, the partials of its own row's items and of the
+// items of the rows above that hold its tile, in a fixed order.
+#ifndef ABIE_SYM_K
+#define ABIE_SYM_K 2
+#endif
+#ifndef ABIE_SYM_MINB
+#define ABIE_SYM_MINB 4
+#endif
+#ifndef ABIE_SYM_UNROLL
+#define ABIE_SYM_UNROLL 2
+#endif
+constexpr int SYM_K = ABIE_SYM_K;  // source tiles per work item
+constexpr int SYM_UNROLL = ABIE_SYM_UNROLL;  // ring steps per loop iteration
+// Partial sums take n^2 / 32 x 12 bytes (6.4 GB at 131,072 bodies); above
+// that the chunked form runs.
+constexpr int SYM_MAX_BODIES = 131072;
+
+__global__ void __launch_bounds__(256, ABIE_SYM_MINB) force_sym_kernel(const Src *__restrict__ src, int n,
+                                                           const int2 *__restrict__ items, int n_items,
+                                                           int nt, double *__restrict__ apart,
+                                                           double *__restrict__ bpart,
+                                                           unsigned int *__restrict__ next,
+                                                           const int *__restrict__ n_src_p)
 {
+    __shared__ double tile[8][32][4];  // one staged source tile per warp
+    if (*n_src_p != n) return;  // some body is not massive: the chunked form runs instead
+    const int lane = threadIdx.x & 31;
+    double(*T)[4] = tile[threadIdx.x >> 5];
+    for (;;) {
+        int it = 0;
+        if (lane == 0) it = (int)atomicAdd(next, 1u);
+        it = __shfl_sync(0xffffffffu, it, 0);
+        if (it >= n_items) break;
+        const int2 item = items[it];
+        const int I = item.x, J0 = item.y, J1 = min(nt, J0 + SYM_K);
+        const int i = 32 * I + lane;
+        const bool vi = i < n;
+        const Src si = vi ? src[i] : Src{0.0, 0.0, 0.0, 1.0};
+        double ax = 0.0, ay = 0.0, az = 0.0;
+        for (int J = J0; J < J1; J++) {
+            const int j = 32 * J + lane;
+            const bool vj = j < n;
+            const Src sj = vj ? src[j] : Src{0.0, 0.0, 0.0, 0.0};
+            __syncwarp();
+            T[lane][0] = sj.x;
+            T[lane][1] = sj.y;
+            T[lane][2] = sj.z;
+            T[lane][3] = sj.gm;  // 0 for a missing body: no term
+            __syncwarp();
+            if (J == I) {
+#pragma unroll 1
+                for (int s = 1; s < 32; s++) {
+                    const int k = (lane + s) & 31;
+                    const double gmk = T[k][3];
+                    const double dx = si.x - T[k][0], dy = si.y - T[k][1], dz = si.z - T[k][2];
+                    unsigned long long Mr, Wn;
+                    int Er, eW;
+                    r2_int(dx, dy, dz, Mr, Er);
+                    inv_r3_core(Mr, Er, Wn, eW);
+                    const double wi = __double_as_longlong(gmk) > 0 ? gm_times_inv_r3(Wn, eW, gmk) : 0.0;
+                    ax = fma(-wi, dx, ax);
+                    ay = fma(-wi, dy, ay);
+                    az = fma(-wi, dz, az);
+                }
+            } else {
+                double bx = 0.0, by = 0.0, bz = 0.0;
+#pragma unroll SYM_UNROLL
+                for (int s = 0; s < 32; s++) {
+                    const int k = (lane + s) & 31;
+                    const double gmk = T[k][3];
+                    const double dx = si.x - T[k][0], dy = si.y - T[k][1], dz = si.z - T[k][2];
+                    unsigned long long Mr, Wn;
+                    int Er, eW;
+                    r2_int(dx, dy, dz, Mr, Er);
+                    inv_r3_core(Mr, Er, Wn, eW);
+                    const double wi = __double_as_longlong(gmk) > 0 ? gm_times_inv_r3(Wn, eW, gmk) : 0.0;
+                    const double wj = vi ? gm_times_inv_r3(Wn, eW, si.gm) : 0.0;
+                    ax = fma(-wi, dx, ax);
+                    ay = fma(-wi, dy, ay);
+                    az = fma(-wi, dz, az);
+                    bx = fma(wj, dx, bx);
+                    by = fma(wj, dy, by);
+                    bz = fma(wj, dz, bz);
+                    bx = __shfl_sync(0xffffffffu, bx, (lane + 1) & 31);
+                    by = __shfl_sync(0xffffffffu, by, (lane + 1) & 31);
+                    bz = __shfl_sync(0xffffffffu, bz, (lane + 1) & 31);
+                }
+                double *bp = bpart + (((long long)it * SYM_K + (J - J0)) * 32 + lane) * 3;
+                bp[0] = bx;
+                bp[1] = by;
+                bp[2] = bz;
+            }
+        }
+        double *ap = apart + ((long long)it * 32 + lane) * 3;
+        ap[0] = ax;
+        ap[1] = ay;
+        ap[2] = az;
+    }
+}
+
+// acc of the bodies of tile J (one block): their row's item partials and
+// the partials the rows above left for tile J, spread over the block's
+// SYM_RW warps (warp w takes every SYM_RW-th term) and the warps' sums
+// added in warp order, so the order is fixed.
+constexpr int SYM_RW = 32;
+__global__ void __launch_bounds__(32 * SYM_RW) sym_reduce_kernel(const double *__restrict__ apart,
+                                                         const double *__restrict__ bpart,
+                                                         const int *__restrict__ row_item, int n,
+                                                         double *__restrict__ acc,
+                                                         const int *__restrict__ n_src_p)
+{
+    __shared__ double part[SYM_RW][32][3];
+    if (*n_src_p != n) return;
+    const int J = blockIdx.x, t = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int a0 = row_item[J], na = row_item[J + 1] - a0;
+    double ax = 0.0, ay = 0.0, az = 0.0;
+    for (int k = w; k < na + J; k += SYM_RW) {
+        const double *p;
+        if (k < na) {
+            p = apart + ((long long)(a0 + k) * 32 + t) * 3;
+        } else {
+            const int I = k - na;
+            const int it = row_item[I] + (J - I) / SYM_K, jj = (J - I) % SYM_K;
+            p = bpart + (((long long)it * SYM_K + jj) * 32 + t) * 3;
+        }
+        ax += p[0];
+        ay += p[1];
+        az += p[2];
+    }
+    part[w][t][0] = ax;
+    part[w][t][1] = ay;
+    part[w][t][2] = az;
+    __syncthreads();
+    const int j = 32 * J + t;
+    if (w == 0 && j < n) {
+        double sx = part[0][t][0], sy = part[0][t][1], sz = part[0][t][2];
+#pragma unroll 8
+        for (int q = 1; q < SYM_RW; q++) {
+            sx += part[q][t][0];
+            sy += part[q][t][1];
+            sz += part[q][t][2];
+        }
+        acc[3 * j] = sx;
+        acc[3 * j + 1] = sy;
+        acc[3 * j + 2] = sz;
+    }
+}
+
+__global__ void sum_chunks_kernel(const double *__restrict__ partial, const double *__restrict__ m,
+                                  int n, int chunks, double *__restrict__ acc,
+                                  const int *__restrict__ n_src_p = nullptr)
+{
+    if (n_src_p && *n_src_p == n) return;  // the symmetric form took this call
     int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n || m[j] < 0.0) return;
     const double *p = partial + 3ll * j * chunks;
@@ -441,6 +615,43 @@ int launch_force_published(const double *pos, const double *m, int n, const Src 
     return 0;
 }
 
+bool force_shape_overridden() { return g_shape_override.lanes_per_sink > 0; }
+
+// Work items of the symmetric form for n bodies: row I, first source tile
+// J0, row by row; row_item[I] = the first item of row I.  Partial sums:
+// 32 x 3 per item (its sinks), 32 x 3 x SYM_K per item (its source tiles).
+int sym_reserve(ForceScratch &s, int n)
+{
+    if (s.sym_n == n && s.sym_items) return 0;
+    const int nt = (n + 31) / 32;
+    std::vector<int2> items;
+    std::vector<int> row(nt + 1);
+    for (int I = 0; I < nt; I++) {
+        row[I] = (int)items.size();
+        for (int J0 = I; J0 < nt; J0 += SYM_K) items.push_back(make_int2(I, J0));
+    }
+    row[nt] = (int)items.size();
+    if (s.sym_items) cudaFree(s.sym_items);
+    if (s.sym_row) cudaFree(s.sym_row);
+    if (s.sym_apart) cudaFree(s.sym_apart);
+    if (s.sym_bpart) cudaFree(s.sym_bpart);
+    s.sym_items = nullptr;
+    s.sym_row = nullptr;
+    s.sym_apart = s.sym_bpart = nullptr;
+    s.sym_n = 0;
+    const size_t ni = items.size();
+    ABIE_CUDA(cudaMalloc(&s.sym_items, ni * sizeof(int2)));
+    ABIE_CUDA(cudaMalloc(&s.sym_row, (nt + 1) * sizeof(int)));
+    ABIE_CUDA(cudaMalloc(&s.sym_apart, ni * 32 * 3 * sizeof(double)));
+    ABIE_CUDA(cudaMalloc(&s.sym_bpart, ni * SYM_K * 32 * 3 * sizeof(double)));
+    ABIE_CUDA(cudaMemcpy(s.sym_items, items.data(), ni * sizeof(int2), cudaMemcpyHostToDevice));
+    ABIE_CUDA(cudaMemcpy(s.sym_row, row.data(), (nt + 1) * sizeof(int), cudaMemcpyHostToDevice));
+    s.sym_n = n;
+    s.sym_nt = nt;
+    s.sym_items_n = (int)ni;
+    return 0;
+}
+
 int launch_force(int mode, const double *pos, const double *m, int n, double G, ForceScratch &s,
                  double *acc, cudaStream_t st)
 {
@@ -464,6 +675,28 @@ int launch_force(int mode, const double *pos, const double *m, int n, double G, 
     // fp64: the number of sources is on the device; the shape uses n as its
     // upper bound.
     ForceShape sh = force_shape_default(n, n);
+    bool sym = false;
+    if (sh.lanes_per_sink == 32 && sh.chunks == 2 && !force_shape_overridden() &&
+        n <= SYM_MAX_BODIES) {
+        // the symmetric form; its kernels (and the chunked ones below) see
+        // on the device whether every body is massive and only one of them
+        // does the work
+        int rc2 = sym_reserve(s, n);
+        if (rc2) return rc2;
+        int dev = 0, sms = 152, bps = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        ABIE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, force_sym_kernel, 256, 0));
+        const int blocks = (int)std::max<long long>(
+            1, std::min<long long>((long long)sms * std::max(bps, 1), ((long long)s.sym_items_n + 7) / 8));
+        ABIE_CUDA(cudaMemsetAsync(s.next, 0, sizeof(unsigned int), st));
+        force_sym_kernel<<<blocks, 256, 0, st>>>(s.src, n, s.sym_items, s.sym_items_n, s.sym_nt,
+                                                 s.sym_apart, s.sym_bpart, s.next, s.n_src);
+        sym_reduce_kernel<<<s.sym_nt, 32 * SYM_RW, 0, st>>>(s.sym_apart, s.sym_bpart, s.sym_row, n,
+                                                             acc, s.n_src);
+        ABIE_CUDA(cudaGetLastError());
+        sym = true;
+    }
     if (sh.chunks > 1) {
         size_t need = 3ull * (size_t)n * (size_t)sh.chunks;
         if (need > s.partial_cap) {
@@ -514,7 +747,7 @@ int launch_force(int mode, const double *pos, const double *m, int n, double G, 
         break;
     case 32:
         force_fp64_kernel<32><<<blocks, 256, 0, st>>>(pos, m, n, s.src, s.n_src, sh.chunks, acc,
-                                                      s.partial);
+                                                      s.partial, sym);
         break;
     default:
         set_error(ABIE_ERR_ARGUMENT, "lanes_per_sink must be 1, 8 or 32");
@@ -522,7 +755,8 @@ int launch_force(int mode, const double *pos, const double *m, int n, double G, 
     }
     ABIE_CUDA(cudaGetLastError());
     if (sh.chunks > 1) {
-        sum_chunks_kernel<<<(n + 255) / 256, 256, 0, st>>>(s.partial, m, n, sh.chunks, acc);
+        sum_chunks_kernel<<<(n + 255) / 256, 256, 0, st>>>(s.partial, m, n, sh.chunks, acc,
+                                                           sym ? s.n_src : nullptr);
         ABIE_CUDA(cudaGetLastError());
     }
     return 0;

@@ -15,6 +15,12 @@ struct ForceScratch {
     unsigned long long *gm_max = nullptr;  // mixed form: largest G m (as ordered bits)
     unsigned int *next = nullptr;          // fp64 form: next sink to hand out
     int *counts = nullptr;      // parallel compaction: massive bodies per chunk
+    // symmetric form (every body massive): work items, first item per row,
+    // partial sums of the items' sinks and source tiles
+    int2 *sym_items = nullptr;
+    int *sym_row = nullptr;
+    double *sym_apart = nullptr, *sym_bpart = nullptr;
+    int sym_n = 0, sym_nt = 0, sym_items_n = 0;
     size_t cap = 0;             // bodies
     size_t partial_cap = 0;     // doubles
 };

@@ -53,13 +53,39 @@ FP64_INSTR_PER_INTERACTION = 6  # the fast form's pair term (abie_gb300/csrc/com
 DRAM_BYTES_PER_LAUNCH = {("fp64", 16385): 945920}
 
 
-def launches_per_force_call(m):
-    """Kernels of one fast FP64 force call (abie_gb300/csrc/force.cu): the
-    source compaction (one block, or a count and a scatter pass above 4,096
-    bodies), the force kernel, and from 8,192 sinks with more than 1,024
-    sources the pass that adds the two source chunks."""
+SYM_MAX_BODIES = 131072  # the symmetric form's limit (abie_gb300/csrc/force.cu)
+
+
+def force_path(m):
+    """Which fast FP64 force form a call takes (abie_gb300/csrc/force.cu):
+    "sym" (8,192 .. 131,072 bodies, all massive), "chunked" (from 8,192
+    sinks with more than 1,024 sources) or "queue"."""
     n, n_src = int(m.size), int((m > 0).sum())
-    return (2 if n > 4096 else 1) + 1 + (1 if (n_src > 1024 and n >= 8192) else 0)
+    if n_src > 1024 and n >= 8192:
+        return "sym" if (n_src == n and n <= SYM_MAX_BODIES) else "chunked"
+    return "queue"
+
+
+def launches_per_force_call(m):
+    """Kernels of one fast FP64 force call: the source compaction (one
+    block, or a count and a scatter pass above 4,096 bodies), then the
+    force kernel, plus: for "chunked" the chunk sum; for "sym" its reduction
+    pass and the chunked pair, launched too and leaving at once (the device
+    picks the form)."""
+    path = force_path(m)
+    comp = 2 if m.size > 4096 else 1
+    return comp + {"queue": 1, "chunked": 2, "sym": 4}[path]
+
+
+def fp64_instructions_per_call(m, inter):
+    """FP64 instructions one force call executes (lanes x warp instructions):
+    6 per interaction (3 separations, 3 sums) in the one-sided forms; in the
+    symmetric form 9 per unordered pair of an off-diagonal 32 x 32 tile (3
+    separations, 3 + 3 sums) and 6 per step of the 31-step diagonal tiles."""
+    if force_path(m) != "sym":
+        return FP64_INSTR_PER_INTERACTION * inter
+    nt = (int(m.size) + 31) // 32
+    return 32 * (nt * 31 * 6 + nt * (nt - 1) // 2 * 32 * 9)
 
 
 def parse():
@@ -369,15 +395,18 @@ def run_ours(args):
             "flop_per_interaction": FLOP_PER_INTERACTION}
     if args.mode == "fp64":
         # The fast form executes 6 FP64 instructions per interaction (3
-        # separations, 3 sums); r^2 and G m r^-3 are integer arithmetic, so the
+        # separations, 3 sums), 4.5 in the symmetric form (each pair once for
+        # both bodies); r^2 and G m r^-3 are integer arithmetic, so the
         # 20-flop convention reads above the FMA peak.  The FP64 pipe's own
         # utilisation: executed FP64 instructions / (FMA peak / 2 flop).
-        roof["fp64_instructions_per_interaction"] = FP64_INSTR_PER_INTERACTION
-        roof["fp64_pipe_frac"] = (FP64_INSTR_PER_INTERACTION * inter / (ms_step * 1e-3)
-                                  / (peak * 1e12 / 2) if peak else None)
+        f64 = fp64_instructions_per_call(m, inter)
+        roof["force_form"] = force_path(m)
+        roof["fp64_instructions_per_interaction"] = f64 / inter
+        roof["fp64_pipe_frac"] = (f64 / (ms_step * 1e-3) / (peak * 1e12 / 2) if peak else None)
         roof["note"] = ("frac uses the 20-flop convention against the FMA peak; the kernel does "
-                        "r^2 and G m r^-3 in integer arithmetic (6 FP64 instructions per "
-                        "interaction), so frac > 1 and fp64_pipe_frac is the FP64 pipe's use")
+                        "r^2 and G m r^-3 in integer arithmetic and, in the symmetric form, each "
+                        "pair once for both bodies, so frac > 1 and fp64_pipe_frac is the FP64 "
+                        "pipe's use")
     roof["traffic"] = DRAM_BYTES_PER_LAUNCH.get((args.mode, int(m.size)))
 
     extra = {}
