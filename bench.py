@@ -49,8 +49,9 @@ G = ics.G_SOLAR
 FLOP_PER_INTERACTION = 20  # the convention of the reference's tiled kernel comments
 FP64_INSTR_PER_INTERACTION = 6  # the fast form's pair term (abie_gb300/csrc/common.cuh pair_fast)
 # dram__bytes_read.sum + dram__bytes_write.sum of one force-kernel launch,
-# from the ncu capture summarised in profiles/force_fp64_disk16385.md.
-DRAM_BYTES_PER_LAUNCH = {("fp64", 16385): 945920}
+# from the ncu capture summarised in profiles/force_fp64_disk16385.md (the
+# symmetric form: 1.25 MB read, 90.8 MB of partial sums written).
+DRAM_BYTES_PER_LAUNCH = {("fp64", 16385): 92033536}
 
 
 SYM_MAX_BODIES = 131072  # the symmetric form's limit (abie_gb300/csrc/force.cu)
