@@ -11,7 +11,9 @@
 //           atomic counter (force_fp64_dyn_kernel); from 8,192 sinks each
 //           sink's sources split into two chunks, one lane group per (sink,
 //           chunk) on a static grid (force_fp64_kernel), and a second pass
-//           adds the chunks' partial sums in chunk order.
+//           adds the chunks' partial sums in chunk order.  When every body
+//           is massive (8,192 .. 131,072 bodies) the symmetric form
+//           (force_sym_kernel) evaluates each pair once for both bodies.
 //   naive : one thread per sink over global memory with rsqrt, the
 //           semantics of the reference's GPU offload (src/gpuforce.cu:61-84):
 //           sources with m == 0 and coincident pairs are skipped, sinks and
