@@ -654,6 +654,33 @@ int sym_reserve(ForceScratch &s, int n)
     return 0;
 }
 
+int launch_force_published_sym(const Src *src, int n, const int *n_src_dev, double *acc,
+                               ForceScratch &s, cudaStream_t st)
+{
+    int rc = force_scratch_reserve(s, (size_t)n);
+    if (rc) return rc;
+    rc = sym_reserve(s, n);
+    if (rc) return rc;
+    int dev = 0, sms = 152, bps = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    ABIE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, force_sym_kernel, 256, 0));
+    const int blocks = (int)std::max<long long>(
+        1, std::min<long long>((long long)sms * std::max(bps, 1), ((long long)s.sym_items_n + 7) / 8));
+    ABIE_CUDA(cudaMemsetAsync(s.next, 0, sizeof(unsigned int), st));
+    force_sym_kernel<<<blocks, 256, 0, st>>>(src, n, s.sym_items, s.sym_items_n, s.sym_nt,
+                                             s.sym_apart, s.sym_bpart, s.next, n_src_dev);
+    sym_reduce_kernel<<<s.sym_nt, 32 * SYM_RW, 0, st>>>(s.sym_apart, s.sym_bpart, s.sym_row, n, acc,
+                                                         n_src_dev);
+    ABIE_CUDA(cudaGetLastError());
+    return 0;
+}
+
+bool force_sym_applies(int n, int n_src)
+{
+    return n_src == n && n >= 8192 && n <= SYM_MAX_BODIES && !force_shape_overridden();
+}
+
 int launch_force(int mode, const double *pos, const double *m, int n, double G, ForceScratch &s,
                  double *acc, cudaStream_t st)
 {

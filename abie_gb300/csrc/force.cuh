@@ -53,6 +53,14 @@ int launch_force_published(const double *pos, const double *m, int n, const Src 
                            const int *n_src_dev, int lanes, double *acc, unsigned int *next,
                            cudaStream_t st, double *partial = nullptr);
 
+// The symmetric form (each pair once for both bodies) on a published source
+// list that holds every body in body order (*n_src_dev == n), with the
+// symmetric scratch of s; force_sym_applies says whether it is used for a
+// system of n bodies and n_src massive ones.
+int launch_force_published_sym(const Src *src, int n, const int *n_src_dev, double *acc,
+                               ForceScratch &s, cudaStream_t st);
+bool force_sym_applies(int n, int n_src);
+
 // Fast FP64 force with caller-provided scratch (src / src_body sized for n
 // entries, n_src one int); allocates nothing.  Uses one source chunk.
 int launch_force_fp64_scratch(const double *pos, const double *m, int n, double G, Src *src,

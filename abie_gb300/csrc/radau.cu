@@ -1531,8 +1531,9 @@ static int stepped_run(const EngineArgs &a, int num_sms, cudaStream_t st, Engine
                                                                        (long long)num_sms * 8));
     long long force_calls = 0, iterations = 0, attempts = 0;
     // lanes per sink and source chunks as the standalone force picks them
-    // (force_shape_default): from 8,192 sinks two chunks, whose order of
-    // sums differs from the persistent engine's
+    // (force_shape_default): from 8,192 sinks two chunks, or the symmetric
+    // form when every body is massive, whose orders of sums differ from the
+    // persistent engine's
     const int lanes = a.n_src <= 64 ? 1 : (a.n_src <= 1024 ? 8 : 32);
     double *partial = nullptr;
     if (lanes == 32 && a.n >= 8192) {
@@ -1546,10 +1547,13 @@ static int stepped_run(const EngineArgs &a, int num_sms, cudaStream_t st, Engine
         }
         partial = e.partial;
     }
+    // every body massive: the symmetric form on the published list
+    const bool sym = force_sym_applies(a.n, a.n_src);
     auto force = [&](int buf) {
         const double *pos = buf < 2 ? a.yp[buf] : a.ypa;
         const Src *src = buf < 2 ? a.src[buf] : a.srca;
         force_calls++;
+        if (sym) return launch_force_published_sym(src, a.n, &ctl->n_src, acc, g_sim.fs, st);
         return launch_force_published(pos, a.m, a.n, src, &ctl->n_src, lanes, acc, &ctl->next_sink, st,
                                       partial);
     };
