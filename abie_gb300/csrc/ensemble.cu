@@ -259,6 +259,7 @@ __global__ void __launch_bounds__(32 * WARPS, (EnsOccupancy<W, LEARN>::value)) e
     constexpr int GROUPS = WARPS / W;
     __shared__ double s_pos[GROUPS][32][4];
     __shared__ double s_acc[GROUPS][32][3];
+    __shared__ double s_ctr[W == 1 ? GROUPS : 1][10][9][4];  // one-warp symmetric pair terms
     __shared__ double s_red[GROUPS][2 * W + 1];
     __shared__ int s_flg[GROUPS][2 * W];
     extern __shared__ __align__(16) unsigned char ens_dyn[];  // learned path only
@@ -321,11 +322,20 @@ __global__ void __launch_bounds__(32 * WARPS, (EnsOccupancy<W, LEARN>::value)) e
             grp.sync();
         };
         auto force_here = [&]() -> double { return alive ? sa[gl / 3][gl % 3] : 0.0; };
+        // the forces of the published positions: one warp in the fast form
+        // takes each pair once for both bodies
+        auto forces = [&]() {
+            if constexpr (W == 1 && MODE != ABIE_FORCE_EXACT) {
+                group_force_sym(grp, n, sp, sa, s_ctr[grp.gidx]);
+            } else {
+                group_force<MODE, W>(grp, n, sp, sa);
+            }
+        };
 
         if (S.phase == 0) {
             // F1 = f(y0), then initial_time_step (:75-120)
             publish(X.y0);
-            group_force<MODE, W>(grp, n, sp, sa);
+            forces();
             if (has) X.F1 = force_here();
             S.force_calls++;
             // d0, d1 over the first n of the 3n entries, as the reference does
@@ -339,7 +349,7 @@ __global__ void __launch_bounds__(32 * WARPS, (EnsOccupancy<W, LEARN>::value)) e
             double dt0 = (d0 < 1e-5 || d1 < 1e-5) ? 1e-6 : 0.01 * (d0 / d1);
             grp.sync();
             publish(X.y0 + dt0 * X.dy0);
-            group_force<MODE, W>(grp, n, sp, sa);
+            forces();
             S.force_calls++;
             const double d2 = grp.maxk(has ? absmax_key(force_here() - X.F1) : 0ull) / dt0;
             double dt1;
@@ -368,7 +378,7 @@ __global__ void __launch_bounds__(32 * WARPS, (EnsOccupancy<W, LEARN>::value)) e
                     grp.sync();
                     const double sh = e_hs[ih], ds = h * sh, hh = 0.5 * ds * ds;
                     publish(e_pred_pos<MODE>(X, ih, sh, h, ds, hh));
-                    group_force<MODE, W>(grp, n, sp, sa);
+                    forces();
                     if (has) {
                         const double F = force_here();
                         e_gb_update<MODE>(X, ih, F);
@@ -392,7 +402,7 @@ __global__ void __launch_bounds__(32 * WARPS, (EnsOccupancy<W, LEARN>::value)) e
             const double ya = e_pred_pos<MODE>(X, 8, 1.0, h, h, hh1);
             const double va = e_pred_vel<MODE>(X, h);
             publish(ya);
-            group_force<MODE, W>(grp, n, sp, sa);
+            forces();
             S.force_calls++;
             const double dd = has ? force_here() : 0.0;
             const bool bad = has && !(finite_bits(ya) && finite_bits(dd) && finite_bits(va));

@@ -382,4 +382,55 @@ __device__ __forceinline__ void group_force(const Group<W> &grp, int n, const do
 }
 
 
+// One warp's forces with each pair once for both bodies (fast form, n <= 10
+// bodies): lane p takes the p-th pair (i, k), i < k, shares the
+// separation d = x_i - x_k, r^2 and r^-3, and stores for each body the
+// factor and d -- {-G m_k r^-3, d} in ctr[i][k - 1], {G m_i r^-3, d} in
+// ctr[k][i] (each body's partners in index order; the sign set in the
+// integer assembly of the factor).  The lane of component c of body b then
+// sums its row with one FMA per partner, in that order, so each term is
+// rounded once as in group_force.  3 FP64 instructions per pair round and
+// n - 1 per component, against 6 per pair term and a shuffle tree.
+__device__ __forceinline__ void group_force_sym(const Group<1> &grp, int n, const double (*sp)[4],
+                                                double (*sa)[3], double (*ctr)[9][4])
+{
+    const int lane = grp.lane;
+    const int P = n * (n - 1) / 2;
+    for (int p0 = 0; p0 < P; p0 += 32) {
+        const int p = p0 + lane;
+        if (p < P) {
+            int i = 0, rem = p;
+            while (rem >= n - 1 - i) {
+                rem -= n - 1 - i;
+                i++;
+            }
+            const int k = i + 1 + rem;
+            const double dx = sp[i][0] - sp[k][0], dy = sp[i][1] - sp[k][1], dz = sp[i][2] - sp[k][2];
+            unsigned long long Mr, Wn;
+            int Er, eW;
+            r2_int(dx, dy, dz, Mr, Er);
+            inv_r3_core(Mr, Er, Wn, eW);
+            const double gi = sp[i][3], gk = sp[k][3];
+            const double wi = __double_as_longlong(gk) > 0 ? gm_times_inv_r3(Wn, eW, gk) : 0.0;
+            const double wk = __double_as_longlong(gi) > 0 ? gm_times_inv_r3(Wn, eW, gi) : 0.0;
+            ctr[i][k - 1][0] = __longlong_as_double(__double_as_longlong(wi) ^ (long long)0x8000000000000000ull);
+            ctr[i][k - 1][1] = dx;
+            ctr[i][k - 1][2] = dy;
+            ctr[i][k - 1][3] = dz;
+            ctr[k][i][0] = wk;
+            ctr[k][i][1] = dx;
+            ctr[k][i][2] = dy;
+            ctr[k][i][3] = dz;
+        }
+    }
+    __syncwarp();
+    if (lane < 3 * n) {
+        const int b = lane / 3, c = lane % 3;
+        double s = 0.0;
+        for (int q = 0; q < n - 1; q++) s = fma(ctr[b][q][0], ctr[b][q][1 + c], s);
+        sa[b][c] = s;
+    }
+    grp.sync();
+}
+
 }  // namespace abie
