@@ -259,7 +259,8 @@ __global__ void __launch_bounds__(32 * WARPS, (EnsOccupancy<W, LEARN>::value)) e
     constexpr int GROUPS = WARPS / W;
     __shared__ double s_pos[GROUPS][32][4];
     __shared__ double s_acc[GROUPS][32][3];
-    __shared__ double s_ctr[W == 1 ? GROUPS : 1][10][9][4];  // one-warp symmetric pair terms
+    constexpr int NB = W == 1 ? 10 : ENS_MAX_BODIES;  // bodies a group of W warps holds
+    __shared__ double s_ctr[MODE == ABIE_FORCE_EXACT ? 1 : GROUPS][NB][NB - 1][4];  // pair terms
     __shared__ double s_red[GROUPS][2 * W + 1];
     __shared__ int s_flg[GROUPS][2 * W];
     extern __shared__ __align__(16) unsigned char ens_dyn[];  // learned path only
@@ -322,11 +323,11 @@ __global__ void __launch_bounds__(32 * WARPS, (EnsOccupancy<W, LEARN>::value)) e
             grp.sync();
         };
         auto force_here = [&]() -> double { return alive ? sa[gl / 3][gl % 3] : 0.0; };
-        // the forces of the published positions: one warp in the fast form
-        // takes each pair once for both bodies
+        // the forces of the published positions: the fast form takes each
+        // pair once for both bodies
         auto forces = [&]() {
-            if constexpr (W == 1 && MODE != ABIE_FORCE_EXACT) {
-                group_force_sym(grp, n, sp, sa, s_ctr[grp.gidx]);
+            if constexpr (MODE != ABIE_FORCE_EXACT) {
+                group_force_sym<W, NB>(grp, n, sp, sa, s_ctr[grp.gidx]);
             } else {
                 group_force<MODE, W>(grp, n, sp, sa);
             }

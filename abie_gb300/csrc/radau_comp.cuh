@@ -382,8 +382,8 @@ __device__ __forceinline__ void group_force(const Group<W> &grp, int n, const do
 }
 
 
-// One warp's forces with each pair once for both bodies (fast form, n <= 10
-// bodies): lane p takes the p-th pair (i, k), i < k, shares the
+// A group's forces with each pair once for both bodies (fast form, n <= NB
+// bodies): group lane p takes the p-th pair (i, k), i < k, shares the
 // separation d = x_i - x_k, r^2 and r^-3, and stores for each body the
 // factor and d -- {-G m_k r^-3, d} in ctr[i][k - 1], {G m_i r^-3, d} in
 // ctr[k][i] (each body's partners in index order; the sign set in the
@@ -391,13 +391,14 @@ __device__ __forceinline__ void group_force(const Group<W> &grp, int n, const do
 // sums its row with one FMA per partner, in that order, so each term is
 // rounded once as in group_force.  3 FP64 instructions per pair round and
 // n - 1 per component, against 6 per pair term and a shuffle tree.
-__device__ __forceinline__ void group_force_sym(const Group<1> &grp, int n, const double (*sp)[4],
-                                                double (*sa)[3], double (*ctr)[9][4])
+template <int W, int NB>
+__device__ __forceinline__ void group_force_sym(const Group<W> &grp, int n, const double (*sp)[4],
+                                                double (*sa)[3], double (*ctr)[NB - 1][4])
 {
-    const int lane = grp.lane;
+    const int gl = grp.gl;
     const int P = n * (n - 1) / 2;
-    for (int p0 = 0; p0 < P; p0 += 32) {
-        const int p = p0 + lane;
+    for (int p0 = 0; p0 < P; p0 += 32 * W) {
+        const int p = p0 + gl;
         if (p < P) {
             int i = 0, rem = p;
             while (rem >= n - 1 - i) {
@@ -423,9 +424,9 @@ __device__ __forceinline__ void group_force_sym(const Group<1> &grp, int n, cons
             ctr[k][i][3] = dz;
         }
     }
-    __syncwarp();
-    if (lane < 3 * n) {
-        const int b = lane / 3, c = lane % 3;
+    grp.sync();
+    if (gl < 3 * n) {
+        const int b = gl / 3, c = gl % 3;
         double s = 0.0;
         for (int q = 0; q < n - 1; q++) s = fma(ctr[b][q][0], ctr[b][q][1 + c], s);
         sa[b][c] = s;
