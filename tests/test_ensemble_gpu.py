@@ -116,3 +116,28 @@ def test_edge_sizes_vs_oracle(clib, oracle, mode):
         p, v = at_time(out["pos"][sv], out["vel"][sv], M[sm], out["t"][s], ref["t"], oracle)
         assert rel_err_per_body(p, ref["pos"]) <= TOL
         assert rel_err_per_body(v, ref["vel"]) <= TOL
+
+
+def test_every_group_class_with_test_particles(clib, oracle):
+    """Three 21-body and two 10-body systems, each with massless test
+    particles, in the fast form: the slowest system runs on four warps and
+    at least two 21-body systems on two, so each group size evaluates its
+    pairs with massless bodies on one side or both."""
+    systems = []
+    for k, (npl, ntp) in enumerate([(14, 6), (12, 8), (16, 4), (6, 3), (5, 4)]):
+        p, v, m, r = ics.planetary_system(seed=950 + k, n_planets=npl, n_tp=ntp, tp_a=(2.0, 20.0))
+        systems.append((p, v, m))
+    P, V, M, offs = _pack(systems)
+    old = clib.set_force_mode("fp64")
+    try:
+        out = clib.gr_ensemble(P, V, M, offs, G, 0.0, 0.3)
+    finally:
+        clib.set_force_mode(old)
+    assert (out["status"] == 0).all()
+    for s in range(len(systems)):
+        sv, sm = _sl(offs, s)
+        ref = oracle.radau15(P[sv], V[sv], M[sm], np.zeros(M[sm].size), G, 0.0, 0.3)
+        assert abs(out["t"][s] - ref["t"]) <= TIME_TOL_FAST * ref["t"]
+        p, v = at_time(out["pos"][sv], out["vel"][sv], M[sm], out["t"][s], ref["t"], oracle)
+        assert rel_err_per_body(p, ref["pos"]) <= TOL
+        assert rel_err_per_body(v, ref["vel"]) <= TOL
