@@ -1661,10 +1661,11 @@ static int launch_engine(const EngineArgs &a, int num_sms, int block, cudaStream
 static int dispatch_engine(int mode, int js, int block, const EngineArgs &a, int num_sms,
                            cudaStream_t st, int *grid)
 {
-    if (a.C > 0.0) {  // post-Newtonian variants: one or four lanes per body
+    if (a.C > 0.0) {  // post-Newtonian variants: one, four or (fast form) 32 lanes per body
         if (mode == ABIE_FORCE_EXACT)
             return js >= 4 ? launch_engine<ABIE_FORCE_EXACT, 4, true>(a, num_sms, block, st, grid)
                            : launch_engine<ABIE_FORCE_EXACT, 1, true>(a, num_sms, block, st, grid);
+        if (js >= 32) return launch_engine<ABIE_FORCE_FP64, 32, true>(a, num_sms, block, st, grid);
         return js >= 4 ? launch_engine<ABIE_FORCE_FP64, 4, true>(a, num_sms, block, st, grid)
                        : launch_engine<ABIE_FORCE_FP64, 1, true>(a, num_sms, block, st, grid);
     }
@@ -1699,14 +1700,16 @@ static const void *split_fn(int mode, bool pn)
 // sources split JS ways; with one lane per body that lane does everything.
 // The shape minimising that estimate is taken (small systems spread thin,
 // large ones keep every lane busy), with blocks small enough that every SM
-// gets work.
-static void engine_shape(int mode, int n, int n_src, int num_sms, int *js, int *block)
+// gets work.  A post-Newtonian pair term (a square root, two divisions and
+// ~80 other operations) costs about 110 FP64 instructions more; its fast
+// form has variants of 1, 4 and 32 lanes per body.
+static void engine_shape(int mode, int n, int n_src, int num_sms, bool pn, int *js, int *block)
 {
     const long long subparts = 4LL * num_sms;
-    const int cand_fast[5] = {1, 4, 8, 16, 32}, cand_exact[2] = {1, 4};
-    const int *cand = mode == ABIE_FORCE_EXACT ? cand_exact : cand_fast;
-    const int nc = mode == ABIE_FORCE_EXACT ? 2 : 5;
-    const double pair = mode == ABIE_FORCE_EXACT ? 20.0 : 13.0;  // FP64 instructions per pair
+    const int cand_fast[5] = {1, 4, 8, 16, 32}, cand_exact[2] = {1, 4}, cand_pn[3] = {1, 4, 32};
+    const int *cand = mode == ABIE_FORCE_EXACT ? cand_exact : (pn ? cand_pn : cand_fast);
+    const int nc = mode == ABIE_FORCE_EXACT ? 2 : (pn ? 3 : 5);
+    const double pair = (mode == ABIE_FORCE_EXACT ? 20.0 : 13.0) + (pn ? 110.0 : 0.0);  // FP64 instructions
     const double sweep = mode == ABIE_FORCE_EXACT ? 50.0 : 30.0; // per component and substep
     double best = 0.0;
     for (int k = 0; k < nc; k++) {
@@ -1831,7 +1834,7 @@ int radau_run(const SystemView &sys, double t, double t_end, int mode, EventStat
     ABIE_CUDA(cudaStreamSynchronize(st));
 
     int js = 1, block = 256;
-    engine_shape(mode, n, n_src, g_sim.num_sms, &js, &block);
+    engine_shape(mode, n, n_src, g_sim.num_sms, a.C > 0.0, &js, &block);
     // few massive bodies: the split engine (a replica of them per block),
     // unless a launch shape is forced or the particles exceed one
     // resident wave

@@ -103,8 +103,9 @@ def parse():
     ap.add_argument("--gr-years", type=float, default=1.0)
     ap.add_argument("--disk-years", type=float, default=1.0)
     ap.add_argument("--no-extras", action="store_true", help="only the headline force line")
-    ap.add_argument("--extras", default="ensemble,wh,radau,disk",
-                    help="comma list of sub-measurements: ensemble, wh, radau, disk")
+    ap.add_argument("--extras", default="ensemble,wh,radau,disk,next",
+                    help="comma list of sub-measurements: ensemble, wh, radau, disk, next "
+                         "(Runge-Kutta 4, post-Newtonian Radau15, snapshots)")
     ap.add_argument("--ensemble-forms", default="plain_fp64,fp64,learned",
                     help="comma list of ensemble forms to time")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -255,6 +256,16 @@ def cpu_baselines_extras(args, extra):
                                                   "particles from the same generator (the star and "
                                                   "5 planets; oracle orc_wh with the reference's "
                                                   "O(N^2) accelerations)")
+    if "next" in extra and "rk4_1009" in extra["next"]:
+        p, v, m, r = ics.planetary_system()
+        steps = 5
+        t0 = time.perf_counter()
+        O.rk(p, v, m, G, 0.0, steps * 1e-3, 1e-3)
+        dt = time.perf_counter() - t0
+        extra["next"]["rk4_1009"]["cpu_baseline"] = {
+            "steps_per_s": steps / dt, "cores": 1, "kind": "port",
+            "sample": "5 steps of the same system (oracle orc_rk, the reference's stages and "
+                      "O(N^2) accelerations)"}
     if "radau_1009" in extra:
         p, v, m, r = ics.planetary_system()
         t0 = time.perf_counter()
@@ -421,6 +432,8 @@ def run_ours(args):
             extra["radau_1009"] = run_radau_single(lib, args)
         if args.disk_years > 0 and "disk" in which:
             extra["radau_disk"] = run_radau_disk(lib, args)
+        if "next" in which:
+            extra["next"] = run_next(lib, args)
 
     if rank == 0:
         cpu = None
@@ -576,6 +589,82 @@ def run_radau_single(lib, args):
         out[mode] = {"seconds": dt, "accepts": c["accepts"], "rejects": c["rejects"],
                      "attempts": c["attempts"], "ms_per_attempt": 1e3 * dt / max(c["attempts"], 1),
                      "force_calls": c["force_calls"], "abs_dE_over_E": abs((e1 - e0) / e0)}
+    return out
+
+
+def run_next(lib, args):
+    """The rows around the path, each on a bounded workload (fast FP64 form,
+    wall clock around the ABI call, device-resident state):
+    Runge-Kutta 4 (integrator_rk) on the 1,009-body system and the 16,385-body
+    disk; Radau15 with the post-Newtonian terms on a 1,025-body all-massive
+    disk over 0.2 yr against the same run without them; Radau15 on the 1,009-body system
+    with a snapshot (state, a/e/i about the centre of mass, energy) every
+    0.01 yr against the same run without snapshots.  The close-encounter and
+    collision scan runs after every accepted Radau15 step in every run."""
+    import time as _t
+    out = {}
+    lib.initialize_code(G, 0.0, 1 << 21, MAX_CE_EVENTS=3, MAX_COLLISION_EVENTS=2, deviceID=0)
+    old = lib.set_force_mode("fp64")
+    try:
+        for name, (p, v, m, r), h, years in (
+                ("rk4_1009", ics.planetary_system(), 1e-3, 0.2),
+                ("rk4_disk16385", ics.planetesimal_disk(), 1e-3, 0.01)):
+            lib.set_state(p, v, m, r, m.size, G, 0.0)
+            lib.integrator_rk(0.0, 2 * h, h)  # warm-up: kernels, graph, buffers
+            lib.set_state(p, v, m, r, m.size, G, 0.0)
+            e0 = lib.get_total_energy()
+            lib.reset_counters()
+            t0 = _t.perf_counter()
+            lib.integrator_rk(0.0, years, h)
+            dt = _t.perf_counter() - t0
+            steps = lib.counters()["force_calls"] // 4  # the reference's while t < t_end count
+            e1 = lib.get_total_energy()
+            out[name] = {"bodies": int(m.size), "step": h, "steps": steps, "seconds": dt,
+                         "steps_per_s": steps / dt,
+                         "gint_per_s": 4 * steps * interactions(m) / dt / 1e9,
+                         "abs_dE_over_E": abs((e1 - e0) / e0)}
+        p, v, m, r = ics.planetesimal_disk(n=1024)
+        c_light = 63239.7263  # au / yr
+        res = {"bodies": int(m.size), "years": 0.2, "C": c_light}
+        for key, C in (("newtonian", 0.0), ("post_newtonian", c_light)):
+            lib.set_state(p, v, m, r, m.size, G, C)
+            lib.integrator_gr(0.0, 1e-3, 1.0)
+            lib.set_state(p, v, m, r, m.size, G, C)
+            lib.reset_counters()
+            t0 = _t.perf_counter()
+            lib.integrator_gr(0.0, 0.2, 1.0)
+            dt = _t.perf_counter() - t0
+            c = lib.counters()
+            res[key] = {"seconds": dt, "attempts": c["attempts"], "force_calls": c["force_calls"],
+                        "ms_per_attempt": 1e3 * dt / max(c["attempts"], 1),
+                        "ms_per_force_call": 1e3 * dt / max(c["force_calls"], 1)}
+        out["pn_radau_1025"] = res
+        p, v, m, r = ics.planetary_system()
+        res = {"bodies": int(m.size), "years": 1.0, "store_dt": 0.01}
+        lib.set_state(p, v, m, r, m.size, G, 0.0)
+        lib.integrate_snapshots(0.0, 0.02, 0.01)  # warm-up
+        # integrate() restarts the step control in every chunk, as the
+        # reference does, so the snapshot run makes more step attempts
+        lib.set_state(p, v, m, r, m.size, G, 0.0)
+        lib.reset_counters()
+        t0 = _t.perf_counter()
+        snaps = lib.integrate_snapshots(0.0, 1.0, 0.01)
+        res["with_snapshots_s"] = _t.perf_counter() - t0
+        res["with_snapshots_attempts"] = lib.counters()["attempts"]
+        res["snapshots"] = int(snaps["t"].size)
+        lib.set_state(p, v, m, r, m.size, G, 0.0)
+        lib.reset_counters()
+        t0 = _t.perf_counter()
+        lib.integrator_gr(0.0, 1.0, 1.0)
+        res["plain_s"] = _t.perf_counter() - t0
+        res["plain_attempts"] = lib.counters()["attempts"]
+        per_att = res["plain_s"] / max(res["plain_attempts"], 1)
+        res["ms_per_snapshot"] = 1e3 * (res["with_snapshots_s"] - res["plain_s"]) / max(res["snapshots"], 1)
+        res["ms_per_snapshot_beyond_attempts"] = 1e3 * (
+            res["with_snapshots_s"] - per_att * res["with_snapshots_attempts"]) / max(res["snapshots"], 1)
+        out["snapshots_1009"] = res
+    finally:
+        lib.set_force_mode(old)
     return out
 
 
