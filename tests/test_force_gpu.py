@@ -97,3 +97,26 @@ def test_large_mixed_masses_parallel_compaction(clib, oracle):
     live = np.repeat(m >= 0, 3)
     assert np.all(fast[~live] == 0.0)
     assert rel_err_per_body(fast[live], ref[live]) <= 1e-13
+
+
+@pytest.mark.parametrize("n", [8192, 8200, 131072, 131073])
+def test_symmetric_form_sizes(clib, oracle, n):
+    """All-massive systems about the symmetric form's limits: 8,192 bodies
+    (its first size), 8,200 (a partial last tile of 32), 131,072 (its last
+    size) and 131,073 (the chunked form again).  The fast form agrees with
+    the exact one on every sink to 1e-13 at the smaller sizes and with the
+    oracle on sampled sinks at the larger ones, and a second call gives the
+    same doubles (the partial sums are added in a fixed order)."""
+    p, v, m, r = ics.planetesimal_disk(seed=40 + n % 97, n=n - 1)
+    fast = clib.force(p, m, G, "fp64")
+    assert np.array_equal(clib.force(p, m, G, "fp64"), fast)
+    if n <= 8200:
+        assert rel_err_per_body(fast, clib.force(p, m, G, "exact")) <= 1e-13
+        return
+    ref = np.zeros(p.size)
+    los = (0, n // 2 - 17, n - 64)
+    for lo in los:
+        oracle.force(p, m, G, j0=lo, j1=lo + 64, acc=ref, threads=8)
+    sinks = np.concatenate([np.arange(lo, lo + 64) for lo in los])
+    idx = (3 * sinks[:, None] + np.arange(3)).reshape(-1)
+    assert rel_err_per_body(fast[idx], ref[idx]) <= 1e-13
