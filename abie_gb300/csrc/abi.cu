@@ -123,7 +123,8 @@ static int host_force(const double *pos, const double *m, size_t n, double G, do
     if (vel && C > 0.0) {  // src/common.c:101-107 -> src/additional_forces.c:14-121
         if ((rc = reserve(&s.tmp_vel, &s.tmp_vel_cap, 3 * n))) return rc;
         ABIE_CUDA(cudaMemcpyAsync(s.tmp_vel, vel, 3 * n * sizeof(double), cudaMemcpyHostToDevice, s.st));
-        rc = launch_post_newtonian(s.tmp_pos, s.tmp_vel, s.tmp_m, (int)n, G, C, s.tmp_acc, s.st);
+        rc = launch_post_newtonian(s.tmp_pos, s.tmp_vel, s.tmp_m, (int)n, G, C, s.tmp_acc, s.st,
+                                   mode == ABIE_FORCE_FP64 || mode == ABIE_FORCE_MIXED);
         if (rc) return rc;
     }
     ABIE_CUDA(cudaMemcpyAsync(acc, s.tmp_acc, 3 * n * sizeof(double), cudaMemcpyDeviceToHost, s.st));

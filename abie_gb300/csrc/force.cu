@@ -927,7 +927,9 @@ int launch_force_fp64_scratch(const double *pos, const double *m, int n, double 
     return 0;
 }
 
-// One thread per sink, sources in index order (src/additional_forces.c:46-117).
+// One thread per sink, sources in index order (src/additional_forces.c:46-117);
+// MODE selects the reference's pair term or the regrouped fast one.
+template <int MODE>
 __global__ void __launch_bounds__(256) post_newtonian_kernel(const double *__restrict__ pos,
                                                              const double *__restrict__ vel,
                                                              const double *__restrict__ m, int n,
@@ -942,7 +944,7 @@ __global__ void __launch_bounds__(256) post_newtonian_kernel(const double *__res
     for (int k = 0; k < n; k++) {
         const double Mk = m[k];
         if (k == j || Mk == 0.0) continue;
-        pn_pair(K, x, y, z, vx, vy, vz, Mj, pos[3 * k], pos[3 * k + 1], pos[3 * k + 2], vel[3 * k],
+        pn_term<MODE>(K, x, y, z, vx, vy, vz, Mj, pos[3 * k], pos[3 * k + 1], pos[3 * k + 2], vel[3 * k],
                 vel[3 * k + 1], vel[3 * k + 2], Mk, ax, ay, az);
     }
     acc[3 * j] += ax;
@@ -951,10 +953,15 @@ __global__ void __launch_bounds__(256) post_newtonian_kernel(const double *__res
 }
 
 int launch_post_newtonian(const double *pos, const double *vel, const double *m, int n, double G,
-                          double C, double *acc, cudaStream_t st)
+                          double C, double *acc, cudaStream_t st, bool fast)
 {
     if (n <= 0) return 0;
-    post_newtonian_kernel<<<(n + 255) / 256, 256, 0, st>>>(pos, vel, m, n, pn_const(G, C), acc);
+    if (fast)
+        post_newtonian_kernel<ABIE_FORCE_FP64>
+            <<<(n + 255) / 256, 256, 0, st>>>(pos, vel, m, n, pn_const(G, C), acc);
+    else
+        post_newtonian_kernel<ABIE_FORCE_EXACT>
+            <<<(n + 255) / 256, 256, 0, st>>>(pos, vel, m, n, pn_const(G, C), acc);
     ABIE_CUDA(cudaGetLastError());
     return 0;
 }

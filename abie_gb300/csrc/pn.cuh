@@ -1,7 +1,9 @@
-// Post-Newtonian pair terms (src/additional_forces.c:14-121), on the device,
-// in the reference's expressions and order (built with --fmad=false):
+// Post-Newtonian pair terms (src/additional_forces.c:14-121), on the device:
 // 1PN, 2PN and 2.5PN of source k acting on sink j, summed over k by the
-// caller and added to the Newtonian acceleration.
+// caller and added to the Newtonian acceleration.  pn_pair keeps the
+// reference's expressions and order (built with --fmad=false; the exact
+// force form); pn_pair_fast regroups them without square root or division
+// (the fast form).
 //
 // Sources of zero mass contribute exact zeros to a sink of nonzero mass
 // (every term carries G m_k or nu = m_j m_k / (m_j + m_k)^2), so callers may
@@ -75,8 +77,71 @@ static __device__ __noinline__ void pn_pair(const PnConst &K, double x, double y
     az += H0 * (H1 * dvz + H2 * dz);
 }
 
+// Fast form of pn_pair: the same three terms, regrouped so that each sums
+// to A d + B dv,
+//   A = (F1 + F2) + P (G0 + G1) + H0 H2,   B = F0 + P G2 + H0 H1,
+// with F1 + F2 = (G m_k / c^2) r^-3 (4 G m_k / r - v^2) and, since
+// (G M)^2 nu = G^2 m_j m_k, H0 = -8/5 G^2 m_j m_k c^-5 r^-3: no square root
+// and no division (r^-3 from the integer core of the Newtonian term, r^-1 =
+// r^2 r^-3), two FMAs per component, ~60 FP64 instructions against ~136.
+// Coincident bodies (r = 0) add nothing.  The terms round differently from
+// the reference's expressions; they are ~(v/c)^2 of the Newtonian
+// acceleration, so the difference stays far below FP64 rounding of the total.
+static __device__ __noinline__ void pn_pair_fast(const PnConst &K, double x, double y, double z,
+                                                 double vx, double vy, double vz, double Mj,
+                                                 double xk, double yk, double zk, double vxk,
+                                                 double vyk, double vzk, double Mk, double &ax,
+                                                 double &ay, double &az)
+{
+    const double dx = x - xk, dy = y - yk, dz = z - zk;
+    unsigned long long Mr, Wn;
+    int Er, eW;
+    r2_int(dx, dy, dz, Mr, Er);
+    if (Mr == 0ull) return;
+    inv_r3_core(Mr, Er, Wn, eW);
+    const double d3 = gm_times_inv_r3(Wn, eW, 1.0);
+    const double dvx = vx - vxk, dvy = vy - vyk, dvz = vz - vzk;
+    const double r2 = fma(dz, dz, fma(dy, dy, dx * dx));
+    const double rv = fma(dz, dvz, fma(dy, dvy, dx * dvx));
+    const double vv = fma(dvz, dvz, fma(dvy, dvy, dvx * dvx));
+    const double d1 = r2 * d3, d2 = d1 * d1;
+    const double GM = K.G * Mk, gc = GM * K.CM2;
+    // 1PN
+    const double F0 = 4.0 * gc * rv * d3;
+    const double F12 = gc * d3 * fma(4.0 * GM, d1, -vv);
+    // 2PN
+    const double P = GM * gc * K.CM2 * (d2 * d2);
+    const double G01 = fma(2.0 * rv * rv, d2, -9.0 * GM * d1);
+    const double G2 = -2.0 * rv;
+    // 2.5PN
+    const double GMt = K.G * (Mj + Mk);
+    const double H0 = -(8.0 / 5.0) * (K.G * Mj) * GM * K.CM5 * d3;
+    const double H1 = fma(3.0 * GMt, d1, vv);
+    const double H2 = -fma(3.0, vv, (17.0 / 3.0) * GMt * d1) * rv * d2;
+    const double A = F12 + fma(P, G01, H0 * H2);
+    const double B = F0 + fma(P, G2, H0 * H1);
+    ax = fma(A, dx, fma(B, dvx, ax));
+    ay = fma(A, dy, fma(B, dvy, ay));
+    az = fma(A, dz, fma(B, dvz, az));
+}
+
+// The pair term of the force form: the reference's expressions (exact) or
+// the regrouped fast form.
+template <int MODE>
+__device__ __forceinline__ void pn_term(const PnConst &K, double x, double y, double z, double vx,
+                                        double vy, double vz, double Mj, double xk, double yk,
+                                        double zk, double vxk, double vyk, double vzk, double Mk,
+                                        double &ax, double &ay, double &az)
+{
+    if (MODE == ABIE_FORCE_EXACT)
+        pn_pair(K, x, y, z, vx, vy, vz, Mj, xk, yk, zk, vxk, vyk, vzk, Mk, ax, ay, az);
+    else
+        pn_pair_fast(K, x, y, z, vx, vy, vz, Mj, xk, yk, zk, vxk, vyk, vzk, Mk, ax, ay, az);
+}
+
 // acc[j] += sum over k != j with m_k != 0 of the pair terms, for all n sinks.
+// fast: the regrouped pair term (pn_pair_fast) instead of the reference's.
 int launch_post_newtonian(const double *pos, const double *vel, const double *m, int n, double G,
-                          double C, double *acc, cudaStream_t st);
+                          double C, double *acc, cudaStream_t st, bool fast = false);
 
 }  // namespace abie

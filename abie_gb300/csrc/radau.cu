@@ -219,7 +219,7 @@ __device__ __noinline__ void sink_pn(const EngineArgs &a, int j, const Src *src,
             const int k = a.src_body[q];
             if (k == j) continue;
             const Src sk = load_src(src + q);
-            pn_pair(a.pn, xj, yj, zj, vxj, vyj, vzj, mj, sk.x, sk.y, sk.z, vel[3 * k],
+            pn_term<MODE>(a.pn, xj, yj, zj, vxj, vyj, vzj, mj, sk.x, sk.y, sk.z, vel[3 * k],
                     vel[3 * k + 1], vel[3 * k + 2], a.m[k], ax, ay, az);
         }
     }
@@ -1021,7 +1021,7 @@ __global__ void __launch_bounds__(64) radau_split(EngineArgs a)
                     double ax = 0.0, ay = 0.0, az = 0.0;
                     for (int k = 0; k < n_m; k++) {
                         if (k == lane) continue;
-                        pn_pair(a.pn, P[lane][0], P[lane][1], P[lane][2], V[lane][0], V[lane][1],
+                        pn_term<MODE>(a.pn, P[lane][0], P[lane][1], P[lane][2], V[lane][0], V[lane][1],
                                 V[lane][2], V[lane][3], P[k][0], P[k][1], P[k][2], V[k][0], V[k][1],
                                 V[k][2], V[k][3], ax, ay, az);
                     }
@@ -1047,7 +1047,7 @@ __global__ void __launch_bounds__(64) radau_split(EngineArgs a)
                     const double(*P)[4] = s_sp[ib];
                     const double(*V)[4] = s_sv[ib];
                     for (int k = 0; k < n_m; k++)
-                        pn_pair(a.pn, x, y, z, vx, vy, vz, my_m, P[k][0], P[k][1], P[k][2],
+                        pn_term<MODE>(a.pn, x, y, z, vx, vy, vz, my_m, P[k][0], P[k][1], P[k][2],
                                 V[k][0], V[k][1], V[k][2], V[k][3], ax, ay, az);
                 }
                 fx += __shfl_sync(0xffffffffu, ax, 0, 4);
