@@ -338,7 +338,7 @@ double calculate_energy(void)
         set_error(ABIE_ERR_NOT_INITIALIZED, "calculate_energy before initialize_code");
         return 0.0;
     }
-    if (reserve(&s.energy_partials, &s.energy_cap, 2 * (s.n / 256 + 2))) return 0.0;
+    if (reserve(&s.energy_partials, &s.energy_cap, 2 * (s.n / 8 + 2))) return 0.0;
     double e = 0.0;
     if (launch_energy(s.pos, s.vel, s.m, (int)s.n, s.G, s.energy_partials, &e, s.st)) return 0.0;
     return e;
@@ -351,7 +351,7 @@ double abie_energy_host(const double *pos, const double *vel, const double *m, s
     if (ensure_device(-1)) return 0.0;
     if (reserve(&s.tmp_pos, &s.tmp_pos_cap, 3 * N) || reserve(&s.tmp_acc, &s.tmp_acc_cap, 3 * N) ||
         reserve(&s.tmp_m, &s.tmp_m_cap, N) ||
-        reserve(&s.energy_partials, &s.energy_cap, 2 * (N / 256 + 2)))
+        reserve(&s.energy_partials, &s.energy_cap, 2 * (N / 8 + 2)))
         return 0.0;
     if (cudaMemcpyAsync(s.tmp_pos, pos, 3 * N * 8, cudaMemcpyHostToDevice, s.st) ||
         cudaMemcpyAsync(s.tmp_acc, vel, 3 * N * 8, cudaMemcpyHostToDevice, s.st) ||

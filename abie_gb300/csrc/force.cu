@@ -792,9 +792,8 @@ int launch_force(int mode, const double *pos, const double *m, int n, double G, 
 }
 
 // ---------------------------------------------------------------------------
-// Energy: src/common.c:464-481.  Each thread sums its body's kinetic term and
-// pair terms in the reference's order; thread partials are combined as
-// double-double values in a fixed tree, block results summed on the host.
+// Energy: src/common.c:340-357, the reference's kinetic and pair terms summed
+// as double-double values in a fixed order (energy_kernel below).
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void two_sum(double a, double b, double &s, double &e)
 {
@@ -811,25 +810,38 @@ __device__ __forceinline__ void dd_add(double &hi, double &lo, double v)
     two_sum(s, e, hi, lo);
 }
 
-__global__ void __launch_bounds__(256) energy_kernel(const double *__restrict__ pos,
-                                                     const double *__restrict__ vel,
-                                                     const double *__restrict__ m, int n, double G,
-                                                     double *__restrict__ partials)
+// calculate_energy (src/common.c:340-357): one warp per body i with m_i != 0.
+// Lane 0 starts from the kinetic term 0.5 m |v|^2 (|v| from sqrt, squared,
+// as the reference does); the lanes take the partners j = lane, lane + 32,
+// ... (m_j != 0, j != i), each adding the reference's term -(G m_i / 2) m_j
+// / sqrt(r^2) to a double-double sum; the lanes, then the block's 8 warps,
+// meet in a fixed order, and the host adds the blocks' sums in block order.
+// (One thread per body left the FP64 pipe idle: 512 warps for 16,385
+// bodies.)
+constexpr int ENERGY_WARPS = 8;
+__global__ void __launch_bounds__(32 * ENERGY_WARPS) energy_kernel(const double *__restrict__ pos,
+                                                                   const double *__restrict__ vel,
+                                                                   const double *__restrict__ m, int n,
+                                                                   double G,
+                                                                   double *__restrict__ partials)
 {
-    __shared__ double sh_hi[256], sh_lo[256];
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ double sh[ENERGY_WARPS][2];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int i = blockIdx.x * ENERGY_WARPS + w;
     double hi = 0.0, lo = 0.0;
     if (i < n && m[i] != 0.0) {
-        double vx = vel[3 * i], vy = vel[3 * i + 1], vz = vel[3 * i + 2];
-        double s = 0.0;
-        s += vx * vx;
-        s += vy * vy;
-        s += vz * vz;
-        double nv = sqrt(s);
-        dd_add(hi, lo, 0.5 * m[i] * (nv * nv));
+        if (lane == 0) {
+            double vx = vel[3 * i], vy = vel[3 * i + 1], vz = vel[3 * i + 2];
+            double s = 0.0;
+            s += vx * vx;
+            s += vy * vy;
+            s += vz * vz;
+            double nv = sqrt(s);
+            dd_add(hi, lo, 0.5 * m[i] * (nv * nv));
+        }
         double xi = pos[3 * i], yi = pos[3 * i + 1], zi = pos[3 * i + 2];
         double c = 0.5 * G * m[i];
-        for (int j = 0; j < n; j++) {
+        for (int j = lane; j < n; j += 32) {
             double mj = m[j];
             if (j == i || mj == 0.0) continue;
             double dx = xi - pos[3 * j], dy = yi - pos[3 * j + 1], dz = zi - pos[3 * j + 2];
@@ -840,22 +852,27 @@ __global__ void __launch_bounds__(256) energy_kernel(const double *__restrict__ 
             dd_add(hi, lo, -(c * mj / sqrt(r2)));
         }
     }
-    sh_hi[threadIdx.x] = hi;
-    sh_lo[threadIdx.x] = lo;
-    __syncthreads();
-    for (int w = 128; w > 0; w >>= 1) {
-        if (threadIdx.x < w) {
-            double h2 = sh_hi[threadIdx.x], l2 = sh_lo[threadIdx.x];
-            dd_add(h2, l2, sh_hi[threadIdx.x + w]);
-            dd_add(h2, l2, sh_lo[threadIdx.x + w]);
-            sh_hi[threadIdx.x] = h2;
-            sh_lo[threadIdx.x] = l2;
+    for (int o = 16; o > 0; o >>= 1) {
+        const double h2 = __shfl_down_sync(0xffffffffu, hi, o);
+        const double l2 = __shfl_down_sync(0xffffffffu, lo, o);
+        if (lane < o) {
+            dd_add(hi, lo, h2);
+            dd_add(hi, lo, l2);
         }
-        __syncthreads();
     }
+    if (lane == 0) {
+        sh[w][0] = hi;
+        sh[w][1] = lo;
+    }
+    __syncthreads();
     if (threadIdx.x == 0) {
-        partials[2 * blockIdx.x] = sh_hi[0];
-        partials[2 * blockIdx.x + 1] = sh_lo[0];
+        double h = sh[0][0], l = sh[0][1];
+        for (int q = 1; q < ENERGY_WARPS; q++) {
+            dd_add(h, l, sh[q][0]);
+            dd_add(h, l, sh[q][1]);
+        }
+        partials[2 * blockIdx.x] = h;
+        partials[2 * blockIdx.x + 1] = l;
     }
 }
 
@@ -866,8 +883,8 @@ int launch_energy(const double *pos, const double *vel, const double *m, int n, 
         *h_out = 0.0;
         return 0;
     }
-    int blocks = (n + 255) / 256;
-    energy_kernel<<<blocks, 256, 0, st>>>(pos, vel, m, n, G, d_partials);
+    const int blocks = (n + ENERGY_WARPS - 1) / ENERGY_WARPS;
+    energy_kernel<<<blocks, 32 * ENERGY_WARPS, 0, st>>>(pos, vel, m, n, G, d_partials);
     ABIE_CUDA(cudaGetLastError());
     double *host = (double *)malloc(2 * (size_t)blocks * sizeof(double));
     if (!host) {

@@ -74,7 +74,7 @@ struct ForceShape {
 ForceShape force_shape_default(int n_sink, int n_src);
 void force_shape_override(int lanes_per_sink, int chunks);  // 0,0 = automatic
 
-// Energy (src/common.c:464-481) of a state on the device, FP64.
+// Energy (src/common.c:340-357) of a state on the device, FP64.
 int launch_energy(const double *pos, const double *vel, const double *m, int n, double G,
                   double *d_partials, double *h_out, cudaStream_t st);
 

@@ -84,7 +84,7 @@ int integrator_wh(double t, double t_end, double dt);
  * form reproduces the reference's doubles for non-negative masses); like
  * the reference, it leaves the model time unchanged. */
 int integrator_rk(double t, double t_end, double dt);
-/* src/common.c:464-481.  Total energy of the stored state (FP64). */
+/* src/common.c:340-357.  Total energy of the stored state (FP64). */
 double calculate_energy(void);
 /* src/common.c:163-201 (and the GPU offload src/gpuforce.cu:129-170):
  * accelerations of N bodies from host arrays, computed on the GPU in the

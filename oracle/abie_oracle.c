@@ -132,7 +132,7 @@ static double cross_norm3(const double *a, const double *b)
 static double sgn(double x) { return (double)((x > 0) - (x < 0)); }
 
 /* ------------------------------------------------------------------ */
-/* Energy: src/common.c:464-481                                         */
+/* Energy: src/common.c:340-357                                         */
 /* ------------------------------------------------------------------ */
 double orc_energy(const double *pos, const double *vel, const double *m,
                   size_t n, double G)

@@ -42,7 +42,7 @@ void orc_force(const double *pos, size_t n, double G, const double *m,
 /* The same arithmetic per sink, sinks split over nthreads POSIX threads. */
 int orc_force_threads(const double *pos, size_t n, double G, const double *m,
                       double *acc, size_t j0, size_t j1, int nthreads);
-/* src/common.c:464-481 */
+/* src/common.c:340-357 */
 double orc_energy(const double *pos, const double *vel, const double *m,
                   size_t n, double G);
 /* src/common.c:240-282 */
