@@ -944,14 +944,42 @@ int launch_force_fp64_scratch(const double *pos, const double *m, int n, double 
     return 0;
 }
 
-// One thread per sink, sources in index order (src/additional_forces.c:46-117);
-// MODE selects the reference's pair term or the regrouped fast one.
+// Exact form: one thread per sink, sources in index order
+// (src/additional_forces.c:46-117), the reference's pair term.  Fast form:
+// one warp per sink, the lanes over the sources, the regrouped pair term,
+// the lanes' sums added in a fixed shuffle tree.
 template <int MODE>
 __global__ void __launch_bounds__(256) post_newtonian_kernel(const double *__restrict__ pos,
                                                              const double *__restrict__ vel,
                                                              const double *__restrict__ m, int n,
                                                              PnConst K, double *__restrict__ acc)
 {
+    if constexpr (MODE != ABIE_FORCE_EXACT) {
+        const int lane = threadIdx.x & 31;
+        const int j = blockIdx.x * 8 + (threadIdx.x >> 5);
+        if (j >= n) return;  // whole warps leave together
+        const double x = pos[3 * j], y = pos[3 * j + 1], z = pos[3 * j + 2];
+        const double vx = vel[3 * j], vy = vel[3 * j + 1], vz = vel[3 * j + 2];
+        const double Mj = m[j];
+        double ax = 0.0, ay = 0.0, az = 0.0;
+        for (int k = lane; k < n; k += 32) {
+            const double Mk = m[k];
+            if (k == j || Mk == 0.0) continue;
+            pn_term<MODE>(K, x, y, z, vx, vy, vz, Mj, pos[3 * k], pos[3 * k + 1], pos[3 * k + 2],
+                          vel[3 * k], vel[3 * k + 1], vel[3 * k + 2], Mk, ax, ay, az);
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            ax += __shfl_xor_sync(0xffffffffu, ax, o);
+            ay += __shfl_xor_sync(0xffffffffu, ay, o);
+            az += __shfl_xor_sync(0xffffffffu, az, o);
+        }
+        if (lane == 0) {
+            acc[3 * j] += ax;
+            acc[3 * j + 1] += ay;
+            acc[3 * j + 2] += az;
+        }
+        return;
+    }
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
     const double x = pos[3 * j], y = pos[3 * j + 1], z = pos[3 * j + 2];
@@ -975,7 +1003,7 @@ int launch_post_newtonian(const double *pos, const double *vel, const double *m,
     if (n <= 0) return 0;
     if (fast)
         post_newtonian_kernel<ABIE_FORCE_FP64>
-            <<<(n + 255) / 256, 256, 0, st>>>(pos, vel, m, n, pn_const(G, C), acc);
+            <<<(n + 7) / 8, 256, 0, st>>>(pos, vel, m, n, pn_const(G, C), acc);
     else
         post_newtonian_kernel<ABIE_FORCE_EXACT>
             <<<(n + 255) / 256, 256, 0, st>>>(pos, vel, m, n, pn_const(G, C), acc);
