@@ -120,3 +120,46 @@ def test_symmetric_form_sizes(clib, oracle, n):
     sinks = np.concatenate([np.arange(lo, lo + 64) for lo in los])
     idx = (3 * sinks[:, None] + np.arange(3)).reshape(-1)
     assert rel_err_per_body(fast[idx], ref[idx]) <= 1e-13
+
+
+def _energy_terms_fsum(p, v, m, G):
+    """The reference's energy terms (src/common.c:340-357), each rounded as
+    the reference rounds it, summed exactly (math.fsum)."""
+    import math
+    p, v = p.reshape(-1, 3), v.reshape(-1, 3)
+    terms = []
+    for i in range(m.size):
+        if m[i] == 0.0:
+            continue
+        s = v[i, 0] * v[i, 0]
+        s = s + v[i, 1] * v[i, 1]
+        s = s + v[i, 2] * v[i, 2]
+        nv = np.sqrt(s)
+        terms.append(0.5 * m[i] * (nv * nv))
+        j = np.array([k for k in range(m.size) if k != i and m[k] != 0.0], dtype=int)
+        if j.size:
+            d = p[i] - p[j]
+            r2 = d[:, 0] * d[:, 0]
+            r2 = r2 + d[:, 1] * d[:, 1]
+            r2 = r2 + d[:, 2] * d[:, 2]
+            c = 0.5 * G * m[i]
+            terms.extend((-((c * m[j]) / np.sqrt(r2))).tolist())
+    return math.fsum(terms), math.fsum(abs(t) for t in terms)
+
+
+@pytest.mark.parametrize("n", [1, 2, 7, 9, 33, 300])
+def test_energy_sums_the_reference_terms(clib, n):
+    """One warp per body, double-double sums: the energy equals the exact
+    sum of the reference's own rounded terms to about one rounding of the
+    result, with massless and negative-mass bodies mixed in and sizes that
+    leave blocks of 8 warps part-filled."""
+    rng = np.random.default_rng(700 + n)
+    p = rng.normal(0.0, 5.0, 3 * n)
+    v = rng.normal(0.0, 2.0, 3 * n)
+    m = 10 ** rng.uniform(-9, -3, n)
+    if n > 2:
+        m[rng.integers(0, n, max(1, n // 5))] = 0.0
+        m[rng.integers(0, n, max(1, n // 7))] *= -1.0
+    e = clib.energy(p, v, m, G)
+    exact, scale = _energy_terms_fsum(p, v, m, G)
+    assert abs(e - exact) <= 2.0 * np.spacing(abs(exact)) + 1e-28 * scale

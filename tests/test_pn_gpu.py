@@ -112,3 +112,28 @@ def test_pn_general_engine_vs_oracle(sim, oracle, mode, tol_t):
     # the terms matter at this tolerance (about 3e-7 here)
     npos, nvel = at_time(newton["pos"], newton["vel"], m, newton["t"], ref["t"], oracle)
     assert rel_err_per_body(nvel, ref["vel"]) > 100 * TOL
+
+
+@pytest.mark.parametrize("n", [3, 9, 37])
+def test_pn_accelerations_fast_form_sizes(sim, oracle, n):
+    """calculate_accelerations with C > 0 at sizes that leave the fast
+    kernel's blocks of 8 sinks part-filled, one massless body among them:
+    the fast form (one warp per sink, the regrouped pair term) agrees with
+    the exact form to 1e-13 per body, and the exact form with the oracle's
+    Newton + post-Newtonian sum bit for bit."""
+    p, v, m, r = ics.planetary_system(seed=800 + n, n_planets=n - 2, n_tp=1)
+    Cl = 63239.7263
+    sim.set_state(p, v, m, np.zeros(m.size), m.size, G, Cl)
+    try:
+        out = {}
+        for mode in ("exact", "fp64"):
+            old = sim.set_force_mode(mode)
+            try:
+                out[mode] = _accelerations(sim, p, v, m)
+            finally:
+                sim.set_force_mode(old)
+    finally:
+        sim.set_state(p, v, m, np.zeros(m.size), m.size, G, 0.0)
+    ref = oracle.post_newtonian(p, v, m, G, Cl, acc=oracle.force(p, m, G))
+    assert np.array_equal(out["exact"], ref)
+    assert rel_err_per_body(out["fp64"], out["exact"]) <= 1e-13
