@@ -126,7 +126,10 @@ def interactions(m):
 
 # ---------------------------------------------------------------------------
 class Clocks:
-    """nvidia-smi sampling while the timed region runs."""
+    """nvidia-smi sampling every 50 ms from just before the timed region to
+    its end.  start(busy) keeps the GPU under the same load (untimed steps)
+    while the sampler comes up, so the samples see the clocks of that load
+    and not of an idle GPU; the timed region follows without a gap."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -137,16 +140,21 @@ class Clocks:
         self.proc = None
         self.path = None
 
-    def start(self):
+    def start(self, busy=None):
         fd, self.path = tempfile.mkstemp(suffix=".csv")
         os.close(fd)
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+                 "-lms", "50"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
-        time.sleep(0.3)
+        t_end = time.perf_counter() + 0.3
+        while time.perf_counter() < t_end:
+            if busy is None:
+                time.sleep(0.3)
+            else:
+                busy()
 
     def stop(self):
         if self.proc is None:
@@ -178,7 +186,9 @@ class Clocks:
         reasons = sorted({names[k] for r in rows for k in range(4) if "Active" == r[5 + k]})
         return {"sm_mhz": statistics.median(sm) if sm else None,
                 "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
-                "samples": len(rows), "power_w_max": max(num(r[3]) or 0 for r in rows)}
+                "samples": len(rows), "power_w_max": max(num(r[3]) or 0 for r in rows),
+                "window": "every 50 ms from 0.3 s of untimed steps of the same work "
+                          "through the end of the timed region"}
 
 
 # ---------------------------------------------------------------------------
@@ -352,7 +362,15 @@ def run_ours(args):
     stream.synchronize()
     peaks = lib.measure_peaks()
     clocks = Clocks(local)
-    clocks.start()
+
+    def busy():  # untimed steps under the sampler, then the timed region
+        with torch.cuda.stream(stream):
+            for _ in range(8):
+                flush.zero_()
+                step()
+        stream.synchronize()
+
+    clocks.start(busy)
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
