@@ -84,7 +84,9 @@ int integrator_wh(double t, double t_end, double dt);
  * form reproduces the reference's doubles for non-negative masses); like
  * the reference, it leaves the model time unchanged. */
 int integrator_rk(double t, double t_end, double dt);
-/* src/common.c:340-357.  Total energy of the stored state (FP64). */
+/* src/common.c:340-357.  Total energy of the stored state (FP64): the
+ * reference's kinetic and pair terms, summed in double-double in a fixed
+ * order and rounded once. */
 double calculate_energy(void);
 /* src/common.c:163-201 (and the GPU offload src/gpuforce.cu:129-170):
  * accelerations of N bodies from host arrays, computed on the GPU in the
@@ -93,9 +95,10 @@ size_t ode_n_body_second_order(const double *pos, size_t N, double G,
                                const double *masses, const double *radii,
                                double *acc);
 /* src/common.c:206-238: ode_n_body_second_order, the post-Newtonian terms
- * when the stored C is positive (src/additional_forces.c:14-121, in the
- * reference's operations), then the external accelerations set by
- * set_additional_forces. */
+ * when the stored C is positive (src/additional_forces.c:14-121: in the
+ * exact form the reference's operations, bit for bit; in the fast form the
+ * same terms regrouped without square root or division, within 1e-13 per
+ * body), then the external accelerations set by set_additional_forces. */
 size_t calculate_accelerations(const double *pos, const double *vel, size_t N,
                                double G, const double *masses,
                                const double *radii, double *acc);
