@@ -1,6 +1,6 @@
-"""bench.py's bookkeeping of the force forms (no GPU): which form a call
-takes, how many kernels it launches and how many FP64 instructions it
-executes, mirroring abie_gb300/csrc/force.cu."""
+"""bench.py's bookkeeping (no GPU): which force form a call takes, how many
+kernels it launches and how many FP64 instructions it executes, mirroring
+abie_gb300/csrc/force.cu; and the clock record read from nvidia-smi."""
 import numpy as np
 
 import bench
@@ -28,3 +28,31 @@ def test_symmetric_instruction_count():
     m2[5] = 0.0
     inter2 = bench.interactions(m2)
     assert bench.fp64_instructions_per_call(m2, inter2) == 6 * inter2
+
+
+def test_clock_record_parsing(tmp_path):
+    """The clock record reads nvidia-smi's CSV: median SM clock, the largest
+    max clock, every throttle reason seen Active, the sample count."""
+    import bench
+
+    class _Done:
+        def terminate(self):
+            pass
+
+        def wait(self, timeout=None):
+            return 0
+
+    rows = [
+        "0, 2070, 2070, 250.5, 0x0, Not Active, Not Active, Not Active, Not Active",
+        "0, 2040, 2070, 260.1, 0x4, Not Active, Not Active, Not Active, Active",
+        "0, 1980, 2070, 262.0, 0x40, Not Active, Active, Not Active, Not Active",
+        "garbage line",
+    ]
+    path = tmp_path / "clocks.csv"
+    path.write_text("\n".join(rows) + "\n")
+    c = bench.Clocks(0)
+    c.proc, c.path = _Done(), str(path)
+    rec = c.stop()
+    assert rec["sm_mhz"] == 2040.0 and rec["sm_max_mhz"] == 2070.0
+    assert rec["reasons"] == ["hw_thermal_slowdown", "sw_power_cap"]
+    assert rec["samples"] == 3 and rec["power_w_max"] == 262.0
