@@ -2,7 +2,7 @@
 //
 // A group of threads integrates one system (at most 21 bodies) from a work
 // queue -- one warp for up to 10 bodies, two warps (a named barrier each)
-// for 11-21, four warps for the slowest 1 in 256 systems, each class a
+// for 11-21, four warps for the slowest quarter of the systems, each class a
 // kernel on its own stream -- and a finished group takes the next system,
 // so systems of uneven size and difficulty do not wait for each other.  Each thread owns
 // one of the system's 3N components and keeps its Radau state (y0, dy0,
@@ -500,6 +500,16 @@ __global__ void __launch_bounds__(32 * WARPS, (EnsOccupancy<W, LEARN>::value)) e
 }
 
 static double g_last_seconds = 0.0;
+// The slowest 1 in heavy_div systems (longest first) run on four warps.  On
+// 4,096 planetary systems over 1 yr in the fast form the batch took 81-84
+// ms with 1 in 256, 79-80 with 1 in 16, 76 with 1 in 8, 70-72 with 1 in 4,
+// 85 with 1 in 2 and 78 with all: a batch ends with its slow systems, and a
+// four-warp group cuts their per-step latency at the cost of more warps per
+// system.  The exact form, whose group force does not split a pair's work,
+// keeps 1 in 256 (with 1 in 4 its batch ran 76k system-steps/s against
+// 100k).  abie_debug_ensemble_heavy sets one share for both.
+static int g_heavy_div = 0;
+static int heavy_div(int mode) { return g_heavy_div > 0 ? g_heavy_div : (mode == ABIE_FORCE_EXACT ? 256 : 4); }
 
 template <int MODE, bool LEARN>
 static const void *ensemble_fn_l(int w)
@@ -611,7 +621,7 @@ int ensemble_run(double *pos, double *vel, const double *m, const long long *off
     }
     std::vector<unsigned char> cls(ns);
     {
-        const int heavy = std::min(ns, std::max(1, ns / 256));
+        const int heavy = std::min(ns, std::max(1, ns / heavy_div(mode)));
         for (int q = 0; q < ns; q++) {
             const int s2 = active[q];
             cls[s2] = q < heavy ? 2 : (3 * (offsets[s2 + 1] - offsets[s2]) <= 32 ? 0 : 1);
@@ -730,6 +740,10 @@ double ensemble_last_seconds() { return g_last_seconds; }
 using namespace abie;
 
 extern "C" {
+// The share of systems (the slowest 1 in div, longest first) that run on
+// four-warp groups; 0 restores the default.  For tests and tuning.
+void abie_debug_ensemble_heavy(int div) { abie::g_heavy_div = div > 0 ? div : 0; }
+
 
 int abie_gr_ensemble(double *pos, double *vel, const double *m, const long long *offsets,
                      int n_systems, double G, double t0, double t_end, double *t_out, int *status,

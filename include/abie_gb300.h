@@ -240,6 +240,10 @@ int abie_force_device_noalloc(const double *d_pos, const double *d_m, size_t N,
  * {1, 8, 32} and the number of source chunks; (0, 0) restores the
  * automatic choice.  For tests and the autotuner. */
 void abie_debug_force_shape(int lanes_per_sink, int chunks);
+/* abie_gr_ensemble: the slowest 1 in div systems (longest first) run on
+ * four-warp groups; 0 restores the default (1 in 4 in the fast forms, 1 in
+ * 256 in the exact form).  For tests and tuning. */
+void abie_debug_ensemble_heavy(int div);
 /* Fixes the Radau15 engine's launch shape: lanes per body in {1, 4, 8, 16,
  * 32} (the exact form takes 1 or 4) and threads per block (a multiple of 32
  * up to 256); 0 keeps the automatic choice.  For tests and tuning. */
