@@ -386,8 +386,9 @@ __device__ __forceinline__ void group_force(const Group<W> &grp, int n, const do
 // bodies): group lane p takes the p-th pair (i, k), i < k, shares the
 // separation d = x_i - x_k, r^2 and r^-3, and stores for each body the
 // factor and d -- {-G m_k r^-3, d} in ctr[i][k - 1], {G m_i r^-3, d} in
-// ctr[k][i] (each body's partners in index order; the sign set in the
-// integer assembly of the factor).  The lane of component c of body b then
+// ctr[k][i] (each body's partners in index order: partner j at slot j
+// below the body, j - 1 above it; the first factor's sign flipped on its bit
+// pattern, an integer operation).  The lane of component c of body b then
 // sums its row with one FMA per partner, in that order, so each term is
 // rounded once as in group_force.  3 FP64 instructions per pair round and
 // n - 1 per component, against 6 per pair term and a shuffle tree.
