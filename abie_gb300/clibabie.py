@@ -105,7 +105,13 @@ class CLibABIE(object):
         return self.lib.calculate_energy()
 
     def set_additional_forces(self, ext_acc):
+        """A constant 3N acceleration added to every force call; None
+        switches it off (an addition of this library)."""
+        if ext_acc is None:
+            self.lib.set_additional_forces(_c.c_int(0), None)
+            return
         ext_acc = _f64(ext_acc)
+        self._ext = ext_acc  # the library copies it; kept only for inspection
         self.lib.set_additional_forces(_c.c_int(len(ext_acc) // 3), _vp(ext_acc))
 
     # The reference's wrappers of the direct entry points (abie/clibabie.py:112-146)

@@ -1,4 +1,4 @@
-// C ABI shell: the reference's libabie entry points (src/common.c:200-537)
+// C ABI shell: the reference's libabie entry points (src/common.c:200-413)
 // over a device-resident simulation state.
 //
 // The reference keeps one global Simulation (src/common.h:26-70) on the
@@ -176,7 +176,7 @@ int initialize_code(double G, double C, size_t N_MAX, size_t MAX_N_CE, size_t MA
                     int deviceID)
 {
     Sim &s = g_sim;
-    if (s.inited) return 0;  // once per process, src/common.c:351
+    if (s.inited) return 0;  // once per process, src/common.c:227
     if (deviceID < 0) {
         set_error(ABIE_ERR_NO_DEVICE,
                   "deviceID=%d: this library runs the GPU path only; pass a GPU id", deviceID);
@@ -229,7 +229,7 @@ int finalize_code(void)
     free_wh_buffers();
     free_rk_buffers();
     // like the reference, a finalized library is not re-initialized in the
-    // same process (src/common.c:506-522 leaves code_inited set)
+    // same process (src/common.c:382-398 leaves code_inited set)
     return 0;
 }
 
@@ -321,8 +321,10 @@ size_t set_additional_forces(size_t N, double *ext_acc)
         set_error(ABIE_ERR_CAPACITY, "set_additional_forces: N=%zu above N_MAX=%zu", N, s.n_max);
         return 0;
     }
-    s.ext_enabled = true;
-    if (N) {
+    // a NULL vector switches the external accelerations off again (the
+    // reference has no way to do so)
+    s.ext_enabled = ext_acc != nullptr;
+    if (N && ext_acc) {
         cudaError_t e = cudaMemcpyAsync(s.ext_acc, ext_acc, 3 * N * sizeof(double),
                                         cudaMemcpyHostToDevice, s.st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(s.st);

@@ -248,7 +248,7 @@ __device__ __forceinline__ double rcp_fast(double x)
 }
 
 // Exact FP64 pair contribution, in the reference's operation order
-// (src/common.c:185-194): r = sqrt(r2); r3 = r * r2; a -= (gm*d)/r3.
+// (src/common.c:61-70): r = sqrt(r2); r3 = r * r2; a -= (gm*d)/r3.
 __device__ __forceinline__ void pair_exact(double xj, double yj, double zj, const Src &s,
                                            double &ax, double &ay, double &az)
 {
@@ -284,7 +284,7 @@ __device__ __forceinline__ void pair_fast(double xj, double yj, double zj, const
 
 // Non-negative doubles keep their order when read as unsigned integers, so
 // a max over |v| can be an integer atomicMax.  0 encodes "no value seen";
-// NaN is skipped, like the reference's vector_max_abs (src/common.c:316-322).
+// NaN is skipped, like the reference's vector_max_abs (src/common.c:192-198).
 __device__ __forceinline__ unsigned long long absmax_key(double v)
 {
     // integer instructions only: |v|'s bits, NaN (above the infinity

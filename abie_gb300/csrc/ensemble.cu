@@ -12,7 +12,7 @@
 // summing every L-th source, partial sums added as a fixed tree (L = 1 and
 // the reference's operations in the exact form).  The
 // sweep itself -- predictor, g/b updates, convergence test, step control,
-// refine_bs -- is the reference's (src/integrator_gauss_radau15.c:287-446)
+// refine_bs -- is the reference's (src/integrator_gauss_radau15.c:221-380)
 // component by component, as in the single-system engine.  The fast form
 // runs the corrector on the Newton-form coefficients g alone: predicted
 // positions come straight from g with tabulated weights, b = C g is formed
@@ -334,7 +334,7 @@ __global__ void __launch_bounds__(32 * WARPS, (EnsOccupancy<W, LEARN>::value)) e
         };
 
         if (S.phase == 0) {
-            // F1 = f(y0), then initial_time_step (:75-120)
+            // F1 = f(y0), then initial_time_step (:9-54)
             publish(X.y0);
             forces();
             if (has) X.F1 = force_here();

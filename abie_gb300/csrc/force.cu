@@ -2,7 +2,7 @@
 //
 //   exact : one thread per sink, sources visited in body order with the
 //           reference's operations (sqrt, r*r2, (gm*d)/r3), so every
-//           acceleration is bit-identical to src/common.c:163-201.
+//           acceleration is bit-identical to src/common.c:39-77.
 //   fp64  : the production FP64 form.  A group of 1, 8 or 32 lanes shares a
 //           sink and splits its sources; partial sums meet in a fixed
 //           butterfly of warp shuffles, so results are deterministic.  The
@@ -570,12 +570,18 @@ __global__ void force_naive_kernel(const double *__restrict__ pos, const double 
 
 ForceShape force_shape_default(int n_sink, int n_src)
 {
-    ForceShape s;
     if (g_shape_override.lanes_per_sink > 0) {
+        ForceShape s;
         s.lanes_per_sink = g_shape_override.lanes_per_sink;
         s.chunks = g_shape_override.chunks > 0 ? g_shape_override.chunks : 1;
         return s;
     }
+    return force_shape_auto(n_sink, n_src);
+}
+
+ForceShape force_shape_auto(int n_sink, int n_src)
+{
+    ForceShape s;
     s.lanes_per_sink = n_src <= 64 ? 1 : (n_src <= 1024 ? 8 : 32);
     // from 8,192 sinks two source chunks per sink (partial sums added in
     // chunk order): finer work items than the sink queue's and fewer idle
@@ -919,15 +925,17 @@ namespace abie {
 
 // Fast FP64 force with scratch the caller provides (compact source list,
 // its body indices and count); launches the compaction and one force kernel
-// and allocates nothing.
+// and allocates nothing.  Always the one-chunk kernel (no partial sums) with
+// the automatic lanes per sink (1, 8 or 32); the debug shape override does
+// not apply here.
 int launch_force_fp64_scratch(const double *pos, const double *m, int n, double G, Src *src,
                               int *src_body, int *n_src, double *acc, cudaStream_t st)
 {
     if (n <= 0) return 0;
     compact_sources_kernel<<<1, 1024, 0, st>>>(pos, m, n, G, src, src_body, n_src);
     ABIE_CUDA(cudaGetLastError());
-    ForceShape sh = force_shape_default(n, n);
-    int gpb = 256 / sh.lanes_per_sink;
+    const ForceShape sh = force_shape_auto(n, n);
+    const int gpb = 256 / sh.lanes_per_sink;
     int blocks = (n + gpb - 1) / gpb;
     switch (sh.lanes_per_sink) {
     case 1:

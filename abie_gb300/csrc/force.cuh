@@ -28,7 +28,7 @@ struct ForceScratch {
 int force_scratch_reserve(ForceScratch &s, size_t n);
 void force_scratch_free(ForceScratch &s);
 
-// Order-preserving compaction of the bodies with m > 0 (src/common.c:184:
+// Order-preserving compaction of the bodies with m > 0 (src/common.c:60:
 // only positive masses act as sources).
 int launch_compact_sources(const double *pos, const double *m, int n, double G, Src *src,
                            int *src_body, int *n_src, cudaStream_t st);
@@ -38,7 +38,7 @@ int launch_compact_sources_parallel(const double *pos, const double *m, int n, d
                                     int *src_body, int *n_src, int *counts, cudaStream_t st);
 
 // acc[3j..3j+2] for every sink j in [0, n).  Sinks with m < 0 are skipped
-// (their entries are not written), as in src/common.c:173-176.
+// (their entries are not written), as in src/common.c:49-52.
 int launch_force(int mode, const double *pos, const double *m, int n, double G,
                  ForceScratch &s, double *acc, cudaStream_t st);
 
@@ -71,7 +71,8 @@ struct ForceShape {
     int lanes_per_sink;   // 1, 8 or 32
     int chunks;           // source chunks per sink (1 = no split)
 };
-ForceShape force_shape_default(int n_sink, int n_src);
+ForceShape force_shape_default(int n_sink, int n_src);  // honours abie_debug_force_shape
+ForceShape force_shape_auto(int n_sink, int n_src);     // the automatic choice only
 void force_shape_override(int lanes_per_sink, int chunks);  // 0,0 = automatic
 
 // Energy (src/common.c:340-357) of a state on the device, FP64.

@@ -1,6 +1,6 @@
 // Gauss-Radau 15 on the device for one system of any size.
 //
-// The reference (src/integrator_gauss_radau15.c:287-446) loops on the host
+// The reference (src/integrator_gauss_radau15.c:221-380) loops on the host
 // and calls the force on every Radau substep, copying positions to the GPU
 // and accelerations back each time (src/gpuforce.cu:142-156).  Here the
 // whole predictor-corrector sweep runs inside one cooperative persistent
@@ -116,19 +116,24 @@ __device__ __forceinline__ unsigned long long gtimer()
 // Grid barrier: block 0 adds 2^31 - (nblocks - 1), every other block adds 1,
 // so the top bit of the counter flips exactly when all blocks have arrived.
 // The wait is bounded; on timeout the error word is set and every block
-// leaves at its next barrier.
+// leaves at its next barrier.  Thread 0 alone reads the error word and hands
+// its verdict to the block through shared memory, so all threads of a block
+// leave (or go on) together.  The clock is read every 256 spins, or every
+// spin for limits below a millisecond (set only by the debug setter).
 __device__ __forceinline__ bool grid_sync(EngineCtl *ctl, long long timeout_ns)
 {
+    __shared__ int s_grid_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
         unsigned int nb = gridDim.x;
         unsigned int inc = (blockIdx.x == 0) ? (0x80000000u - (nb - 1u)) : 1u;
+        const unsigned int every = timeout_ns < 1000000ll ? 0u : 255u;
         __threadfence();
         unsigned int old = atomicAdd(&ctl->bar, inc);
         unsigned long long t0 = gtimer();
         unsigned int spins = 0;
         while (((*(volatile unsigned int *)&ctl->bar ^ old) & 0x80000000u) == 0u) {
-            if ((++spins & 255u) == 0u) {
+            if ((++spins & every) == 0u) {
                 if (*(volatile int *)&ctl->err) break;
                 if (gtimer() - t0 > (unsigned long long)timeout_ns) {
                     atomicCAS(&ctl->err, 0, ABIE_ERR_TIMEOUT);
@@ -137,9 +142,10 @@ __device__ __forceinline__ bool grid_sync(EngineCtl *ctl, long long timeout_ns)
             }
         }
         __threadfence();
+        s_grid_ok = *(volatile int *)&ctl->err == 0;
     }
     __syncthreads();
-    return *(volatile int *)&ctl->err == 0;
+    return s_grid_ok != 0;
 }
 
 __device__ __forceinline__ Src load_src(const Src *p)
@@ -270,7 +276,7 @@ template <int JS>
 __device__ __forceinline__ int comp_hi(int lane) { return JS >= 4 ? (lane < 3 ? lane + 1 : 0) : 3; }
 
 // Predicted position of component i at spacing s = c_hs[row] (row 8:
-// s = 1) of a step dt (src/integrator_gauss_radau15.c:122-134).  Exact
+// s = 1) of a step dt (src/integrator_gauss_radau15.c:56-68).  Exact
 // form: the reference's Horner polynomial in b with its divisions by
 // constants.  Fast form: the same polynomial on the Newton-form
 // coefficients g (b = C g), y0 + ds dy0 + hh (F1 + sum_j g_j W_j(s)), the
@@ -377,7 +383,7 @@ __device__ __forceinline__ void publish_comp(const EngineArgs &a, int j, int c, 
 }
 
 // Exact form: g and b after the force F at substep IH (1..7) for component
-// i (src/integrator_gauss_radau15.c:136-241; only g[IH-1] is new, the lower
+// i (src/integrator_gauss_radau15.c:70-175; only g[IH-1] is new, the lower
 // g the reference recomputes are bitwise the stored ones), in the
 // reference's order and roundings.  Fast form: only g[IH-1], from the
 // expanded recurrence (F - F1) rsp[IH][0] - sum_{l<IH-1} g_l rsp[IH][l+1];
@@ -463,7 +469,7 @@ __device__ __forceinline__ void refine_g(const EngineArgs &a, int i, double q, b
     }
 }
 
-// src/integrator_gauss_radau15.c:244-284 (bd is always zero there).
+// src/integrator_gauss_radau15.c:178-218 (bd is always zero there).
 __device__ __forceinline__ void refine_b(const EngineArgs &a, int i, double q)
 {
     const int d = a.dim;
@@ -656,7 +662,7 @@ __global__ void __launch_bounds__(256) radau_engine(EngineArgs a)
         }
         if (leader) ctl->force_calls++;
         if (!grid_sync(ctl, T)) return;
-        // --- initial_time_step (src/integrator_gauss_radau15.c:75-120): the
+        // --- initial_time_step (src/integrator_gauss_radau15.c:9-54): the
         // reference scans only the first n of the 3n entries for d0 and d1
         unsigned long long k0 = 0, k1 = 0;
         for (int i = tid; i < n; i += nthreads) {
@@ -781,7 +787,7 @@ __global__ void __launch_bounds__(256) radau_engine(EngineArgs a)
             if (leader) ctl->force_calls += 7;
             double db6, f8;
             read2(ctl, red_idx++, db6, f8);
-            if (corrector_converged<MODE>(db6, f8)) break;  // src/integrator_gauss_radau15.c:366
+            if (corrector_converged<MODE>(db6, f8)) break;  // src/integrator_gauss_radau15.c:300
             for (int j = gid; j < n; j += ngroups)
                 for (int c = c0; c < c1; c++) a.b6p[3 * j + c] = b6_at<MODE>(a, 3 * j + c);
         }
@@ -816,7 +822,7 @@ __global__ void __launch_bounds__(256) radau_engine(EngineArgs a)
         }
         double mb6, mdd;
         read2(ctl, red_idx++, mb6, mdd);
-        // ---------------- step control (src/integrator_gauss_radau15.c:379-433) ----------------
+        // ---------------- step control (src/integrator_gauss_radau15.c:313-367) ----------------
         double estim_b6 = mb6 / mdd;
         double err, dtreq, rq;
         step_size<MODE>(estim_b6, h, err, dtreq, rq);
@@ -1065,7 +1071,7 @@ __global__ void __launch_bounds__(64) radau_split(EngineArgs a)
     int loop_count, red_idx;
     long long my_attempts = 0;
     if (ctl->phase == 0) {
-        // F1 = f(y0), then initial_time_step (src/integrator_gauss_radau15.c:75-120)
+        // F1 = f(y0), then initial_time_step (src/integrator_gauss_radau15.c:9-54)
         X.F1 = forces(X.y0, X.dy0);
         if (leader) ctl->force_calls++;
         unsigned long long k0 = 0, k1 = 0;
@@ -1123,7 +1129,7 @@ __global__ void __launch_bounds__(64) radau_split(EngineArgs a)
             if (!grid_sync(ctl, T)) return;
             double db6, f8;
             read2(ctl, red_idx++, db6, f8);
-            if (corrector_converged<MODE>(db6, f8)) break;  // src/integrator_gauss_radau15.c:366
+            if (corrector_converged<MODE>(db6, f8)) break;  // src/integrator_gauss_radau15.c:300
             X.b6p = e_b6<MODE>(X);
         }
         // advance (spacing 1)
@@ -1149,7 +1155,7 @@ __global__ void __launch_bounds__(64) radau_split(EngineArgs a)
         }
         double mb6, mdd;
         read2(ctl, red_idx++, mb6, mdd);
-        // step control (src/integrator_gauss_radau15.c:379-433)
+        // step control (src/integrator_gauss_radau15.c:313-367)
         const double estim_b6 = mb6 / mdd;
         double err, dtreq, rq;
         step_size<MODE>(estim_b6, h, err, dtreq, rq);
@@ -1346,7 +1352,7 @@ __global__ void __launch_bounds__(256) st_f1_kernel(EngineArgs a, const double *
     st_keys(&a.ctl->red[0][0], k0, k1);
 }
 
-// initial_time_step's dt0 (src/integrator_gauss_radau15.c:75-120), one thread
+// initial_time_step's dt0 (src/integrator_gauss_radau15.c:9-54), one thread
 __global__ void st_dt0_kernel(EngineArgs a)
 {
     EngineCtl *ctl = a.ctl;
@@ -1449,7 +1455,7 @@ __global__ void __launch_bounds__(256) st_advance_kernel(EngineArgs a, const dou
     st_keys(&a.ctl->red[0][0], kb6, kdd);
 }
 
-// step control (src/integrator_gauss_radau15.c:379-433) as radau_engine
+// step control (src/integrator_gauss_radau15.c:313-367) as radau_engine
 // runs it, one thread; the decision goes to the host through ctl
 template <int MODE>
 __global__ void st_control_kernel(EngineArgs a)
@@ -1637,6 +1643,7 @@ static int stepped_run(const EngineArgs &a, int num_sms, cudaStream_t st, Engine
 }
 
 static int g_radau_path = 0;  // debug override: 0 automatic, 1 persistent engine, 2 stepped
+static long long g_engine_timeout_ns = -1;  // debug override of the barrier wait limit (-1: automatic)
 
 template <int MODE, int JS, bool PN = false>
 static int launch_engine(const EngineArgs &a, int num_sms, int block, cudaStream_t st, int *grid_out)
@@ -1815,6 +1822,7 @@ int radau_run(const SystemView &sys, double t, double t_end, int mode, EventStat
     a.ctl = e.ctl;
     // a phase's work bounds its barrier wait (post-Newtonian pairs cost ~20x more)
     a.timeout_ns = 2000000000ll + (a.C > 0.0 ? 240ll : 12ll) * (long long)n * (long long)std::max(n_src, 1);
+    if (g_engine_timeout_ns >= 0) a.timeout_ns = g_engine_timeout_ns;
 
     ABIE_CUDA(cudaMemcpyAsync(a.y0, sys.pos, d * sizeof(double), cudaMemcpyDeviceToDevice, st));
     ABIE_CUDA(cudaMemcpyAsync(a.dy0, sys.vel, d * sizeof(double), cudaMemcpyDeviceToDevice, st));
@@ -1934,6 +1942,8 @@ extern "C" {
 
 void abie_debug_radau_path(int path) { g_radau_path = (path == 1 || path == 2) ? path : 0; }
 
+void abie_debug_engine_timeout(long long ns) { g_engine_timeout_ns = ns >= 0 ? ns : -1; }
+
 void abie_debug_engine_shape(int lanes_per_body, int block)
 {
     const bool ok_js = lanes_per_body == 0 || lanes_per_body == 1 || lanes_per_body == 4 ||
@@ -1977,7 +1987,10 @@ size_t integrator_gauss_radau15(double *pos, double *vel, double *m_vec, double 
     cudaMemcpy(dv, vel, 3 * N * 8, cudaMemcpyHostToDevice);
     cudaMemcpy(dm, m_vec, N * 8, cudaMemcpyHostToDevice);
     cudaMemcpy(dr, r_vec, N * 8, cudaMemcpyHostToDevice);
-    SystemView v{dp, dv, dm, dr, nullptr, m_vec, r_vec, (int)N, G};
+    // the external accelerations of set_additional_forces apply here too,
+    // as the reference's calculate_accelerations adds them to every call
+    const double *ext = (s.inited && s.ext_enabled && N <= s.n_max) ? s.ext_acc : nullptr;
+    SystemView v{dp, dv, dm, dr, ext, m_vec, r_vec, (int)N, G};
     EventState ev{s.ce_dist, s.max_ce, s.max_coll, &s.n_ce, &s.n_coll, &s.buf_ce, &s.buf_coll};
     double t_out = t;
     rc = radau_run(v, t, t_end, s.force_mode, s.inited ? &ev : nullptr, &t_out, &s.ctr, s.st);

@@ -1,4 +1,4 @@
-// Radau15 on one component per thread (src/integrator_gauss_radau15.c:56-284),
+// Radau15 on one component per thread (src/integrator_gauss_radau15.c:56-218),
 // shared by the batched ensemble (ensemble.cu) and the split engine for
 // systems with few massive bodies (radau_split.cu).  Each thread keeps its
 // component's state -- y0, dy0, F1, b[7], g[7], previous b6 -- in
@@ -84,7 +84,7 @@ __device__ __forceinline__ double e_pred_vel(const Comp &c, double dt)
 }
 
 // Predicted velocity at spacing s = e_hs[row] (row 8: s = 1), needed only
-// by velocity-dependent forces (src/integrator_gauss_radau15.c:129-134).
+// by velocity-dependent forces (src/integrator_gauss_radau15.c:63-68).
 template <int MODE>
 __device__ __forceinline__ double e_pred_vel_at(const Comp &c, int row, double s, double dt)
 {
@@ -110,7 +110,7 @@ __device__ __forceinline__ double e_b6(const Comp &c)
     return MODE == ABIE_FORCE_EXACT ? c.b[6] : c.g[6];
 }
 
-// g and b after the force F of substep IH (src/integrator_gauss_radau15.c:136-241);
+// g and b after the force F of substep IH (src/integrator_gauss_radau15.c:70-175);
 // one fully static variant per substep keeps the coefficients in registers.
 template <int MODE, int IH>
 __device__ __forceinline__ void e_gb_update_ih(Comp &c, double F)
@@ -211,7 +211,7 @@ __device__ __forceinline__ unsigned long long warp_maxk(unsigned long long v)
     return v;
 }
 
-// The corrector's convergence test (src/integrator_gauss_radau15.c:366),
+// The corrector's convergence test (src/integrator_gauss_radau15.c:300),
 // db6 / f8 < tolpc.  The fast form multiplies instead of dividing.
 template <int MODE>
 __device__ __forceinline__ bool corrector_converged(double db6, double f8)
@@ -219,7 +219,7 @@ __device__ __forceinline__ bool corrector_converged(double db6, double f8)
     return MODE == ABIE_FORCE_EXACT ? db6 / f8 < TOLPC : db6 < TOLPC * f8;
 }
 
-// Step control (src/integrator_gauss_radau15.c:379-433): err =
+// Step control (src/integrator_gauss_radau15.c:313-367): err =
 // (estim_b6 / epsb)^(1/7) and dtreq = h / err.  The fast form returns
 // rq = 1 / err as well (so dtreq = h rq, and the ratio dtreq / h the
 // controller tests is rq) and takes the seventh root in single precision
@@ -259,7 +259,7 @@ __device__ __forceinline__ void step_size(double estim_b6, double h, double &err
 // change of basis b_k = sum_{j>=k} cs[j][k] g_j, so that the corrector's
 // first sweep starts from the polynomial the guess describes.  (The
 // reference keeps the previous step's g, which the first sweep mixes into
-// every b it rebuilds, src/integrator_gauss_radau15.c:189-241.)
+// every b it rebuilds, src/integrator_gauss_radau15.c:123-175.)
 __device__ __forceinline__ void consistent_g(Comp &c)
 {
 #pragma unroll

@@ -1,6 +1,6 @@
 // Wisdom-Holman kick-drift-kick on the device.
 //
-// Reference: src/integrator_wisdom_holman.c:471-537.  Bodies split into
+// Reference: src/integrator_wisdom_holman.c:456-522.  Bodies split into
 //   head: 0 .. the last body with nonzero mass (at least body 1), and
 //   tail: the massless bodies after it.
 // Massless bodies add exact zeros to every running sum of the reference
@@ -70,7 +70,7 @@ __device__ __forceinline__ double norm3(double a, double b, double c)
     return sqrt(s);
 }
 
-// src/integrator_wisdom_holman.c:30-47
+// src/integrator_wisdom_holman.c:15-32
 __device__ __forceinline__ void stumpff(double psi, double &c2, double &c3)
 {
     if (psi > 1.e-10) {
@@ -88,7 +88,7 @@ __device__ __forceinline__ void stumpff(double psi, double &c2, double &c3)
     }
 }
 
-// src/integrator_wisdom_holman.c:66-147 on one body's Jacobi state.
+// src/integrator_wisdom_holman.c:51-132 on one body's Jacobi state.
 // Returns 1 when Newton did not converge within the iteration cap.
 __device__ int kepler_drift(double r0v[3], double v0v[3], double gm, double dt)
 {
@@ -291,7 +291,7 @@ __device__ int kepler_drift_fast(double r0v[3], double v0v[3], double gm, const 
 }
 
 // One block.  init != 0: only Jacobi coordinates and accelerations (the
-// set-up at the start of integrator_wh, :524-525); otherwise a full step.
+// set-up at the start of integrator_wh, :509-510); otherwise a full step.
 // MODE as for the tail: the fast form divides by multiplying with
 // rcp_fast, drifts with kepler_drift_fast and takes r^-3 from gm_inv_r3.
 // The head is latency-bound (a few bodies, sequential prefixes), so its
@@ -333,7 +333,7 @@ __global__ void __launch_bounds__(256) wh_head_kernel(WhArgs a, int init, int pa
             for (int c = 0; c < 3; c++) a.vel[3 * i + c] += a.acc[3 * i + c] * half;
     __syncthreads();
     if (threadIdx.x == 0) {
-        // interior masses and Kepler parameters (:189-206, :224-229)
+        // interior masses and Kepler parameters (:174-191, :209-214)
         a.eta[0] = m[0];
         for (int i = 1; i < H; i++) a.eta[i] = m[i] + a.eta[i - 1];
         double eta0 = m[0];
@@ -351,7 +351,7 @@ __global__ void __launch_bounds__(256) wh_head_kernel(WhArgs a, int init, int pa
             sh->gm_tail_k[2] = 1.0 / sqrt(gmt);
             sh->gm_tail_k[3] = sqrt(gmt) * a.dt;
         }
-        // helio -> Jacobi for the head (:221-280)
+        // helio -> Jacobi for the head (:206-265)
         double *jp = a.jpos, *jv = a.jvel;
         for (int c = 0; c < 3; c++) {
             jp[c] = 0.0;
@@ -387,7 +387,7 @@ __global__ void __launch_bounds__(256) wh_head_kernel(WhArgs a, int init, int pa
     }
     __syncthreads();
     if (!init) {
-        // drift the head bodies (:189-206), independent given Jacobi states
+        // drift the head bodies (:174-191), independent given Jacobi states
         for (int i = 1 + threadIdx.x; i < H; i += blockDim.x) {
             double r[3] = {a.jpos[3 * i], a.jpos[3 * i + 1], a.jpos[3 * i + 2]};
             double v[3] = {a.jvel[3 * i], a.jvel[3 * i + 1], a.jvel[3 * i + 2]};
@@ -407,7 +407,7 @@ __global__ void __launch_bounds__(256) wh_head_kernel(WhArgs a, int init, int pa
         }
         __syncthreads();
         if (threadIdx.x == 0) {
-            // Jacobi -> helio for the head (:295-347)
+            // Jacobi -> helio for the head (:280-332)
             const double *jp = a.jpos, *jv = a.jvel;
             for (int c = 0; c < 3; c++) {
                 a.pos[3 + c] = jp[3 + c];
@@ -453,7 +453,7 @@ __global__ void __launch_bounds__(256) wh_head_kernel(WhArgs a, int init, int pa
             q++;
         }
     }
-    // accelerations of the head (:364-451)
+    // accelerations of the head (:349-436)
     for (int i = threadIdx.x; i < H; i += blockDim.x) {
         double h = 0.0, j = 0.0;
         if (i >= 2) {
@@ -714,7 +714,7 @@ int wh_run(const SystemView &sys, double t, double t_end, double dt, double *t_o
 
     long long steps = 0;
     double tt = t;
-    while (tt < t_end) {  // :528-535, the same accumulation of t
+    while (tt < t_end) {  // :513-520, the same accumulation of t
         tt += dt;
         steps++;
     }
@@ -726,7 +726,7 @@ int wh_run(const SystemView &sys, double t, double t_end, double dt, double *t_o
         ABIE_CUDA(cudaFuncSetAttribute(wh_tail_kernel<ABIE_FORCE_FP64>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     }
-    // set-up (:524-525): Jacobi coordinates and accelerations, in order
+    // set-up (:509-510): Jacobi coordinates and accelerations, in order
     wh_launch_head(a, 1, 0, mode, st);
     wh_launch_tail(a, 1, 0, n_src, mode, st);
     ABIE_CUDA(cudaGetLastError());

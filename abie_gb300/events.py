@@ -1,7 +1,13 @@
-"""Event exceptions raised by the ctypes binding.
+"""Event exceptions raised by this package's ctypes binding.
 
-Same classes, fields and messages as the reference's abie/events.py:1-34, so
-code that catches the reference's events catches these too.
+They have the names, fields (t, obj1, obj2, distance) and messages of the
+reference's abie/events.py:1-34, so handlers written against those classes
+read the same attributes.  They are separate classes: an ``except`` clause
+naming ``abie.events.CloseEncounterException`` does not catch this module's
+exception.  Code that runs the reference's own Python package on this
+library (its unchanged abie/clibabie.py loading libabie_gb300) raises the
+reference's classes, since that binding turns the return codes 1 / 2 into
+its own exceptions.
 """
 
 

@@ -48,9 +48,10 @@ from abie_gb300 import ics  # noqa: E402
 G = ics.G_SOLAR
 FLOP_PER_INTERACTION = 20  # the convention of the reference's tiled kernel comments
 FP64_INSTR_PER_INTERACTION = 6  # the fast form's pair term (abie_gb300/csrc/common.cuh pair_fast)
-# dram__bytes_read.sum + dram__bytes_write.sum of one force-kernel launch,
-# from the ncu capture summarised in profiles/force_fp64_disk16385.md (the
-# symmetric form: 1.25 MB read, 90.8 MB of partial sums written).
+# dram__bytes_read.sum + dram__bytes_write.sum of one launch of the force
+# kernel, from one ncu capture of this workload (fp64 form, 16,385 bodies,
+# symmetric kernel: 1.25 MB read, 90.8 MB of partial sums written).  Not
+# measured by the bench itself, which runs without a profiler.
 DRAM_BYTES_PER_LAUNCH = {("fp64", 16385): 92033536}
 
 
@@ -288,6 +289,15 @@ def cpu_baselines_extras(args, extra):
             "sample": "0.2 yr of the same system (oracle orc_radau15, the reference's operations)"}
 
 
+def headline_config(args, m, inter, world):
+    """The ``config`` of the headline line, the same for both arms."""
+    return {"workload": "all-pairs %s force, planetesimal disk of %d bodies (1 star + %d x 1e-9 MSun)"
+                        % (args.mode, m.size, m.size - 1),
+            "bodies": int(m.size), "interactions_per_step": int(inter),
+            "force_mode": args.mode, "l2": "flushed (256 MiB write) between timed GPU steps",
+            "parallelism": "replicas" if world > 1 else "single GPU"}
+
+
 def run_reference(args):
     rank, world, local = dist_env()
     if rank != 0:
@@ -307,12 +317,11 @@ def run_reference(args):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * float(np.mean(times)), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "all-pairs FP64 force, planetesimal disk of %d bodies" % m.size,
-                   "bodies": int(m.size), "interactions_per_step": int(interactions(m))},
+        "config": headline_config(args, m, interactions(m), world),
         "cpu_baseline": {"value": value, "unit": "Ginteractions/s", "cores": threads, "kind": "port",
                          "sample": "full force evaluation per step (all %d sinks), sinks split "
                                    "over %d threads; oracle/abie_oracle.c orc_force, bit-identical "
-                                   "to src/common.c:163-201" % (m.size, threads)},
+                                   "to src/common.c:39-77" % (m.size, threads)},
         "e2e": {"value": value, "unit": "Ginteractions/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -416,28 +425,41 @@ def run_ours(args):
     e2e_s, e2e_units = D.reduce_timing(time.perf_counter() - t0, inter * args.steps, device=dev)
     e2e_value = e2e_units / e2e_s / 1e9
 
-    # roofline of the force kernel (FP64 pipe)
-    ach = FLOP_PER_INTERACTION * inter / (ms_step * 1e-3) / 1e12
+    # Roofline of the force kernel.  The fast FP64 form is bound by the FP64
+    # pipe: frac = executed FP64 instructions per second / the pipe's
+    # instruction rate (the measured FMA peak / 2 flop), each executed FP64
+    # lane instruction counted as one FMA (2 flop) in `achieved`.  The fast
+    # form executes 6 FP64 instructions per interaction (3 separations, 3
+    # sums), 4.52 in the symmetric form (each pair once for both bodies),
+    # with r^2 and G m r^-3 in integer arithmetic; the count is the model of
+    # fp64_instructions_per_call, which the ncu capture of the kernel
+    # (smsp__inst_executed_pipe_fp64.sum x 32 lanes) confirms.  The
+    # reference's 20-flop-per-interaction convention is kept beside it as
+    # `convention_frac`: it reads above 1 because those flops are not all
+    # executed on the FP64 pipe.
     peak = peaks["fp64_tflops"] if args.mode != "mixed" else peaks["fp32_tflops"]
-    roof = {"bound": "fp64" if args.mode != "mixed" else "fp32", "achieved": ach, "peak": peak,
-            "unit": "TFLOP/s", "frac": ach / peak if peak else None, "traffic": None,
-            "peak_source": "measured FMA throughput (abie_measure_fp64_peak) on this GPU",
-            "flop_per_interaction": FLOP_PER_INTERACTION}
+    conv = FLOP_PER_INTERACTION * inter / (ms_step * 1e-3) / 1e12
+    roof = {"bound": "fp64" if args.mode != "mixed" else "fp32", "unit": "TFLOP/s",
+            "peak": peak,
+            "peak_source": "FMA throughput measured by abie_measure_fp64_peak (fp32: "
+                           "abie_measure_fp32_peak) on this GPU in this run; the driver's "
+                           "measured peaks hold only HBM and bf16 figures",
+            "flop_per_interaction": FLOP_PER_INTERACTION,
+            "convention_achieved": conv, "convention_frac": conv / peak if peak else None}
     if args.mode == "fp64":
-        # The fast form executes 6 FP64 instructions per interaction (3
-        # separations, 3 sums), 4.5 in the symmetric form (each pair once for
-        # both bodies); r^2 and G m r^-3 are integer arithmetic, so the
-        # 20-flop convention reads above the FMA peak.  The FP64 pipe's own
-        # utilisation: executed FP64 instructions / (FMA peak / 2 flop).
         f64 = fp64_instructions_per_call(m, inter)
-        roof["force_form"] = force_path(m)
-        roof["fp64_instructions_per_interaction"] = f64 / inter
-        roof["fp64_pipe_frac"] = (f64 / (ms_step * 1e-3) / (peak * 1e12 / 2) if peak else None)
-        roof["note"] = ("frac uses the 20-flop convention against the FMA peak; the kernel does "
-                        "r^2 and G m r^-3 in integer arithmetic and, in the symmetric form, each "
-                        "pair once for both bodies, so frac > 1 and fp64_pipe_frac is the FP64 "
-                        "pipe's use")
+        ach = 2.0 * f64 / (ms_step * 1e-3) / 1e12
+        roof.update({"achieved": ach, "frac": ach / peak if peak else None,
+                     "force_form": force_path(m),
+                     "fp64_instructions_per_interaction": f64 / inter,
+                     "fp64_instructions_source": "model (fp64_instructions_per_call), checked "
+                                                 "against ncu smsp__inst_executed_pipe_fp64.sum"})
+    else:
+        roof.update({"achieved": conv, "frac": conv / peak if peak else None})
     roof["traffic"] = DRAM_BYTES_PER_LAUNCH.get((args.mode, int(m.size)))
+    roof["traffic_source"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum, one capture of "
+                              "force_sym_kernel on this workload (fp64, 16,385 bodies)"
+                              if roof["traffic"] else None)
 
     extra = {}
     if not args.no_extras:
@@ -461,17 +483,13 @@ def run_ours(args):
             cpu = {"value": g, "unit": "Ginteractions/s", "cores": threads, "kind": "port",
                    "sample": "3 full force evaluations of the same %d-body disk, sinks split over "
                              "%d threads (oracle/abie_oracle.c orc_force, bit-identical to "
-                             "src/common.c:163-201)" % (m.size, threads)}
+                             "src/common.c:39-77)" % (m.size, threads)}
         line = {
             "metric": "Gint/s", "value": value, "unit": "Ginteractions/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.mode != "mixed" else "f32+f64",
             "data": "synthetic",
-            "config": {"workload": "all-pairs %s force, planetesimal disk of %d bodies (1 star + %d x 1e-9 MSun)"
-                                   % (args.mode, m.size, m.size - 1),
-                       "bodies": int(m.size), "interactions_per_step": int(inter),
-                       "force_mode": args.mode, "l2": "flushed (256 MiB write) between timed steps",
-                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "config": headline_config(args, m, inter, world),
             "roofline": roof,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "Ginteractions/s",

@@ -39,47 +39,51 @@ extern "C" {
 #define ABIE_ERR_NUMERICS (-8)        /* NaN/Inf in the state */
 
 /* Force forms (abie_set_force_mode). */
-#define ABIE_FORCE_EXACT 0  /* reference operation order per sink: bit-identical to src/common.c:163-201 */
+#define ABIE_FORCE_EXACT 0  /* reference operation order per sink: bit-identical to src/common.c:39-77 */
 #define ABIE_FORCE_FP64 1   /* fast FP64: reassociated sums, refined reciprocal square root */
 #define ABIE_FORCE_MIXED 2  /* FP32 pair terms on anchored coordinates, compensated sums; heavy sources in FP64 */
 #define ABIE_FORCE_NAIVE 3  /* one thread per sink over global memory: src/gpuforce.cu:61-84 semantics */
 
 /* ---- reference-compatible entry points (src/common.h:74-122) ---------- */
 
-/* src/common.c:350-399.  Binds GPU deviceID, sizes device buffers for
+/* src/common.c:226-275.  Binds GPU deviceID, sizes device buffers for
  * N_MAX bodies and the event ring buffers.  Once per process, like the
  * reference (a second call returns 0 and does nothing). */
 int initialize_code(double G, double C, size_t N_MAX, size_t MAX_N_CE,
                     size_t MAX_N_COLLISIONS, int deviceID);
-/* src/common.c:506-522.  Frees device and host buffers. */
+/* src/common.c:382-398.  Frees device and host buffers. */
 int finalize_code(void);
-/* src/common.c:433-449.  Copies the caller's arrays into device memory. */
+/* src/common.c:309-325.  Copies the caller's arrays into device memory. */
 void set_state(double *pos, double *vel, double *m, double *r, size_t N,
                double G, double C);
-/* src/common.c:451-462.  Copies the device state out; returns N. */
+/* src/common.c:327-338.  Copies the device state out; returns N. */
 int get_state(double *pos, double *vel, double *m, double *r);
-/* src/common.c:324-326 */
+/* src/common.c:200-202 */
 double get_model_time(void);
-/* src/common.c:401-407 */
+/* src/common.c:277-283 */
 void set_close_encounter_distance(double d);
 double get_close_encounter_distance(void);
-/* src/common.c:409-431 (4*MAX doubles each: t, i, j, distance) */
+/* src/common.c:285-307 (4*MAX doubles each: t, i, j, distance) */
 void get_close_encounter_buffer(double *buf_ce);
 void get_collision_buffer(double *buf_collision);
 void reset_close_encounter_buffer(void);
 void reset_collision_buffer(void);
-/* src/common.c:488-504.  A constant 3N acceleration added to every force call. */
+/* src/common.c:364-380.  A constant 3N acceleration added to every force
+ * call of calculate_accelerations and Radau15 (stateful and on caller
+ * arrays), as the reference's calculate_accelerations adds it
+ * (src/common.c:107-112).  ext_acc == NULL switches it off again (an
+ * addition: the reference cannot). */
 size_t set_additional_forces(size_t N, double *ext_acc);
-/* src/common.c:524-527 -> src/integrator_gauss_radau15.c:287-446.
+/* src/common.c:400-403 -> src/integrator_gauss_radau15.c:221-380.
  * Gauss-Radau 15 from t to the first accepted time past t_end, on the
  * device-resident state; dt is ignored as in the reference.  With a stored
  * C > 0 the accelerations include the post-Newtonian terms
  * (src/additional_forces.c) of the massive bodies. */
 int integrator_gr(double t, double t_end, double dt);
-/* src/common.c:534-537 -> src/integrator_wisdom_holman.c:513-537.
+/* src/common.c:410-413 -> src/integrator_wisdom_holman.c:498-522.
  * Fixed-step Wisdom-Holman on a heliocentric state. */
 int integrator_wh(double t, double t_end, double dt);
-/* src/common.c:529-532 -> src/integrator_runge_kutta.c:6-50.  Classical
+/* src/common.c:405-408 -> src/integrator_runge_kutta.c:6-50.  Classical
  * RK4 on the device-resident state in the current force form (the exact
  * form reproduces the reference's doubles for non-negative masses); like
  * the reference, it leaves the model time unchanged. */
@@ -88,13 +92,13 @@ int integrator_rk(double t, double t_end, double dt);
  * reference's kinetic and pair terms, summed in double-double in a fixed
  * order and rounded once. */
 double calculate_energy(void);
-/* src/common.c:163-201 (and the GPU offload src/gpuforce.cu:129-170):
+/* src/common.c:39-77 (and the GPU offload src/gpuforce.cu:129-170):
  * accelerations of N bodies from host arrays, computed on the GPU in the
  * current force form.  Does not touch the stored simulation state. */
 size_t ode_n_body_second_order(const double *pos, size_t N, double G,
                                const double *masses, const double *radii,
                                double *acc);
-/* src/common.c:206-238: ode_n_body_second_order, the post-Newtonian terms
+/* src/common.c:82-114: ode_n_body_second_order, the post-Newtonian terms
  * when the stored C is positive (src/additional_forces.c:14-121: in the
  * exact form the reference's operations, bit for bit; in the fast form the
  * same terms regrouped without square root or division, within 1e-13 per
@@ -102,7 +106,7 @@ size_t ode_n_body_second_order(const double *pos, size_t N, double G,
 size_t calculate_accelerations(const double *pos, const double *vel, size_t N,
                                double G, const double *masses,
                                const double *radii, double *acc);
-/* src/integrator_gauss_radau15.c:287: Radau15 on caller arrays (the
+/* src/integrator_gauss_radau15.c:221: Radau15 on caller arrays (the
  * state is uploaded, integrated on the device and copied back). */
 size_t integrator_gauss_radau15(double *pos, double *vel, double *m_vec,
                                 double *r_vec, size_t N, double G, double t,
@@ -111,7 +115,7 @@ size_t integrator_gauss_radau15(double *pos, double *vel, double *m_vec,
 void integrator_runge_kutta(double *pos, double *vel, double *m_vec,
                             double *r_vec, size_t N, double G, double t,
                             double t_end, double dt);
-/* src/integrator_wisdom_holman.c:513 on caller arrays. */
+/* src/integrator_wisdom_holman.c:498 on caller arrays. */
 void integrator_wisdom_holman(double *pos, double *vel, double *m_vec,
                               double *r_vec, size_t N, double G, double t,
                               double t_end, double dt);
@@ -223,16 +227,21 @@ int abie_measure_fp32_peak(int iters, double *tflops);
  * costs the FP64 pipe. */
 int abie_measure_fp64_issue(int active_lanes, double *tflops);
 /* No counterpart in the reference.  The fast FP64 all-pairs force on device
- * pointers, like abie_force_device with mode ABIE_FORCE_FP64, for callers
- * that cannot allocate GPU memory (inside a stream capture that must hold
- * no allocation, in a loop that may not wait on the allocator, or under a
- * budget that allows only their own buffers).  Scratch is a fixed area
- * compiled into the library, held by every GPU that loads it until exit:
- * N above ABIE_NOALLOC_MAX_BODIES returns ABIE_ERR_CAPACITY.  Calls share
- * that area, so calls that overlap on the GPU race; order them on one
- * stream.  The first call on each device (with it current) looks up the
- * area's device address; make it before any stream capture.  Runs on the
- * given stream (NULL: the default stream) and returns once queued. */
+ * pointers for callers that cannot call cudaMalloc: a real-time or
+ * host-callback loop that must not block on the allocator, or a process
+ * whose memory budget gives the library only the caller's own buffers.
+ * Scratch is a fixed area compiled into the library, held by every GPU that
+ * loads it until exit: N above ABIE_NOALLOC_MAX_BODIES (checked on the full
+ * size_t) returns ABIE_ERR_CAPACITY.  It always runs the one-chunk,
+ * one-sided force kernel: below 8,192 bodies that is the kernel
+ * abie_force_device(ABIE_FORCE_FP64) runs; from 8,192 bodies that entry
+ * point takes the symmetric or two-chunk forms, and the results agree to
+ * rounding (1e-13 per body), not bit for bit.  Sinks with m < 0 keep their
+ * acc entries, as in abie_force_device.  Calls share the scratch area, so
+ * calls that overlap on the GPU race; order them on one stream.  The first
+ * call on each device (with it current) looks up the area's device address;
+ * make it before any stream capture.  Runs on the given stream (NULL: the
+ * default stream) and returns once queued. */
 #define ABIE_NOALLOC_MAX_BODIES 65536
 int abie_force_device_noalloc(const double *d_pos, const double *d_m, size_t N,
                               double G, double *d_acc, void *stream);
@@ -254,6 +263,12 @@ void abie_debug_engine_shape(int lanes_per_body, int block);
  * post-Newtonian terms only), 0 automatic (stepped from 2^20 interactions
  * per force evaluation).  For tests and tuning. */
 void abie_debug_radau_path(int path);
+/* Sets the persistent Radau15 engines' grid-barrier wait limit in
+ * nanoseconds (a negative value restores the automatic limit, two seconds
+ * plus a term for the phase's work).  A wait past the limit stops the run
+ * with ABIE_ERR_TIMEOUT and every block leaves at its next barrier.  For the
+ * failure-detection tests. */
+void abie_debug_engine_timeout(long long ns);
 
 #ifdef __cplusplus
 }

@@ -44,12 +44,17 @@ def build_oracle(quiet=True):
     return ORACLE_SO
 
 
-def build_reference(ref_root="/root/reference"):
-    """Compile the reference C library from its sources, when they exist."""
-    if not os.path.isfile(os.path.join(ref_root, "src", "common.c")):
+def build_reference(ref_root=None):
+    """Compile the reference C library from its sources, when they exist.
+
+    ``ref_root`` (or the environment variable ABIE_REFERENCE_ROOT) names the
+    reference project's root; without either, oracle/build_ref.sh looks in
+    its own default location and skips the build when no sources are there."""
+    ref_root = ref_root or os.environ.get("ABIE_REFERENCE_ROOT")
+    if ref_root and not os.path.isfile(os.path.join(ref_root, "src", "common.c")):
         return None
-    out = subprocess.run(["bash", os.path.join(HERE, "build_ref.sh"), ref_root],
-                         capture_output=True, text=True)
+    cmd = ["bash", os.path.join(HERE, "build_ref.sh")] + ([ref_root] if ref_root else [])
+    out = subprocess.run(cmd, capture_output=True, text=True)
     if out.returncode != 0:
         raise RuntimeError("reference build failed:\n" + out.stdout + out.stderr)
     return REF_SO if os.path.isfile(REF_SO) else None
@@ -117,8 +122,11 @@ class Oracle:
         return acc
 
     def radau15(self, pos, vel, m, r, G, t, t_end, ce_dist=0.0, max_ce=1, max_coll=1,
-                events=True, C=0.0):
+                events=True, C=0.0, ext=None):
+        """src/integrator_gauss_radau15.c:221-380; ``ext`` (3N) is added to
+        every force call, as set_additional_forces does."""
         pos, vel, m, r = (_f64(pos).copy(), _f64(vel).copy(), _f64(m), _f64(r))
+        ext = None if ext is None else _f64(ext).copy()
         ev = _Events()
         buf_ce = np.zeros(4 * max(max_ce, 1))
         buf_coll = np.zeros(4 * max(max_coll, 1))
@@ -129,6 +137,7 @@ class Oracle:
         st = RadauStats()
         t_out = ctypes.c_double(t)
         self.lib.orc_set_pn(ctypes.c_double(C))
+        self.lib.orc_set_ext(_ptr(ext) if ext is not None else None)
         try:
             flag = self.lib.orc_radau15(_ptr(pos), _ptr(vel), _ptr(m), _ptr(r),
                                         ctypes.c_size_t(m.size), ctypes.c_double(G),
@@ -137,6 +146,7 @@ class Oracle:
                                         ctypes.byref(t_out), ctypes.byref(st))
         finally:
             self.lib.orc_set_pn(ctypes.c_double(0.0))
+            self.lib.orc_set_ext(None)
         return {"pos": pos, "vel": vel, "t": t_out.value, "flag": flag,
                 "stats": st.as_dict(), "n_ce": ev.n_ce, "n_coll": ev.n_coll,
                 "buf_ce": buf_ce, "buf_coll": buf_coll}
@@ -268,19 +278,27 @@ class Reference:
         self._load(pos, vel, m, np.zeros(m.size), G)
         return self.lib.calculate_energy()
 
-    def accelerations(self, pos, vel, m, G, C):
-        """calculate_accelerations (Newton, then post-Newtonian terms for C > 0)."""
+    def accelerations(self, pos, vel, m, G, C, ext=None):
+        """calculate_accelerations (Newton, then post-Newtonian terms for C > 0,
+        then the external accelerations ``ext`` when given)."""
         pos, vel, m = _f64(pos), _f64(vel), _f64(m)
         self._load(pos, vel, m, np.zeros(m.size), G, C=C)
+        if ext is not None:
+            ext = _f64(ext)
+            self.lib.set_additional_forces(ctypes.c_size_t(m.size), _ptr(ext))
         acc = np.zeros(pos.size)
         self.lib.calculate_accelerations(_ptr(pos), _ptr(vel), ctypes.c_size_t(m.size),
                                          ctypes.c_double(G), _ptr(m), _ptr(np.zeros(m.size)),
                                          _ptr(acc))
         return acc
 
-    def radau15(self, pos, vel, m, r, G, t, t_end, ce_dist=0.0, max_ce=1, max_coll=1, C=0.0):
+    def radau15(self, pos, vel, m, r, G, t, t_end, ce_dist=0.0, max_ce=1, max_coll=1, C=0.0,
+                ext=None):
         pos, vel, m, r = _f64(pos), _f64(vel), _f64(m), _f64(r)
         self._load(pos, vel, m, r, G, C=C, max_ce=max_ce, max_coll=max_coll, ce_dist=ce_dist)
+        if ext is not None:
+            ext = _f64(ext)
+            self.lib.set_additional_forces(ctypes.c_size_t(m.size), _ptr(ext))
         flag = _run_big_stack(lambda: self.lib.integrator_gr(
             ctypes.c_double(t), ctypes.c_double(t_end), ctypes.c_double(1.0)))
         p, v = self._state(m.size)

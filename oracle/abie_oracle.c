@@ -20,17 +20,17 @@
 #include "radau_constants.h"
 
 /* ------------------------------------------------------------------ */
-/* Force: src/common.c:163-201                                          */
+/* Force: src/common.c:39-77                                          */
 /* ------------------------------------------------------------------ */
 void orc_force(const double *pos, size_t n, double G, const double *m,
                double *acc, size_t j0, size_t j1)
 {
     for (size_t j = j0; j < j1 && j < n; j++) {
-        if (m[j] < 0.0) continue; /* deleted particle: acc left as is (:173) */
+        if (m[j] < 0.0) continue; /* deleted particle: acc left as is (:49) */
         const double xj = pos[3 * j], yj = pos[3 * j + 1], zj = pos[3 * j + 2];
         double ax = 0.0, ay = 0.0, az = 0.0;
         for (size_t k = 0; k < n; k++) {
-            if (k == j || m[k] <= 0.0) continue; /* :184 */
+            if (k == j || m[k] <= 0.0) continue; /* :60 */
             const double gm = G * m[k];
             const double dx = xj - pos[3 * k];
             const double dy = yj - pos[3 * k + 1];
@@ -95,7 +95,7 @@ int orc_force_threads(const double *pos, size_t n, double G, const double *m,
 }
 
 /* ------------------------------------------------------------------ */
-/* Small vector helpers: src/common.c:316-347                           */
+/* Small vector helpers: src/common.c:192-223                           */
 /* ------------------------------------------------------------------ */
 static double max_abs(const double *v, size_t n)
 {
@@ -154,7 +154,7 @@ double orc_energy(const double *pos, const double *vel, const double *m,
 }
 
 /* ------------------------------------------------------------------ */
-/* Close encounters and collisions: src/common.c:240-282                */
+/* Close encounters and collisions: src/common.c:116-158                */
 /* ------------------------------------------------------------------ */
 static void ring_put(double *buf, size_t count, size_t cap, double t, size_t i,
                      size_t j, double d)
@@ -171,7 +171,7 @@ int orc_check_events(const double *pos, const double *r, size_t n, double t,
                      orc_events *ev)
 {
     for (size_t j = 0; j < n; j++) {
-        for (size_t k = j + 1; k < n; k++) { /* the reference tests j<k (:257,:268) */
+        for (size_t k = j + 1; k < n; k++) { /* the reference tests j<k (:133,:144) */
             double dx = pos[3 * j] - pos[3 * k];
             double dy = pos[3 * j + 1] - pos[3 * k + 1];
             double dz = pos[3 * j + 2] - pos[3 * k + 2];
@@ -269,24 +269,32 @@ void orc_post_newtonian(const double *pos, const double *vel, size_t n, double G
     }
 }
 
-/* src/common.c:82-114 without external accelerations: Newton, then the
- * post-Newtonian terms when C > 0. */
+/* src/common.c:82-114: Newton, then the post-Newtonian terms when C > 0,
+ * then the external accelerations when set (:107-112, added component by
+ * component after the other terms). */
 static double g_orc_C = 0.0;
+static const double *g_orc_ext = NULL;
 static void force_counted_v(const double *y, const double *dy, size_t n, double G, const double *m,
                             double *acc, orc_radau_stats *st)
 {
-    /* sinks with negative mass keep a zero acceleration (see DESIGN notes on
-     * the reference leaving them untouched in malloc'd buffers) */
+    /* sinks with negative mass keep a zero acceleration (the reference leaves
+     * their entries of freshly malloc'd buffers untouched) */
     memset(acc, 0, 3 * n * sizeof(double));
     orc_force(y, n, G, m, acc, 0, n);
     if (g_orc_C > 0.0) orc_post_newtonian(y, dy, n, G, g_orc_C, m, acc);
+    if (g_orc_ext)
+        for (size_t i = 0; i < 3 * n; i++) acc[i] += g_orc_ext[i];
     if (st) st->force_calls++;
 }
 
 /* Speed of light for the oracle's Radau15 (0: no post-Newtonian terms). */
 void orc_set_pn(double C) { g_orc_C = C; }
 
-/* :75-120 */
+/* External accelerations (3N, kept by pointer) added to every force call of
+ * the oracle's Radau15, like src/common.c:364-380 with :107-112; NULL: none. */
+void orc_set_ext(const double *ext) { g_orc_ext = ext; }
+
+/* :9-54 */
 static double initial_step(const double *y0, const double *dy0, double G,
                            const double *m, size_t n, orc_radau_stats *st)
 {
@@ -298,7 +306,7 @@ static double initial_step(const double *y0, const double *dy0, double G,
     double *dy1 = (double *)malloc(dim * sizeof(double));
     double dt0, dt1;
     force_counted_v(y0, dy0, n, G, m, f0, st);
-    double d0 = max_abs(y0, n); /* the reference scans n (not 3n) entries (:89-90) */
+    double d0 = max_abs(y0, n); /* the reference scans n (not 3n) entries (:23-24) */
     double d1 = max_abs(f0, n);
     if (d0 < 1e-5 || d1 < 1e-5) dt0 = 1e-6;
     else dt0 = 0.01 * (d0 / d1);
@@ -320,7 +328,7 @@ static double initial_step(const double *y0, const double *dy0, double G,
     return dt;
 }
 
-/* :122-127 and :129-134.  The reference's parameter named h receives the
+/* :56-61 and :63-68.  The reference's parameter named h receives the
  * Radau spacing s (hs[ih], or 1 for the advance) and the one named T receives
  * the step dt: y = y1 + dt s (dy1 + dt s (F1 + s (b0/3 + s (b1/6 + ...))) / 2). */
 static void predict_pos(const double *y1, const double *dy1, const double *F1,
@@ -340,7 +348,7 @@ static void predict_vel(const double *dy1, const double *F1, double s,
     }
 }
 
-/* :136-187.  At substep ih the reference recomputes g[0..ih-1] from the
+/* :70-121.  At substep ih the reference recomputes g[0..ih-1] from the
  * sampled forces; the nested form below is the same recurrence, evaluated
  * in the same order: g_k = ((..((F_{k+1}-F_0)*r_{k+1,0} - g_0)*r_{k+1,1} ..)
  *                          - g_{k-1}) * r_{k+1,k}. */
@@ -355,7 +363,7 @@ static void update_g(double *const F[8], int ih, size_t dim, double *g[7])
     }
 }
 
-/* :189-241.  b_k = sum_{j>=k} cs[j][k] g_j for k < ih, added left to right
+/* :123-175.  b_k = sum_{j>=k} cs[j][k] g_j for k < ih, added left to right
  * starting from j = k (the reference writes b[0] starting with cs[0][0]*g0). */
 static void update_b(double *const g[7], int ih, size_t dim, double *b[7])
 {
@@ -368,7 +376,7 @@ static void update_b(double *const g[7], int ih, size_t dim, double *b[7])
     }
 }
 
-/* :244-284.  The reference's 'inited' flag is never set, so bd is always 0
+/* :178-218.  The reference's 'inited' flag is never set, so bd is always 0
  * and b <- E(q) + 0. */
 static void refine_b(double *b[7], double q, double *E[7], size_t dim)
 {
@@ -407,13 +415,13 @@ int orc_radau15(double *pos, double *vel, const double *m, const double *r,
     memcpy(y0, pos, dim * sizeof(double));
     memcpy(dy0, vel, dim * sizeof(double));
     int flag = 0;
-    force_counted_v(y0, dy0, n, G, m, ddy0, st);         /* :336 */
-    double h = initial_step(y0, dy0, G, m, n, st);        /* :339 */
+    force_counted_v(y0, dy0, n, G, m, ddy0, st);         /* :270 */
+    double h = initial_step(y0, dy0, G, m, n, st);        /* :273 */
 
     int running = 1, rejects_in_row = 0;
     while (running) {
         int iters = 0;
-        for (int ipc = 0; ipc < 12; ipc++) {               /* :347 */
+        for (int ipc = 0; ipc < 12; ipc++) {               /* :281 */
             iters++;
             for (int k = 0; k < 8; k++) memset(F[k], 0, dim * sizeof(double));
             for (int ih = 0; ih < 8; ih++) {
@@ -424,7 +432,7 @@ int orc_radau15(double *pos, double *vel, const double *m, const double *r,
                 update_b(g, ih, dim, b);
             }
             for (size_t i = 0; i < dim; i++) db6[i] = b[6][i] - b0[6][i];
-            if (max_abs(db6, dim) / max_abs(F[7], dim) < TOLPC) break; /* :366 */
+            if (max_abs(db6, dim) / max_abs(F[7], dim) < TOLPC) break; /* :300 */
             for (int k = 0; k < 7; k++) memcpy(b0[k], b[k], dim * sizeof(double));
         }
         if (st) {
@@ -432,13 +440,13 @@ int orc_radau15(double *pos, double *vel, const double *m, const double *r,
             st->attempts++;
             st->iter_hist[iters]++;
         }
-        predict_pos(y0, dy0, ddy0, 1., b, dim, h, y);        /* :375 */
+        predict_pos(y0, dy0, ddy0, 1., b, dim, h, y);        /* :309 */
         predict_vel(dy0, ddy0, 1., b, dim, h, dy);
         force_counted_v(y, dy, n, G, m, ddy, st);
         double estim_b6 = max_abs(b[6], dim) / max_abs(ddy, dim);
         double err = pow(estim_b6 / EPSB, EXPONENT);
         double dtreq = h / err;
-        if (err <= 1 || rejects_in_row > 100) {             /* :386 */
+        if (err <= 1 || rejects_in_row > 100) {             /* :320 */
             t += h;
             if (t_out) *t_out = t;
             rejects_in_row = 0;
@@ -458,13 +466,13 @@ int orc_radau15(double *pos, double *vel, const double *m, const double *r,
             rejects_in_row += 1;
             if (st) st->rejects++;
         }
-        if (dtreq / h > 1.0 / FAC) h /= FAC;                 /* :415 */
+        if (dtreq / h > 1.0 / FAC) h /= FAC;                 /* :349 */
         else if (dtreq < 1.e-12) h *= FAC;
         else h = dtreq;
         if (h < H_MIN) h = H_MIN;
         if (st) st->h_last = h;
     }
-    memcpy(pos, y0, dim * sizeof(double));                  /* :437-440 */
+    memcpy(pos, y0, dim * sizeof(double));                  /* :371-374 */
     memcpy(vel, dy, dim * sizeof(double));
     free(slab);
     return flag;
@@ -477,7 +485,7 @@ static const double KEPLER_TOL = 1e-12;   /* .h:7 */
 static const double TOL_ENERGY = 0.0;     /* .h:11 */
 static const size_t KEPLER_MAX_IT = 500;  /* .h:12 */
 
-/* :30-47 */
+/* :15-32 */
 static void stumpff(double psi, double *c2, double *c3)
 {
     if (psi > 1.e-10) {
@@ -492,7 +500,7 @@ static void stumpff(double psi, double *c2, double *c3)
     }
 }
 
-/* :66-147 */
+/* :51-132 */
 int orc_kepler(double *jpos, double *jvel, double gm, double dt, size_t id)
 {
     double r0v[3], v0v[3];
@@ -536,7 +544,7 @@ int orc_kepler(double *jpos, double *jvel, double gm, double dt, size_t id)
     return failed;
 }
 
-/* :221-280.  auxR/auxV are running mass-weighted sums over bodies 1..i,
+/* :206-265.  auxR/auxV are running mass-weighted sums over bodies 1..i,
  * R/V = aux/eta_i. */
 void orc_helio2jacobi(const double *pos, const double *vel, const double *m,
                       size_t n, double *jpos, double *jvel)
@@ -570,7 +578,7 @@ void orc_helio2jacobi(const double *pos, const double *vel, const double *m,
     free(eta);
 }
 
-/* :295-347.  Here R/V accumulate m_i * x_i / eta_i term by term. */
+/* :280-332.  Here R/V accumulate m_i * x_i / eta_i term by term. */
 void orc_jacobi2helio(const double *jpos, const double *jvel, const double *m,
                       size_t n, double *pos, double *vel)
 {
@@ -602,7 +610,7 @@ void orc_jacobi2helio(const double *jpos, const double *jvel, const double *m,
     free(eta);
 }
 
-/* :364-451.  With sparse != 0 the pairwise loop (:430-443) visits only pairs
+/* :349-436.  With sparse != 0 the pairwise loop (:415-428) visits only pairs
  * whose other member has nonzero mass; a zero-mass partner adds an exact
  * zero to the reference's sums, so the massive-partner terms and their order
  * are unchanged. */
@@ -678,7 +686,7 @@ void orc_wh_accel(const double *pos, const double *jpos, const double *m,
     free(ir3h); free(ir3j); free(a3); free(a2);
 }
 
-/* :471-492 */
+/* :456-477 */
 long orc_wh_step(double *pos, double *vel, double *jpos, double *jvel,
                  const double *m, size_t n, double G, double dt, double *accel,
                  int sparse)
@@ -687,7 +695,7 @@ long orc_wh_step(double *pos, double *vel, double *jpos, double *jvel,
     for (size_t i = 3; i < 3 * n; i++) vel[i] += accel[i] * (dt / 2);
     orc_helio2jacobi(pos, vel, m, n, jpos, jvel);
     double eta0 = m[0];
-    for (size_t i = 1; i < n; i++) {                     /* :189-206 */
+    for (size_t i = 1; i < n; i++) {                     /* :174-191 */
         double eta = eta0 + m[i];
         double gm = G * m[0] * eta / eta0;
         failed += orc_kepler(jpos, jvel, gm, dt, i);
@@ -699,7 +707,7 @@ long orc_wh_step(double *pos, double *vel, double *jpos, double *jvel,
     return failed;
 }
 
-/* :513-537 */
+/* :498-522 */
 long orc_wh(double *pos, double *vel, const double *m, size_t n, double G,
             double t, double t_end, double dt, double *t_out, int sparse)
 {

@@ -10,7 +10,8 @@ integrator_wh, integrator_rk,
 the event buffers) driven through ctypes by ``oracle.Reference``.  The
 inputs are the package's seeded generators.  The resulting ``golden.npz``
 is small, committed, and travels with the tests; nothing at test time reads
-the reference sources.  ``golden_aei.npz`` (``make_golden.py aei``) holds
+the reference sources.  ``golden_ext.npz`` (``make_golden.py ext``) holds
+the external-acceleration cases.  ``golden_aei.npz`` (``make_golden.py aei``) holds
 orbital elements from the reference's own Python (abie/particles.py,
 abie/tools.py), imported from its source tree.
 """
@@ -118,10 +119,15 @@ def main(out=os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden.np
     print("wrote", out, os.path.getsize(out), "bytes,", len(gold), "arrays")
 
 
-def _reference_python(ref_root="/root/reference"):
+def _reference_python(ref_root=None):
     """The reference's abie.particles and abie.tools, imported from its
-    source tree without running abie/__init__.py (which needs h5py/toml)."""
+    source tree (``ref_root`` or the environment variable
+    ABIE_REFERENCE_ROOT) without running abie/__init__.py (which needs
+    h5py/toml)."""
     import types
+    ref_root = ref_root or os.environ.get("ABIE_REFERENCE_ROOT")
+    if not ref_root:
+        raise SystemExit("set ABIE_REFERENCE_ROOT to the reference project's root")
     if "abie" not in sys.modules:
         pkg = types.ModuleType("abie")
         pkg.__path__ = [os.path.join(ref_root, "abie")]
@@ -152,9 +158,30 @@ def main_aei(out=os.path.join(os.path.dirname(os.path.abspath(__file__)), "golde
     print("wrote", out, os.path.getsize(out), "bytes,", len(gold), "arrays")
 
 
+def main_ext(out=os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden_ext.npz")):
+    """External accelerations (set_additional_forces, src/common.c:364-380)
+    through the reference's calculate_accelerations (:107-112) and its
+    Radau15 run, which adds them to every force call."""
+    build_reference()
+    R = Reference()
+    p, v, m, r = ics.planetary_system(seed=91, n_planets=5, n_tp=20)
+    ext = np.random.default_rng(92).normal(scale=1e-3, size=p.size)
+    gold = {"ext_in_pos": p, "ext_in_vel": v, "ext_m": m, "ext_r": r, "ext_acc_in": ext,
+            "ext_span": np.array([0.0, 2.0])}
+    gold["ext_accel"] = R.accelerations(p, v, m, G, 0.0, ext=ext)
+    out_ = R.radau15(p, v, m, r, G, 0.0, 2.0, ext=ext)
+    gold["ext_gr_pos"], gold["ext_gr_vel"] = out_["pos"], out_["vel"]
+    gold["ext_gr_t"] = np.array([out_["t"]])
+    np.savez_compressed(out, **gold)
+    print("wrote", out, os.path.getsize(out), "bytes,", len(gold), "arrays")
+
+
 if __name__ == "__main__":
     if sys.argv[1:] == ["aei"]:
         main_aei()
+    elif sys.argv[1:] == ["ext"]:
+        main_ext()
     else:
         main()
         main_aei()
+        main_ext()

@@ -1,0 +1,144 @@
+"""Long-horizon reference runs, committed as small fixtures.
+
+Run in a container where the reference sources exist:
+
+    oracle/build_ref.sh && python tests/golden/make_horizons.py [cfg1|ensemble|all]
+
+* ``horizon_cfg1.npz``: the 1,009-body planetary system (1 MSun star, 8
+  planets, 1,000 test particles; ``ics.planetary_system(seed=1001)``)
+  integrated by the unmodified reference library's ``integrator_gr`` from
+  0 to 100 yr in one call, with its final state, model time and the energy
+  of ``calculate_energy`` before and after.  A second run from the same
+  state with body 1's x coordinate moved by one unit in the last place
+  gives the spread that rounding alone produces over the same span; the
+  GPU tests compare against the first run with tolerances scaled by it.
+* ``horizon_ensemble.npz``: the first 64 systems of the batched-ensemble
+  workload (``ics.ensemble(seed0=10000)``: 0.5..1.5 MSun stars with 3..12
+  planets) integrated by the reference library from 0 to 1, 100 and 10,000
+  yr (three runs from t = 0 each), one process per host core.  Per system:
+  |dE/E| at each horizon, the model time, and the final state of the
+  10,000-yr run.  This is the distribution the reference method itself
+  reaches on these systems, against which the GPU forms' distributions are
+  judged.
+
+Without the reference library the C restatement in ``oracle/`` (bit for
+bit the same doubles, pinned by tests/test_oracle.py) stands in, and the
+file records which one ran.
+"""
+import multiprocessing as mp
+import os
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from abie_gb300 import ics  # noqa: E402
+
+G = ics.G_SOLAR
+HERE = os.path.dirname(os.path.abspath(__file__))
+ENS_SYSTEMS = 64
+ENS_HORIZONS = (1.0, 100.0, 10000.0)
+
+
+def _build_checkers():
+    """Build the reference library (where its sources are) and the oracle,
+    once, in the parent process: the workers only load them."""
+    import oracle
+    try:
+        oracle.build_reference()
+    except RuntimeError:
+        pass
+    oracle.build_oracle()
+
+
+def _checker():
+    """(name, object with radau15 and energy) -- the reference when built."""
+    import oracle
+    if oracle.reference_available():
+        return "reference", oracle.Reference()
+    return "oracle", oracle.Oracle()
+
+
+def cfg1_run(perturb):
+    kind, R = _checker()
+    p, v, m, r = ics.planetary_system(seed=1001)
+    if perturb:
+        p = p.copy()
+        p[3] = np.nextafter(p[3], np.inf)
+    e0 = R.energy(p, v, m, G)
+    t0 = time.time()
+    out = R.radau15(p, v, m, r, G, 0.0, 100.0)
+    wall = time.time() - t0
+    e1 = R.energy(out["pos"], out["vel"], m, G)
+    return {"kind": kind, "pos": out["pos"], "vel": out["vel"], "t": out["t"], "e0": e0,
+            "e1": e1, "wall": wall}
+
+
+def main_cfg1(out=os.path.join(HERE, "horizon_cfg1.npz")):
+    _build_checkers()
+    with mp.get_context("spawn").Pool(2) as pool:
+        base, pert = pool.map(cfg1_run, [False, True])
+    np.savez_compressed(
+        out, kind=np.array(base["kind"]), seed=np.array([1001]), span=np.array([0.0, 100.0]),
+        pos=base["pos"], vel=base["vel"], t=np.array([base["t"]]),
+        energy=np.array([base["e0"], base["e1"]]),
+        pert_pos=pert["pos"], pert_vel=pert["vel"], pert_t=np.array([pert["t"]]),
+        pert_energy=np.array([pert["e0"], pert["e1"]]), wall=np.array([base["wall"]]))
+    de = abs((base["e1"] - base["e0"]) / base["e0"])
+    print("cfg1: %s, t=%.6f, |dE/E|=%.3g, %.0f s; wrote %s" % (base["kind"], base["t"], de,
+                                                              base["wall"], out))
+
+
+def ens_run(job):
+    s, t_end = job
+    kind, R = _checker()
+    P, V, M, offs = ics.ensemble(n_systems=1, seed0=10000 + s)
+    r = np.zeros(M.size)
+    e0 = R.energy(P, V, M, G)
+    t0 = time.time()
+    out = R.radau15(P, V, M, r, G, 0.0, t_end)
+    wall = time.time() - t0
+    e1 = R.energy(out["pos"], out["vel"], M, G)
+    return {"s": s, "t_end": t_end, "kind": kind, "t": out["t"], "de": abs((e1 - e0) / e0),
+            "pos": out["pos"], "vel": out["vel"], "wall": wall}
+
+
+def main_ensemble(out=os.path.join(HERE, "horizon_ensemble.npz"), cores=None):
+    _build_checkers()
+    cores = cores or max(1, (os.cpu_count() or 2) - 1)
+    # longest runs first so the pool's tail is short
+    jobs = [(s, T) for T in sorted(ENS_HORIZONS, reverse=True) for s in range(ENS_SYSTEMS)]
+    t0 = time.time()
+    with mp.get_context("spawn").Pool(cores) as pool:
+        res = pool.map(ens_run, jobs, chunksize=1)
+    H = len(ENS_HORIZONS)
+    de = np.zeros((ENS_SYSTEMS, H))
+    tt = np.zeros((ENS_SYSTEMS, H))
+    wall = np.zeros((ENS_SYSTEMS, H))
+    P, V, M, offs = ics.ensemble(n_systems=ENS_SYSTEMS)
+    fpos, fvel = np.zeros_like(P), np.zeros_like(V)
+    for r in res:
+        h = ENS_HORIZONS.index(r["t_end"])
+        de[r["s"], h], tt[r["s"], h], wall[r["s"], h] = r["de"], r["t"], r["wall"]
+        if r["t_end"] == ENS_HORIZONS[-1]:
+            a, b = offs[r["s"]], offs[r["s"] + 1]
+            fpos[3 * a:3 * b], fvel[3 * a:3 * b] = r["pos"], r["vel"]
+    np.savez_compressed(out, kind=np.array(res[0]["kind"]), seed0=np.array([10000]),
+                        horizons=np.array(ENS_HORIZONS), de=de, t=tt, wall=wall,
+                        offsets=offs, pos=fpos, vel=fvel)
+    for h, T in enumerate(ENS_HORIZONS):
+        q = np.percentile(de[:, h], [50, 90, 99, 100])
+        print("ensemble %g yr: |dE/E| median %.2g p90 %.2g p99 %.2g max %.2g; <=1e-12: %d/%d"
+              % (T, q[0], q[1], q[2], q[3], int((de[:, h] <= 1e-12).sum()), ENS_SYSTEMS))
+    print("%s, %.0f s on %d cores; wrote %s" % (res[0]["kind"], time.time() - t0, cores, out))
+
+
+if __name__ == "__main__":
+    what = sys.argv[1] if len(sys.argv) > 1 else "all"
+    if what in ("cfg1", "all"):
+        main_cfg1()
+    if what in ("ensemble", "all"):
+        main_ensemble()

@@ -122,3 +122,23 @@ def test_oracle_planted_mistake_is_caught(oracle, golden):
     acc = oracle.force(p, m, G)
     acc[7] = np.nextafter(acc[7], np.inf)
     assert not np.array_equal(acc, golden["force_sys_acc"])
+
+
+def test_external_accelerations_golden(oracle):
+    """set_additional_forces: the oracle's Radau15 with a constant external
+    acceleration added to every force call equals the reference's run, and
+    its force plus the vector equals the reference's calculate_accelerations."""
+    import os
+    gold = np.load(os.path.join(os.path.dirname(__file__), "golden", "golden_ext.npz"))
+    p, v, m, r, ext = (gold["ext_in_pos"], gold["ext_in_vel"], gold["ext_m"], gold["ext_r"],
+                       gold["ext_acc_in"])
+    acc = oracle.force(p, m, G, acc=np.zeros(p.size)) + ext
+    assert np.array_equal(acc, gold["ext_accel"])
+    t0, t1 = gold["ext_span"]
+    out = oracle.radau15(p, v, m, r, G, t0, t1, ext=ext)
+    assert np.array_equal(out["pos"], gold["ext_gr_pos"])
+    assert np.array_equal(out["vel"], gold["ext_gr_vel"])
+    assert out["t"] == gold["ext_gr_t"][0]
+    # without the vector the run differs (the term is live)
+    plain = oracle.radau15(p, v, m, r, G, t0, t1)
+    assert not np.array_equal(plain["pos"], gold["ext_gr_pos"])

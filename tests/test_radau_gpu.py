@@ -54,7 +54,7 @@ def at_time(pos, vel, m, t_from, t_to, oracle):
 
 
 def _direct(clib, pos, vel, m, r, t0, t1, mode):
-    """integrator_gauss_radau15 on caller arrays (src/integrator_gauss_radau15.c:287)."""
+    """integrator_gauss_radau15 on caller arrays (src/integrator_gauss_radau15.c:221)."""
     import ctypes as C
     lib = clib.lib
     old = clib.set_force_mode(mode)

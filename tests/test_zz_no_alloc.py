@@ -1,6 +1,14 @@
-"""The allocation-free force entry point (for callers that cannot allocate
-GPU memory: inside a capture that must hold no allocation, or with only
-their own buffers to spend) against the allocating one, through the C ABI.
+"""The allocation-free force entry point against the allocating one, through
+the C ABI.  It serves callers that may not call cudaMalloc (a real-time
+loop that must not block on the allocator, or a budget limited to their own
+buffers).
+
+Sizes: 3,000 and 709 bodies take the same one-chunk kernel in both entry
+points; 8,192 and 65,536 all-massive bodies (the scratch's limit) meet the
+symmetric form of abie_force_device, and 10,000 bodies with massless and
+deleted ones meet its two-chunk form, so those agree to rounding (1e-13 per
+body).  Deleted sinks (m < 0) keep their acc entries in both.  Every case
+runs two calls in a row.
 
 Collected last on purpose: it runs after every other test, and must also
 pass alone in a fresh process."""
@@ -16,6 +24,8 @@ pytestmark = pytest.mark.gpu
 G = ics.G_SOLAR
 C = ctypes
 ERR_CAPACITY = -6
+MAX_BODIES = 65536
+SENTINEL = 12345.0
 
 
 def _bind(lib):
@@ -25,35 +35,55 @@ def _bind(lib):
     return lib
 
 
+def _cases():
+    p, v, m, r = ics.planetesimal_disk(seed=21, n=3000)
+    yield "disk-3001", p, m
+    p, v, m, r = ics.planetary_system(seed=22, n_planets=9, n_tp=700)  # fewer sources, some massless
+    yield "system-710", p, m
+    p, v, m, r = ics.planetesimal_disk(seed=23, n=8191)                 # 8,192 bodies, all massive
+    yield "disk-8192", p, m
+    p, v, m, r = ics.planetesimal_disk(seed=24, n=9999)                 # 10,000 bodies
+    rng = np.random.default_rng(25)
+    idx = rng.permutation(m.size)
+    m = m.copy()
+    m[idx[:2000]] = 0.0      # massless
+    m[idx[2000:2100]] = -1.0  # deleted
+    yield "mixed-10000", p, m
+    p, v, m, r = ics.planetesimal_disk(seed=26, n=MAX_BODIES - 1)       # the scratch's limit
+    yield "disk-65536", p, m
+
+
 def test_noalloc_matches_allocating_entry_point_on_consecutive_calls(clib):
     import torch
     lib = _bind(clib.lib)
     dev = torch.device("cuda", 0)
-    cases = []
-    p, v, m, r = ics.planetesimal_disk(seed=21, n=3000)
-    cases.append((p, m))
-    p, v, m, r = ics.planetary_system(seed=22, n_planets=9, n_tp=700)  # fewer sources, some massless
-    cases.append((p, m))
-    for p, m in cases:
+    for name, p, m in _cases():
         pos = torch.from_numpy(p).to(dev)
         mass = torch.from_numpy(m).to(dev)
-        a_ref = torch.zeros_like(pos)
-        a_new = torch.full_like(pos, np.nan)
+        a_ref = torch.full_like(pos, SENTINEL)
         torch.cuda.synchronize()
         rc = lib.abie_force_device(C.c_void_p(pos.data_ptr()), C.c_void_p(mass.data_ptr()),
                                    C.c_size_t(m.size), C.c_double(G), C.c_void_p(a_ref.data_ptr()),
                                    C.c_int(FORCE_FP64), None)
-        assert rc == 0
-        rc = lib.abie_force_device_noalloc(pos.data_ptr(), mass.data_ptr(), m.size, G,
-                                           a_new.data_ptr(), None)
-        assert rc == 0
+        assert rc == 0, name
         torch.cuda.synchronize()
-        ref, new = a_ref.cpu().numpy(), a_new.cpu().numpy()
-        assert np.isfinite(new).all()
-        assert rel_err_per_body(new, ref) <= 1e-13
+        ref = a_ref.cpu().numpy()
+        live = np.repeat(m >= 0.0, 3)
+        for call in range(2):  # two calls in a row share the scratch
+            a_new = torch.full_like(pos, SENTINEL)
+            rc = lib.abie_force_device_noalloc(pos.data_ptr(), mass.data_ptr(), m.size, G,
+                                               a_new.data_ptr(), None)
+            assert rc == 0, (name, call)
+            torch.cuda.synchronize()
+            new = a_new.cpu().numpy()
+            assert np.isfinite(new).all(), (name, call)
+            assert (new[~live] == SENTINEL).all() and (ref[~live] == SENTINEL).all(), (name, call)
+            err = rel_err_per_body(new[live], ref[live])
+            assert err <= 1e-13, (name, call, err)
 
 
 def test_noalloc_rejects_sizes_beyond_its_scratch(clib):
     lib = _bind(clib.lib)
-    rc = lib.abie_force_device_noalloc(None, None, 65537, G, None, None)
-    assert rc == ERR_CAPACITY
+    assert lib.abie_force_device_noalloc(None, None, MAX_BODIES + 1, G, None, None) == ERR_CAPACITY
+    # the full size_t is checked: 2^32 + 10 is not run as 10 bodies
+    assert lib.abie_force_device_noalloc(None, None, (1 << 32) + 10, G, None, None) == ERR_CAPACITY
