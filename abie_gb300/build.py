@@ -4,7 +4,8 @@ Each .cu under csrc/ compiles to its own object in parallel; the objects link
 into one shared library with the CUDA runtime linked statically, so the
 library loads on machines without a GPU driver (its calls then report that
 no device is present).  Device code is sm_103a only; every unit is built
-with --fmad=false (see csrc/common.cuh).
+with --fmad=false (see csrc/common.cuh), except the plain FP64 ensemble
+form (ensemble_plain.cu), built with FMA contraction.
 """
 import concurrent.futures as cf
 import glob
@@ -38,12 +39,23 @@ def _sources():
     return sorted(glob.glob(os.path.join(CSRC, "*.cu")))
 
 
+# Units whose flags differ: the plain FP64 ensemble form is the reference's
+# expressions compiled with FMA contraction, as a straightforward port.
+FMAD_TRUE = {"ensemble_plain.cu"}
+
+
+def _flags(src):
+    if os.path.basename(src) in FMAD_TRUE:
+        return [f if f != "--fmad=false" else "--fmad=true" for f in NVCC_FLAGS]
+    return NVCC_FLAGS
+
+
 def _fingerprint():
     h = hashlib.sha256()
     for p in sorted(glob.glob(os.path.join(CSRC, "*")) + glob.glob(os.path.join(INCLUDE, "*.h"))):
         with open(p, "rb") as fh:
             h.update(p.encode() + fh.read())
-    h.update(" ".join(ARCH + NVCC_FLAGS).encode())
+    h.update(" ".join(ARCH + NVCC_FLAGS + sorted(FMAD_TRUE)).encode())
     h.update(os.uname().machine.encode())
     return h.hexdigest()
 
@@ -62,7 +74,7 @@ def build(force=False, verbose=False, ptxas_verbose=False):
 
     def compile_one(src):
         obj = os.path.join(OUT, os.path.basename(src)[:-3] + ".o")
-        cmd = [nvcc] + ARCH + NVCC_FLAGS + extra + ["-c", src, "-o", obj]
+        cmd = [nvcc] + ARCH + _flags(src) + extra + ["-c", src, "-o", obj]
         res = subprocess.run(cmd, capture_output=True, text=True)
         return src, obj, res
 

@@ -178,9 +178,14 @@ int initialize_code(double G, double C, size_t N_MAX, size_t MAX_N_CE, size_t MA
     Sim &s = g_sim;
     if (s.inited) return 0;  // once per process, src/common.c:227
     if (deviceID < 0) {
-        set_error(ABIE_ERR_NO_DEVICE,
-                  "deviceID=%d: this library runs the GPU path only; pass a GPU id", deviceID);
-        return ABIE_ERR_NO_DEVICE;
+        // The reference's default (abie/__init__.py:31) selects its CPU code;
+        // this library has only the GPU path, so it runs on GPU 0 and says so
+        // (the reference's binding ignores initialize_code's return value).
+        fprintf(stderr,
+                "abie_gb300: deviceID=%d selects the reference's CPU code; this library has "
+                "only the GPU path and runs on GPU 0\n",
+                deviceID);
+        deviceID = 0;
     }
     int rc = ensure_device(deviceID);
     if (rc) return rc;

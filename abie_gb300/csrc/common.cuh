@@ -282,6 +282,130 @@ __device__ __forceinline__ void pair_fast(double xj, double yj, double zj, const
     az = fma(-w, dz, az);
 }
 
+// The plain FP64 GPU pair term of the reference's gpuforce_v2
+// (src/gpuforce.cu:61-84, without softening): d2 = dx^2 + dy^2 + dz^2,
+// skipped when zero, 1/sqrt by the CUDA rsqrt, inv^3, a -= G m d inv^3.
+// Written as plain expressions: the unit that uses it is compiled with FMA
+// contraction, as a straightforward port would be.
+__device__ __forceinline__ void pair_naive(double xj, double yj, double zj, const Src &s,
+                                           double &ax, double &ay, double &az)
+{
+    const double dx = xj - s.x;
+    const double dy = yj - s.y;
+    const double dz = zj - s.z;
+    const double d2 = dx * dx + dy * dy + dz * dz;
+    if (d2 == 0.0) return;
+    const double inv = rsqrt(d2);
+    const double inv3 = inv * inv * inv;
+    ax -= s.gm * dx * inv3;
+    ay -= s.gm * dy * inv3;
+    az -= s.gm * dz * inv3;
+}
+
+// A double as the sum of two floats of 24 significant bits each, by integer
+// instructions only: hi is x truncated to 24 bits, lo the rest truncated to
+// 24 bits, so |x - (hi + lo)| < 2^-47 |x| and both carry x's sign.  x must
+// be zero or have its magnitude within the float range (about 1.2e-38 ..
+// 3.4e38); values below it give (0, 0), and a lo part below it is dropped.
+__device__ __forceinline__ float2 split_ff(double x)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned sgn = (unsigned)(b >> 32) & 0x80000000u;
+    const int ex = (int)((b >> 52) & 0x7FF);
+    const int fe = ex - 1023 + 127;
+    if (fe < 1) return make_float2(0.0f, 0.0f);
+    const unsigned long long M = b & 0xFFFFFFFFFFFFFull;
+    const float hi = __uint_as_float(sgn | ((unsigned)min(fe, 254) << 23) | (unsigned)(M >> 29));
+    const unsigned r = (unsigned)(M & 0x1FFFFFFFull);  // the 29 bits below hi
+    const int lz = __clz(r);                           // 3..32
+    const int le = ex - 917 - lz;                      // float exponent of r's leading bit
+    const float lo = (r == 0u || le < 1)
+                         ? 0.0f
+                         : __uint_as_float(sgn | ((unsigned)le << 23) | (((r << lz) >> 8) & 0x7FFFFFu));
+    return make_float2(hi, lo);
+}
+
+// A float as a double, exactly, by integer instructions (zero and subnormal
+// floats give zero; infinities and NaN are not expected).
+__device__ __forceinline__ double f32_to_f64_exact(float f)
+{
+    const unsigned b = __float_as_uint(f);
+    if ((b & 0x7F800000u) == 0u) return 0.0;
+    const unsigned sgn = b & 0x80000000u;
+    const unsigned a = b & 0x7FFFFFFFu;
+    return __hiloint2double((int)(((a >> 3) + ((1023 - 127) << 20)) | sgn), (int)(a << 29));
+}
+
+// One term w d added to the two-float sum (S, C) in single precision: the
+// product of the two-float factors to about 2^-46 (the exact error of
+// w_hi d_hi by fmaf, plus the cross terms) and S + p by TwoSum, whose exact
+// rounding error goes to C with the product's.  The unit is built without
+// FMA contraction, so every other operation rounds as written.
+__device__ __forceinline__ void ff_add_product(float2 w, float2 d, float &S, float &C)
+{
+    const float p = w.x * d.x;
+    float pe = fmaf(w.x, d.x, -p);
+    pe = fmaf(w.x, d.y, pe);
+    pe = fmaf(w.y, d.x, pe);
+    const float sm = S + p;
+    const float z = sm - S;
+    const float t = (S - (sm - z)) + (p - z);
+    C = C + (t + pe);
+    S = sm;
+}
+
+// Two-float (hi + lo) arithmetic in single precision for the mixed forms,
+// after Dekker and Knuth: TwoSum and FMA-based TwoProd give the exact
+// rounding errors, renormalised by Fast2Sum, about 2^-46 relative.  The
+// library is built without FMA contraction, so every step rounds as written.
+__device__ __forceinline__ float2 ff_fast_two_sum(float a, float b)
+{
+    const float s = a + b;
+    return make_float2(s, b - (s - a));
+}
+
+__device__ __forceinline__ float2 ff_add(float2 a, float2 b)
+{
+    const float s = a.x + b.x;
+    const float z = s - a.x;
+    const float e = (a.x - (s - z)) + (b.x - z);
+    return ff_fast_two_sum(s, e + (a.y + b.y));
+}
+
+__device__ __forceinline__ float2 ff_sub(float2 a, float2 b)
+{
+    return ff_add(a, make_float2(-b.x, -b.y));
+}
+
+__device__ __forceinline__ float2 ff_mul(float2 a, float2 b)
+{
+    const float p = a.x * b.x;
+    float e = fmaf(a.x, b.x, -p);
+    e = fmaf(a.x, b.y, e);
+    e = fmaf(a.y, b.x, e);
+    return ff_fast_two_sum(p, e);
+}
+
+__device__ __forceinline__ float2 ff_sqr(float2 a)
+{
+    const float p = a.x * a.x;
+    const float e = fmaf(a.x, a.x, -p);
+    return ff_fast_two_sum(p, fmaf(2.0f * a.x, a.y, e));
+}
+
+// 1/sqrt(x) for a positive two-float x within the float range: the
+// rsqrtf seed y and one correction from the expansion
+// x^(-1/2) = y (1 - e)^(-1/2) = y (1 + e/2 + 3/8 e^2 + O(e^3)), e = 1 - x y^2
+// evaluated in two-float arithmetic (e itself is below 2^-21).
+__device__ __forceinline__ float2 ff_rsqrt(float2 x)
+{
+    const float y = rsqrtf(x.x);
+    const float2 t = ff_mul(x, ff_sqr(make_float2(y, 0.0f)));
+    const float2 e = ff_sub(make_float2(1.0f, 0.0f), t);
+    const float k = e.x * fmaf(0.375f, e.x, 0.5f);
+    return ff_fast_two_sum(y, y * k);
+}
+
 // Non-negative doubles keep their order when read as unsigned integers, so
 // a max over |v| can be an integer atomicMax.  0 encodes "no value seen";
 // NaN is skipped, like the reference's vector_max_abs (src/common.c:192-198).

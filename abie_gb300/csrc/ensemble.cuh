@@ -26,6 +26,8 @@ int ensemble_run(double *pos, double *vel, const double *m, const long long *off
                  double G, double t0, double t_end, double *t_out, int *status, long long *steps,
                  int mode, const LearnedPredictor *mlp, cudaStream_t st, EnsembleStats *stats,
                  const EnsembleLearnIO *learn_io, bool consistent_g, const float *mlp_tau);
+// The plain FP64 form's kernel for groups of w warps (ensemble_plain.cu).
+const void *ensemble_plain_fn(int w);
 // Host copy of the output scales of the enabled learned predictor.
 const float *learned_predictor_tau();
 double ensemble_last_seconds();

@@ -212,9 +212,15 @@ int launch_force_mixed(const double *pos, const double *m, int n, double G, Forc
 {
     (void)G;
     // s.src / s.n_src were filled by launch_force's compaction
+    return launch_force_mixed_src(pos, m, n, s.src, s.n_src, s, acc, st);
+}
+
+int launch_force_mixed_src(const double *pos, const double *m, int n, const Src *src,
+                           const int *n_src, ForceScratch &s, double *acc, cudaStream_t st)
+{
     if (!s.gm_max) ABIE_CUDA(cudaMalloc(&s.gm_max, sizeof(unsigned long long)));
     ABIE_CUDA(cudaMemsetAsync(s.gm_max, 0, sizeof(unsigned long long), st));
-    max_gm_kernel<<<std::max(1, std::min(152, (n + 255) / 256)), 256, 0, st>>>(s.src, s.n_src, s.gm_max);
+    max_gm_kernel<<<std::max(1, std::min(152, (n + 255) / 256)), 256, 0, st>>>(src, n_src, s.gm_max);
     ABIE_CUDA(cudaGetLastError());
     const int sink_blocks = (n + SINKS_PER_BLOCK - 1) / SINKS_PER_BLOCK;
     int num_sms = 152;
@@ -231,7 +237,7 @@ int launch_force_mixed(const double *pos, const double *m, int n, double G, Forc
             s.partial_cap = need;
         }
     }
-    force_mixed_kernel<<<sink_blocks * chunks, MT, 0, st>>>(pos, m, n, s.src, s.n_src, s.gm_max,
+    force_mixed_kernel<<<sink_blocks * chunks, MT, 0, st>>>(pos, m, n, src, n_src, s.gm_max,
                                                              g_heavy_fraction, chunks, acc, s.partial);
     ABIE_CUDA(cudaGetLastError());
     if (chunks > 1) {

@@ -37,6 +37,7 @@
 #include "pn.cuh"
 #include "radau_comp.cuh"
 #include "radau_constants.h"
+#include "mixed.cuh"
 
 namespace abie {
 
@@ -1528,7 +1529,8 @@ __global__ void st_commit_kernel(EngineArgs a)
 
 // The host loop; the state sits in the engine's buffers (phase 0 start).
 template <int MODE>
-static int stepped_run(const EngineArgs &a, int num_sms, cudaStream_t st, EngineCtl *out)
+static int stepped_run(const EngineArgs &a, int num_sms, cudaStream_t st, EngineCtl *out,
+                       bool mixed = false)
 {
     EngineCtl *ctl = a.ctl;
     double *acc = a.vp[0];  // force output (the velocity buffers serve post-Newtonian runs only)
@@ -1559,6 +1561,7 @@ static int stepped_run(const EngineArgs &a, int num_sms, cudaStream_t st, Engine
         const double *pos = buf < 2 ? a.yp[buf] : a.ypa;
         const Src *src = buf < 2 ? a.src[buf] : a.srca;
         force_calls++;
+        if (mixed) return launch_force_mixed_src(pos, a.m, a.n, src, &ctl->n_src, g_sim.fs, acc, st);
         if (sym) return launch_force_published_sym(src, a.n, &ctl->n_src, acc, g_sim.fs, st);
         return launch_force_published(pos, a.m, a.n, src, &ctl->n_src, lanes, acc, &ctl->next_sink, st,
                                       partial);
@@ -1749,7 +1752,22 @@ int radau_run(const SystemView &sys, double t, double t_end, int mode, EventStat
         *t_out = t;
         return 0;
     }
-    if (mode == ABIE_FORCE_NAIVE || mode == ABIE_FORCE_MIXED) mode = ABIE_FORCE_FP64;
+    if (mode == ABIE_FORCE_NAIVE) {
+        set_error(ABIE_ERR_UNSUPPORTED,
+                  "Radau15: the naive force form is the force comparator only; integrate in the "
+                  "exact, fp64 or mixed form");
+        return ABIE_ERR_UNSUPPORTED;
+    }
+    // The mixed form: the fast sweep with the mixed all-pairs force (FP32
+    // pair terms for light sources) on every substep, through the stepped
+    // engine, whatever the size.
+    const bool mixed = mode == ABIE_FORCE_MIXED;
+    if (mixed && g_sim.C > 0.0) {
+        set_error(ABIE_ERR_UNSUPPORTED,
+                  "Radau15: the post-Newtonian terms have no mixed form; use the exact or fp64 form");
+        return ABIE_ERR_UNSUPPORTED;
+    }
+    if (mixed) mode = ABIE_FORCE_FP64;
     size_t max_ce = evs ? evs->max_ce : 0, max_coll = evs ? evs->max_coll : 0;
     int rc = engine_reserve((size_t)n, max_ce, max_coll);
     if (rc) return rc;
@@ -1847,7 +1865,7 @@ int radau_run(const SystemView &sys, double t, double t_end, int mode, EventStat
     // unless a launch shape is forced or the particles exceed one
     // resident wave
     bool split = false;
-    if (n_src <= 10 && g_engine_js == 0) {
+    if (n_src <= 10 && g_engine_js == 0 && !mixed) {
         int bps = 0;
         ABIE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, split_fn(mode, a.C > 0.0), 64, 0));
         split = (long long)std::max(1, (n_tp + SPLIT_TPW - 1) / SPLIT_TPW) <=
@@ -1857,11 +1875,11 @@ int radau_run(const SystemView &sys, double t, double t_end, int mode, EventStat
     // large systems in the fast form without post-Newtonian terms: the
     // stepped engine (the standalone force kernel for every substep)
     const bool stepped =
-        !split && a.C <= 0.0 && mode == ABIE_FORCE_FP64 &&
-        (g_radau_path == 2 ||
-         (g_radau_path == 0 && g_engine_js == 0 && (long long)n * (long long)n_src >= (1ll << 20)));
+        mixed || (!split && a.C <= 0.0 && mode == ABIE_FORCE_FP64 &&
+                  (g_radau_path == 2 ||
+                   (g_radau_path == 0 && g_engine_js == 0 && (long long)n * (long long)n_src >= (1ll << 20))));
     if (stepped) {
-        rc = stepped_run<ABIE_FORCE_FP64>(a, g_sim.num_sms, st, &c);
+        rc = stepped_run<ABIE_FORCE_FP64>(a, g_sim.num_sms, st, &c, mixed);
         if (rc) return rc;
         if (c.err) {
             set_error(c.err, "radau engine stopped (code %d, t=%g)", c.err, c.t);

@@ -1,15 +1,26 @@
 // Radau15 on one component per thread (src/integrator_gauss_radau15.c:56-218),
 // shared by the batched ensemble (ensemble.cu) and the split engine for
-// systems with few massive bodies (radau_split.cu).  Each thread keeps its
+// systems with few massive bodies (radau.cu).  Each thread keeps its
 // component's state -- y0, dy0, F1, b[7], g[7], previous b6 -- in
 // registers.  MODE ABIE_FORCE_EXACT repeats the reference's expressions in
-// its order (built with --fmad=false); the fast form runs the corrector on
-// the Newton-form coefficients g with tabulated weights.
+// its order (built with --fmad=false); ABIE_FORCE_NAIVE, the plain FP64
+// form, runs the same expressions in a unit built with FMA contraction; the
+// fast and mixed forms run the corrector on the Newton-form coefficients g
+// with tabulated weights.
 #pragma once
 #include "common.cuh"
 #include "radau_constants.h"
 
 namespace abie {
+
+// Forms that run the reference's operations: its Horner predictor on b, b
+// rebuilt from g after every force, the division in the convergence test
+// and pow in the step control.
+template <int MODE>
+__host__ __device__ constexpr bool ref_ops()
+{
+    return MODE == ABIE_FORCE_EXACT || MODE == ABIE_FORCE_NAIVE;
+}
 
 static __constant__ double e_hs[8] = ABIE_RADAU_HS_INIT;
 static __constant__ double e_rs[8][8] = ABIE_RADAU_RS_INIT;
@@ -49,7 +60,7 @@ __device__ __forceinline__ double e_pred_pos(const Comp &c, int row, double s, d
                                              double hh)
 {
     const double *b = c.b;
-    if (MODE == ABIE_FORCE_EXACT)
+    if (ref_ops<MODE>())
         return c.y0 + dt * s * (c.dy0 + dt * s * (c.F1 + s * (b[0] / 0.3e1 + s * (b[1] / 0.6e1 + s * (b[2] / 0.10e2 + s * (b[3] / 0.15e2 + s * (b[4] / 0.21e2 + s * (b[5] / 0.28e2 + s * b[6] / 0.36e2))))))) / 0.2e1);
     const double *w = e_wg[row];
     const double *g = c.g;
@@ -68,7 +79,7 @@ template <int MODE>
 __device__ __forceinline__ double e_pred_vel(const Comp &c, double dt)
 {
     const double *b = c.b;
-    if (MODE == ABIE_FORCE_EXACT) {
+    if (ref_ops<MODE>()) {
         const double s = 1.0;
         return c.dy0 + dt * s * (c.F1 + s * (b[0] / 0.2e1 + s * (b[1] / 0.3e1 + s * (b[2] / 0.4e1 + s * (b[3] / 0.5e1 + s * (b[4] / 0.6e1 + s * (b[5] / 0.7e1 + s * b[6] / 0.8e1)))))));
     }
@@ -89,7 +100,7 @@ template <int MODE>
 __device__ __forceinline__ double e_pred_vel_at(const Comp &c, int row, double s, double dt)
 {
     const double *b = c.b;
-    if (MODE == ABIE_FORCE_EXACT)
+    if (ref_ops<MODE>())
         return c.dy0 + dt * s * (c.F1 + s * (b[0] / 0.2e1 + s * (b[1] / 0.3e1 + s * (b[2] / 0.4e1 + s * (b[3] / 0.5e1 + s * (b[4] / 0.6e1 + s * (b[5] / 0.7e1 + s * b[6] / 0.8e1)))))));
     const double *w = e_vgs[row];
     const double *g = c.g;
@@ -107,7 +118,7 @@ __device__ __forceinline__ double e_pred_vel_at(const Comp &c, int row, double s
 template <int MODE>
 __device__ __forceinline__ double e_b6(const Comp &c)
 {
-    return MODE == ABIE_FORCE_EXACT ? c.b[6] : c.g[6];
+    return ref_ops<MODE>() ? c.b[6] : c.g[6];
 }
 
 // g and b after the force F of substep IH (src/integrator_gauss_radau15.c:70-175);
@@ -124,7 +135,7 @@ __device__ __forceinline__ void e_gb_update_ih(Comp &c, double F)
         double s = e_cs[k][k] * c.g[k];
 #pragma unroll
         for (int jj = k + 1; jj < 7; jj++) {
-            if (MODE == ABIE_FORCE_EXACT) s = s + e_cs[jj][k] * c.g[jj];  // reference roundings
+            if (ref_ops<MODE>()) s = s + e_cs[jj][k] * c.g[jj];  // reference roundings
             else s = fma(e_cs[jj][k], c.g[jj], s);
         }
         c.b[k] = s;
@@ -146,7 +157,7 @@ __device__ __forceinline__ void e_g_update_ih(Comp &c, double F)
 template <int MODE>
 __device__ __forceinline__ void e_gb_update(Comp &c, int ih, double F)
 {
-    if (MODE == ABIE_FORCE_EXACT) {
+    if (ref_ops<MODE>()) {
         switch (ih) {
         case 1: e_gb_update_ih<MODE, 1>(c, F); break;
         case 2: e_gb_update_ih<MODE, 2>(c, F); break;
@@ -216,7 +227,7 @@ __device__ __forceinline__ unsigned long long warp_maxk(unsigned long long v)
 template <int MODE>
 __device__ __forceinline__ bool corrector_converged(double db6, double f8)
 {
-    return MODE == ABIE_FORCE_EXACT ? db6 / f8 < TOLPC : db6 < TOLPC * f8;
+    return ref_ops<MODE>() ? db6 / f8 < TOLPC : db6 < TOLPC * f8;
 }
 
 // Step control (src/integrator_gauss_radau15.c:313-367): err =
@@ -234,7 +245,7 @@ template <int MODE>
 __device__ __forceinline__ void step_size(double estim_b6, double h, double &err, double &dtreq,
                                           double &rq)
 {
-    if (MODE == ABIE_FORCE_EXACT) {  // the reference's operations
+    if (ref_ops<MODE>()) {  // the reference's operations
         err = pow(estim_b6 / EPSB, 1. / 7);
         dtreq = h / err;
         rq = dtreq / h;
@@ -343,6 +354,7 @@ __device__ __forceinline__ void group_force(const Group<W> &grp, int n, const do
 {
     const int spw = (n + W - 1) / W;
     const int L = MODE == ABIE_FORCE_EXACT ? 1 : max(1, 32 / max(spw, 1));
+    static_assert(MODE != ABIE_FORCE_MIXED, "the mixed form uses group_force_sym_mixed");
     const int lane = grp.lane;
     const int gw = lane / L, hh = lane % L;
     const int g = grp.wig * spw + gw;
@@ -357,6 +369,7 @@ __device__ __forceinline__ void group_force(const Group<W> &grp, int n, const do
             if (k == g || __double_as_longlong(gm) <= 0) continue;
             Src s{sp[k][0], sp[k][1], sp[k][2], gm};
             if (MODE == ABIE_FORCE_EXACT) pair_exact(xi, yi, zi, s, ax, ay, az);
+            else if (MODE == ABIE_FORCE_NAIVE) pair_naive(xi, yi, zi, s, ax, ay, az);
             else pair_fast(xi, yi, zi, s, ax, ay, az);
         }
     }
@@ -433,6 +446,111 @@ __device__ __forceinline__ void group_force_sym(const Group<W> &grp, int n, cons
         sa[b][c] = s;
     }
     grp.sync();
+}
+
+// Mixed form of group_force_sym: the pair lanes work as there (FP64
+// separations, the integer r^-3 core), and a partner counts as heavy when
+// bit j of hmask is set (a G m of at least 1/128 of the system's largest:
+// the star, or both stars of a binary).  A body's terms from heavy partners
+// are stored and summed as in the fast form (one FP64 FMA each); a term from
+// a light partner is stored as two-float pairs (w and the separation split
+// exactly to 48 bits, split_ff) in the same 32-byte slot and summed in FP32
+// two-float arithmetic with compensated sums (ff_add_product), about 2^-46
+// relative to the light terms.  Per component that leaves one FP64 FMA per
+// heavy partner and two FP64 additions (the two-float sum, converted exactly)
+// in place of n - 1 FMAs.
+template <int W, int NB>
+__device__ __forceinline__ void group_force_sym_mixed(const Group<W> &grp, int n,
+                                                      const double (*sp)[4], double (*sa)[3],
+                                                      double (*ctr)[NB - 1][4], unsigned hmask)
+{
+    const int gl = grp.gl;
+    const int P = n * (n - 1) / 2;
+    for (int p0 = 0; p0 < P; p0 += 32 * W) {
+        const int p = p0 + gl;
+        if (p < P) {
+            int i = 0, rem = p;
+            while (rem >= n - 1 - i) {
+                rem -= n - 1 - i;
+                i++;
+            }
+            const int k = i + 1 + rem;
+            const double dx = sp[i][0] - sp[k][0], dy = sp[i][1] - sp[k][1], dz = sp[i][2] - sp[k][2];
+            unsigned long long Mr, Wn;
+            int Er, eW;
+            r2_int(dx, dy, dz, Mr, Er);
+            inv_r3_core(Mr, Er, Wn, eW);
+            const double gi = sp[i][3], gk = sp[k][3];
+            const double wi = __double_as_longlong(gk) > 0 ? gm_times_inv_r3(Wn, eW, gk) : 0.0;
+            const double wk = __double_as_longlong(gi) > 0 ? gm_times_inv_r3(Wn, eW, gi) : 0.0;
+            const double nwi = __longlong_as_double(__double_as_longlong(wi) ^ (long long)0x8000000000000000ull);
+            const bool k_heavy = (hmask >> k) & 1u, i_heavy = (hmask >> i) & 1u;
+            float2 fx = make_float2(0.f, 0.f), fy = fx, fz = fx;
+            if (!(k_heavy && i_heavy)) {
+                fx = split_ff(dx);
+                fy = split_ff(dy);
+                fz = split_ff(dz);
+            }
+            double *e1 = ctr[i][k - 1];  // body i, partner k
+            if (k_heavy) {
+                e1[0] = nwi;
+                e1[1] = dx;
+                e1[2] = dy;
+                e1[3] = dz;
+            } else {
+                float4 *f = reinterpret_cast<float4 *>(e1);
+                const float2 w = split_ff(nwi);
+                f[0] = make_float4(w.x, w.y, fx.x, fx.y);
+                f[1] = make_float4(fy.x, fy.y, fz.x, fz.y);
+            }
+            double *e2 = ctr[k][i];  // body k, partner i
+            if (i_heavy) {
+                e2[0] = wk;
+                e2[1] = dx;
+                e2[2] = dy;
+                e2[3] = dz;
+            } else {
+                float4 *f = reinterpret_cast<float4 *>(e2);
+                const float2 w = split_ff(wk);
+                f[0] = make_float4(w.x, w.y, fx.x, fx.y);
+                f[1] = make_float4(fy.x, fy.y, fz.x, fz.y);
+            }
+        }
+    }
+    grp.sync();
+    if (gl < 3 * n) {
+        const int b = gl / 3, c = gl % 3;
+        float S = 0.0f, C = 0.0f;
+        for (int q = 0; q < n - 1; q++) {
+            const int j = q + (q >= b ? 1 : 0);
+            if ((hmask >> j) & 1u) continue;
+            const float *f = reinterpret_cast<const float *>(ctr[b][q]);
+            ff_add_product(make_float2(f[0], f[1]), make_float2(f[2 + 2 * c], f[3 + 2 * c]), S, C);
+        }
+        double s = f32_to_f64_exact(S) + f32_to_f64_exact(C);
+        for (int q = 0; q < n - 1; q++) {
+            const int j = q + (q >= b ? 1 : 0);
+            if ((hmask >> j) & 1u) s = fma(ctr[b][q][0], ctr[b][q][1 + c], s);
+        }
+        sa[b][c] = s;
+    }
+    grp.sync();
+}
+
+// The heavy partners of a system for group_force_sym_mixed: bit j set when
+// body j's G m (sp[j][3], zero for massless and deleted bodies) is at least
+// 1/128 of the largest (the exponent lowered by 7); compared on bit patterns
+// (positive doubles order as integers), so no FP64 instruction.
+__device__ __forceinline__ unsigned heavy_mask(int n, const double (*sp)[4])
+{
+    long long top = 0;
+    for (int j = 0; j < n; j++) top = max(top, __double_as_longlong(sp[j][3]));
+    if (top <= 0) return 0u;
+    const long long thr = top - (7ll << 52);
+    unsigned m = 0u;
+    for (int j = 0; j < n; j++)
+        if (__double_as_longlong(sp[j][3]) >= thr && __double_as_longlong(sp[j][3]) > 0) m |= 1u << j;
+    return m;
 }
 
 }  // namespace abie

@@ -531,13 +531,28 @@ __global__ void __launch_bounds__(256) wh_head_kernel(WhArgs a, int init, int pa
 // MODE: ABIE_FORCE_EXACT keeps the reference's expressions (sqrt, divisions,
 // correctly rounded cubes, closed-form Stumpff functions); the fast form
 // uses kepler_drift_fast and the one-instruction r^-3 of the force kernels.
+//
+// ABIE_FORCE_MIXED is the fast form with the planets' pull on the particle
+// in FP32 two-float arithmetic: heliocentric coordinates are relative to
+// the star, which serves as the FP64 anchor; the particle's and each
+// planet's coordinates and G m are split exactly into two floats (48
+// bits), the separation, r^2, r^-1/2 (rsqrtf and one correction), r^-3 and
+// the products are two-float operations, and each component's sum is a
+// compensated two-float sum, added once to the FP64 indirect and accel2
+// terms: about 2^-44 relative to the planet terms, no FP64 instruction per
+// planet (the fast form spends six).
 template <int MODE>
 __global__ void __launch_bounds__(256) wh_tail_kernel(WhArgs a, int init, int parity, int n_src)
 {
     extern __shared__ double hs[];  // 4 doubles per massive head body: x y z G*m
+    // mixed form: the same values split into two floats, after the doubles
+    float2 *hf = reinterpret_cast<float2 *>(hs + 4 * n_src);
     const int H = a.head;
     const double *hsrc = a.hsrc + parity * 4 * WH_HEAD_MAX;
-    for (int e = threadIdx.x; e < 4 * n_src; e += blockDim.x) hs[e] = hsrc[e];
+    for (int e = threadIdx.x; e < 4 * n_src; e += blockDim.x) {
+        hs[e] = hsrc[e];
+        if (MODE == ABIE_FORCE_MIXED) hf[e] = split_ff(hsrc[e]);
+    }
     __syncthreads();
     const long long i = (long long)H + (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
@@ -574,6 +589,24 @@ __global__ void __launch_bounds__(256) wh_tail_kernel(WhArgs a, int init, int pa
             double aux = 1.0 / cube_cr(norm3(d[0], d[1], d[2]));
             for (int c = 0; c < 3; c++) a3[c] -= hs[4 * q + 3] * aux * d[c];
         }
+    } else if (MODE == ABIE_FORCE_MIXED) {
+        ir3h = wh_gm_ir3(p[0], p[1], p[2], a.G * a.m[0]);
+        ir3j = wh_gm_ir3(jp[0], jp[1], jp[2], a.G * a.m[0]);
+        const float2 px = split_ff(p[0]), py = split_ff(p[1]), pz = split_ff(p[2]);
+        float S[3] = {0.0f, 0.0f, 0.0f}, C[3] = {0.0f, 0.0f, 0.0f};
+        for (int q = 0; q < n_src; q++) {
+            const float2 dx = ff_sub(px, hf[4 * q]), dy = ff_sub(py, hf[4 * q + 1]),
+                         dz = ff_sub(pz, hf[4 * q + 2]);
+            const float2 r2 = ff_add(ff_add(ff_sqr(dx), ff_sqr(dy)), ff_sqr(dz));
+            const float2 y = ff_rsqrt(r2);
+            const float2 w = ff_mul(hf[4 * q + 3], ff_mul(ff_sqr(y), y));  // G m r^-3
+            const float2 nw = make_float2(-w.x, -w.y);
+            ff_add_product(nw, dx, S[0], C[0]);
+            ff_add_product(nw, dy, S[1], C[1]);
+            ff_add_product(nw, dz, S[2], C[2]);
+        }
+        for (int c = 0; c < 3; c++)
+            a3[c] = sh->ind_a2[c] + (f32_to_f64_exact(S[c]) + f32_to_f64_exact(C[c]));
     } else {
         // G m0 folded into the inverse cubes; the planets' sum starts from
         // the indirect and accel2 terms
@@ -631,6 +664,14 @@ static void wh_launch_head(const WhArgs &a, int init, int parity, int mode, cuda
     else wh_head_kernel<ABIE_FORCE_FP64><<<1, 256, 0, st>>>(a, init, parity);
 }
 
+// Dynamic shared memory of the tail kernel: the massive head bodies as
+// doubles, and in the mixed form also as two-float pairs.
+static size_t wh_tail_smem(int n_src, int mode)
+{
+    const size_t k = 4 * (size_t)std::max(n_src, 1);
+    return k * sizeof(double) + (mode == ABIE_FORCE_MIXED ? k * sizeof(float2) : 0);
+}
+
 static void wh_launch_tail(const WhArgs &a, int init, int parity, int n_src, int mode, cudaStream_t st)
 {
     long long tail = (long long)a.n - a.head;
@@ -639,6 +680,9 @@ static void wh_launch_tail(const WhArgs &a, int init, int parity, int n_src, int
     size_t smem = 4 * sizeof(double) * (size_t)std::max(n_src, 1);
     if (mode == ABIE_FORCE_EXACT)
         wh_tail_kernel<ABIE_FORCE_EXACT><<<blocks, 256, smem, st>>>(a, init, parity, n_src);
+    else if (mode == ABIE_FORCE_MIXED)
+        wh_tail_kernel<ABIE_FORCE_MIXED><<<blocks, 256, wh_tail_smem(n_src, mode), st>>>(a, init, parity,
+                                                                                         n_src);
     else
         wh_tail_kernel<ABIE_FORCE_FP64><<<blocks, 256, smem, st>>>(a, init, parity, n_src);
 }
@@ -718,12 +762,20 @@ int wh_run(const SystemView &sys, double t, double t_end, double dt, double *t_o
         tt += dt;
         steps++;
     }
-    const int mode = g_sim.force_mode == ABIE_FORCE_EXACT ? ABIE_FORCE_EXACT : ABIE_FORCE_FP64;
-    size_t smem = 4 * sizeof(double) * (size_t)std::max(n_src, 1);
+    const int mode = g_sim.force_mode;
+    if (mode == ABIE_FORCE_NAIVE) {
+        set_error(ABIE_ERR_UNSUPPORTED,
+                  "integrator_wh: the naive force form is the force comparator only; use the exact, "
+                  "fp64 or mixed form");
+        return ABIE_ERR_UNSUPPORTED;
+    }
+    size_t smem = wh_tail_smem(n_src, mode);
     if (smem > 48 * 1024) {  // up to WH_HEAD_MAX massive head bodies
         ABIE_CUDA(cudaFuncSetAttribute(wh_tail_kernel<ABIE_FORCE_EXACT>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         ABIE_CUDA(cudaFuncSetAttribute(wh_tail_kernel<ABIE_FORCE_FP64>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        ABIE_CUDA(cudaFuncSetAttribute(wh_tail_kernel<ABIE_FORCE_MIXED>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     }
     // set-up (:509-510): Jacobi coordinates and accelerations, in order

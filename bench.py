@@ -48,11 +48,16 @@ from abie_gb300 import ics  # noqa: E402
 G = ics.G_SOLAR
 FLOP_PER_INTERACTION = 20  # the convention of the reference's tiled kernel comments
 FP64_INSTR_PER_INTERACTION = 6  # the fast form's pair term (abie_gb300/csrc/common.cuh pair_fast)
-# dram__bytes_read.sum + dram__bytes_write.sum of one launch of the force
-# kernel, from one ncu capture of this workload (fp64 form, 16,385 bodies,
-# symmetric kernel: 1.25 MB read, 90.8 MB of partial sums written).  Not
-# measured by the bench itself, which runs without a profiler.
-DRAM_BYTES_PER_LAUNCH = {("fp64", 16385): 92033536}
+# From one ncu capture of this workload's force kernel (fp64 form, 16,385
+# bodies, force_sym_kernel; ncu --metrics smsp__inst_executed_pipe_fp64.sum,
+# sm__thread_inst_executed_pipe_fp64_pred_on.sum, dram__bytes_read.sum,
+# dram__bytes_write.sum): DRAM bytes per launch (1,075,968 read, 89,481,728
+# of partial sums written) and FP64 thread instructions per launch
+# (37,917,882 warp instructions x 32 lanes), which equals the instruction
+# model below to the instruction.  Not measured by the bench itself, which
+# runs without a profiler.
+DRAM_BYTES_PER_LAUNCH = {("fp64", 16385): 1075968 + 89481728}
+NCU_FP64_THREAD_INSTR_PER_LAUNCH = {("fp64", 16385): 1213372224}
 
 
 SYM_MAX_BODIES = 131072  # the symmetric form's limit (abie_gb300/csrc/force.cu)
@@ -107,7 +112,7 @@ def parse():
     ap.add_argument("--extras", default="ensemble,wh,radau,disk,next",
                     help="comma list of sub-measurements: ensemble, wh, radau, disk, next "
                          "(Runge-Kutta 4, post-Newtonian Radau15, snapshots)")
-    ap.add_argument("--ensemble-forms", default="plain_fp64,fp64,learned",
+    ap.add_argument("--ensemble-forms", default="reference_ops,plain_fp64,fp64,mixed,learned",
                     help="comma list of ensemble forms to time")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
@@ -449,11 +454,13 @@ def run_ours(args):
     if args.mode == "fp64":
         f64 = fp64_instructions_per_call(m, inter)
         ach = 2.0 * f64 / (ms_step * 1e-3) / 1e12
+        ncu_f64 = NCU_FP64_THREAD_INSTR_PER_LAUNCH.get((args.mode, int(m.size)))
         roof.update({"achieved": ach, "frac": ach / peak if peak else None,
                      "force_form": force_path(m),
                      "fp64_instructions_per_interaction": f64 / inter,
-                     "fp64_instructions_source": "model (fp64_instructions_per_call), checked "
-                                                 "against ncu smsp__inst_executed_pipe_fp64.sum"})
+                     "fp64_instructions_source": "model (fp64_instructions_per_call)",
+                     "fp64_instructions_ncu_per_launch": ncu_f64,
+                     "fp64_instructions_model_per_launch": int(f64)})
     else:
         roof.update({"achieved": conv, "frac": conv / peak if peak else None})
     roof["traffic"] = DRAM_BYTES_PER_LAUNCH.get((args.mode, int(m.size)))
@@ -526,12 +533,16 @@ def run_ensemble(lib, args, rank, dev):
     bodies: a 0.5..1.5 MSun star and 3..12 planets) for a bounded slice of
     time.  Every rank draws its own systems (weak scaling).
 
-    Forms: plain_fp64 = the reference's FP64 operations and predictor in the
-    batched kernel (the comparator); fp64 = 6-instruction pair terms and
-    the corrector on the Newton-form coefficients, each step starting from
-    g consistent with the reference's plain guess; learned = that with the
-    BF16 network's guess, trained online on samples the ensemble records on
-    a separate set of systems."""
+    Forms: reference_ops = the reference's FP64 operations and predictor in
+    the batched kernel without FMA (bit-level parity form); plain_fp64 = the
+    plain FP64 GPU port, the comparator: the same operations compiled with
+    FMA contraction and gpuforce_v2's rsqrt pair term; fp64 = the fast form
+    (integer r^-3, each pair once for both bodies, the corrector on the
+    Newton-form coefficients, each step starting from g consistent with the
+    reference's plain guess); mixed = the fast form with light partners'
+    terms summed in FP32 two-float arithmetic; learned = the fast form with
+    the BF16 network's guess, trained online on samples the ensemble records
+    on a separate set of systems."""
     import time as _t
 
     from abie_gb300.learned import collect_samples, train_predictor
@@ -548,7 +559,8 @@ def run_ensemble(lib, args, rank, dev):
         out["training"] = {"systems": 2048, "years": 1.0, "samples": info["samples"],
                            "seconds": _t.perf_counter() - t0, "holdout_loss": info["holdout_loss"],
                            "holdout_loss_plain_guess": info["holdout_loss_plain"]}
-    forms = (("plain_fp64", "exact", {}), ("fp64", "fp64", {}), ("learned", "fp64", {"learned": True}))
+    forms = (("reference_ops", "exact", {}), ("plain_fp64", "naive", {}), ("fp64", "fp64", {}),
+             ("mixed", "mixed", {}), ("learned", "fp64", {"learned": True}))
     for label, mode, kw in forms:
         if label not in wanted:
             continue
@@ -572,7 +584,7 @@ def run_ensemble(lib, args, rank, dev):
             out[label]["attempts_redone_from_plain_guess"] = int(c["learned_fallbacks"])
     lib.mlp_enable(False)
     base = out.get("plain_fp64", {}).get("system_steps_per_s")
-    for label in ("fp64", "learned"):
+    for label in ("reference_ops", "fp64", "mixed", "learned"):
         if base and label in out and out[label]["system_steps_per_s"]:
             out[label]["speedup_vs_plain_fp64"] = out[label]["system_steps_per_s"] / base
     return out

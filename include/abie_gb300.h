@@ -29,7 +29,7 @@ extern "C" {
 #define ABIE_OK 0
 #define ABIE_EXIT_MAX_N_CE 1          /* src/common.h:6 */
 #define ABIE_EXIT_MAX_N_COLLISIONS 2  /* src/common.h:7 */
-#define ABIE_ERR_NO_DEVICE (-1)       /* no usable sm_103 GPU, or deviceID < 0 */
+#define ABIE_ERR_NO_DEVICE (-1)       /* no usable sm_103 GPU */
 #define ABIE_ERR_NOT_INITIALIZED (-2)
 #define ABIE_ERR_CUDA (-3)
 #define ABIE_ERR_UNSUPPORTED (-4)     /* valid call, feature not on the GPU path */
@@ -48,7 +48,9 @@ extern "C" {
 
 /* src/common.c:226-275.  Binds GPU deviceID, sizes device buffers for
  * N_MAX bodies and the event ring buffers.  Once per process, like the
- * reference (a second call returns 0 and does nothing). */
+ * reference (a second call returns 0 and does nothing).  A negative
+ * deviceID (the reference's default, which selects its CPU code) binds
+ * GPU 0, with a notice on stderr: this library has no CPU path. */
 int initialize_code(double G, double C, size_t N_MAX, size_t MAX_N_CE,
                     size_t MAX_N_COLLISIONS, int deviceID);
 /* src/common.c:382-398.  Frees device and host buffers. */

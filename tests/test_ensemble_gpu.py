@@ -26,7 +26,11 @@ def _sl(offs, s):
     return slice(3 * offs[s], 3 * offs[s + 1]), slice(offs[s], offs[s + 1])
 
 
-@pytest.mark.parametrize("mode", ["exact", "fp64"])
+TIME_TOLS = {"exact": TIME_TOL, "fp64": TIME_TOL_FAST, "naive": TIME_TOL_FAST,
+             "mixed": TIME_TOL_FAST}
+
+
+@pytest.mark.parametrize("mode", ["exact", "fp64", "naive", "mixed"])
 def test_golden_systems(clib, oracle, golden, mode):
     cases = ["gr_ens0", "gr_ens1", "gr_ens2"]
     systems = [(golden[c + "_in_pos"], golden[c + "_in_vel"], golden[c + "_m"]) for c in cases]
@@ -40,7 +44,7 @@ def test_golden_systems(clib, oracle, golden, mode):
     for s, c in enumerate(cases):
         sv, sm = _sl(offs, s)
         t_ref = golden[c + "_t"][0]
-        assert abs(out["t"][s] - t_ref) <= (TIME_TOL if mode == "exact" else TIME_TOL_FAST) * t_ref
+        assert abs(out["t"][s] - t_ref) <= TIME_TOLS[mode] * t_ref
         p, v = at_time(out["pos"][sv], out["vel"][sv], M[sm], out["t"][s], t_ref, oracle)
         assert rel_err_per_body(p, golden[c + "_pos"]) <= TOL
         assert rel_err_per_body(v, golden[c + "_vel"]) <= TOL
@@ -92,7 +96,7 @@ def test_rejects_oversized_system(clib):
         clib.gr_ensemble(P, V, M, offs, G, 0.0, 0.1)
 
 
-@pytest.mark.parametrize("mode", ["exact", "fp64"])
+@pytest.mark.parametrize("mode", ["exact", "fp64", "naive", "mixed"])
 def test_edge_sizes_vs_oracle(clib, oracle, mode):
     """Systems of 2, 3, 10, 11 (the first two-warp size) and 21 bodies (the
     largest), each against the oracle.  (A lone body is no case: with zero
@@ -111,24 +115,24 @@ def test_edge_sizes_vs_oracle(clib, oracle, mode):
     for s in range(len(systems)):
         sv, sm = _sl(offs, s)
         ref = oracle.radau15(P[sv], V[sv], M[sm], np.zeros(M[sm].size), G, 0.0, 0.3)
-        tol_t = TIME_TOL if mode == "exact" else TIME_TOL_FAST
-        assert abs(out["t"][s] - ref["t"]) <= tol_t * ref["t"]
+        assert abs(out["t"][s] - ref["t"]) <= TIME_TOLS[mode] * ref["t"]
         p, v = at_time(out["pos"][sv], out["vel"][sv], M[sm], out["t"][s], ref["t"], oracle)
         assert rel_err_per_body(p, ref["pos"]) <= TOL
         assert rel_err_per_body(v, ref["vel"]) <= TOL
 
 
-def test_every_group_class_with_test_particles(clib, oracle):
+@pytest.mark.parametrize("mode", ["fp64", "mixed"])
+def test_every_group_class_with_test_particles(clib, oracle, mode):
     """Three 21-body and two 10-body systems, each with massless test
-    particles, in the fast form: the slowest system runs on four warps and
-    at least two 21-body systems on two, so each group size evaluates its
-    pairs with massless bodies on one side or both."""
+    particles, in the fast and mixed forms: the slowest system runs on four
+    warps and at least two 21-body systems on two, so each group size
+    evaluates its pairs with massless bodies on one side or both."""
     systems = []
     for k, (npl, ntp) in enumerate([(14, 6), (12, 8), (16, 4), (6, 3), (5, 4)]):
         p, v, m, r = ics.planetary_system(seed=950 + k, n_planets=npl, n_tp=ntp, tp_a=(2.0, 20.0))
         systems.append((p, v, m))
     P, V, M, offs = _pack(systems)
-    old = clib.set_force_mode("fp64")
+    old = clib.set_force_mode(mode)
     try:
         out = clib.gr_ensemble(P, V, M, offs, G, 0.0, 0.3)
     finally:
@@ -141,3 +145,52 @@ def test_every_group_class_with_test_particles(clib, oracle):
         p, v = at_time(out["pos"][sv], out["vel"][sv], M[sm], out["t"][s], ref["t"], oracle)
         assert rel_err_per_body(p, ref["pos"]) <= TOL
         assert rel_err_per_body(v, ref["vel"]) <= TOL
+
+
+def test_forms_error_against_the_oracle(clib, oracle):
+    """Each ensemble form's error against the oracle (the reference's
+    algorithm on the CPU), stated and bounded: 64 systems of the benchmark
+    workload over 1 yr; the state at a common time (relative, max over
+    bodies and systems) and |dE/E| from the oracle's energy.
+
+    * exact: the reference's operations (no FMA);
+    * naive: the plain FP64 port (the reference's operations with FMA,
+      gpuforce_v2's rsqrt pair term);
+    * fp64: the fast form (Newton-form corrector, integer r^-3, pair-once);
+    * mixed: the fast form with light partners' terms in FP32 two-float
+      arithmetic (about 2^-46 relative to those terms)."""
+    P, V, M, offs = ics.ensemble(n_systems=64, seed0=10000)
+    ns = offs.size - 1
+    refs = []
+    for s in range(ns):
+        sv, sm = _sl(offs, s)
+        refs.append(oracle.radau15(P[sv], V[sv], M[sm], np.zeros(M[sm].size), G, 0.0, 1.0))
+    e0 = [oracle.energy(P[_sl(offs, s)[0]], V[_sl(offs, s)[0]], M[_sl(offs, s)[1]], G)
+          for s in range(ns)]
+    ref_de = max(abs((oracle.energy(r["pos"], r["vel"], M[_sl(offs, s)[1]], G) - e0[s]) / e0[s])
+                 for s, r in enumerate(refs))
+    table = {}
+    for mode in ("exact", "naive", "fp64", "mixed"):
+        old = clib.set_force_mode(mode)
+        try:
+            out = clib.gr_ensemble(P, V, M, offs, G, 0.0, 1.0)
+        finally:
+            clib.set_force_mode(old)
+        assert (out["status"] == 0).all(), mode
+        err, de = 0.0, 0.0
+        for s in range(ns):
+            sv, sm = _sl(offs, s)
+            r = refs[s]
+            assert abs(out["t"][s] - r["t"]) <= TIME_TOLS[mode] * r["t"], (mode, s)
+            p, v = at_time(out["pos"][sv], out["vel"][sv], M[sm], out["t"][s], r["t"], oracle)
+            err = max(err, rel_err_per_body(p, r["pos"]), rel_err_per_body(v, r["vel"]))
+            e1 = oracle.energy(out["pos"][sv], out["vel"][sv], M[sm], G)
+            de = max(de, abs((e1 - e0[s]) / e0[s]))
+        table[mode] = (err, de)
+    print("ensemble forms vs the oracle, 64 systems, 1 yr (max rel state error at a common time, "
+          "max |dE/E|; the oracle's own max |dE/E| %.2e):" % ref_de)
+    for mode, (err, de) in table.items():
+        print("  %-6s %.2e  %.2e" % (mode, err, de))
+    for mode, (err, de) in table.items():
+        assert err <= TOL, (mode, err)
+        assert de <= 1e-12, (mode, de)
