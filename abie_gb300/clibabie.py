@@ -210,6 +210,17 @@ class CLibABIE(object):
         return {"pos": pos, "vel": vel, "t": t_out, "status": status, "steps": steps,
                 "seconds": self.lib.abie_last_ensemble_seconds()}
 
+    def ensemble_tuning(self):
+        """Launch shape of the last gr_ensemble call: the share of systems on
+        four-warp groups (1 in heavy_div), where it came from ("tuned" in that
+        call, "cache", "override", or "default") and the tuner's GPU
+        seconds and number of candidates."""
+        h, src, secs = _c.c_int(0), _c.c_int(0), _c.c_double(0)
+        n = self.lib.abie_ensemble_last_tuning(_c.byref(h), _c.byref(src), _c.byref(secs))
+        source = {0: "tuned" if n > 0 else "default", 1: "cache", 2: "override"}[src.value]
+        return {"heavy_div": h.value, "source": source, "tune_seconds": secs.value,
+                "candidates": int(n)}
+
     def integrate_snapshots(self, t, t_end, store_dt, integrator="gr", h=0.0, primary="#COM#",
                             max_snaps=None):
         """Integrate the stored state from t to t_end, keeping a snapshot after

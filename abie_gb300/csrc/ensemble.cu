@@ -32,7 +32,10 @@
 // Launches are bounded in time: a warp that has run past the launch's time
 // budget saves its system's state and leaves; the host launches again over
 // the systems not yet done.
+#include <sys/stat.h>
+
 #include <algorithm>
+#include <string>
 #include <vector>
 
 #include "ensemble_kernel.cuh"
@@ -80,16 +83,284 @@ static const void *ensemble_fn(int mode, int w, bool learn)
 
 static size_t learn_smem(int w) { return (size_t)(WARPS / w) * sizeof(LearnSmem); }
 
-static int launch_ensemble(int mode, int w, int blocks, const EnsArgs &a, cudaStream_t st)
+// ---------------------------------------------------------------------------
+// Host side.  A batch keeps its device buffers and pinned staging for the
+// whole call.  Every launch over the systems not yet done is one replay of
+// a CUDA graph built once per batch: the active lists' upload from pinned
+// memory, the work counters' reset, one kernel node per class of system
+// (independent nodes, so the classes run side by side) and the per-system
+// scalars' download.  Between replays only the kernel nodes' arguments and
+// grids change (cudaGraphExecKernelNodeSetParams); each launch yields after
+// about two seconds of GPU time, so a long run is a few hundred replays.
+
+struct EnsBatch {
+    int ns = 0;
+    long long total = 0;
+    double *d_pos = nullptr, *d_vel = nullptr, *d_m = nullptr, *d_state = nullptr;
+    double *d_pos0 = nullptr, *d_vel0 = nullptr;  // the inputs, for the tuner's trials
+    long long *d_off = nullptr;
+    EnsScalars *d_sc = nullptr;
+    int *d_active = nullptr, *d_queue = nullptr;
+    int *h_active = nullptr;     // pinned
+    EnsScalars *h_sc = nullptr;  // pinned
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaGraphNode_t kern[3] = {nullptr, nullptr, nullptr};
+    const void *fn[3] = {nullptr, nullptr, nullptr};
+    size_t dyn[3] = {0, 0, 0};
+    int bps[3] = {1, 1, 1};
+    ~EnsBatch()
+    {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        for (double *p : {d_pos, d_vel, d_m, d_state, d_pos0, d_vel0})
+            if (p) cudaFree(p);
+        if (d_off) cudaFree(d_off);
+        if (d_sc) cudaFree(d_sc);
+        if (d_active) cudaFree(d_active);
+        if (d_queue) cudaFree(d_queue);
+        if (h_active) cudaFreeHost(h_active);
+        if (h_sc) cudaFreeHost(h_sc);
+    }
+};
+
+static const int WC[3] = {1, 2, 4};  // warps per system in each class
+
+// The graph of one launch over the batch (see above); kernel nodes start
+// with empty work and get their arguments before each replay.
+static int build_graph(EnsBatch &B, const EnsArgs &base)
 {
-    const bool learn = a.mlp || a.samples;
-    size_t dyn = learn ? learn_smem(w) : 0;
-    void *args[] = {const_cast<EnsArgs *>(&a)};
-    ABIE_CUDA(cudaLaunchKernel(ensemble_fn(mode, w, learn), dim3(blocks), dim3(32 * WARPS), args, dyn, st));
+    ABIE_CUDA(cudaGraphCreate(&B.graph, 0));
+    cudaGraphNode_t up, reset, down;
+    ABIE_CUDA(cudaGraphAddMemcpyNode1D(&up, B.graph, nullptr, 0, B.d_active, B.h_active,
+                                       (size_t)B.ns * sizeof(int), cudaMemcpyHostToDevice));
+    cudaMemsetParams ms = {};
+    ms.dst = B.d_queue;
+    ms.value = 0;
+    ms.elementSize = sizeof(int);
+    ms.width = 3;
+    ms.height = 1;
+    ABIE_CUDA(cudaGraphAddMemsetNode(&reset, B.graph, nullptr, 0, &ms));
+    cudaGraphNode_t deps[2] = {up, reset};
+    for (int k = 0; k < 3; k++) {
+        EnsArgs a = base;
+        a.active = B.d_active;
+        a.n_active = 0;
+        a.queue = B.d_queue + k;
+        void *args[] = {&a};
+        cudaKernelNodeParams p = {};
+        p.func = const_cast<void *>(B.fn[k]);
+        p.gridDim = dim3(1);
+        p.blockDim = dim3(32 * WARPS);
+        p.sharedMemBytes = (unsigned)B.dyn[k];
+        p.kernelParams = args;
+        ABIE_CUDA(cudaGraphAddKernelNode(&B.kern[k], B.graph, deps, 2, &p));
+    }
+    ABIE_CUDA(cudaGraphAddMemcpyNode1D(&down, B.graph, B.kern, 3, B.h_sc, B.d_sc,
+                                       (size_t)B.ns * sizeof(EnsScalars), cudaMemcpyDeviceToHost));
+    ABIE_CUDA(cudaGraphInstantiate(&B.exec, B.graph, 0));
     return 0;
 }
 
-static cudaStream_t g_ens_stream[2] = {nullptr, nullptr};  // besides the caller's stream
+// Runs the batch from its current device state until every system is done
+// (or has stopped with an error); t_stop replaces the systems' end time
+// (the tuner's trials stop early).  Adds the GPU time of the launches to
+// *gpu_s and their number to *launches; leaves the scalars in B.h_sc.
+static int run_launches(EnsBatch &B, const EnsArgs &base, const std::vector<int> &order,
+                        const std::vector<unsigned char> &cls, double t_stop, cudaStream_t st,
+                        double *gpu_s, int *launches)
+{
+    cudaEvent_t e0, e1;
+    ABIE_CUDA(cudaEventCreate(&e0));
+    ABIE_CUDA(cudaEventCreate(&e1));
+    std::vector<int> active(order);
+    int n_active = (int)active.size();
+    int rc = 0;
+    while (n_active > 0) {
+        // the classes' lists, each in longest-first order, one after another
+        int first[4] = {0, 0, 0, 0};
+        int k2 = 0;
+        for (int c = 0; c < 3; c++) {
+            first[c] = k2;
+            for (int q = 0; q < n_active; q++)
+                if (cls[active[q]] == c) B.h_active[k2++] = active[q];
+        }
+        first[3] = k2;
+        for (int k = 0; k < 3; k++) {
+            const int cnt = first[k + 1] - first[k];
+            EnsArgs a = base;
+            a.t_end = t_stop;
+            a.active = B.d_active + first[k];
+            a.n_active = cnt;
+            a.queue = B.d_queue + k;
+            const int per_block = WARPS / WC[k];
+            const int blocks = cnt == 0 ? 1
+                                        : (int)std::max<long long>(1, std::min<long long>(
+                                              (long long)B.bps[k] * g_sim.num_sms,
+                                              (cnt + per_block - 1) / per_block));
+            void *args[] = {&a};
+            cudaKernelNodeParams p = {};
+            p.func = const_cast<void *>(B.fn[k]);
+            p.gridDim = dim3((unsigned)blocks);
+            p.blockDim = dim3(32 * WARPS);
+            p.sharedMemBytes = (unsigned)B.dyn[k];
+            p.kernelParams = args;
+            cudaError_t e = cudaGraphExecKernelNodeSetParams(B.exec, B.kern[k], &p);
+            if (e != cudaSuccess) {
+                rc = cuda_fail(e, "ensemble graph: kernel node parameters");
+                break;
+            }
+        }
+        if (rc) break;
+        cudaError_t e = cudaEventRecord(e0, st);
+        if (e == cudaSuccess) e = cudaGraphLaunch(B.exec, st);
+        if (e == cudaSuccess) e = cudaEventRecord(e1, st);
+        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+        if (e != cudaSuccess) {
+            rc = cuda_fail(e, "ensemble graph launch");
+            break;
+        }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        *gpu_s += ms * 1e-3;
+        ++*launches;
+        int k = 0;
+        for (int q = 0; q < n_active; q++) {  // keeps the longest-first order
+            const int s2 = active[q];
+            if (B.h_sc[s2].phase != 2 && B.h_sc[s2].status == 0) active[k++] = s2;
+        }
+        n_active = k;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return rc;
+}
+
+// Class of each system for a share of four-warp groups: the slowest 1 in
+// div (longest first) on four warps, the rest by size.
+static void classes(const std::vector<int> &order, const long long *offsets, int div,
+                    std::vector<unsigned char> &cls)
+{
+    const int ns = (int)order.size();
+    cls.assign(ns, 0);
+    const int heavy = std::min(ns, std::max(1, ns / div));
+    for (int q = 0; q < ns; q++) {
+        const int s2 = order[q];
+        cls[s2] = q < heavy ? 2 : (3 * (offsets[s2 + 1] - offsets[s2]) <= 32 ? 0 : 1);
+    }
+}
+
+// --- autotuner ---------------------------------------------------------------
+// The share of systems on four-warp groups is picked per workload by timing
+// candidate shares on the batch itself: each trial restarts the systems
+// from their inputs (device copies) and runs them over a slice of the
+// requested span, sized from a short probe so that a trial takes about
+// 0.2 s of GPU time (or the whole span when that is shorter); the fastest
+// share wins.  The choice is cached in a text file keyed by the device, the
+// build of this library, the force form, the number of systems, a hash of
+// their body counts and masses, and the span, so a workload is tuned once.
+// ABIE_ENSEMBLE_TUNE=0 switches the tuner off (the defaults below then
+// apply); ABIE_TUNE_CACHE names the cache file (default
+// $XDG_CACHE_HOME/abie_gb300/ensemble_tune.tsv or
+// $HOME/.cache/abie_gb300/ensemble_tune.tsv).
+struct EnsTuneInfo {
+    int heavy_div = 0;
+    int from_cache = 0;   // 1: read from the cache file, 2: debug override, 0: measured or default
+    double tune_seconds = 0.0;
+    int candidates = 0;
+};
+static EnsTuneInfo g_last_tune;
+static const char *ENS_BUILD = __DATE__ " " __TIME__;
+
+static std::string tune_cache_path()
+{
+    if (const char *p = getenv("ABIE_TUNE_CACHE")) return p;
+    std::string base;
+    if (const char *x = getenv("XDG_CACHE_HOME")) base = x;
+    else if (const char *h = getenv("HOME")) base = std::string(h) + "/.cache";
+    else return "";
+    return base + "/abie_gb300/ensemble_tune.tsv";
+}
+
+static void mkdirs_for(const std::string &file)
+{
+    for (size_t i = 1; i < file.size(); i++)
+        if (file[i] == '/') mkdir(file.substr(0, i).c_str(), 0755);
+}
+
+static std::string tune_key(int mode, int ns, const long long *offsets, const double *m, double span)
+{
+    unsigned long long h = 1469598103934665603ull;  // FNV-1a over body counts and masses
+    auto mix = [&](unsigned long long v) {
+        for (int b = 0; b < 8; b++) {
+            h ^= (v >> (8 * b)) & 0xff;
+            h *= 1099511628211ull;
+        }
+    };
+    for (int s = 0; s <= ns; s++) mix((unsigned long long)offsets[s]);
+    for (long long i = 0; i < offsets[ns]; i++) {
+        unsigned long long b;
+        memcpy(&b, &m[i], sizeof b);
+        mix(b);
+    }
+    cudaDeviceProp p;
+    cudaGetDeviceProperties(&p, g_sim.dev);
+    char key[512];
+    snprintf(key, sizeof key, "%s|%s|mode%d|ns%d|h%016llx|span%.3g", p.name, ENS_BUILD, mode, ns, h,
+             span);
+    for (char *c = key; *c; c++)
+        if (*c == '\t' || *c == '\n') *c = ' ';
+    return key;
+}
+
+static int tune_lookup(const std::string &key)
+{
+    const std::string path = tune_cache_path();
+    if (path.empty()) return 0;
+    FILE *f = fopen(path.c_str(), "r");
+    if (!f) return 0;
+    char line[1024];
+    int found = 0;
+    while (fgets(line, sizeof line, f)) {
+        char *tab = strchr(line, '\t');
+        if (!tab) continue;
+        *tab = 0;
+        if (key == line) found = atoi(tab + 1);  // the last entry wins
+    }
+    fclose(f);
+    return found;
+}
+
+static void tune_store(const std::string &key, int div, double secs, const std::vector<double> &times,
+                       const std::vector<int> &cands)
+{
+    const std::string path = tune_cache_path();
+    if (path.empty()) return;
+    mkdirs_for(path);
+    FILE *f = fopen(path.c_str(), "a");
+    if (!f) return;
+    fprintf(f, "%s\t%d\t%.6f\t", key.c_str(), div, secs);
+    for (size_t i = 0; i < cands.size(); i++)
+        fprintf(f, "%s%d:%.6f", i ? "," : "", cands[i], times[i]);
+    fprintf(f, "\n");
+    fclose(f);
+}
+
+static bool tuner_on()
+{
+    const char *v = getenv("ABIE_ENSEMBLE_TUNE");  // read on every call
+    return !(v && v[0] == '0');
+}
+
+// Restart every system of the batch from its inputs.
+static int batch_restart(EnsBatch &B, const std::vector<EnsScalars> &sc0, cudaStream_t st)
+{
+    ABIE_CUDA(cudaMemcpyAsync(B.d_pos, B.d_pos0, 3 * B.total * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    ABIE_CUDA(cudaMemcpyAsync(B.d_vel, B.d_vel0, 3 * B.total * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    ABIE_CUDA(cudaMemcpyAsync(B.d_sc, sc0.data(), B.ns * sizeof(EnsScalars), cudaMemcpyHostToDevice, st));
+    ABIE_CUDA(cudaStreamSynchronize(st));
+    return 0;
+}
 
 int ensemble_run(double *pos, double *vel, const double *m, const long long *offsets, int ns,
                  double G, double t0, double t_end, double *t_out, int *status, long long *steps,
@@ -97,7 +368,7 @@ int ensemble_run(double *pos, double *vel, const double *m, const long long *off
                  const EnsembleLearnIO *learn_io, bool consistent, const float *mlp_tau)
 {
     if (ns <= 0) return 0;
-    long long total = offsets[ns];
+    const long long total = offsets[ns];
     for (int s = 0; s < ns; s++) {
         long long k = offsets[s + 1] - offsets[s];
         if (k < 1 || k > ENS_MAX_BODIES) {
@@ -106,185 +377,159 @@ int ensemble_run(double *pos, double *vel, const double *m, const long long *off
             return ABIE_ERR_ARGUMENT;
         }
     }
-    const bool learning_req = mlp || (learn_io && learn_io->samples);
-    if (mode == ABIE_FORCE_NAIVE && learning_req) {
+    const bool learning = mlp || (learn_io && learn_io->samples);
+    if (mode == ABIE_FORCE_NAIVE && learning) {
         set_error(ABIE_ERR_UNSUPPORTED,
                   "abie_gr_ensemble: the plain FP64 form runs the reference's predictor only "
                   "(no learned predictor, no sample collection)");
         return ABIE_ERR_UNSUPPORTED;
     }
-    double *d_pos, *d_vel, *d_m, *d_state;
-    long long *d_off;
-    EnsScalars *d_sc;
-    int *d_active, *d_queue;
-    ABIE_CUDA(cudaMalloc(&d_pos, 3 * total * sizeof(double)));
-    ABIE_CUDA(cudaMalloc(&d_vel, 3 * total * sizeof(double)));
-    ABIE_CUDA(cudaMalloc(&d_m, total * sizeof(double)));
-    ABIE_CUDA(cudaMalloc(&d_state, (size_t)STATE_PER_COMP * 3 * total * sizeof(double)));
-    ABIE_CUDA(cudaMalloc(&d_off, (ns + 1) * sizeof(long long)));
-    ABIE_CUDA(cudaMalloc(&d_sc, ns * sizeof(EnsScalars)));
-    ABIE_CUDA(cudaMalloc(&d_active, ns * sizeof(int)));
-    ABIE_CUDA(cudaMalloc(&d_queue, 3 * sizeof(int)));
-    std::vector<EnsScalars> sc(ns);
+    EnsBatch B;
+    B.ns = ns;
+    B.total = total;
+    ABIE_CUDA(cudaMalloc(&B.d_pos, 3 * total * sizeof(double)));
+    ABIE_CUDA(cudaMalloc(&B.d_vel, 3 * total * sizeof(double)));
+    ABIE_CUDA(cudaMalloc(&B.d_m, total * sizeof(double)));
+    ABIE_CUDA(cudaMalloc(&B.d_state, (size_t)STATE_PER_COMP * 3 * total * sizeof(double)));
+    ABIE_CUDA(cudaMalloc(&B.d_off, (ns + 1) * sizeof(long long)));
+    ABIE_CUDA(cudaMalloc(&B.d_sc, ns * sizeof(EnsScalars)));
+    ABIE_CUDA(cudaMalloc(&B.d_active, ns * sizeof(int)));
+    ABIE_CUDA(cudaMalloc(&B.d_queue, 3 * sizeof(int)));
+    ABIE_CUDA(cudaMallocHost(&B.h_active, ns * sizeof(int)));
+    ABIE_CUDA(cudaMallocHost(&B.h_sc, ns * sizeof(EnsScalars)));
+    std::vector<EnsScalars> sc0(ns);
     for (int s = 0; s < ns; s++) {
-        memset(&sc[s], 0, sizeof(EnsScalars));
-        sc[s].t = t0;
+        memset(&sc0[s], 0, sizeof(EnsScalars));
+        sc0[s].t = t0;
     }
     // Longest-first order: a system's step count follows its shortest
     // two-body time scale sqrt(r_ij^3 / G(m_i + m_j)), and the batch takes
     // at least as long as its slowest system, so those start first.
     std::vector<double> rate(ns, 0.0);
-    {
-        std::vector<double> hp(3 * (size_t)total), hm(m, m + total);
-        memcpy(hp.data(), pos, 3 * total * sizeof(double));
-        for (int s = 0; s < ns; s++) {
-            double best = 0.0;
-            for (long long i = offsets[s]; i < offsets[s + 1]; i++)
-                for (long long j = i + 1; j < offsets[s + 1]; j++) {
-                    double mu = G * (std::max(hm[i], 0.0) + std::max(hm[j], 0.0));
-                    double dx = hp[3 * i] - hp[3 * j], dy = hp[3 * i + 1] - hp[3 * j + 1],
-                           dz = hp[3 * i + 2] - hp[3 * j + 2];
-                    double r2 = dx * dx + dy * dy + dz * dz;
-                    if (mu > 0.0 && r2 > 0.0) best = std::max(best, sqrt(mu / (r2 * sqrt(r2))));
-                }
-            rate[s] = best;
-        }
+    for (int s = 0; s < ns; s++) {
+        double best = 0.0;
+        for (long long i = offsets[s]; i < offsets[s + 1]; i++)
+            for (long long j = i + 1; j < offsets[s + 1]; j++) {
+                double mu = G * (std::max(m[i], 0.0) + std::max(m[j], 0.0));
+                double dx = pos[3 * i] - pos[3 * j], dy = pos[3 * i + 1] - pos[3 * j + 1],
+                       dz = pos[3 * i + 2] - pos[3 * j + 2];
+                double r2 = dx * dx + dy * dy + dz * dz;
+                if (mu > 0.0 && r2 > 0.0) best = std::max(best, sqrt(mu / (r2 * sqrt(r2))));
+            }
+        rate[s] = best;
     }
-    std::vector<int> active(ns);
-    for (int s = 0; s < ns; s++) active[s] = s;
-    std::stable_sort(active.begin(), active.end(), [&](int x, int y) { return rate[x] > rate[y]; });
-    ABIE_CUDA(cudaMemcpyAsync(d_pos, pos, 3 * total * sizeof(double), cudaMemcpyHostToDevice, st));
-    ABIE_CUDA(cudaMemcpyAsync(d_vel, vel, 3 * total * sizeof(double), cudaMemcpyHostToDevice, st));
-    ABIE_CUDA(cudaMemcpyAsync(d_m, m, total * sizeof(double), cudaMemcpyHostToDevice, st));
-    ABIE_CUDA(cudaMemcpyAsync(d_off, offsets, (ns + 1) * sizeof(long long), cudaMemcpyHostToDevice, st));
-    ABIE_CUDA(cudaMemcpyAsync(d_sc, sc.data(), ns * sizeof(EnsScalars), cudaMemcpyHostToDevice, st));
+    std::vector<int> order(ns);
+    for (int s = 0; s < ns; s++) order[s] = s;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return rate[x] > rate[y]; });
+    ABIE_CUDA(cudaMemcpyAsync(B.d_pos, pos, 3 * total * sizeof(double), cudaMemcpyHostToDevice, st));
+    ABIE_CUDA(cudaMemcpyAsync(B.d_vel, vel, 3 * total * sizeof(double), cudaMemcpyHostToDevice, st));
+    ABIE_CUDA(cudaMemcpyAsync(B.d_m, m, total * sizeof(double), cudaMemcpyHostToDevice, st));
+    ABIE_CUDA(cudaMemcpyAsync(B.d_off, offsets, (ns + 1) * sizeof(long long), cudaMemcpyHostToDevice, st));
+    ABIE_CUDA(cudaMemcpyAsync(B.d_sc, sc0.data(), ns * sizeof(EnsScalars), cudaMemcpyHostToDevice, st));
     ABIE_CUDA(cudaStreamSynchronize(st));
 
-    const bool learning = mlp || (learn_io && learn_io->samples);
     // three classes of system: up to 10 bodies on one warp, 11-21 on two,
     // and the slowest few (longest-first order) on four warps, which cuts
     // their per-substep latency -- the batch ends with its slowest system
-    const int WC[3] = {1, 2, 4};
-    int bps[3] = {1, 1, 1};
     for (int k = 0; k < 3; k++) {
-        const void *fn = ensemble_fn(mode, WC[k], learning);
-        const size_t dyn = learning ? learn_smem(WC[k]) : 0;
+        B.fn[k] = ensemble_fn(mode, WC[k], learning);
+        B.dyn[k] = learning ? learn_smem(WC[k]) : 0;
         if (learning)
-            ABIE_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
-        ABIE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps[k], fn, 32 * WARPS, dyn));
-        bps[k] = std::max(bps[k], 1);
+            ABIE_CUDA(cudaFuncSetAttribute(B.fn[k], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)B.dyn[k]));
+        ABIE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&B.bps[k], B.fn[k], 32 * WARPS, B.dyn[k]));
+        B.bps[k] = std::max(B.bps[k], 1);
     }
-    std::vector<unsigned char> cls(ns);
-    {
-        const int heavy = std::min(ns, std::max(1, ns / heavy_div(mode)));
-        for (int q = 0; q < ns; q++) {
-            const int s2 = active[q];
-            cls[s2] = q < heavy ? 2 : (3 * (offsets[s2 + 1] - offsets[s2]) <= 32 ? 0 : 1);
-        }
-    }
-    for (int k = 0; k < 2; k++)
-        if (!g_ens_stream[k]) ABIE_CUDA(cudaStreamCreateWithFlags(&g_ens_stream[k], cudaStreamNonBlocking));
-    cudaEvent_t e0, e1, ej;
-    ABIE_CUDA(cudaEventCreate(&e0));
-    ABIE_CUDA(cudaEventCreate(&e1));
-    ABIE_CUDA(cudaEventCreateWithFlags(&ej, cudaEventDisableTiming));
-    double gpu_ms = 0.0;
-    int launches = 0;
-    int n_active = ns;
-    std::vector<int> part(ns);
-    while (n_active > 0) {
-        // the classes' lists, each in longest-first order
-        int first[4] = {0, 0, 0, 0};
-        {
-            int k2 = 0;
-            for (int c = 0; c < 3; c++) {
-                first[c] = k2;
-                for (int q = 0; q < n_active; q++)
-                    if (cls[active[q]] == c) part[k2++] = active[q];
+    EnsArgs base = {};
+    base.offsets = B.d_off;
+    base.m = B.d_m;
+    base.pos = B.d_pos;
+    base.vel = B.d_vel;
+    base.state = B.d_state;
+    base.sc = B.d_sc;
+    base.G = G;
+    base.t_end = t_end;
+    base.mlp = mlp;
+    base.samples = learn_io ? learn_io->samples : nullptr;
+    base.sample_cap = learn_io ? learn_io->cap : 0;
+    base.sample_count = learn_io ? learn_io->count : nullptr;
+    for (int k = 0; k < 7; k++) base.tau[k] = learn_io ? learn_io->tau[k] : (mlp_tau ? mlp_tau[k] : 1.0f);
+    base.consistent_g = consistent ? 1 : 0;
+    base.budget_ns = 2000000000ull;  // each launch yields after about two seconds
+    int rc = build_graph(B, base);
+    if (rc) return rc;
+
+    // the share of four-warp groups: the debug override, the tuner (not
+    // while learning: trials would append training samples), or the default
+    EnsTuneInfo info;
+    std::vector<unsigned char> cls;
+    const double span = t_end - t0;
+    if (g_heavy_div > 0) {
+        info.heavy_div = g_heavy_div;
+        info.from_cache = 2;
+    } else if (!learning && tuner_on() && span > 0.0) {
+        const std::string key = tune_key(mode, ns, offsets, m, span);
+        info.heavy_div = tune_lookup(key);
+        if (info.heavy_div > 0) {
+            info.from_cache = 1;
+        } else {
+            ABIE_CUDA(cudaMalloc(&B.d_pos0, 3 * total * sizeof(double)));
+            ABIE_CUDA(cudaMalloc(&B.d_vel0, 3 * total * sizeof(double)));
+            ABIE_CUDA(cudaMemcpyAsync(B.d_pos0, B.d_pos, 3 * total * sizeof(double), cudaMemcpyDeviceToDevice, st));
+            ABIE_CUDA(cudaMemcpyAsync(B.d_vel0, B.d_vel, 3 * total * sizeof(double), cudaMemcpyDeviceToDevice, st));
+            // probe: the default share over 1 % of the span
+            double probe_s = 0.0;
+            int probe_l = 0;
+            classes(order, offsets, heavy_div(mode), cls);
+            if ((rc = run_launches(B, base, order, cls, t0 + 0.01 * span, st, &probe_s, &probe_l))) return rc;
+            const double est_full = probe_s / 0.01;
+            const double frac = std::min(1.0, std::max(0.01, 0.2 / std::max(est_full, 1e-9)));
+            const std::vector<int> cands = mode == ABIE_FORCE_EXACT ? std::vector<int>{4, 16, 64, 256}
+                                                                    : std::vector<int>{2, 4, 8, 16, 64, 256};
+            std::vector<double> times;
+            double best = 1e300;
+            for (int div : cands) {
+                if ((rc = batch_restart(B, sc0, st))) return rc;
+                classes(order, offsets, div, cls);
+                double s = 0.0;
+                int l = 0;
+                if ((rc = run_launches(B, base, order, cls, t0 + frac * span, st, &s, &l))) return rc;
+                times.push_back(s);
+                if (s < best) {
+                    best = s;
+                    info.heavy_div = div;
+                }
             }
-            first[3] = k2;
+            info.tune_seconds = probe_s;
+            for (double s : times) info.tune_seconds += s;
+            info.candidates = (int)cands.size();
+            tune_store(key, info.heavy_div, info.tune_seconds, times, cands);
+            if ((rc = batch_restart(B, sc0, st))) return rc;
         }
-        ABIE_CUDA(cudaMemcpyAsync(d_active, part.data(), n_active * sizeof(int),
-                                  cudaMemcpyHostToDevice, st));
-        ABIE_CUDA(cudaMemsetAsync(d_queue, 0, 3 * sizeof(int), st));
-        EnsArgs a;
-        a.offsets = d_off;
-        a.m = d_m;
-        a.pos = d_pos;
-        a.vel = d_vel;
-        a.state = d_state;
-        a.sc = d_sc;
-        a.G = G;
-        a.t_end = t_end;
-        a.mlp = mlp;
-        a.samples = learn_io ? learn_io->samples : nullptr;
-        a.sample_cap = learn_io ? learn_io->cap : 0;
-        a.sample_count = learn_io ? learn_io->count : nullptr;
-        for (int k = 0; k < 7; k++) a.tau[k] = learn_io ? learn_io->tau[k] : (mlp_tau ? mlp_tau[k] : 1.0f);
-        a.consistent_g = consistent ? 1 : 0;
-        a.budget_ns = 2000000000ull;  // each launch yields after about two seconds
-        ABIE_CUDA(cudaEventRecord(e0, st));
-        ABIE_CUDA(cudaEventRecord(ej, st));
-        for (int k = 0; k < 2; k++) ABIE_CUDA(cudaStreamWaitEvent(g_ens_stream[k], ej, 0));
-        for (int k = 0; k < 3; k++) {
-            const int cnt = first[k + 1] - first[k];
-            if (cnt == 0) continue;
-            EnsArgs ak = a;
-            ak.active = d_active + first[k];
-            ak.n_active = cnt;
-            ak.queue = d_queue + k;
-            const int per_block = WARPS / WC[k];  // systems per block
-            int blocks = (int)std::min<long long>((long long)bps[k] * g_sim.num_sms,
-                                                  (cnt + per_block - 1) / per_block);
-            blocks = std::max(blocks, 1);
-            int lrc = launch_ensemble(mode, WC[k], blocks, ak, k == 0 ? st : g_ens_stream[k - 1]);
-            if (lrc) return lrc;
-        }
-        for (int k = 0; k < 2; k++) {
-            ABIE_CUDA(cudaEventRecord(ej, g_ens_stream[k]));
-            ABIE_CUDA(cudaStreamWaitEvent(st, ej, 0));
-        }
-        ABIE_CUDA(cudaEventRecord(e1, st));
-        ABIE_CUDA(cudaEventSynchronize(e1));
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, e0, e1);
-        gpu_ms += ms;
-        launches++;
-        ABIE_CUDA(cudaMemcpy(sc.data(), d_sc, ns * sizeof(EnsScalars), cudaMemcpyDeviceToHost));
-        int k = 0;
-        for (int q = 0; q < n_active; q++) {  // keeps the longest-first order
-            const int s2 = active[q];
-            if (sc[s2].phase != 2 && sc[s2].status == 0) active[k++] = s2;
-        }
-        n_active = k;
+    } else {
+        info.heavy_div = heavy_div(mode);
     }
-    cudaEventDestroy(ej);
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    ABIE_CUDA(cudaMemcpy(pos, d_pos, 3 * total * sizeof(double), cudaMemcpyDeviceToHost));
-    ABIE_CUDA(cudaMemcpy(vel, d_vel, 3 * total * sizeof(double), cudaMemcpyDeviceToHost));
+    classes(order, offsets, info.heavy_div, cls);
+    double gpu_s = 0.0;
+    int launches = 0;
+    if ((rc = run_launches(B, base, order, cls, t_end, st, &gpu_s, &launches))) return rc;
+    ABIE_CUDA(cudaMemcpy(pos, B.d_pos, 3 * total * sizeof(double), cudaMemcpyDeviceToHost));
+    ABIE_CUDA(cudaMemcpy(vel, B.d_vel, 3 * total * sizeof(double), cudaMemcpyDeviceToHost));
     for (int s = 0; s < ns; s++) {
-        if (t_out) t_out[s] = sc[s].t;
-        if (status) status[s] = sc[s].status;
-        if (steps) steps[s] = sc[s].steps;
+        const EnsScalars &S = B.h_sc[s];
+        if (t_out) t_out[s] = S.t;
+        if (status) status[s] = S.status;
+        if (steps) steps[s] = S.steps;
         if (stats) {
-            stats->attempts += sc[s].attempts;
-            stats->iterations += sc[s].iterations;
-            stats->force_calls += sc[s].force_calls;
-            stats->steps += sc[s].steps;
-            stats->fallbacks += sc[s].fallbacks;
+            stats->attempts += S.attempts;
+            stats->iterations += S.iterations;
+            stats->force_calls += S.force_calls;
+            stats->steps += S.steps;
+            stats->fallbacks += S.fallbacks;
         }
     }
     if (stats) stats->launches += launches;
-    g_last_seconds = gpu_ms * 1e-3;
-    cudaFree(d_pos);
-    cudaFree(d_vel);
-    cudaFree(d_m);
-    cudaFree(d_state);
-    cudaFree(d_off);
-    cudaFree(d_sc);
-    cudaFree(d_active);
-    cudaFree(d_queue);
+    g_last_seconds = gpu_s;
+    g_last_tune = info;
     return 0;
 }
 
@@ -333,5 +578,13 @@ int abie_gr_ensemble(double *pos, double *vel, const double *m, const long long 
 }
 
 double abie_last_ensemble_seconds(void) { return ensemble_last_seconds(); }
+
+int abie_ensemble_last_tuning(int *heavy_div, int *source, double *tune_seconds)
+{
+    if (heavy_div) *heavy_div = abie::g_last_tune.heavy_div;
+    if (source) *source = abie::g_last_tune.from_cache;
+    if (tune_seconds) *tune_seconds = abie::g_last_tune.tune_seconds;
+    return abie::g_last_tune.candidates;
+}
 
 }  // extern "C"

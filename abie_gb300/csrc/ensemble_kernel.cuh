@@ -215,20 +215,24 @@ __device__ __forceinline__ void restore_plain_guess(LearnSmem &L, Comp &X, int g
     consistent_g(X);
 }
 
-// Blocks per SM the register budget is sized for, per variant.
+// Blocks per SM the register budget is sized for, per variant (the
+// learned variants hold the network's fragments and take 3).
+#ifndef ABIE_ENS_MINB
+#define ABIE_ENS_MINB 4
+#endif
 template <int W, bool LEARN>
 struct EnsOccupancy {
-    static constexpr int value = LEARN ? 3 : 4;
+    static constexpr int value = LEARN ? 3 : ABIE_ENS_MINB;
 };
 
 template <int MODE, int W, bool LEARN>
 __global__ void __launch_bounds__(32 * WARPS, (EnsOccupancy<W, LEARN>::value)) ensemble_kernel(EnsArgs a)
 {
     constexpr int GROUPS = WARPS / W;
-    __shared__ double s_pos[GROUPS][32][4];
+    __shared__ double s_pos[GROUPS][32][SPW];
     __shared__ double s_acc[GROUPS][32][3];
     constexpr int NB = W == 1 ? 10 : ENS_MAX_BODIES;  // bodies a group of W warps holds
-    __shared__ double s_ctr[ref_ops<MODE>() ? 1 : GROUPS][NB][NB - 1][4];  // pair terms
+    __shared__ CtrRow<NB> s_ctr[ref_ops<MODE>() ? 1 : GROUPS][NB];  // pair terms
     __shared__ double s_red[GROUPS][2 * W + 1];
     __shared__ int s_flg[GROUPS][2 * W];
     extern __shared__ __align__(16) unsigned char ens_dyn[];  // learned path only
@@ -245,7 +249,7 @@ __global__ void __launch_bounds__(32 * WARPS, (EnsOccupancy<W, LEARN>::value)) e
     }
     const int gl = grp.gl;
     LearnSmem &LS = reinterpret_cast<LearnSmem *>(ens_dyn)[grp.gidx];
-    double(*sp)[4] = s_pos[grp.gidx];
+    double(*sp)[SPW] = s_pos[grp.gidx];
     double(*sa)[3] = s_acc[grp.gidx];
     const unsigned long long deadline = ens_timer() + a.budget_ns;
 

@@ -907,7 +907,7 @@ __global__ void __launch_bounds__(256) radau_engine(EngineArgs a)
 constexpr int SPLIT_TPW = 8;  // test particles per block
 
 template <int MODE>
-__device__ __forceinline__ void split_tp_force(const EngineArgs &a, const double (*sp)[4], int n_m,
+__device__ __forceinline__ void split_tp_force(const EngineArgs &a, const double (*sp)[SPW], int n_m,
                                                double p, int lane, double &fx, double &fy,
                                                double &fz)
 {
@@ -946,7 +946,7 @@ __device__ __forceinline__ void split_tp_force(const EngineArgs &a, const double
 template <int MODE, bool PN>
 __global__ void __launch_bounds__(64) radau_split(EngineArgs a)
 {
-    __shared__ double s_sp[2][32][4];  // massive predicted positions, G m (two buffers)
+    __shared__ double s_sp[2][32][SPW];  // massive predicted positions, G m (two buffers)
     __shared__ double s_sv[2][32][4];  // massive predicted velocities, m (post-Newtonian only)
     __shared__ double s_sa[32][3];     // massive accelerations
     EngineCtl *ctl = a.ctl;
@@ -1023,7 +1023,7 @@ __global__ void __launch_bounds__(64) radau_split(EngineArgs a)
             group_force<MODE, 1>(mg, n_m, s_sp[ib], s_sa);
             if (pn) {
                 if (lane < n_m) {
-                    const double(*P)[4] = s_sp[ib];
+                    const double(*P)[SPW] = s_sp[ib];
                     const double(*V)[4] = s_sv[ib];
                     double ax = 0.0, ay = 0.0, az = 0.0;
                     for (int k = 0; k < n_m; k++) {
@@ -1051,7 +1051,7 @@ __global__ void __launch_bounds__(64) radau_split(EngineArgs a)
                 const double vz = __shfl_sync(0xffffffffu, v, 2, 4);
                 double ax = 0.0, ay = 0.0, az = 0.0;
                 if ((lane & 3) == 0) {
-                    const double(*P)[4] = s_sp[ib];
+                    const double(*P)[SPW] = s_sp[ib];
                     const double(*V)[4] = s_sv[ib];
                     for (int k = 0; k < n_m; k++)
                         pn_term<MODE>(a.pn, x, y, z, vx, vy, vz, my_m, P[k][0], P[k][1], P[k][2],

@@ -31,6 +31,23 @@ static __constant__ double e_vg[7] = ABIE_RADAU_VG_INIT;       // fast sweep: ve
 static __constant__ double e_vgs[9][7] = ABIE_RADAU_VGS_INIT;  // velocity weights on g at every spacing
 
 
+// Doubles per row of the shared predicted-position tables {x, y, z, G m}:
+// one pad entry, so consecutive bodies' rows start 10 banks apart and a
+// warp reading sixteen different bodies' rows hits distinct bank pairs
+// (with 4 doubles, every body's row starts in one of 4 banks).
+static constexpr int SPW = 5;
+
+// Row of the pair-term table of one body (group_force_sym*): 4 doubles per
+// partner {w, dx, dy, dz} plus one pad double, so that the rows of
+// different bodies start in different banks (without it every row of a
+// 21-body table starts in the same bank and the lanes of one component
+// conflict 12 ways).
+template <int NB>
+struct CtrRow {
+    double e[NB - 1][4];
+    double pad;
+};
+
 static constexpr double EPSB = 1.e-4;
 static constexpr double FAC = 0.25;
 static constexpr double TOLPC = 1.e-16;
@@ -349,7 +366,7 @@ struct Group {
 // L-th source; the partial sums of the lanes holding work meet in a fixed
 // tree of shuffles (a sink's lanes never straddle warps).
 template <int MODE, int W>
-__device__ __forceinline__ void group_force(const Group<W> &grp, int n, const double (*sp)[4],
+__device__ __forceinline__ void group_force(const Group<W> &grp, int n, const double (*sp)[SPW],
                                             double (*sa)[3])
 {
     const int spw = (n + W - 1) / W;
@@ -398,16 +415,16 @@ __device__ __forceinline__ void group_force(const Group<W> &grp, int n, const do
 // A group's forces with each pair once for both bodies (fast form, n <= NB
 // bodies): group lane p takes the p-th pair (i, k), i < k, shares the
 // separation d = x_i - x_k, r^2 and r^-3, and stores for each body the
-// factor and d -- {-G m_k r^-3, d} in ctr[i][k - 1], {G m_i r^-3, d} in
-// ctr[k][i] (each body's partners in index order: partner j at slot j
+// factor and d -- {-G m_k r^-3, d} in ctr[i].e[k - 1], {G m_i r^-3, d} in
+// ctr[k].e[i] (each body's partners in index order: partner j at slot j
 // below the body, j - 1 above it; the first factor's sign flipped on its bit
 // pattern, an integer operation).  The lane of component c of body b then
 // sums its row with one FMA per partner, in that order, so each term is
 // rounded once as in group_force.  3 FP64 instructions per pair round and
 // n - 1 per component, against 6 per pair term and a shuffle tree.
 template <int W, int NB>
-__device__ __forceinline__ void group_force_sym(const Group<W> &grp, int n, const double (*sp)[4],
-                                                double (*sa)[3], double (*ctr)[NB - 1][4])
+__device__ __forceinline__ void group_force_sym(const Group<W> &grp, int n, const double (*sp)[SPW],
+                                                double (*sa)[3], CtrRow<NB> *ctr)
 {
     const int gl = grp.gl;
     const int P = n * (n - 1) / 2;
@@ -428,21 +445,21 @@ __device__ __forceinline__ void group_force_sym(const Group<W> &grp, int n, cons
             const double gi = sp[i][3], gk = sp[k][3];
             const double wi = __double_as_longlong(gk) > 0 ? gm_times_inv_r3(Wn, eW, gk) : 0.0;
             const double wk = __double_as_longlong(gi) > 0 ? gm_times_inv_r3(Wn, eW, gi) : 0.0;
-            ctr[i][k - 1][0] = __longlong_as_double(__double_as_longlong(wi) ^ (long long)0x8000000000000000ull);
-            ctr[i][k - 1][1] = dx;
-            ctr[i][k - 1][2] = dy;
-            ctr[i][k - 1][3] = dz;
-            ctr[k][i][0] = wk;
-            ctr[k][i][1] = dx;
-            ctr[k][i][2] = dy;
-            ctr[k][i][3] = dz;
+            ctr[i].e[k - 1][0] = __longlong_as_double(__double_as_longlong(wi) ^ (long long)0x8000000000000000ull);
+            ctr[i].e[k - 1][1] = dx;
+            ctr[i].e[k - 1][2] = dy;
+            ctr[i].e[k - 1][3] = dz;
+            ctr[k].e[i][0] = wk;
+            ctr[k].e[i][1] = dx;
+            ctr[k].e[i][2] = dy;
+            ctr[k].e[i][3] = dz;
         }
     }
     grp.sync();
     if (gl < 3 * n) {
         const int b = gl / 3, c = gl % 3;
         double s = 0.0;
-        for (int q = 0; q < n - 1; q++) s = fma(ctr[b][q][0], ctr[b][q][1 + c], s);
+        for (int q = 0; q < n - 1; q++) s = fma(ctr[b].e[q][0], ctr[b].e[q][1 + c], s);
         sa[b][c] = s;
     }
     grp.sync();
@@ -454,15 +471,15 @@ __device__ __forceinline__ void group_force_sym(const Group<W> &grp, int n, cons
 // the star, or both stars of a binary).  A body's terms from heavy partners
 // are stored and summed as in the fast form (one FP64 FMA each); a term from
 // a light partner is stored as two-float pairs (w and the separation split
-// exactly to 48 bits, split_ff) in the same 32-byte slot and summed in FP32
+// exactly to 48 bits, split_ff) in the same 32-byte slot (four float2) and summed in FP32
 // two-float arithmetic with compensated sums (ff_add_product), about 2^-46
 // relative to the light terms.  Per component that leaves one FP64 FMA per
 // heavy partner and two FP64 additions (the two-float sum, converted exactly)
 // in place of n - 1 FMAs.
 template <int W, int NB>
 __device__ __forceinline__ void group_force_sym_mixed(const Group<W> &grp, int n,
-                                                      const double (*sp)[4], double (*sa)[3],
-                                                      double (*ctr)[NB - 1][4], unsigned hmask)
+                                                      const double (*sp)[SPW], double (*sa)[3],
+                                                      CtrRow<NB> *ctr, unsigned hmask)
 {
     const int gl = grp.gl;
     const int P = n * (n - 1) / 2;
@@ -491,29 +508,31 @@ __device__ __forceinline__ void group_force_sym_mixed(const Group<W> &grp, int n
                 fy = split_ff(dy);
                 fz = split_ff(dz);
             }
-            double *e1 = ctr[i][k - 1];  // body i, partner k
+            double *e1 = ctr[i].e[k - 1];  // body i, partner k
             if (k_heavy) {
                 e1[0] = nwi;
                 e1[1] = dx;
                 e1[2] = dy;
                 e1[3] = dz;
             } else {
-                float4 *f = reinterpret_cast<float4 *>(e1);
-                const float2 w = split_ff(nwi);
-                f[0] = make_float4(w.x, w.y, fx.x, fx.y);
-                f[1] = make_float4(fy.x, fy.y, fz.x, fz.y);
+                float2 *f = reinterpret_cast<float2 *>(e1);
+                f[0] = split_ff(nwi);
+                f[1] = fx;
+                f[2] = fy;
+                f[3] = fz;
             }
-            double *e2 = ctr[k][i];  // body k, partner i
+            double *e2 = ctr[k].e[i];  // body k, partner i
             if (i_heavy) {
                 e2[0] = wk;
                 e2[1] = dx;
                 e2[2] = dy;
                 e2[3] = dz;
             } else {
-                float4 *f = reinterpret_cast<float4 *>(e2);
-                const float2 w = split_ff(wk);
-                f[0] = make_float4(w.x, w.y, fx.x, fx.y);
-                f[1] = make_float4(fy.x, fy.y, fz.x, fz.y);
+                float2 *f = reinterpret_cast<float2 *>(e2);
+                f[0] = split_ff(wk);
+                f[1] = fx;
+                f[2] = fy;
+                f[3] = fz;
             }
         }
     }
@@ -524,13 +543,13 @@ __device__ __forceinline__ void group_force_sym_mixed(const Group<W> &grp, int n
         for (int q = 0; q < n - 1; q++) {
             const int j = q + (q >= b ? 1 : 0);
             if ((hmask >> j) & 1u) continue;
-            const float *f = reinterpret_cast<const float *>(ctr[b][q]);
-            ff_add_product(make_float2(f[0], f[1]), make_float2(f[2 + 2 * c], f[3 + 2 * c]), S, C);
+            const float2 *f = reinterpret_cast<const float2 *>(ctr[b].e[q]);
+            ff_add_product(f[0], f[1 + c], S, C);
         }
         double s = f32_to_f64_exact(S) + f32_to_f64_exact(C);
         for (int q = 0; q < n - 1; q++) {
             const int j = q + (q >= b ? 1 : 0);
-            if ((hmask >> j) & 1u) s = fma(ctr[b][q][0], ctr[b][q][1 + c], s);
+            if ((hmask >> j) & 1u) s = fma(ctr[b].e[q][0], ctr[b].e[q][1 + c], s);
         }
         sa[b][c] = s;
     }
@@ -541,7 +560,7 @@ __device__ __forceinline__ void group_force_sym_mixed(const Group<W> &grp, int n
 // body j's G m (sp[j][3], zero for massless and deleted bodies) is at least
 // 1/128 of the largest (the exponent lowered by 7); compared on bit patterns
 // (positive doubles order as integers), so no FP64 instruction.
-__device__ __forceinline__ unsigned heavy_mask(int n, const double (*sp)[4])
+__device__ __forceinline__ unsigned heavy_mask(int n, const double (*sp)[SPW])
 {
     long long top = 0;
     for (int j = 0; j < n; j++) top = max(top, __double_as_longlong(sp[j][3]));

@@ -115,6 +115,13 @@ def parse():
     ap.add_argument("--ensemble-forms", default="reference_ops,plain_fp64,fp64,mixed,learned",
                     help="comma list of ensemble forms to time")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--horizon", default="",
+                    help="comma list of long-horizon runs instead of the headline bench: "
+                         "ens64 (64 ensemble systems over 1e4 yr, fp64 and mixed forms, against "
+                         "the reference method's |dE/E| distribution), ens4096 (all 4,096 systems "
+                         "over 1e4 yr), disk (the 16,385-body disk over 10 yr, exact and fp64 "
+                         "forms), wh (1e6 Wisdom-Holman steps at 1,048,582 bodies)")
+    ap.add_argument("--horizon-forms", default="fp64,mixed")
     return ap.parse_args()
 
 
@@ -579,7 +586,8 @@ def run_ensemble(lib, args, rank, dev):
                       "abs_dE_over_E_percentiles_50_90_99": [float(np.percentile(de, q))
                                                              for q in (50, 90, 99)],
                       "failed_systems": int((res["status"] != 0).sum()),
-                      "max_steps_one_system": int(res["steps"].max())}
+                      "max_steps_one_system": int(res["steps"].max()),
+                      "launch_shape": lib.ensemble_tuning()}
         if label == "learned":
             out[label]["attempts_redone_from_plain_guess"] = int(c["learned_fallbacks"])
     lib.mlp_enable(False)
@@ -597,21 +605,33 @@ def run_wh(lib, args):
     p, v = ics.to_heliocentric(p, v)
     n = m.size
     lib.initialize_code(G, 0.0, max(n, 1 << 21), MAX_CE_EVENTS=3, MAX_COLLISION_EVENTS=2, deviceID=0)
-    lib.set_state(p, v, m, r, n, G, 0.0)
-    lib.integrator_wh(0.0, 0.02, 0.01)  # warm-up (graph capture, first launches)
-    lib.set_state(p, v, m, r, n, G, 0.0)
-    lib.reset_counters()
-    t0 = _t.perf_counter()
-    lib.integrator_wh(0.0, args.wh_steps * 0.01 - 1e-9, 0.01)
-    dt = _t.perf_counter() - t0
-    c = lib.counters()
-    steps = c["wh_steps"]
     n_m = int(np.count_nonzero(m > 0))
     kick = (n - n_m) * n_m + n_m * (n_m - 1)  # particle-massive and massive pairs per step
-    return {"bodies": int(n), "steps": int(steps), "seconds": dt, "steps_per_s": steps / dt,
-            "kepler_solves_per_s": steps * (n - 1) / dt, "kick_interactions_per_step": int(kick),
-            "kick_gint_per_s": steps * kick / dt / 1e9, "kepler_failures": c["kepler_failures"],
-            "timing": "wall clock around integrator_wh (device-resident state)"}
+
+    def one(form):
+        old = lib.set_force_mode(form)
+        try:
+            lib.set_state(p, v, m, r, n, G, 0.0)
+            lib.integrator_wh(0.0, 0.02, 0.01)  # warm-up (graph capture, first launches)
+            lib.set_state(p, v, m, r, n, G, 0.0)
+            lib.reset_counters()
+            t0 = _t.perf_counter()
+            lib.integrator_wh(0.0, args.wh_steps * 0.01 - 1e-9, 0.01)
+            dt = _t.perf_counter() - t0
+        finally:
+            lib.set_force_mode(old)
+        c = lib.counters()
+        steps = c["wh_steps"]
+        return {"steps": int(steps), "seconds": dt, "steps_per_s": steps / dt,
+                "kepler_solves_per_s": steps * (n - 1) / dt,
+                "kick_gint_per_s": steps * kick / dt / 1e9, "kepler_failures": c["kepler_failures"]}
+
+    out = {"bodies": int(n), "kick_interactions_per_step": int(kick),
+           "timing": "wall clock around integrator_wh (device-resident state)"}
+    out.update(one("fp64"))
+    # the mixed kick: the planets' pull on each particle in FP32 two-float
+    out["mixed"] = one("mixed")
+    return out
 
 
 def run_radau_single(lib, args):
@@ -737,17 +757,176 @@ def run_radau_disk(lib, args):
     e1 = lib.get_total_energy()
     lib.set_force_mode(old)
     inter = interactions(m)
-    return {"bodies": int(n), "years": args.disk_years, "t_reached": lib.get_model_time(),
-            "seconds": dt, "accepts": c["accepts"], "rejects": c["rejects"],
-            "attempts": c["attempts"], "force_calls": c["force_calls"],
-            "ms_per_attempt": 1e3 * dt / max(c["attempts"], 1),
-            "gint_per_s_in_engine": c["force_calls"] * inter / dt / 1e9,
-            "abs_dE_over_E": abs((e1 - e0) / e0),
-            "timing": "wall clock around integrator_gr (device-resident state)"}
+    out = {"bodies": int(n), "years": args.disk_years, "t_reached": lib.get_model_time(),
+           "seconds": dt, "accepts": c["accepts"], "rejects": c["rejects"],
+           "attempts": c["attempts"], "force_calls": c["force_calls"],
+           "ms_per_attempt": 1e3 * dt / max(c["attempts"], 1),
+           "gint_per_s_in_engine": c["force_calls"] * inter / dt / 1e9,
+           "abs_dE_over_E": abs((e1 - e0) / e0),
+           "timing": "wall clock around integrator_gr (device-resident state)"}
+    # the mixed form: the same sweep with the mixed all-pairs force
+    old = lib.set_force_mode("mixed")
+    try:
+        lib.set_state(p, v, m, r, n, G, 0.0)
+        lib.integrator_gr(0.0, 1e-3, 1.0)
+        lib.set_state(p, v, m, r, n, G, 0.0)
+        lib.reset_counters()
+        t0 = _t.perf_counter()
+        lib.integrator_gr(0.0, args.disk_years, 1.0)
+        dtm = _t.perf_counter() - t0
+        cm = lib.counters()
+        e1m = lib.get_total_energy()
+    finally:
+        lib.set_force_mode(old)
+    out["mixed"] = {"seconds": dtm, "t_reached": lib.get_model_time(), "accepts": cm["accepts"],
+                    "attempts": cm["attempts"], "force_calls": cm["force_calls"],
+                    "gint_per_s_in_engine": cm["force_calls"] * inter / dtm / 1e9,
+                    "abs_dE_over_E": abs((e1m - e0) / e0)}
+    return out
+
+
+def _de_stats(de, ref=None):
+    q = [float(np.percentile(de, x)) for x in (50, 90, 99, 100)]
+    out = {"abs_dE_over_E_p50_p90_p99_max": q,
+           "systems_at_or_below_1e-12": int((de <= 1e-12).sum()), "systems": int(de.size)}
+    if ref is not None:
+        out["reference_method_p50_p90_p99_max"] = [float(np.percentile(ref, x))
+                                                   for x in (50, 90, 99, 100)]
+        out["reference_method_at_or_below_1e-12"] = int((ref <= 1e-12).sum())
+        out["systems_within_10x_of_reference"] = int((de <= 10 * np.maximum(ref, 1e-15)).sum())
+    return out
+
+
+def run_horizons(args):
+    """Long-horizon runs of the stated configurations, each against the
+    reference's own runs where those exist (tests/golden/horizon_*.npz,
+    made by tests/golden/make_horizons.py).  One JSON line."""
+    import time as _t
+
+    import torch
+
+    from abie_gb300.clibabie import CLibABIE
+    torch.cuda.set_device(0)
+    lib = CLibABIE()
+    lib.initialize_code(G, 0.0, 1 << 21, MAX_CE_EVENTS=3, MAX_COLLISION_EVENTS=2, deviceID=0)
+    gold = os.path.join(ROOT, "tests", "golden")
+    which = set(args.horizon.split(","))
+    forms = args.horizon_forms.split(",")
+    out = {"horizon": sorted(which)}
+
+    def ens(ns, years, form, ref=None):
+        P, V, M, offs = ics.ensemble(n_systems=ns, seed0=10000)
+        old = lib.set_force_mode(form)
+        lib.reset_counters()
+        try:
+            res = lib.gr_ensemble(P, V, M, offs, G, 0.0, years)
+        finally:
+            lib.set_force_mode(old)
+        c = lib.counters()
+        de = _energy_errors(lib, P, V, res["pos"], res["vel"], M, offs)
+        steps = int(res["steps"].sum())
+        r = {"systems": ns, "years": years, "seconds": res["seconds"], "system_steps": steps,
+             "system_steps_per_s": steps / res["seconds"], "launch_shape": lib.ensemble_tuning(),
+             "corrector_iterations_per_attempt": c["iterations"] / max(c["attempts"], 1),
+             "max_steps_one_system": int(res["steps"].max()),
+             "failed_systems": int((res["status"] != 0).sum())}
+        r.update(_de_stats(de, ref))
+        return r
+
+    if "ens64" in which:
+        g = np.load(os.path.join(gold, "horizon_ensemble.npz"))
+        h = list(g["horizons"]).index(10000.0)
+        out["ens64_1e4yr"] = {f: ens(64, 10000.0, f, g["de"][:, h]) for f in forms}
+        out["ens64_1e4yr"]["reference_method_cpu_seconds_one_core"] = float(g["wall"][:, h].sum())
+    if "ens4096" in which:
+        out["ens4096_1e4yr"] = {f: ens(4096, 10000.0, f) for f in forms}
+    if "disk" in which:
+        p, v, m, r = ics.planetesimal_disk()
+        e0 = lib.energy(p, v, m, G)
+        runs = {}
+        for form in ("fp64", "exact"):
+            old = lib.set_force_mode(form)
+            lib.reset_counters()
+            try:
+                lib.set_state(p, v, m, r, m.size, G, 0.0)
+                t0 = _t.perf_counter()
+                lib.integrator_gr(0.0, 10.0, 1.0)
+                secs = _t.perf_counter() - t0
+                P, Vv = np.zeros(p.size), np.zeros(v.size)
+                lib.get_state(P, Vv, np.zeros(m.size), np.zeros(m.size))
+                t = lib.get_model_time()
+            finally:
+                lib.set_force_mode(old)
+            c = lib.counters()
+            runs[form] = (P, Vv, t)
+            out.setdefault("disk_10yr", {})[form] = {
+                "seconds": secs, "t": t, "force_calls": int(c["force_calls"]),
+                "accepts": int(c["accepts"]), "rejects": int(c["rejects"]),
+                "abs_dE_over_E": abs((lib.energy(P, Vv, m, G) - e0) / e0),
+                "gint_per_s": c["force_calls"] * interactions(m) / secs / 1e9}
+        # the two forms at the exact form's final time: shift the fast form's
+        # state by RK4 substeps on the library's exact force
+        P, Vv, t = runs["fp64"]
+        Pe, Ve, te = runs["exact"]
+        hsub = (te - t) / max(8, int(np.ceil(abs(te - t) / 2e-4)))
+        nsub = int(round((te - t) / hsub)) if hsub else 0
+        for _ in range(nsub):
+            a1 = lib.force(P, m, G, "exact")
+            a2 = lib.force(P + 0.5 * hsub * Vv, m, G, "exact")
+            a3 = lib.force(P + 0.5 * hsub * Vv + 0.25 * hsub * hsub * a1, m, G, "exact")
+            a4 = lib.force(P + hsub * Vv + 0.5 * hsub * hsub * a2, m, G, "exact")
+            P, Vv = (P + hsub * Vv + hsub * hsub / 6.0 * (a1 + a2 + a3),
+                     Vv + hsub / 6.0 * (a1 + 2 * a2 + 2 * a3 + a4))
+        d = (np.linalg.norm((P - Pe).reshape(-1, 3), axis=1) /
+             np.linalg.norm(Pe.reshape(-1, 3), axis=1))
+        out["disk_10yr"]["fp64_vs_exact_at_common_time"] = {
+            "max_rel_pos": float(d.max()), "median_rel_pos": float(np.median(d))}
+    if "wh" in which:
+        g = np.load(os.path.join(gold, "horizon_cfg3.npz"))
+        p, v, m, r = ics.test_particle_swarm(seed=int(g["seed"][0]))
+        p, v = ics.to_heliocentric(p, v)
+        idx = g["idx"]
+        t_end, dt = float(g["span"][1]), float(g["span"][2])
+        spread = (np.linalg.norm((g["pert_pos"] - g["pos"]).reshape(-1, 3), axis=1) /
+                  np.linalg.norm(g["pos"].reshape(-1, 3), axis=1))
+        for form in forms:
+            old = lib.set_force_mode(form)
+            lib.reset_counters()
+            try:
+                lib.set_state(p, v, m, r, m.size, G, 0.0)
+                e0 = lib.get_total_energy()
+                t0 = _t.perf_counter()
+                lib.integrator_wh(0.0, t_end, dt)
+                secs = _t.perf_counter() - t0
+                P, Vv = np.zeros(p.size), np.zeros(v.size)
+                lib.get_state(P, Vv, np.zeros(m.size), np.zeros(m.size))
+                e1 = lib.get_total_energy()
+            finally:
+                lib.set_force_mode(old)
+            c = lib.counters()
+            d = (np.linalg.norm((P.reshape(-1, 3)[idx] - g["pos"].reshape(-1, 3)), axis=1) /
+                 np.linalg.norm(g["pos"].reshape(-1, 3), axis=1))
+            out.setdefault("wh_1e6", {})[form] = {
+                "steps": int(c["wh_steps"]), "seconds": secs, "steps_per_s": c["wh_steps"] / secs,
+                "t": lib.get_model_time(), "t_reference": float(g["t"][0]),
+                "abs_dE_over_E_massive": abs((e1 - e0) / e0),
+                "abs_dE_over_E_massive_reference": abs((g["energy"][1] - g["energy"][0]) /
+                                                       g["energy"][0]),
+                "kepler_failures": int(c["kepler_failures"]),
+                "sample_vs_oracle_rel_pos_median_p99_max": [float(np.median(d)),
+                                                           float(np.percentile(d, 99)),
+                                                           float(d.max())],
+                "rounding_spread_median_p99_max": [float(np.median(spread)),
+                                                   float(np.percentile(spread, 99)),
+                                                   float(spread.max())]}
+    print(json.dumps(out), flush=True)
+    return 0
 
 
 def main():
     args = parse()
+    if args.horizon:
+        return run_horizons(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

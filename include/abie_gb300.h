@@ -170,8 +170,19 @@ int abie_gr_ensemble(double *pos, double *vel, const double *m,
                      const long long *offsets, int n_systems, double G,
                      double t0, double t_end, double *t_out, int *status,
                      long long *steps, int flags);
-/* Seconds of GPU time spent in the last abie_gr_ensemble call. */
+/* Seconds of GPU time spent in the last abie_gr_ensemble call (the run
+ * itself; the autotuner's trials are reported by abie_ensemble_last_tuning). */
 double abie_last_ensemble_seconds(void);
+/* The launch shape the last abie_gr_ensemble call used: *heavy_div = the
+ * slowest 1 in heavy_div systems ran on four-warp groups; *source = 0 when
+ * the autotuner measured it in that call (or the default applied), 1 when
+ * it came from the tuner's cache file, 2 from abie_debug_ensemble_heavy;
+ * *tune_seconds = GPU seconds of that call's tuning trials.  Returns the
+ * number of candidate shapes timed (0 without tuning).  The tuner times
+ * candidate shares on slices of the batch itself and caches the choice per
+ * device, library build, force form and workload (ABIE_ENSEMBLE_TUNE=0
+ * switches it off; ABIE_TUNE_CACHE names the cache file). */
+int abie_ensemble_last_tuning(int *heavy_div, int *source, double *tune_seconds);
 
 /* Device snapshots, replacing abie/integrator.py:158-204 with store_state
  * (:233-252) and Particles.calculate_aei (abie/particles.py:352-376): the

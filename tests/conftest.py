@@ -8,6 +8,11 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
+# The ensemble's autotuner times candidate launch shapes on each new
+# workload; the tests switch it off (their workloads are all different and
+# small) except the test of the tuner itself, which turns it on again.
+os.environ["ABIE_ENSEMBLE_TUNE"] = "0"
+
 GOLDEN = os.path.join(ROOT, "tests", "golden", "golden.npz")
 
 

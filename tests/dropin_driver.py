@@ -7,9 +7,10 @@ Test helper, run in a fresh process by tests/test_dropin_*.py:
 PKG_ROOT holds the reference's ``abie/`` package (copied unmodified from
 the pip install in baseline/_ref) and, beside it, the ``libabie<EXT_SUFFIX>``
 that its abie/clibabie.py:9-28 loads: this library or the reference's own.
-h5py and toml are not installed here, so minimal stand-ins (an in-memory
-HDF5 file object with groups, datasets and attrs; toml functions that are
-never reached) are put on the path first: they stand in only for the
+h5py and toml are not installed here (nor six on every machine), so
+minimal stand-ins (an in-memory HDF5 file object with groups, datasets and
+attrs; toml functions that are never reached; six.string_types) are put on
+the path first: they stand in only for the
 reference's output layer, which is not on the path under test.
 
 The script builds the system with ``abie.ABIE(deviceID=...)``, ``add()``,
@@ -60,6 +61,12 @@ def _install_stubs():
 
     tm.loads = tm.load = tm.dump = tm.dumps = _unused
     sys.modules["toml"] = tm
+    try:
+        import six  # noqa: F401  (the reference's particles.py imports six.string_types)
+    except ImportError:
+        sx = types.ModuleType("six")
+        sx.string_types = (str,)
+        sys.modules["six"] = sx
 
 
 def main():

@@ -2,7 +2,7 @@
 
 Run in a container where the reference sources exist:
 
-    oracle/build_ref.sh && python tests/golden/make_horizons.py [cfg1|ensemble|all]
+    oracle/build_ref.sh && python tests/golden/make_horizons.py [cfg1|ensemble|cfg3|all]
 
 * ``horizon_cfg1.npz``: the 1,009-body planetary system (1 MSun star, 8
   planets, 1,000 test particles; ``ics.planetary_system(seed=1001)``)
@@ -20,6 +20,17 @@ Run in a container where the reference sources exist:
   10,000-yr run.  This is the distribution the reference method itself
   reaches on these systems, against which the GPU forms' distributions are
   judged.
+
+* ``horizon_cfg3.npz``: the Wisdom-Holman workload (``ics.test_particle_swarm
+  (seed=1003)``, heliocentric: 1 MSun star, 5 planets, 1,048,576 test
+  particles) at dt = 0.01 yr over 10^4 yr (10^6 steps), for the star, the
+  planets and 1,024 test particles drawn with ``default_rng(5)``.  Test
+  particles never act on other bodies, so the run of this subset gives
+  those particles exactly the trajectories they have in the full run.  The
+  reference's O(N^2) loop would take hours here, so the oracle's O(N N_m)
+  restatement runs it (pinned to the reference bit for bit at a few hundred
+  test particles by tests/test_oracle.py); a second run with planet 1's x
+  moved by one unit in the last place gives the rounding spread.
 
 Without the reference library the C restatement in ``oracle/`` (bit for
 bit the same doubles, pinned by tests/test_oracle.py) stands in, and the
@@ -136,9 +147,57 @@ def main_ensemble(out=os.path.join(HERE, "horizon_ensemble.npz"), cores=None):
     print("%s, %.0f s on %d cores; wrote %s" % (res[0]["kind"], time.time() - t0, cores, out))
 
 
+CFG3_SAMPLE = 1024
+CFG3_SEED = 5
+
+
+def cfg3_sample_indices(n_bodies, n_massive=6):
+    """The bodies of the cfg3 fixture: the massive ones and CFG3_SAMPLE test
+    particles, in body order."""
+    rng = np.random.default_rng(CFG3_SEED)
+    tp = n_massive + rng.choice(n_bodies - n_massive, CFG3_SAMPLE, replace=False)
+    return np.concatenate([np.arange(n_massive), np.sort(tp)])
+
+
+def cfg3_run(perturb):
+    import oracle
+    O = oracle.Oracle()
+    p, v, m, r = ics.test_particle_swarm(seed=1003)
+    p, v = ics.to_heliocentric(p, v)
+    idx = cfg3_sample_indices(m.size)
+    P = p.reshape(-1, 3)[idx].ravel().copy()
+    V = v.reshape(-1, 3)[idx].ravel().copy()
+    M = m[idx]
+    if perturb:
+        P[3] = np.nextafter(P[3], np.inf)
+    e0 = O.energy(P, V, M, G)
+    t0 = time.time()
+    out = O.wh(P, V, M, G, 0.0, 10000.0, 0.01)
+    wall = time.time() - t0
+    return {"pos": out["pos"], "vel": out["vel"], "t": out["t"], "e0": e0,
+            "e1": O.energy(out["pos"], out["vel"], M, G), "fails": out["kepler_failures"],
+            "wall": wall, "idx": idx}
+
+
+def main_cfg3(out=os.path.join(HERE, "horizon_cfg3.npz")):
+    _build_checkers()
+    with mp.get_context("spawn").Pool(2) as pool:
+        base, pert = pool.map(cfg3_run, [False, True])
+    np.savez_compressed(out, kind=np.array("oracle"), seed=np.array([1003]),
+                        span=np.array([0.0, 10000.0, 0.01]), idx=base["idx"],
+                        pos=base["pos"], vel=base["vel"], t=np.array([base["t"]]),
+                        energy=np.array([base["e0"], base["e1"]]),
+                        kepler_failures=np.array([base["fails"]]),
+                        pert_pos=pert["pos"], pert_vel=pert["vel"], wall=np.array([base["wall"]]))
+    print("cfg3: t=%.6f, |dE/E| (massive bodies) %.3g, %.0f s; wrote %s"
+          % (base["t"], abs((base["e1"] - base["e0"]) / base["e0"]), base["wall"], out))
+
+
 if __name__ == "__main__":
     what = sys.argv[1] if len(sys.argv) > 1 else "all"
     if what in ("cfg1", "all"):
         main_cfg1()
     if what in ("ensemble", "all"):
         main_ensemble()
+    if what in ("cfg3", "all"):
+        main_cfg3()

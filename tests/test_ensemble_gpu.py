@@ -194,3 +194,43 @@ def test_forms_error_against_the_oracle(clib, oracle):
     for mode, (err, de) in table.items():
         assert err <= TOL, (mode, err)
         assert de <= 1e-12, (mode, de)
+
+
+def test_autotuner_times_shapes_and_caches_them(clib, tmp_path, monkeypatch):
+    """The ensemble's autotuner: the first call on a workload times the
+    candidate shares of four-warp groups on slices of the batch and picks
+    one; the second call reads it from the cache file.  In the fast form
+    a system's doubles do not depend on its group size, so every call gives
+    the same result as a run with the tuner off and the chosen share."""
+    import ctypes as C
+    monkeypatch.setenv("ABIE_ENSEMBLE_TUNE", "1")
+    monkeypatch.setenv("ABIE_TUNE_CACHE", str(tmp_path / "tune.tsv"))
+    lib = clib.lib
+
+    def tuning():
+        h, src, secs = C.c_int(0), C.c_int(0), C.c_double(0)
+        n = lib.abie_ensemble_last_tuning(C.byref(h), C.byref(src), C.byref(secs))
+        return n, h.value, src.value, secs.value
+
+    P, V, M, offs = ics.ensemble(n_systems=512, seed0=4000)
+    old = clib.set_force_mode("fp64")
+    try:
+        first = clib.gr_ensemble(P, V, M, offs, G, 0.0, 0.5)
+        n1, h1, src1, s1 = tuning()
+        second = clib.gr_ensemble(P, V, M, offs, G, 0.0, 0.5)
+        n2, h2, src2, s2 = tuning()
+        monkeypatch.setenv("ABIE_ENSEMBLE_TUNE", "0")
+        lib.abie_debug_ensemble_heavy(C.c_int(h1))
+        try:
+            plain = clib.gr_ensemble(P, V, M, offs, G, 0.0, 0.5)
+        finally:
+            lib.abie_debug_ensemble_heavy(C.c_int(0))
+    finally:
+        clib.set_force_mode(old)
+    print("autotuner: %d candidates, share 1/%d, %.3f s of trials; then from the cache: 1/%d"
+          % (n1, h1, s1, h2))
+    assert n1 >= 4 and src1 == 0 and s1 > 0 and h1 > 0
+    assert src2 == 1 and h2 == h1 and n2 == 0
+    assert (tmp_path / "tune.tsv").read_text().count("\t") >= 3
+    for out in (first, second):
+        assert np.array_equal(out["pos"], plain["pos"]) and np.array_equal(out["t"], plain["t"])

@@ -6,12 +6,18 @@
   corrector iterations per attempt against the reference's predictor, which
   keeps the previous step's g.
 * Samples collected from the ensemble's own runs train a network whose
-  held-out loss beats the plain guess; with it the corrector needs fewer
-  iterations per attempt than with the reference's predictor on systems it
-  has not seen, while final states agree with the reference-predictor run
-  at a common time to 1e-10 (the convergence test is unchanged).  An
-  attempt whose network guess ends in a non-finite state is redone from the
-  plain guess, so every system reaches t_end."""
+  held-out loss beats the plain guess.  What the network gains over the
+  same method without it (the fast form: plain guess, consistent g) is
+  measured on systems it has not seen and printed: corrector iterations
+  per attempt with and without the network.  Measured so far the gain is
+  nil or negative (7.0 against 6.7 iterations per attempt): a lower loss
+  does not move the iteration count, which falls only about 0.35 per
+  decade of guess-error reduction.  The test bounds that difference to
+  half an iteration either way, and checks that final states agree with
+  the reference-predictor run at a common time to 1e-10 (the convergence
+  test is unchanged).  An attempt whose network guess ends in a
+  non-finite state is redone from the plain guess, so every system
+  reaches t_end."""
 import numpy as np
 import pytest
 
@@ -63,12 +69,18 @@ def test_collect_train_and_fewer_iterations(clib, oracle):
     cons, it_cons, _ = run("exact", consistent=True)    # same arithmetic, consistent g
     fast, it_fast, _ = run("fp64")                      # fast form (consistent g)
     learned, it_learned, cl = run("fp64", learned=True)
+    gain = it_fast - it_learned
     print("iterations per attempt: reference predictor %.3f consistent g %.3f fast form %.3f "
-          "learned %.3f; attempts redone from the plain guess: %d"
-          % (it_ref, it_cons, it_fast, it_learned, cl["learned_fallbacks"]))
+          "learned %.3f; the network's gain over the same method without it: %+.3f "
+          "iterations per attempt; attempts redone from the plain guess: %d"
+          % (it_ref, it_cons, it_fast, it_learned, gain, cl["learned_fallbacks"]))
     for r in (ref, cons, fast, learned):
         assert (r["status"] == 0).all() and (r["t"] >= 0.5).all()
-    assert it_cons < it_ref and it_fast < it_ref and it_learned < it_ref
+    # consistent g is the gain over the reference's predictor ...
+    assert it_cons < it_ref and it_fast < it_ref
+    # ... the network's own effect against the same method without it is
+    # small either way (measured: about -0.3)
+    assert abs(gain) < 0.5
     for s in range(0, 512, 37):
         a, b = offs2[s], offs2[s + 1]
         tp, tl = ref["t"][s], learned["t"][s]
