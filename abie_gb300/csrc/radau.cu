@@ -582,6 +582,80 @@ __device__ void scan_events(const EngineArgs &a, double t, int tid, int nthreads
     }
 }
 
+// The event test of one pair on the accepted positions, in the
+// reference's arithmetic (src/common.c:125-152): the separation of the
+// lower index j minus the higher k, r2 = dx^2 + dy^2 + dz^2, sep = sqrt(r2);
+// a close encounter when sep <= the close-encounter distance, a collision
+// when the radii sum is positive and sep <= it.  (pj, pk) are the two
+// bodies' positions in either order; the squares do not depend on it.
+__device__ __forceinline__ void event_pair(const EngineArgs &a, int j, int k, double xj, double yj,
+                                           double zj, double xk, double yk, double zk)
+{
+    const double dx = xj - xk, dy = yj - yk, dz = zj - zk;
+    const double r2 = dx * dx + dy * dy + dz * dz;
+    if (!(r2 <= a.thr2)) return;
+    const int lo = j < k ? j : k, hi = j < k ? k : j;
+    const double sep = sqrt(r2);
+    const double rr = a.r[lo] + a.r[hi];
+    EngineCtl *ctl = a.ctl;
+    if (sep <= a.ce_dist) {
+        int e = atomicAdd(&ctl->n_ev, 1);
+        if (e < a.ev_cap) a.ev[e] = EventRec{lo, hi, 0, sep};
+    }
+    if (rr > 0 && sep <= rr) {
+        int e = atomicAdd(&ctl->n_ev, 1);
+        if (e < a.ev_cap) a.ev[e] = EventRec{lo, hi, 1, sep};
+    }
+}
+
+// The event check fused into the advance force evaluation (spacing 1,
+// whose positions become the accepted ones): while the force loop walks a
+// sink's sources, each (sink, source) pair is tested as well -- a pair of
+// two sources once, from the lower index; a massless or deleted sink with
+// every source.  Records of an attempt that is rejected are dropped; the
+// pairs the force never visits (two bodies without positive mass) are
+// tested by scan_events_nonsources after an accepted step.
+template <int JS>
+__device__ __forceinline__ void sink_events(const EngineArgs &a, int j, const Src *src, double xj,
+                                            double yj, double zj, int lane)
+{
+    const bool j_src = a.src_slot[j] >= 0;
+    for (int q = lane; q < a.n_src; q += JS) {
+        const int k = a.src_body[q];
+        if (k == j || (j_src && k < j)) continue;
+        const Src s = load_src(src + q);
+        event_pair(a, j, k, xj, yj, zj, s.x, s.y, s.z);
+    }
+}
+
+// Pairs of two bodies without positive mass (the split and persistent
+// engines' remaining check after an accepted step): scan_events' warp
+// layout and prefilter over the bodies listed in tp_body.
+__device__ void scan_events_nonsources(const EngineArgs &a, int tid, int nthreads)
+{
+    const int lane = tid & 31;
+    const int warp = tid >> 5, nwarps = nthreads >> 5;
+    const float T = __double2float_ru(sqrt(a.thr2) * (1.0 + 0x1p-20));
+    const float widen = 1.0f + 0x1p-21f;
+    for (int u = warp; u < a.n_tp; u += nwarps) {
+        const int j = a.tp_body[u];
+        const float2 fx = __ldcg(a.ypf + 3 * j), fy = __ldcg(a.ypf + 3 * j + 1),
+                     fz = __ldcg(a.ypf + 3 * j + 2);
+        const float tx = T + fx.y, ty = T + fy.y, tz = T + fz.y;
+        for (int v = u + 1 + lane; v < a.n_tp; v += 32) {
+            const int k = a.tp_body[v];
+            const float2 gx = __ldcg(a.ypf + 3 * k), gy = __ldcg(a.ypf + 3 * k + 1),
+                         gz = __ldcg(a.ypf + 3 * k + 2);
+            if (fabsf(fx.x - gx.x) > (tx + gx.y) * widen || fabsf(fy.x - gy.x) > (ty + gy.y) * widen ||
+                fabsf(fz.x - gz.x) > (tz + gz.y) * widen)
+                continue;
+            event_pair(a, j, k, __ldcg(a.ypa + 3 * j), __ldcg(a.ypa + 3 * j + 1),
+                       __ldcg(a.ypa + 3 * j + 2), __ldcg(a.ypa + 3 * k), __ldcg(a.ypa + 3 * k + 1),
+                       __ldcg(a.ypa + 3 * k + 2));
+        }
+    }
+}
+
 // One thread: order the events of this check as the reference's loops
 // would meet them, append them to the ring buffers, compute the flag.
 __device__ void commit_events(const EngineArgs &a, double t)
@@ -801,6 +875,8 @@ __global__ void __launch_bounds__(256) radau_engine(EngineArgs a)
             sink_force<MODE, JS, PN>(a, j, a.srca, a.dyp, a.ypa[3 * j], a.ypa[3 * j + 1],
                                  a.ypa[3 * j + 2], lane, f);
             if (!live) continue;
+            if (a.thr2 > 0.0)  // the event check, fused into this force loop
+                sink_events<JS>(a, j, a.srca, a.ypa[3 * j], a.ypa[3 * j + 1], a.ypa[3 * j + 2], lane);
             const bool alive = a.m[j] >= 0.0;
             for (int c = c0; c < c1; c++) {
                 const int i = 3 * j + c;
@@ -851,11 +927,14 @@ __global__ void __launch_bounds__(256) radau_engine(EngineArgs a)
                     }
                 }
             }
-            scan_events(a, t, tid, nthreads);
+            if (a.thr2 > 0.0) scan_events_nonsources(a, tid, nthreads);
             if (leader) ctl->accepts++;
         } else {
             loop_count += 1;
-            if (leader) ctl->rejects++;
+            if (leader) {
+                ctl->rejects++;
+                ctl->n_ev = 0;  // the fused check's records of a rejected attempt
+            }
         }
         if (!stop) {
             if ((MODE == ABIE_FORCE_EXACT ? dtreq / h : rq) > 1.0 / FAC) h /= FAC;
@@ -1012,13 +1091,43 @@ __global__ void __launch_bounds__(64) radau_split(EngineArgs a)
     // group force or the particle's sum over the massive sources.  Newton,
     // then the post-Newtonian sum, then the external acceleration, as
     // src/common.c:82-114 adds them.
-    auto forces = [&](double p, double v) -> double {
+    // With events on, the advance evaluation (whose positions become the
+    // accepted ones) also runs the event test on the pairs it visits: the
+    // massive pairs once, in block 0, and each particle with every massive
+    // body (sink_events' rule; scan_events_nonsources covers the rest).
+    auto forces = [&](double p, double v, bool advance = false) -> double {
         if (warp == 0 && has) {
             s_sp[ib][lane / 3][lane % 3] = p;
             if (pn) s_sv[ib][lane / 3][lane % 3] = v;
         }
         __syncthreads();
         double F = 0.0;
+        if (advance && a.thr2 > 0.0) {
+            const double(*P)[SPW] = s_sp[ib];
+            if (warp == 0) {
+                if (blockIdx.x == 0)
+                    for (int pr = lane; pr < n_m * (n_m - 1) / 2; pr += 32) {
+                        int i = 0, rem = pr;
+                        while (rem >= n_m - 1 - i) {
+                            rem -= n_m - 1 - i;
+                            i++;
+                        }
+                        const int k = i + 1 + rem;
+                        event_pair(a, a.src_body[i], a.src_body[k], P[i][0], P[i][1], P[i][2], P[k][0],
+                                   P[k][1], P[k][2]);
+                    }
+            } else {
+                const double x = __shfl_sync(0xffffffffu, p, 0, 4);
+                const double y = __shfl_sync(0xffffffffu, p, 1, 4);
+                const double z = __shfl_sync(0xffffffffu, p, 2, 4);
+                const int tpi = blockIdx.x * SPLIT_TPW + lane / 4;
+                if ((lane & 3) == 0 && tpi < a.n_tp) {
+                    const int body = a.tp_body[tpi];
+                    for (int k = 0; k < n_m; k++)
+                        event_pair(a, body, a.src_body[k], x, y, z, P[k][0], P[k][1], P[k][2]);
+                }
+            }
+        }
         if (warp == 0) {
             group_force<MODE, 1>(mg, n_m, s_sp[ib], s_sa);
             if (pn) {
@@ -1137,7 +1246,7 @@ __global__ void __launch_bounds__(64) radau_split(EngineArgs a)
         const double hh1 = 0.5 * h * h;
         const double ya = has ? e_pred_pos<MODE>(X, 8, 1.0, h, h, hh1) : 0.0;
         const double va = has ? e_pred_vel<MODE>(X, h) : 0.0;
-        const double dd = forces(ya, va);
+        const double dd = forces(ya, va, true);
         unsigned long long kb6 = 0, kdd = 0;
         if (has && writer) {
             a.ypa[gi] = ya;
@@ -1177,11 +1286,14 @@ __global__ void __launch_bounds__(64) radau_split(EngineArgs a)
             X.b6p = X.b[6];
             e_refine(X, q);
             if (MODE != ABIE_FORCE_EXACT) consistent_g(X);
-            scan_events(a, t, tid, nthreads);
+            if (a.thr2 > 0.0) scan_events_nonsources(a, tid, nthreads);
             if (leader) ctl->accepts++;
         } else {
             loop_count += 1;
-            if (leader) ctl->rejects++;
+            if (leader) {
+                ctl->rejects++;
+                ctl->n_ev = 0;  // the fused check's records of a rejected attempt
+            }
         }
         if (!stop) {
             if ((MODE == ABIE_FORCE_EXACT ? dtreq / h : rq) > 1.0 / FAC) h /= FAC;
