@@ -478,13 +478,13 @@ int ensemble_run(double *pos, double *vel, const double *m, const long long *off
             ABIE_CUDA(cudaMalloc(&B.d_vel0, 3 * total * sizeof(double)));
             ABIE_CUDA(cudaMemcpyAsync(B.d_pos0, B.d_pos, 3 * total * sizeof(double), cudaMemcpyDeviceToDevice, st));
             ABIE_CUDA(cudaMemcpyAsync(B.d_vel0, B.d_vel, 3 * total * sizeof(double), cudaMemcpyDeviceToDevice, st));
-            // probe: the default share over 1 % of the span
+            // probe: the default share over 0.2 % of the span
             double probe_s = 0.0;
             int probe_l = 0;
             classes(order, offsets, heavy_div(mode), cls);
-            if ((rc = run_launches(B, base, order, cls, t0 + 0.01 * span, st, &probe_s, &probe_l))) return rc;
-            const double est_full = probe_s / 0.01;
-            const double frac = std::min(1.0, std::max(0.01, 0.2 / std::max(est_full, 1e-9)));
+            if ((rc = run_launches(B, base, order, cls, t0 + 0.002 * span, st, &probe_s, &probe_l))) return rc;
+            const double est_full = probe_s / 0.002;
+            const double frac = std::min(1.0, std::max(0.002, 0.2 / std::max(est_full, 1e-9)));
             const std::vector<int> cands = mode == ABIE_FORCE_EXACT ? std::vector<int>{4, 16, 64, 256}
                                                                     : std::vector<int>{2, 4, 8, 16, 64, 256};
             // each candidate timed twice (the faster counts); the default
