@@ -112,7 +112,8 @@ def parse():
     ap.add_argument("--extras", default="ensemble,wh,radau,disk,next",
                     help="comma list of sub-measurements: ensemble, wh, radau, disk, next "
                          "(Runge-Kutta 4, post-Newtonian Radau15, snapshots)")
-    ap.add_argument("--ensemble-forms", default="reference_ops,plain_fp64,fp64,mixed,learned",
+    ap.add_argument("--ensemble-forms",
+                    default="reference_ops,plain_fp64,fp64,mixed,learned,mixed_learned",
                     help="comma list of ensemble forms to time")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--horizon", default="",
@@ -549,7 +550,8 @@ def run_ensemble(lib, args, rank, dev):
     reference's plain guess); mixed = the fast form with light partners'
     terms summed in FP32 two-float arithmetic; learned = the fast form with
     the BF16 network's guess, trained online on samples the ensemble records
-    on a separate set of systems."""
+    on a separate set of systems; mixed_learned = the mixed form with that
+    guess (the three patterns together)."""
     import time as _t
 
     from abie_gb300.learned import collect_samples, train_predictor
@@ -558,7 +560,7 @@ def run_ensemble(lib, args, rank, dev):
     out = {"systems": int(offs.size - 1), "bodies": int(M.size), "years": args.ensemble_years}
     # online training on other systems
     wanted = set(args.ensemble_forms.split(","))
-    if "learned" in wanted:
+    if wanted & {"learned", "mixed_learned"}:
         t0 = _t.perf_counter()
         TP, TV, TM, toffs = ics.ensemble(n_systems=2048, seed0=900000 + 4096 * rank)
         samples, _ = collect_samples(lib, TP, TV, TM, toffs, G, 1.0)
@@ -567,7 +569,8 @@ def run_ensemble(lib, args, rank, dev):
                            "seconds": _t.perf_counter() - t0, "holdout_loss": info["holdout_loss"],
                            "holdout_loss_plain_guess": info["holdout_loss_plain"]}
     forms = (("reference_ops", "exact", {}), ("plain_fp64", "naive", {}), ("fp64", "fp64", {}),
-             ("mixed", "mixed", {}), ("learned", "fp64", {"learned": True}))
+             ("mixed", "mixed", {}), ("learned", "fp64", {"learned": True}),
+             ("mixed_learned", "mixed", {"learned": True}))
     for label, mode, kw in forms:
         if label not in wanted:
             continue
@@ -588,11 +591,11 @@ def run_ensemble(lib, args, rank, dev):
                       "failed_systems": int((res["status"] != 0).sum()),
                       "max_steps_one_system": int(res["steps"].max()),
                       "launch_shape": lib.ensemble_tuning()}
-        if label == "learned":
+        if label in ("learned", "mixed_learned"):
             out[label]["attempts_redone_from_plain_guess"] = int(c["learned_fallbacks"])
     lib.mlp_enable(False)
     base = out.get("plain_fp64", {}).get("system_steps_per_s")
-    for label in ("reference_ops", "fp64", "mixed", "learned"):
+    for label in ("reference_ops", "fp64", "mixed", "learned", "mixed_learned"):
         if base and label in out and out[label]["system_steps_per_s"]:
             out[label]["speedup_vs_plain_fp64"] = out[label]["system_steps_per_s"] / base
     return out
@@ -831,6 +834,8 @@ def run_horizons(args):
              "max_steps_one_system": int(res["steps"].max()),
              "failed_systems": int((res["status"] != 0).sum())}
         r.update(_de_stats(de, ref))
+        r["per_system_abs_dE_over_E_first_64"] = [float(x) for x in de[:64]]
+        r["per_system_steps_first_64"] = [int(x) for x in res["steps"][:64]]
         return r
 
     if "ens64" in which:
