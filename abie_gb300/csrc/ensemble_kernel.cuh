@@ -278,8 +278,10 @@ __global__ void __launch_bounds__(32 * WARPS, (EnsOccupancy<W, LEARN>::value)) e
             X.y0 = slot(0);
             X.dy0 = slot(1);
             X.F1 = slot(2);
+            // the fast forms carry g only: b is formed from g at the next
+            // accept, so it is neither saved at a yield nor read back
 #pragma unroll
-            for (int k = 0; k < 7; k++) X.b[k] = slot(3 + k);
+            for (int k = 0; k < 7; k++) X.b[k] = ref_ops<MODE>() ? slot(3 + k) : 0.0;
 #pragma unroll
             for (int k = 0; k < 7; k++) X.g[k] = slot(10 + k);
             X.b6p = slot(17);
@@ -466,8 +468,10 @@ __global__ void __launch_bounds__(32 * WARPS, (EnsOccupancy<W, LEARN>::value)) e
                 slot(0) = X.y0;
                 slot(1) = X.dy0;
                 slot(2) = X.F1;
+                if (ref_ops<MODE>()) {
 #pragma unroll
-                for (int k = 0; k < 7; k++) slot(3 + k) = X.b[k];
+                    for (int k = 0; k < 7; k++) slot(3 + k) = X.b[k];
+                }
 #pragma unroll
                 for (int k = 0; k < 7; k++) slot(10 + k) = X.g[k];
                 slot(17) = X.b6p;

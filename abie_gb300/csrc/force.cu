@@ -57,6 +57,7 @@ void force_scratch_free(ForceScratch &s)
     if (s.n_src) cudaFree(s.n_src);
     if (s.partial) cudaFree(s.partial);
     if (s.gm_max) cudaFree(s.gm_max);
+    if (s.mixed_soa) cudaFree(s.mixed_soa);
     if (s.next) cudaFree(s.next);
     if (s.counts) cudaFree(s.counts);
     if (s.sym_items) cudaFree(s.sym_items);

@@ -13,6 +13,8 @@ struct ForceScratch {
     int *n_src = nullptr;       // device scalar
     double *partial = nullptr;  // per (sink, source chunk) partial sums, 3 doubles each
     unsigned long long *gm_max = nullptr;  // mixed form: largest G m (as ordered bits)
+    float *mixed_soa = nullptr;            // mixed form: anchored two-float sources
+    size_t mixed_cap = 0;                  // floats
     unsigned int *next = nullptr;          // fp64 form: next sink to hand out
     int *counts = nullptr;      // parallel compaction: massive bodies per chunk
     // symmetric form (every body massive): work items, first item per row,

@@ -2,7 +2,7 @@
 //
 // Sources (the massive bodies, compacted in body order) are split by G m:
 //   heavy: G m >= theta * max G m (the star of a planetary system) -> the
-//          fast FP64 pair term (gm_inv_r3), added straight into FP64 sums;
+//          fast FP64 pair term (pair_fast), added straight into FP64 sums;
 //   light: everything else -> FP32 pair terms.
 // Light pairs use coordinates relative to an FP64 anchor (the first source)
 // held as two floats, hi + lo (48 significant bits), so the difference
@@ -12,10 +12,18 @@
 // terms in FP32 and folds the tile sum into FP64, so the FP32 sums never run
 // over more than one tile (compensated two-level accumulation).
 //
-// The kernel works in blocks of SINKS x TILE: every thread owns 4 sinks and
-// reads each source once from shared memory, so shared-memory traffic is 8
-// bytes per interaction.  Sources split into chunks across blocks; chunk
-// partial sums are added in chunk order by a second pass (deterministic).
+// The light pair term runs on Blackwell's packed FP32 instructions
+// (add/sub/mul/fma .f32x2: two single-precision operations per lane and
+// instruction): one instruction serves a sink against two sources, so a
+// pair term costs 12 issued instructions instead of 24.  Each packed
+// operation rounds exactly as its scalar counterpart.
+//
+// A first pass writes the sources once as anchored two-float coordinates
+// and -G m (struct of arrays, +0 marking a heavy source, -0 the padding
+// after the last source); the force kernel works in blocks of SINKS x TILE:
+// every thread owns 4 sinks and reads each source once from shared memory.
+// Sources split into chunks across blocks; chunk partial sums are added in
+// chunk order by a second pass (deterministic).
 #include <algorithm>
 
 #include "mixed.cuh"
@@ -29,15 +37,59 @@ double mixed_heavy_fraction() { return g_heavy_fraction; }
 
 namespace {
 
-constexpr int MT = 128;       // threads per block
-constexpr int MS = 4;         // sinks per thread
+#ifndef ABIE_MIXED_MT
+#define ABIE_MIXED_MT 128
+#endif
+#ifndef ABIE_MIXED_MS
+#define ABIE_MIXED_MS 4
+#endif
+#ifndef ABIE_MIXED_MINB
+#define ABIE_MIXED_MINB 3
+#endif
+constexpr int MT = ABIE_MIXED_MT;  // threads per block
+constexpr int MS = ABIE_MIXED_MS;  // sinks per thread
 constexpr int MTILE = 128;    // sources per shared-memory tile
 constexpr int SINKS_PER_BLOCK = MT * MS;
+constexpr int NSOA = 7;       // xh yh zh xl yl zl -Gm
+static_assert(MT >= MTILE && MT % 32 == 0, "a tile is loaded by the block's first MTILE threads");
 
-struct __align__(16) LightSrc {
-    float xh, yh, zh, gm;  // gm = 0 for heavy sources (they go through FP64)
-    float xl, yl, zl, pad;
-};
+// Two floats in one 64-bit register, the first in the low half.
+typedef unsigned long long f32x2;
+
+__device__ __forceinline__ f32x2 pk2(float lo, float hi)
+{
+    f32x2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ void upk2(f32x2 v, float &lo, float &hi)
+{
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ f32x2 add2(f32x2 a, f32x2 b)
+{
+    f32x2 r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f32x2 sub2(f32x2 a, f32x2 b)
+{
+    f32x2 r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f32x2 mul2(f32x2 a, f32x2 b)
+{
+    f32x2 r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f32x2 fma2(f32x2 a, f32x2 b, f32x2 c)
+{
+    f32x2 r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
 
 __device__ __forceinline__ void split_df(double v, float &hi, float &lo)
 {
@@ -59,19 +111,51 @@ __global__ void max_gm_kernel(const Src *__restrict__ src, const int *__restrict
     if ((threadIdx.x & 31) == 0 && best) atomicMax(gm_max, best);
 }
 
-__global__ void __launch_bounds__(MT) force_mixed_kernel(
-    const double *__restrict__ pos, const double *__restrict__ m, int n,
-    const Src *__restrict__ src, const int *__restrict__ n_src_p,
-    const unsigned long long *__restrict__ gm_max_bits, double heavy_fraction, int chunks,
-    double *__restrict__ acc, double *__restrict__ partial)
+// The sources as anchored two-float coordinates and -G m, struct of arrays
+// of stride entries each: a light source's -G m is negative (-0 if it
+// underflows single precision), a heavy source's +0 (its term runs in FP64),
+// and the entries after the last source hold zeros with -G m = -0.
+__global__ void mixed_sources_kernel(const Src *__restrict__ src, const int *__restrict__ n_src_p,
+                                     const unsigned long long *__restrict__ gm_max_bits,
+                                     double heavy_fraction, float *__restrict__ soa, int stride)
 {
-    __shared__ LightSrc tile[MTILE];
-    __shared__ Src heavy[MTILE];
-    __shared__ int n_heavy;
+    const int n_src = *n_src_p;
+    const double thr = heavy_fraction * __longlong_as_double((long long)*gm_max_bits);
+    double ax0 = 0.0, ay0 = 0.0, az0 = 0.0;
+    if (n_src > 0) {
+        ax0 = src[0].x;
+        ay0 = src[0].y;
+        az0 = src[0].z;
+    }
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < stride; q += gridDim.x * blockDim.x) {
+        float xh = 0.0f, yh = 0.0f, zh = 0.0f, xl = 0.0f, yl = 0.0f, zl = 0.0f, ngm = -0.0f;
+        if (q < n_src) {
+            const Src s = src[q];
+            split_df(s.x - ax0, xh, xl);
+            split_df(s.y - ay0, yh, yl);
+            split_df(s.z - az0, zh, zl);
+            ngm = s.gm >= thr ? 0.0f : -__double2float_rn(s.gm);
+        }
+        soa[q] = xh;
+        soa[stride + q] = yh;
+        soa[2 * stride + q] = zh;
+        soa[3 * stride + q] = xl;
+        soa[4 * stride + q] = yl;
+        soa[5 * stride + q] = zl;
+        soa[6 * stride + q] = ngm;
+    }
+}
+
+__global__ void __launch_bounds__(MT, ABIE_MIXED_MINB) force_mixed_kernel(
+    const double *__restrict__ pos, const double *__restrict__ m, int n,
+    const Src *__restrict__ src, const int *__restrict__ n_src_p, const float *__restrict__ soa,
+    int stride, int chunks, int per, double *__restrict__ acc, double *__restrict__ partial)
+{
+    __shared__ __align__(16) float tile[NSOA][MTILE];
+    __shared__ unsigned heavy_bits[MTILE / 32];
     const int n_src = *n_src_p;
     const int sink_block = blockIdx.x / chunks;
     const int chunk = blockIdx.x % chunks;
-    const double thr = heavy_fraction * __longlong_as_double((long long)*gm_max_bits);
     // anchor: the first source (FP64)
     double ax0 = 0.0, ay0 = 0.0, az0 = 0.0;
     if (n_src > 0) {
@@ -79,99 +163,107 @@ __global__ void __launch_bounds__(MT) force_mixed_kernel(
         ay0 = src[0].y;
         az0 = src[0].z;
     }
-    // sinks of this thread
-    int sj[MS];
-    double px[MS], py[MS], pz[MS];
-    float hx[MS], hy[MS], hz[MS], lx[MS], ly[MS], lz[MS];
+    // sinks of this thread: anchored two-float coordinates in both halves
+    f32x2 HX[MS], HY[MS], HZ[MS], LX[MS], LY[MS], LZ[MS];
     double sx[MS], sy[MS], sz[MS];
 #pragma unroll
     for (int k = 0; k < MS; k++) {
-        int j = sink_block * SINKS_PER_BLOCK + k * MT + threadIdx.x;
-        sj[k] = j;
-        int jj = j < n ? j : (n > 0 ? n - 1 : 0);
-        px[k] = pos[3 * jj];
-        py[k] = pos[3 * jj + 1];
-        pz[k] = pos[3 * jj + 2];
-        split_df(px[k] - ax0, hx[k], lx[k]);
-        split_df(py[k] - ay0, hy[k], ly[k]);
-        split_df(pz[k] - az0, hz[k], lz[k]);
+        const int j = sink_block * SINKS_PER_BLOCK + k * MT + threadIdx.x;
+        const int jj = j < n ? j : (n > 0 ? n - 1 : 0);
+        float hx, hy, hz, lx, ly, lz;
+        split_df(pos[3 * jj] - ax0, hx, lx);
+        split_df(pos[3 * jj + 1] - ay0, hy, ly);
+        split_df(pos[3 * jj + 2] - az0, hz, lz);
+        HX[k] = pk2(hx, hx);
+        HY[k] = pk2(hy, hy);
+        HZ[k] = pk2(hz, hz);
+        LX[k] = pk2(lx, lx);
+        LY[k] = pk2(ly, ly);
+        LZ[k] = pk2(lz, lz);
         sx[k] = sy[k] = sz[k] = 0.0;
     }
+    // r^2 starts at 1e-20 (a self pair gets a finite r^-3 and a zero term)
+    const f32x2 R2MIN = pk2(1e-20f, 1e-20f), MHALF = pk2(-0.5f, -0.5f), THREEHALF = pk2(1.5f, 1.5f);
     const int tiles = (n_src + MTILE - 1) / MTILE;
-    const int per = (tiles + chunks - 1) / chunks;
     const int t0 = chunk * per, t1 = min(tiles, t0 + per);
     for (int t = t0; t < t1; t++) {
         const int base = t * MTILE;
-        __syncthreads();
-        if (threadIdx.x == 0) n_heavy = 0;
-        __syncthreads();
-        {
-            const int q = base + threadIdx.x;
-            LightSrc L;
-            bool is_heavy = false;
-            Src s = {0.0, 0.0, 0.0, 0.0};
-            if (q < n_src) {
-                s = src[q];
-                is_heavy = s.gm >= thr;
-                split_df(s.x - ax0, L.xh, L.xl);
-                split_df(s.y - ay0, L.yh, L.yl);
-                split_df(s.z - az0, L.zh, L.zl);
-                L.gm = is_heavy ? 0.0f : __double2float_rn(s.gm);
-            } else {
-                L.xh = L.yh = L.zh = 0.0f;
-                L.xl = L.yl = L.zl = 0.0f;
-                L.gm = 0.0f;
-            }
-            L.pad = 0.0f;
-            tile[threadIdx.x] = L;
-            // heavy sources in source order: warp ballots, then a running base
-            unsigned bal = __ballot_sync(0xffffffffu, is_heavy);
-            const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-            for (int w = 0; w < MT / 32; w++) {
-                __syncthreads();
-                if (warp == w && is_heavy)
-                    heavy[n_heavy + __popc(bal & ((1u << lane) - 1u))] = s;
-                __syncthreads();
-                if (warp == w && lane == 0) n_heavy += __popc(bal);
-            }
+        __syncthreads();  // the previous tile is consumed
+        if (threadIdx.x < MTILE) {  // one source per thread of the first MTILE
+#pragma unroll
+            for (int a = 0; a < NSOA; a++) tile[a][threadIdx.x] = soa[a * stride + base + threadIdx.x];
+            const bool heavy = base + (int)threadIdx.x < n_src &&
+                               __float_as_uint(tile[6][threadIdx.x]) == 0u;
+            const unsigned bal = __ballot_sync(0xffffffffu, heavy);
+            if ((threadIdx.x & 31) == 0) heavy_bits[threadIdx.x >> 5] = bal;
         }
         __syncthreads();
-        float fx[MS], fy[MS], fz[MS];
+        f32x2 FX[MS], FY[MS], FZ[MS];
 #pragma unroll
-        for (int k = 0; k < MS; k++) fx[k] = fy[k] = fz[k] = 0.0f;
-        const int cnt = min(MTILE, n_src - base);
-#pragma unroll 2
-        for (int q = 0; q < cnt; q++) {
-            const LightSrc L = tile[q];
+        for (int k = 0; k < MS; k++) FX[k] = FY[k] = FZ[k] = 0ull;  // +0, +0
+        // four sources per step (the padding after the last source adds zeros)
+        const int cnt = (min(MTILE, n_src - base) + 3) & ~3;
+#pragma unroll 1
+        for (int q = 0; q < cnt; q += 4) {
+            const ulonglong2 XH = *reinterpret_cast<const ulonglong2 *>(&tile[0][q]);
+            const ulonglong2 YH = *reinterpret_cast<const ulonglong2 *>(&tile[1][q]);
+            const ulonglong2 ZH = *reinterpret_cast<const ulonglong2 *>(&tile[2][q]);
+            const ulonglong2 XL = *reinterpret_cast<const ulonglong2 *>(&tile[3][q]);
+            const ulonglong2 YL = *reinterpret_cast<const ulonglong2 *>(&tile[4][q]);
+            const ulonglong2 ZL = *reinterpret_cast<const ulonglong2 *>(&tile[5][q]);
+            const ulonglong2 NG = *reinterpret_cast<const ulonglong2 *>(&tile[6][q]);
 #pragma unroll
-            for (int k = 0; k < MS; k++) {
-                float dx = (hx[k] - L.xh) + (lx[k] - L.xl);
-                float dy = (hy[k] - L.yh) + (ly[k] - L.yl);
-                float dz = (hz[k] - L.zh) + (lz[k] - L.zl);
-                float r2 = fmaxf(fmaf(dz, dz, fmaf(dy, dy, dx * dx)), 1e-20f);
-                float y = rsqrtf(r2);
-                y = y * fmaf(-0.5f * r2, y * y, 1.5f);  // one Newton step
-                float w = L.gm * (y * y) * y;
-                fx[k] = fmaf(-w, dx, fx[k]);
-                fy[k] = fmaf(-w, dy, fy[k]);
-                fz[k] = fmaf(-w, dz, fz[k]);
+            for (int h = 0; h < 2; h++) {
+                const f32x2 xh = h ? XH.y : XH.x, yh = h ? YH.y : YH.x, zh = h ? ZH.y : ZH.x;
+                const f32x2 xl = h ? XL.y : XL.x, yl = h ? YL.y : YL.x, zl = h ? ZL.y : ZL.x;
+                const f32x2 ng = h ? NG.y : NG.x;
+#pragma unroll
+                for (int k = 0; k < MS; k++) {
+                    const f32x2 dx = add2(sub2(HX[k], xh), sub2(LX[k], xl));
+                    const f32x2 dy = add2(sub2(HY[k], yh), sub2(LY[k], yl));
+                    const f32x2 dz = add2(sub2(HZ[k], zh), sub2(LZ[k], zl));
+                    const f32x2 r2 = fma2(dz, dz, fma2(dy, dy, fma2(dx, dx, R2MIN)));
+                    float r2a, r2b;
+                    upk2(r2, r2a, r2b);
+                    f32x2 y = pk2(rsqrtf(r2a), rsqrtf(r2b));
+                    y = mul2(y, fma2(mul2(MHALF, r2), mul2(y, y), THREEHALF));  // one Newton step
+                    const f32x2 w = mul2(mul2(ng, mul2(y, y)), y);               // -G m r^-3
+                    FX[k] = fma2(w, dx, FX[k]);
+                    FY[k] = fma2(w, dy, FY[k]);
+                    FZ[k] = fma2(w, dz, FZ[k]);
+                }
             }
         }
 #pragma unroll
         for (int k = 0; k < MS; k++) {
-            sx[k] += (double)fx[k];
-            sy[k] += (double)fy[k];
-            sz[k] += (double)fz[k];
+            float a, b;
+            upk2(FX[k], a, b);
+            sx[k] += (double)(a + b);
+            upk2(FY[k], a, b);
+            sy[k] += (double)(a + b);
+            upk2(FZ[k], a, b);
+            sz[k] += (double)(a + b);
         }
-        for (int q = 0; q < n_heavy; q++) {
-            const Src s = heavy[q];
+        // heavy sources of the tile, in source order, in FP64
+#pragma unroll 1
+        for (int wq = 0; wq < MTILE / 32; wq++) {
+            unsigned bits = heavy_bits[wq];
+            while (bits) {
+                const int b = __ffs(bits) - 1;
+                bits &= bits - 1u;
+                const Src s = src[base + 32 * wq + b];
 #pragma unroll
-            for (int k = 0; k < MS; k++) pair_fast(px[k], py[k], pz[k], s, sx[k], sy[k], sz[k]);
+                for (int k = 0; k < MS; k++) {
+                    const int j = sink_block * SINKS_PER_BLOCK + k * MT + threadIdx.x;
+                    const int jj = j < n ? j : (n > 0 ? n - 1 : 0);
+                    pair_fast(pos[3 * jj], pos[3 * jj + 1], pos[3 * jj + 2], s, sx[k], sy[k], sz[k]);
+                }
+            }
         }
     }
 #pragma unroll
     for (int k = 0; k < MS; k++) {
-        const int j = sj[k];
+        const int j = sink_block * SINKS_PER_BLOCK + k * MT + threadIdx.x;
         if (j >= n) continue;
         if (chunks == 1) {
             if (m[j] < 0.0) continue;
@@ -218,16 +310,49 @@ int launch_force_mixed(const double *pos, const double *m, int n, double G, Forc
 int launch_force_mixed_src(const double *pos, const double *m, int n, const Src *src,
                            const int *n_src, ForceScratch &s, double *acc, cudaStream_t st)
 {
+    if (n <= 0) return 0;
     if (!s.gm_max) ABIE_CUDA(cudaMalloc(&s.gm_max, sizeof(unsigned long long)));
+    // n_src <= n stays on the device; the source arrays are sized for n
+    const int stride = (n + MTILE - 1) / MTILE * MTILE;
+    if ((size_t)NSOA * stride > s.mixed_cap) {
+        if (s.mixed_soa) cudaFree(s.mixed_soa);
+        s.mixed_soa = nullptr;
+        ABIE_CUDA(cudaMalloc(&s.mixed_soa, (size_t)NSOA * stride * sizeof(float)));
+        s.mixed_cap = (size_t)NSOA * stride;
+    }
     ABIE_CUDA(cudaMemsetAsync(s.gm_max, 0, sizeof(unsigned long long), st));
     max_gm_kernel<<<std::max(1, std::min(152, (n + 255) / 256)), 256, 0, st>>>(src, n_src, s.gm_max);
     ABIE_CUDA(cudaGetLastError());
+    mixed_sources_kernel<<<std::max(1, std::min(4 * 152, stride / 256 + 1)), 256, 0, st>>>(
+        src, n_src, s.gm_max, g_heavy_fraction, s.mixed_soa, stride);
+    ABIE_CUDA(cudaGetLastError());
     const int sink_blocks = (n + SINKS_PER_BLOCK - 1) / SINKS_PER_BLOCK;
-    int num_sms = 152;
-    cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, 0);
-    // enough blocks to fill the GPU several times; each chunk at least a tile
-    const int tiles = (n + MTILE - 1) / MTILE;
-    int chunks = std::max(1, std::min(tiles, (8 * num_sms + sink_blocks - 1) / sink_blocks));
+    static int resident = 0;  // blocks the GPU holds at once
+    if (!resident) {
+        int num_sms = 152, bps = 1;
+        cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, force_mixed_kernel, MT, 0);
+        resident = std::max(1, bps) * num_sms;
+    }
+    // source chunks per sink block: the fewest that reach the least
+    // (waves of resident blocks) x (tiles per block), i.e. the shortest
+    // launch by whole waves, with no chunk left without tiles and at most
+    // about four waves of blocks (the partial sums take 24 bytes per sink
+    // and chunk)
+    const int tiles = stride / MTILE;
+    const int max_chunks = std::min(tiles, std::max(1, (4 * resident + sink_blocks - 1) / sink_blocks));
+    int chunks = 1, per = tiles;
+    long long best = -1;
+    for (int c = 1; c <= max_chunks; c++) {
+        const int pc = (tiles + c - 1) / c;
+        if ((tiles + pc - 1) / pc != c) continue;
+        const long long waves = ((long long)sink_blocks * c + resident - 1) / resident;
+        if (best < 0 || waves * pc < best) {
+            best = waves * pc;
+            chunks = c;
+            per = pc;
+        }
+    }
     if (chunks > 1) {
         size_t need = 3ull * (size_t)n * (size_t)chunks;
         if (need > s.partial_cap) {
@@ -237,8 +362,8 @@ int launch_force_mixed_src(const double *pos, const double *m, int n, const Src 
             s.partial_cap = need;
         }
     }
-    force_mixed_kernel<<<sink_blocks * chunks, MT, 0, st>>>(pos, m, n, src, n_src, s.gm_max,
-                                                             g_heavy_fraction, chunks, acc, s.partial);
+    force_mixed_kernel<<<sink_blocks * chunks, MT, 0, st>>>(pos, m, n, src, n_src, s.mixed_soa, stride,
+                                                             chunks, per, acc, s.partial);
     ABIE_CUDA(cudaGetLastError());
     if (chunks > 1) {
         mixed_sum_chunks_kernel<<<(n + 255) / 256, 256, 0, st>>>(s.partial, m, n, chunks, acc);

@@ -23,6 +23,7 @@ namespace abie {
 static constexpr double KEPLER_TOL = 1e-12;  // src/integrator_wisdom_holman.h:7
 static constexpr double TOL_ENERGY = 0.0;    // :11
 static constexpr int KEPLER_MAX_IT = 500;    // :12
+static constexpr int KEPLER_FAST_IT = 40;    // fast form: iterations before the reference's solve takes over
 static constexpr int WH_HEAD_MAX = 4096;
 
 // Quantities the head publishes for the tail.
@@ -90,7 +91,7 @@ __device__ __forceinline__ void stumpff(double psi, double &c2, double &c3)
 
 // src/integrator_wisdom_holman.c:51-132 on one body's Jacobi state.
 // Returns 1 when Newton did not converge within the iteration cap.
-__device__ int kepler_drift(double r0v[3], double v0v[3], double gm, double dt)
+__device__ __noinline__ int kepler_drift(double r0v[3], double v0v[3], double gm, double dt)
 {
     double r0 = norm3(r0v[0], r0v[1], r0v[2]);
     double v0 = norm3(v0v[0], v0v[1], v0v[2]);
@@ -200,6 +201,12 @@ __device__ __forceinline__ void stumpff_series_short(double psi, double &c2, dou
 //    sqrt, and sqrt(gm), 1/gm, 1/sqrt(gm) precomputed (k[0..2]).
 // The converged chi is the same root; the state agrees with the reference
 // form to rounding.  Distances must lie within the FP32 exponent range.
+// A solve that has not converged after KEPLER_FAST_IT iterations (the
+// fast start takes 1.1 on average) is redone from the same state by the
+// reference's own iteration (kepler_drift), and only its failure counts:
+// on the 1,048,582-body swarm the fast iteration alone lost some escaping
+// test particles on hyperbolic orbits (no convergence, then a non-finite
+// state) that the reference's iteration takes in its stride.
 // Comparisons on the bit patterns of doubles, with integer instructions
 // (an FP64 compare holds the FP64 pipe like any FP64 instruction): |x| < t
 // and x > t for a positive threshold t, x < t for a negative one.  NaN
@@ -252,7 +259,8 @@ __device__ int kepler_drift_fast(double r0v[3], double v0v[3], double gm, const 
     }
     double chi = 0.0, r = 0.0, c2 = 0.0, c3 = 0.0, psi = 0.0;
     const double rvs = rv * isqrtgm;
-    for (int it = 0; it < KEPLER_MAX_IT; it++) {
+    bool conv = false;  // NaN never converges
+    for (int it = 0; it < KEPLER_FAST_IT; it++) {
         const double chi2 = chi0 * chi0;
         psi = chi2 * alpha;
         if (gt_pos(psi, 1.e-10) || lt_neg(psi, -1.e-6)) {
@@ -268,10 +276,13 @@ __device__ int kepler_drift_fast(double r0v[3], double v0v[3], double gm, const 
         // sgdt - chi^3 c3 - rvs chi^2 c2 - r0 chi s3, nested
         const double num = fma(-chi0, fma(chi0, fma(chi0, c3, rvs * c2), r0 * s3), sgdt);
         chi = fma(num, rcp_fast(r), chi0);
-        if (abs_lt(chi - chi0, KEPLER_TOL)) break;
+        if (abs_lt(chi - chi0, KEPLER_TOL)) {
+            conv = true;
+            break;
+        }
         chi0 = chi;
     }
-    int failed = !abs_le(chi - chi0, KEPLER_TOL);
+    if (!conv) return kepler_drift(r0v, v0v, gm, dt);
     const double chi2 = chi * chi;
     const double f = fma(-chi2 * ir0, c2, 1.0);
     const double g = fma(-chi2 * chi * isqrtgm, c3, dt);
@@ -287,7 +298,7 @@ __device__ int kepler_drift_fast(double r0v[3], double v0v[3], double gm, const 
         r0v[c] = nr[c];
         v0v[c] = nv[c];
     }
-    return failed;
+    return 0;
 }
 
 // One block.  init != 0: only Jacobi coordinates and accelerations (the

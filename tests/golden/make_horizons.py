@@ -2,7 +2,8 @@
 
 Run in a container where the reference sources exist:
 
-    oracle/build_ref.sh && python tests/golden/make_horizons.py [cfg1|ensemble|cfg3|all]
+    oracle/build_ref.sh && python tests/golden/make_horizons.py \
+        [cfg1|ensemble|ensemble_spread|cfg3|all]
 
 * ``horizon_cfg1.npz``: the 1,009-body planetary system (1 MSun star, 8
   planets, 1,000 test particles; ``ics.planetary_system(seed=1001)``)
@@ -20,6 +21,15 @@ Run in a container where the reference sources exist:
   10,000-yr run.  This is the distribution the reference method itself
   reaches on these systems, against which the GPU forms' distributions are
   judged.
+
+* ``horizon_ensemble_spread.npz``: the same 64 systems over 10,000 yr,
+  rerun twice by the reference library with one coordinate moved by one
+  unit in the last place (coordinate 5k mod 3n, up for k = 1, down for
+  k = 2).  Over 10^4 yr several of these systems are chaotic, so |dE/E|
+  of one system depends on the path: the perturbed runs show how far the
+  reference method's own result moves (system 10 of the set: 1.4e-11 to
+  1.1e-9 over such runs), and together with the unperturbed run they give
+  a 192-sample distribution of the reference method's |dE/E| at 10^4 yr.
 
 * ``horizon_cfg3.npz``: the Wisdom-Holman workload (``ics.test_particle_swarm
   (seed=1003)``, heliocentric: 1 MSun star, 5 planets, 1,048,576 test
@@ -104,17 +114,22 @@ def main_cfg1(out=os.path.join(HERE, "horizon_cfg1.npz")):
 
 
 def ens_run(job):
-    s, t_end = job
+    s, t_end = job[0], job[1]
+    k = job[2] if len(job) > 2 else 0
     kind, R = _checker()
     P, V, M, offs = ics.ensemble(n_systems=1, seed0=10000 + s)
+    if k:
+        P = P.copy()
+        i = (5 * k) % P.size
+        P[i] = np.nextafter(P[i], np.inf if k % 2 else -np.inf)
     r = np.zeros(M.size)
     e0 = R.energy(P, V, M, G)
     t0 = time.time()
     out = R.radau15(P, V, M, r, G, 0.0, t_end)
     wall = time.time() - t0
     e1 = R.energy(out["pos"], out["vel"], M, G)
-    return {"s": s, "t_end": t_end, "kind": kind, "t": out["t"], "de": abs((e1 - e0) / e0),
-            "pos": out["pos"], "vel": out["vel"], "wall": wall}
+    return {"s": s, "t_end": t_end, "k": k, "kind": kind, "t": out["t"],
+            "de": abs((e1 - e0) / e0), "pos": out["pos"], "vel": out["vel"], "wall": wall}
 
 
 def main_ensemble(out=os.path.join(HERE, "horizon_ensemble.npz"), cores=None):
@@ -145,6 +160,29 @@ def main_ensemble(out=os.path.join(HERE, "horizon_ensemble.npz"), cores=None):
         print("ensemble %g yr: |dE/E| median %.2g p90 %.2g p99 %.2g max %.2g; <=1e-12: %d/%d"
               % (T, q[0], q[1], q[2], q[3], int((de[:, h] <= 1e-12).sum()), ENS_SYSTEMS))
     print("%s, %.0f s on %d cores; wrote %s" % (res[0]["kind"], time.time() - t0, cores, out))
+
+
+def main_ensemble_spread(out=os.path.join(HERE, "horizon_ensemble_spread.npz"), cores=None,
+                         perturbations=(1, 2)):
+    _build_checkers()
+    cores = cores or max(1, (os.cpu_count() or 2) - 1)
+    T = ENS_HORIZONS[-1]
+    jobs = [(s, T, k) for k in perturbations for s in range(ENS_SYSTEMS)]
+    t0 = time.time()
+    with mp.get_context("spawn").Pool(cores) as pool:
+        res = pool.map(ens_run, jobs, chunksize=1)
+    de = np.zeros((ENS_SYSTEMS, len(perturbations)))
+    wall = np.zeros_like(de)
+    for r in res:
+        j = perturbations.index(r["k"])
+        de[r["s"], j], wall[r["s"], j] = r["de"], r["wall"]
+    np.savez_compressed(out, kind=np.array(res[0]["kind"]), seed0=np.array([10000]),
+                        horizon=np.array([T]), perturbations=np.array(perturbations), de=de,
+                        wall=wall)
+    q = np.percentile(de, [50, 90, 99, 100])
+    print("ensemble %g yr, one-ulp perturbed runs: |dE/E| median %.2g p90 %.2g p99 %.2g max %.2g"
+          "; %s, %.0f s on %d cores; wrote %s"
+          % (T, q[0], q[1], q[2], q[3], res[0]["kind"], time.time() - t0, cores, out))
 
 
 CFG3_SAMPLE = 1024
@@ -199,5 +237,7 @@ if __name__ == "__main__":
         main_cfg1()
     if what in ("ensemble", "all"):
         main_ensemble()
+    if what in ("ensemble_spread", "all"):
+        main_ensemble_spread()
     if what in ("cfg3", "all"):
         main_cfg3()
