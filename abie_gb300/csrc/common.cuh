@@ -41,11 +41,16 @@ int cuda_fail(cudaError_t e, const char *what);
 // fractional bits: e from the high word of the product of r2's 53-bit
 // significand and m^2, e^2 and e^3 in FP32, F = (1 + k) 2^62, the high word
 // of m^3 F, the high word of its product with the significand of G m, and
-// the result assembled as a double.  Every step truncates, so the result
-// sits at most ~2 ulp below the exact value (a C restatement of these
-// operations over 4 million random r2 in [1e-13, 1e13] and G m in
-// [1e-13, 1e4], with the FP32 seed perturbed by 2^-22: at most 2.02 ulp,
-// mean 0.73).  r2 = 0 (a body and itself) gives a finite value, so the
+// the result assembled as a double, rounded half up on the first dropped
+// bit.  The intermediate steps truncate, but at 2^-60 relative and below,
+// so the result is unbiased and within about half an ulp: a C restatement
+// of r2_int and these operations over 2 million random separations (each
+// component 1e-9 .. 2e4 or zero) and G m in [1e-12, 1e2], with the FP32
+// seed perturbed by up to 2^-22, is at most 0.53 ulp from the exact
+// G m |d|^-3, mean signed error +0.001 ulp (truncating the last step
+// instead: at most 1.03 ulp, every factor 0.5 ulp small on average; from
+// a double r2, as gm_inv_r3 takes it, r2's own rounding adds up to 0.75
+// ulp).  r2 = 0 (a body and itself) gives a finite value, so the
 // caller's 0 * w is exactly zero.  r2 must lie within the FP32 exponent
 // range.  The FP64 pipe is left to the separations, r2 and the sums.
 __device__ __forceinline__ int clamp_exp_f32(int hi_rebased)
@@ -141,7 +146,11 @@ __device__ __forceinline__ double gm_times_inv_r3(unsigned long long Wn, int eW,
     const int lz2 = __clzll((long long)Z);
     const ull Zn = Z << lz2;
     const int be = min(max(eg + eW - lz2 + 66, 1), 2046);
-    return __longlong_as_double((long long)(((ull)be << 52) | ((Zn >> 11) & 0xFFFFFFFFFFFFFull)));
+    // round half up on the first dropped bit: adding it to the bit pattern
+    // carries a full significand into the exponent (truncating instead
+    // would make every factor 0.5 ulp small on average)
+    const ull bits = ((ull)be << 52) | ((Zn >> 11) & 0xFFFFFFFFFFFFFull);
+    return __longlong_as_double((long long)(bits + ((Zn >> 10) & 1ull)));
 }
 
 __device__ __forceinline__ double gm_inv_r3_int(unsigned long long Mr, int Er, double gm)
@@ -195,8 +204,9 @@ __device__ __forceinline__ void r2_int(double dx, double dy, double dz, unsigned
     Er = K + 2 - lz;
 }
 
-// 1/sqrt(x) and 1/x for positive normal x within the single-precision
-// exponent range (2^-126 < x < 2^127), each a few ulp from the exact value
+// 1/sqrt(x) for positive normal x and 1/x for normal x of either sign,
+// |x| within the single-precision exponent range (2^-126 < |x| < 2^127),
+// each a few ulp from the exact value
 // in 3 FP64 instructions.  Same construction as gm_inv_r3: a seed y = m 2^E
 // with a 21-bit significand from the FP32 rsqrtf / rcp, assembled into a
 // double by integer instructions, then one correction with its quadratic
@@ -235,16 +245,21 @@ __device__ __forceinline__ double inv_sqrt_fast(double x)
     return fma(y, k, y);
 }
 
+// 1/x of either sign: the construction runs on |x| and the sign bit is
+// copied back by integer instructions (the Kepler iteration's radius
+// function can turn negative far from its root).
 __device__ __forceinline__ double rcp_fast(double x)
 {
+    const long long sgn = __double_as_longlong(x) & (long long)0x8000000000000000ull;
+    const double ax = __longlong_as_double(__double_as_longlong(x) ^ sgn);
     unsigned long long m;
     int E;
-    const double y = seed_to_f64(__frcp_rn(f64_to_f32_trunc23(x)), m, E);
-    const double e = fma(-x, y, 1.0);
+    const double y = seed_to_f64(__frcp_rn(f64_to_f32_trunc23(ax)), m, E);
+    const double e = fma(-ax, y, 1.0);
     const float ef = signed_trunc23(e);
     const float q = ef * ef * (1.0f + ef);
     const double k = e + f32_to_f64_signed(q);
-    return fma(y, k, y);
+    return __longlong_as_double(__double_as_longlong(fma(y, k, y)) ^ sgn);
 }
 
 // Exact FP64 pair contribution, in the reference's operation order
@@ -265,8 +280,10 @@ __device__ __forceinline__ void pair_exact(double xj, double yj, double zj, cons
 
 // Fast FP64 pair contribution: 6 FP64 instructions (3 separations, 3
 // accumulations); r2 and G m r^-3 are integer arithmetic (r2_int,
-// gm_inv_r3_int; a C restatement of the whole term over 4 million random
-// separations and masses: at most 2.02 ulp from the exact G m r^-3).
+// gm_inv_r3_int; a C restatement of the whole term over 2 million random
+// separations (1e-9 .. 2e4 per component, some zero), masses and seeds
+// perturbed by 2^-22: at most 0.53 ulp from the exact G m r^-3, mean
+// signed error +0.001 ulp).
 __device__ __forceinline__ void pair_fast(double xj, double yj, double zj, const Src &s,
                                           double &ax, double &ay, double &az)
 {

@@ -23,7 +23,6 @@ namespace abie {
 static constexpr double KEPLER_TOL = 1e-12;  // src/integrator_wisdom_holman.h:7
 static constexpr double TOL_ENERGY = 0.0;    // :11
 static constexpr int KEPLER_MAX_IT = 500;    // :12
-static constexpr int KEPLER_FAST_IT = 40;    // fast form: iterations before the reference's solve takes over
 static constexpr int WH_HEAD_MAX = 4096;
 
 // Quantities the head publishes for the tail.
@@ -191,8 +190,8 @@ __device__ __forceinline__ void stumpff_series_short(double psi, double &c2, dou
 // Fast form of kepler_drift: the same universal-variable Newton iteration,
 // convergence test (|dchi| < 1e-12) and f, g functions, with
 //  * a starting value from the Taylor series of chi(t) (dchi/dt = sqrt(gm)/r)
-//    to third order when the step covers a small arc (psi_0 < 0.1), so one
-//    or two Newton steps suffice instead of three or four;
+//    to third order when the step covers a short arc (below), so one or
+//    two Newton steps suffice instead of three or four on bound orbits;
 //  * the series Stumpff functions for |psi| <= 0.5 where the reference uses
 //    the closed forms (five terms each up to |psi| = 0.01, nine beyond; its
 //    constants 1/2, 1/6 in -1e-6 <= psi <= 1e-10 and the closed forms
@@ -201,12 +200,20 @@ __device__ __forceinline__ void stumpff_series_short(double psi, double &c2, dou
 //    sqrt, and sqrt(gm), 1/gm, 1/sqrt(gm) precomputed (k[0..2]).
 // The converged chi is the same root; the state agrees with the reference
 // form to rounding.  Distances must lie within the FP32 exponent range.
-// A solve that has not converged after KEPLER_FAST_IT iterations (the
-// fast start takes 1.1 on average) is redone from the same state by the
-// reference's own iteration (kepler_drift), and only its failure counts:
-// on the 1,048,582-body swarm the fast iteration alone lost some escaping
-// test particles on hyperbolic orbits (no convergence, then a non-finite
-// state) that the reference's iteration takes in its stride.
+// A solve that has not converged within the reference's iteration cap is
+// redone from the same state by the reference's own iteration
+// (kepler_drift), and only its failure counts.
+// The start: on a short arc (|w1^2 alpha| < 0.1, w1 = sqrt(gm) dt / r0)
+// the Taylor series of chi(t) to third order for any conic -- the
+// derivatives of chi come from r(t) and do not depend on the sign of
+// alpha -- so an escaping test particle on a hyperbolic orbit needs one or
+// two Newton steps where the reference's logarithmic start takes 27 on
+// average and up to 200 (a C restatement of both iterations over 200,000
+// hyperbolic states, r0 10 .. 3e4 au: the same roots to 1e-11, 1.04
+// iterations on average).  rcp_fast takes either sign: the radius function
+// r(chi) can turn negative far from the root, where a reciprocal for
+// positive numbers only sent the iteration to NaN (escaping particles of
+// the 1,048,582-body swarm did, some hundred over 2 x 10^5 steps).
 // Comparisons on the bit patterns of doubles, with integer instructions
 // (an FP64 compare holds the FP64 pipe like any FP64 instruction): |x| < t
 // and x > t for a positive threshold t, x < t for a negative one.  NaN
@@ -235,7 +242,7 @@ __device__ int kepler_drift_fast(double r0v[3], double v0v[3], double gm, const 
     const double rv = fma(r0v[2], v0v[2], fma(r0v[1], v0v[1], r0v[0] * v0v[0]));
     double chi0;
     const double w1 = sgdt * ir0;  // first-order arc
-    if (gt_pos(alpha, 0.0) && abs_lt(w1 * w1 * alpha, 0.1)) {
+    if (abs_lt(w1 * w1 * alpha, 0.1)) {  // a short arc of any conic
         const double ir02 = ir0 * ir0;
         const double u = rv * ir02;                       // rdot / r
         const double w2 = -0.5 * u * dt;                  // second-order factor
@@ -260,7 +267,7 @@ __device__ int kepler_drift_fast(double r0v[3], double v0v[3], double gm, const 
     double chi = 0.0, r = 0.0, c2 = 0.0, c3 = 0.0, psi = 0.0;
     const double rvs = rv * isqrtgm;
     bool conv = false;  // NaN never converges
-    for (int it = 0; it < KEPLER_FAST_IT; it++) {
+    for (int it = 0; it < KEPLER_MAX_IT; it++) {
         const double chi2 = chi0 * chi0;
         psi = chi2 * alpha;
         if (gt_pos(psi, 1.e-10) || lt_neg(psi, -1.e-6)) {
