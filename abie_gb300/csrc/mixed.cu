@@ -16,14 +16,19 @@
 // (add/sub/mul/fma .f32x2: two single-precision operations per lane and
 // instruction): one instruction serves a sink against two sources, so a
 // pair term costs 12 issued instructions instead of 24.  Each packed
-// operation rounds exactly as its scalar counterpart.
+// operation rounds exactly as its scalar counterpart.  The FMA pipe still
+// does one lane operation per cycle per lane, so the kernel is bound by
+// that pipe (73 % busy on the 16,385-body disk) rather than by issue.
 //
 // A first pass writes the sources once as anchored two-float coordinates
 // and -G m (struct of arrays, +0 marking a heavy source, -0 the padding
 // after the last source); the force kernel works in blocks of SINKS x TILE:
-// every thread owns 4 sinks and reads each source once from shared memory.
+// every thread owns MS sinks and reads each source once from shared memory.
 // Sources split into chunks across blocks; chunk partial sums are added in
-// chunk order by a second pass (deterministic).
+// chunk order by a second pass (deterministic).  Block shape: a sweep on
+// the disk (per force call) gave 984 Gint/s for 256 threads x 2 sinks at
+// 2 blocks per SM, 966 for 128 x 2 at 5, 961 for 128 x 2 at 4 and 922 for
+// 128 x 4 at 3.
 #include <algorithm>
 
 #include "mixed.cuh"
@@ -38,13 +43,13 @@ double mixed_heavy_fraction() { return g_heavy_fraction; }
 namespace {
 
 #ifndef ABIE_MIXED_MT
-#define ABIE_MIXED_MT 128
+#define ABIE_MIXED_MT 256
 #endif
 #ifndef ABIE_MIXED_MS
-#define ABIE_MIXED_MS 4
+#define ABIE_MIXED_MS 2
 #endif
 #ifndef ABIE_MIXED_MINB
-#define ABIE_MIXED_MINB 3
+#define ABIE_MIXED_MINB 2
 #endif
 constexpr int MT = ABIE_MIXED_MT;  // threads per block
 constexpr int MS = ABIE_MIXED_MS;  // sinks per thread

@@ -90,7 +90,7 @@ __device__ __forceinline__ void stumpff(double psi, double &c2, double &c3)
 
 // src/integrator_wisdom_holman.c:51-132 on one body's Jacobi state.
 // Returns 1 when Newton did not converge within the iteration cap.
-__device__ __noinline__ int kepler_drift(double r0v[3], double v0v[3], double gm, double dt)
+__device__ int kepler_drift(double r0v[3], double v0v[3], double gm, double dt)
 {
     double r0 = norm3(r0v[0], r0v[1], r0v[2]);
     double v0 = norm3(v0v[0], v0v[1], v0v[2]);

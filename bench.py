@@ -835,6 +835,10 @@ def run_horizons(args):
              "failed_systems": int((res["status"] != 0).sum())}
         r.update(_de_stats(de, ref))
         r["per_system_abs_dE_over_E_first_64"] = [float(x) for x in de[:64]]
+        worst = np.argsort(-de)[:8]
+        r["worst_systems"] = [{"system": int(s), "abs_dE_over_E": float(de[s]),
+                               "steps": int(res["steps"][s]),
+                               "bodies": int(offs[s + 1] - offs[s])} for s in worst]
         r["per_system_steps_first_64"] = [int(x) for x in res["steps"][:64]]
         return r
 
