@@ -200,11 +200,10 @@ __device__ __forceinline__ void stumpff_series_short(double psi, double &c2, dou
 //    sqrt, and sqrt(gm), 1/gm, 1/sqrt(gm) precomputed (k[0..2]).
 // The converged chi is the same root; the state agrees with the reference
 // form to rounding.  Distances must lie within the FP32 exponent range.
-// A solve that has not converged within the reference's iteration cap is
-// redone from the same state by the reference's own iteration
-// (kepler_drift), and only its failure counts.
-// The start: on a short arc (|w1^2 alpha| < 0.1, w1 = sqrt(gm) dt / r0)
-// the Taylor series of chi(t) to third order for any conic -- the
+// A solve counts as failed as in the reference (its last two iterates
+// still apart after the iteration cap).  The start: on a short arc
+// (|w1^2 alpha| < 0.1, w1 = sqrt(gm) dt / r0) the Taylor series of chi(t)
+// to third order for any conic -- the
 // derivatives of chi come from r(t) and do not depend on the sign of
 // alpha -- so an escaping test particle on a hyperbolic orbit needs one or
 // two Newton steps where the reference's logarithmic start takes 27 on
@@ -266,7 +265,6 @@ __device__ int kepler_drift_fast(double r0v[3], double v0v[3], double gm, const 
     }
     double chi = 0.0, r = 0.0, c2 = 0.0, c3 = 0.0, psi = 0.0;
     const double rvs = rv * isqrtgm;
-    bool conv = false;  // NaN never converges
     for (int it = 0; it < KEPLER_MAX_IT; it++) {
         const double chi2 = chi0 * chi0;
         psi = chi2 * alpha;
@@ -283,13 +281,10 @@ __device__ int kepler_drift_fast(double r0v[3], double v0v[3], double gm, const 
         // sgdt - chi^3 c3 - rvs chi^2 c2 - r0 chi s3, nested
         const double num = fma(-chi0, fma(chi0, fma(chi0, c3, rvs * c2), r0 * s3), sgdt);
         chi = fma(num, rcp_fast(r), chi0);
-        if (abs_lt(chi - chi0, KEPLER_TOL)) {
-            conv = true;
-            break;
-        }
+        if (abs_lt(chi - chi0, KEPLER_TOL)) break;
         chi0 = chi;
     }
-    if (!conv) return kepler_drift(r0v, v0v, gm, dt);
+    const int failed = !abs_le(chi - chi0, KEPLER_TOL);
     const double chi2 = chi * chi;
     const double f = fma(-chi2 * ir0, c2, 1.0);
     const double g = fma(-chi2 * chi * isqrtgm, c3, dt);
@@ -305,7 +300,7 @@ __device__ int kepler_drift_fast(double r0v[3], double v0v[3], double gm, const 
         r0v[c] = nr[c];
         v0v[c] = nv[c];
     }
-    return 0;
+    return failed;
 }
 
 // One block.  init != 0: only Jacobi coordinates and accelerations (the
