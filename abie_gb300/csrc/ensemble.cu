@@ -290,7 +290,8 @@ static void mkdirs_for(const std::string &file)
         if (file[i] == '/') mkdir(file.substr(0, i).c_str(), 0755);
 }
 
-static std::string tune_key(int mode, int ns, const long long *offsets, const double *m, double span)
+static std::string tune_key(int mode, bool net, int ns, const long long *offsets, const double *m,
+                            double span)
 {
     unsigned long long h = 1469598103934665603ull;  // FNV-1a over body counts and masses
     auto mix = [&](unsigned long long v) {
@@ -308,8 +309,8 @@ static std::string tune_key(int mode, int ns, const long long *offsets, const do
     cudaDeviceProp p;
     cudaGetDeviceProperties(&p, g_sim.dev);
     char key[512];
-    snprintf(key, sizeof key, "%s|%s|mode%d|ns%d|h%016llx|span%.3g", p.name, ENS_BUILD, mode, ns, h,
-             span);
+    snprintf(key, sizeof key, "%s|%s|mode%d%s|ns%d|h%016llx|span%.3g", p.name, ENS_BUILD, mode,
+             net ? "+net" : "", ns, h, span);
     for (char *c = key; *c; c++)
         if (*c == '\t' || *c == '\n') *c = ' ';
     return key;
@@ -461,15 +462,17 @@ int ensemble_run(double *pos, double *vel, const double *m, const long long *off
     if (rc) return rc;
 
     // the share of four-warp groups: the debug override, the tuner (not
-    // while learning: trials would append training samples), or the default
+    // while collecting training samples: trials would append some; the
+    // network's inference only reads its weights), or the default
     EnsTuneInfo info;
     std::vector<unsigned char> cls;
     const double span = t_end - t0;
+    const bool collecting = learn_io && learn_io->samples;
     if (g_heavy_div > 0) {
         info.heavy_div = g_heavy_div;
         info.from_cache = 2;
-    } else if (!learning && tuner_on() && span > 0.0) {
-        const std::string key = tune_key(mode, ns, offsets, m, span);
+    } else if (!collecting && tuner_on() && span > 0.0) {
+        const std::string key = tune_key(mode, mlp != nullptr, ns, offsets, m, span);
         info.heavy_div = tune_lookup(key);
         if (info.heavy_div > 0) {
             info.from_cache = 1;
