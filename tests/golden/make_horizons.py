@@ -19,8 +19,8 @@ Run in a container where the reference sources exist:
   yr (three runs from t = 0 each), one process per host core.  Per system:
   |dE/E| at each horizon, the model time, and the final state of the
   10,000-yr run.  This is the distribution the reference method itself
-  reaches on these systems, against which the GPU forms' distributions are
-  judged.
+  reaches on these systems, which the GPU forms' distributions are
+  compared with.
 
 * ``horizon_ensemble_spread.npz``: the same 64 systems over 10,000 yr,
   rerun twice by the reference library with one coordinate moved by one
