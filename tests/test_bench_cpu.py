@@ -56,3 +56,18 @@ def test_clock_record_parsing(tmp_path):
     assert rec["sm_mhz"] == 2040.0 and rec["sm_max_mhz"] == 2070.0
     assert rec["reasons"] == ["hw_thermal_slowdown", "sw_power_cap"]
     assert rec["samples"] == 3 and rec["power_w_max"] == 262.0
+
+
+def test_energy_error_statistics():
+    """The long-horizon runs' |dE/E| summary: percentiles, the count within
+    1e-12, and against a reference distribution the systems within 10x of
+    the reference's value for the same system."""
+    de = np.array([1e-13, 5e-13, 2e-12, 1e-9])
+    ref = np.array([2e-13, 1e-13, 1e-12, 1e-11])
+    out = bench._de_stats(de, ref)
+    assert out["systems"] == 4 and out["systems_at_or_below_1e-12"] == 2
+    assert out["abs_dE_over_E_p50_p90_p99_max"][3] == 1e-9
+    assert out["reference_method_at_or_below_1e-12"] == 3
+    assert out["systems_within_10x_of_reference"] == 3   # 1e-9 > 10 x 1e-11
+    q = out["reference_method_p50_p90_p99_max"]
+    assert q[0] == np.percentile(ref, 50) and q[3] == 1e-11
