@@ -332,13 +332,12 @@ int launch_force_mixed_src(const double *pos, const double *m, int n, const Src 
         src, n_src, s.gm_max, g_heavy_fraction, s.mixed_soa, stride);
     ABIE_CUDA(cudaGetLastError());
     const int sink_blocks = (n + SINKS_PER_BLOCK - 1) / SINKS_PER_BLOCK;
-    static int resident = 0;  // blocks the GPU holds at once
-    if (!resident) {
-        int num_sms = 152, bps = 1;
-        cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, force_mixed_kernel, MT, 0);
-        resident = std::max(1, bps) * num_sms;
-    }
+    // blocks the current GPU holds at once (host-side queries, no sync)
+    int dev = 0, num_sms = 152, bps = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, force_mixed_kernel, MT, 0);
+    const int resident = std::max(1, bps) * num_sms;
     // source chunks per sink block: the fewest that reach the least
     // (waves of resident blocks) x (tiles per block), i.e. the shortest
     // launch by whole waves, with no chunk left without tiles and at most
