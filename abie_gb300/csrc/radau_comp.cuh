@@ -89,10 +89,14 @@ __device__ __forceinline__ double e_pred_pos(const Comp &c, int row, double s, d
     u = fma(g[1], w[1], u);
     u = fma(g[0], w[0], u);
     // the step's displacement first, then one rounding at the position's
-    // scale, as the reference's Horner form adds it (two FMAs into y0
-    // round twice there; over 10^4 yr that doubled the median energy error
-    // of the fast form in a host emulation, with this order 1.5x)
-    return c.y0 + fma(hh, c.F1 + u, ds * c.dy0);
+    // scale, as the reference's Horner form adds it: two FMAs into y0
+    // round twice there, which over 10^4 yr doubled the fast form's median
+    // energy error in a host emulation of its arithmetic (64 systems:
+    // 9.9e-13 against the reference method's 3.1-4.4e-13; this order
+    // 5.0e-13, 46 of 64 within 1e-12 against 43-45).  The part without g
+    // is formed off the chain that waits for u.
+    const double p = fma(ds, c.dy0, hh * c.F1);
+    return c.y0 + fma(hh, u, p);
 }
 
 // Predicted velocity at spacing 1 (the advance).
