@@ -122,9 +122,12 @@ class Oracle:
         return acc
 
     def radau15(self, pos, vel, m, r, G, t, t_end, ce_dist=0.0, max_ce=1, max_coll=1,
-                events=True, C=0.0, ext=None):
+                events=True, C=0.0, ext=None, fastform=False):
         """src/integrator_gauss_radau15.c:221-380; ``ext`` (3N) is added to
-        every force call, as set_additional_forces does."""
+        every force call, as set_additional_forces does.  ``fastform``: the
+        GPU fast form's arithmetic instead of the reference's operations
+        (orc_set_fastform; for the long-horizon accuracy study, Newtonian
+        forces only)."""
         pos, vel, m, r = (_f64(pos).copy(), _f64(vel).copy(), _f64(m), _f64(r))
         ext = None if ext is None else _f64(ext).copy()
         ev = _Events()
@@ -138,6 +141,7 @@ class Oracle:
         t_out = ctypes.c_double(t)
         self.lib.orc_set_pn(ctypes.c_double(C))
         self.lib.orc_set_ext(_ptr(ext) if ext is not None else None)
+        self.lib.orc_set_fastform(ctypes.c_int(1 if fastform else 0))
         try:
             flag = self.lib.orc_radau15(_ptr(pos), _ptr(vel), _ptr(m), _ptr(r),
                                         ctypes.c_size_t(m.size), ctypes.c_double(G),
@@ -147,6 +151,7 @@ class Oracle:
         finally:
             self.lib.orc_set_pn(ctypes.c_double(0.0))
             self.lib.orc_set_ext(None)
+            self.lib.orc_set_fastform(ctypes.c_int(0))
         return {"pos": pos, "vel": vel, "t": t_out.value, "flag": flag,
                 "stats": st.as_dict(), "n_ce": ev.n_ce, "n_coll": ev.n_coll,
                 "buf_ce": buf_ce, "buf_coll": buf_coll}

@@ -269,6 +269,41 @@ void orc_post_newtonian(const double *pos, const double *vel, size_t n, double G
     }
 }
 
+/* The GPU fast form's arithmetic in orc_radau15, for the long-horizon
+ * accuracy study only (not bit-identical to the device: the device takes
+ * G m r^-3 by integer arithmetic within 0.53 ulp and its own single-
+ * precision log2 / exp2).  Five changes from the reference's operations:
+ * each pair term's G m r^-3 formed once and the sums by FMA; the
+ * corrector's new g coefficient from the expanded recurrence (one FMA per
+ * term); positions predicted from g with the tabulated weights, the
+ * displacement formed first and added to y0 once; the step-size seventh
+ * root in single precision; each step started from g consistent with the
+ * refined guess.  Newtonian forces only. */
+static int g_orc_fast = 0;
+void orc_set_fastform(int on) { g_orc_fast = on; }
+
+static void orc_force_fastform(const double *pos, size_t n, double G, const double *m, double *acc)
+{
+    for (size_t j = 0; j < n; j++) {
+        if (m[j] < 0.0) continue;
+        const double xj = pos[3 * j], yj = pos[3 * j + 1], zj = pos[3 * j + 2];
+        double ax = 0.0, ay = 0.0, az = 0.0;
+        for (size_t k = 0; k < n; k++) {
+            if (k == j || m[k] <= 0.0) continue;
+            const double gm = G * m[k];
+            const double dx = xj - pos[3 * k], dy = yj - pos[3 * k + 1], dz = zj - pos[3 * k + 2];
+            const double r2 = dx * dx + dy * dy + dz * dz;
+            const double w = gm / (sqrt(r2) * r2);
+            ax = fma(-w, dx, ax);
+            ay = fma(-w, dy, ay);
+            az = fma(-w, dz, az);
+        }
+        acc[3 * j] = ax;
+        acc[3 * j + 1] = ay;
+        acc[3 * j + 2] = az;
+    }
+}
+
 /* src/common.c:82-114: Newton, then the post-Newtonian terms when C > 0,
  * then the external accelerations when set (:107-112, added component by
  * component after the other terms). */
@@ -280,7 +315,8 @@ static void force_counted_v(const double *y, const double *dy, size_t n, double 
     /* sinks with negative mass keep a zero acceleration (the reference leaves
      * their entries of freshly malloc'd buffers untouched) */
     memset(acc, 0, 3 * n * sizeof(double));
-    orc_force(y, n, G, m, acc, 0, n);
+    if (g_orc_fast) orc_force_fastform(y, n, G, m, acc);
+    else orc_force(y, n, G, m, acc, 0, n);
     if (g_orc_C > 0.0) orc_post_newtonian(y, dy, n, G, g_orc_C, m, acc);
     if (g_orc_ext)
         for (size_t i = 0; i < 3 * n; i++) acc[i] += g_orc_ext[i];
@@ -289,6 +325,7 @@ static void force_counted_v(const double *y, const double *dy, size_t n, double 
 
 /* Speed of light for the oracle's Radau15 (0: no post-Newtonian terms). */
 void orc_set_pn(double C) { g_orc_C = C; }
+
 
 /* External accelerations (3N, kept by pointer) added to every force call of
  * the oracle's Radau15, like src/common.c:364-380 with :107-112; NULL: none. */
@@ -363,6 +400,59 @@ static void update_g(double *const F[8], int ih, size_t dim, double *g[7])
     }
 }
 
+/* The fast form's pieces (orc_set_fastform): the new g from the expanded
+ * recurrence, (F - F1) rsp[ih][0] - sum_l g_l rsp[ih][l+1]; positions from
+ * g with the tabulated weights W_j(s) (row ih of a substep, row 8 for the
+ * step's end); the velocity at the step's end likewise; g = C^-1 b. */
+static const double RSP[8][8] = ABIE_RADAU_RSP_INIT;
+static const double WG[9][7] = ABIE_RADAU_WG_INIT;
+static const double VG[7] = ABIE_RADAU_VG_INIT;
+
+static void update_g_fast(double *const F[8], int ih, size_t dim, double *g[7])
+{
+    if (ih == 0) return;
+    for (size_t i = 0; i < dim; i++) {
+        double v = (F[ih][i] - F[0][i]) * RSP[ih][0];
+        for (int l = 1; l < ih; l++) v = fma(-g[l - 1][i], RSP[ih][l], v);
+        g[ih - 1][i] = v;
+    }
+}
+
+static void predict_pos_fast(const double *y1, const double *dy1, const double *F1, int row,
+                             double s, double *const g[7], size_t dim, double dt, double *y)
+{
+    const double ds = dt * s, hh = 0.5 * ds * ds;
+    for (size_t i = 0; i < dim; i++) {
+        if (row == 0) {
+            y[i] = y1[i];
+            continue;
+        }
+        double u = g[6][i] * WG[row][6];
+        for (int j = 5; j >= 0; j--) u = fma(g[j][i], WG[row][j], u);
+        y[i] = y1[i] + fma(hh, u, fma(ds, dy1[i], hh * F1[i]));
+    }
+}
+
+static void predict_vel_end_fast(const double *dy1, const double *F1, double *const g[7],
+                                 size_t dim, double dt, double *dy)
+{
+    for (size_t i = 0; i < dim; i++) {
+        double u = g[6][i] * VG[6];
+        for (int j = 5; j >= 0; j--) u = fma(g[j][i], VG[j], u);
+        dy[i] = fma(dt, F1[i] + u, dy1[i]);
+    }
+}
+
+static void consistent_g(double *const b[7], size_t dim, double *g[7])
+{
+    for (size_t i = 0; i < dim; i++)
+        for (int k = 6; k >= 0; k--) {
+            double v = b[k][i];
+            for (int j = k + 1; j < 7; j++) v -= CS[j][k] * g[j][i];
+            g[k][i] = v;
+        }
+}
+
 /* :123-175.  b_k = sum_{j>=k} cs[j][k] g_j for k < ih, added left to right
  * starting from j = k (the reference writes b[0] starting with cs[0][0]*g0). */
 static void update_b(double *const g[7], int ih, size_t dim, double *b[7])
@@ -425,10 +515,12 @@ int orc_radau15(double *pos, double *vel, const double *m, const double *r,
             iters++;
             for (int k = 0; k < 8; k++) memset(F[k], 0, dim * sizeof(double));
             for (int ih = 0; ih < 8; ih++) {
-                predict_pos(y0, dy0, ddy0, HS[ih], b, dim, h, y);
+                if (g_orc_fast) predict_pos_fast(y0, dy0, ddy0, ih, HS[ih], g, dim, h, y);
+                else predict_pos(y0, dy0, ddy0, HS[ih], b, dim, h, y);
                 predict_vel(dy0, ddy0, HS[ih], b, dim, h, dy);
                 force_counted_v(y, dy, n, G, m, F[ih], st);
-                update_g(F, ih, dim, g);
+                if (g_orc_fast) update_g_fast(F, ih, dim, g);
+                else update_g(F, ih, dim, g);
                 update_b(g, ih, dim, b);
             }
             for (size_t i = 0; i < dim; i++) db6[i] = b[6][i] - b0[6][i];
@@ -440,12 +532,27 @@ int orc_radau15(double *pos, double *vel, const double *m, const double *r,
             st->attempts++;
             st->iter_hist[iters]++;
         }
-        predict_pos(y0, dy0, ddy0, 1., b, dim, h, y);        /* :309 */
-        predict_vel(dy0, ddy0, 1., b, dim, h, dy);
+        if (g_orc_fast) {
+            predict_pos_fast(y0, dy0, ddy0, 8, 1., g, dim, h, y);
+            predict_vel_end_fast(dy0, ddy0, g, dim, h, dy);
+        } else {
+            predict_pos(y0, dy0, ddy0, 1., b, dim, h, y);    /* :309 */
+            predict_vel(dy0, ddy0, 1., b, dim, h, dy);
+        }
         force_counted_v(y, dy, n, G, m, ddy, st);
         double estim_b6 = max_abs(b[6], dim) / max_abs(ddy, dim);
         double err = pow(estim_b6 / EPSB, EXPONENT);
         double dtreq = h / err;
+        double rq = dtreq / h;
+        if (g_orc_fast) {  /* the seventh root in single precision */
+            const double x = estim_b6 * (1.0 / EPSB);
+            if (isfinite(x) && x >= 0) {
+                const float l7 = log2f((float)x) * (1.0f / 7.0f);
+                err = (double)exp2f(l7);
+                rq = (double)exp2f(-l7);
+                dtreq = h * rq;
+            }
+        }
         if (err <= 1 || rejects_in_row > 100) {             /* :320 */
             t += h;
             if (t_out) *t_out = t;
@@ -459,14 +566,15 @@ int orc_radau15(double *pos, double *vel, const double *m, const double *r,
             memcpy(dy0, dy, dim * sizeof(double));
             memcpy(ddy0, ddy, dim * sizeof(double));
             for (int k = 0; k < 7; k++) memcpy(b0[k], b[k], dim * sizeof(double));
-            refine_b(b, dtreq / h, E, dim);
+            refine_b(b, g_orc_fast ? rq : dtreq / h, E, dim);
+            if (g_orc_fast) consistent_g(b, dim, g);
             if (ev) flag = orc_check_events(y, r, n, t, ev);
             if (flag > 0) break;
         } else {
             rejects_in_row += 1;
             if (st) st->rejects++;
         }
-        if (dtreq / h > 1.0 / FAC) h /= FAC;                 /* :349 */
+        if ((g_orc_fast ? rq : dtreq / h) > 1.0 / FAC) h /= FAC;  /* :349 */
         else if (dtreq < 1.e-12) h *= FAC;
         else h = dtreq;
         if (h < H_MIN) h = H_MIN;

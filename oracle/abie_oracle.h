@@ -76,6 +76,11 @@ void orc_post_newtonian(const double *pos, const double *vel, size_t n, double G
                         const double *m, double *acc);
 /* Speed of light used by orc_radau15's accelerations (0: Newtonian only). */
 void orc_set_pn(double C);
+/* 1: orc_radau15 with the GPU fast form's arithmetic (FMA pair sums, the
+ * expanded g recurrence, positions predicted from g, a single-precision
+ * step-size root, g consistent with each step's guess), for the
+ * long-horizon accuracy study; 0 (default): the reference's operations. */
+void orc_set_fastform(int on);
 /* External accelerations (3N doubles, kept by pointer; NULL: none) added to
  * every force call of orc_radau15 (src/common.c:107-112). */
 void orc_set_ext(const double *ext);

@@ -3,7 +3,7 @@
 Run in a container where the reference sources exist:
 
     oracle/build_ref.sh && python tests/golden/make_horizons.py \
-        [cfg1|ensemble|ensemble_spread|cfg3|all]
+        [cfg1|ensemble|ensemble_spread|ensemble_fastform|cfg3|all]
 
 * ``horizon_cfg1.npz``: the 1,009-body planetary system (1 MSun star, 8
   planets, 1,000 test particles; ``ics.planetary_system(seed=1001)``)
@@ -30,6 +30,14 @@ Run in a container where the reference sources exist:
   reference method's own result moves (system 10 of the set: 1.4e-11 to
   1.1e-9 over such runs), and together with the unperturbed run they give
   a 192-sample distribution of the reference method's |dE/E| at 10^4 yr.
+
+* ``horizon_ensemble_fastform.npz``: the same 64 systems over 10,000 yr
+  by the oracle with the GPU fast form's arithmetic (``Oracle.radau15(...,
+  fastform=True)``: FMA pair sums, the expanded g recurrence, positions
+  predicted from g with one rounding at the position's scale, the
+  single-precision step-size root, g consistent with each step's guess),
+  so that the fast form's energy error over 10^4 yr can be set beside the
+  reference method's on the host.
 
 * ``horizon_cfg3.npz``: the Wisdom-Holman workload (``ics.test_particle_swarm
   (seed=1003)``, heliocentric: 1 MSun star, 5 planets, 1,048,576 test
@@ -185,6 +193,39 @@ def main_ensemble_spread(out=os.path.join(HERE, "horizon_ensemble_spread.npz"), 
           % (T, q[0], q[1], q[2], q[3], res[0]["kind"], time.time() - t0, cores, out))
 
 
+def ens_fastform_run(s):
+    import oracle
+    O = oracle.Oracle()
+    P, V, M, offs = ics.ensemble(n_systems=1, seed0=10000 + s)
+    T = ENS_HORIZONS[-1]
+    e0 = O.energy(P, V, M, G)
+    t0 = time.time()
+    out = O.radau15(P, V, M, np.zeros(M.size), G, 0.0, T, fastform=True)
+    wall = time.time() - t0
+    e1 = O.energy(out["pos"], out["vel"], M, G)
+    return {"s": s, "de": abs((e1 - e0) / e0), "wall": wall, "t": out["t"]}
+
+
+def main_ensemble_fastform(out=os.path.join(HERE, "horizon_ensemble_fastform.npz"), cores=None):
+    _build_checkers()
+    cores = cores or max(1, (os.cpu_count() or 2) - 1)
+    t0 = time.time()
+    with mp.get_context("spawn").Pool(cores) as pool:
+        res = pool.map(ens_fastform_run, range(ENS_SYSTEMS), chunksize=1)
+    de = np.zeros(ENS_SYSTEMS)
+    wall = np.zeros(ENS_SYSTEMS)
+    tt = np.zeros(ENS_SYSTEMS)
+    for r in res:
+        de[r["s"]], wall[r["s"]], tt[r["s"]] = r["de"], r["wall"], r["t"]
+    np.savez_compressed(out, kind=np.array("oracle-fastform"), seed0=np.array([10000]),
+                        horizon=np.array([ENS_HORIZONS[-1]]), de=de, t=tt, wall=wall)
+    q = np.percentile(de, [50, 90, 99, 100])
+    print("ensemble %g yr, fast-form arithmetic: |dE/E| median %.2g p90 %.2g p99 %.2g max %.2g"
+          "; <=1e-12: %d/%d; %.0f s on %d cores; wrote %s"
+          % (ENS_HORIZONS[-1], q[0], q[1], q[2], q[3], int((de <= 1e-12).sum()), ENS_SYSTEMS,
+             time.time() - t0, cores, out))
+
+
 CFG3_SAMPLE = 1024
 CFG3_SEED = 5
 
@@ -239,5 +280,7 @@ if __name__ == "__main__":
         main_ensemble()
     if what in ("ensemble_spread", "all"):
         main_ensemble_spread()
+    if what in ("ensemble_fastform", "all"):
+        main_ensemble_fastform()
     if what in ("cfg3", "all"):
         main_cfg3()

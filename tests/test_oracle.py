@@ -142,3 +142,34 @@ def test_external_accelerations_golden(oracle):
     # without the vector the run differs (the term is live)
     plain = oracle.radau15(p, v, m, r, G, t0, t1)
     assert not np.array_equal(plain["pos"], gold["ext_gr_pos"])
+
+
+def test_fastform_emulation_is_the_same_integrator(oracle):
+    """The oracle's emulation of the GPU fast form's arithmetic (used for the
+    long-horizon energy study) integrates a planetary system to the same
+    trajectory as the reference's operations: states carried to a common
+    time agree to 1e-10, energy to the reference's level."""
+    from abie_gb300 import ics
+    G = ics.G_SOLAR
+    P, V, M, offs = ics.ensemble(n_systems=1, seed0=10003)
+    r = np.zeros(M.size)
+    ref = oracle.radau15(P, V, M, r, G, 0.0, 1.0)
+    fast = oracle.radau15(P, V, M, r, G, 0.0, 1.0, fastform=True)
+    assert abs(fast["t"] - ref["t"]) <= 1e-6 * ref["t"]
+    # carry the emulation's state to the reference's final time (RK4 substeps)
+    x, v = fast["pos"].copy(), fast["vel"].copy()
+    sub = 64
+    hs = (ref["t"] - fast["t"]) / sub
+    for _ in range(sub):
+        a1 = oracle.force(x, M, G)
+        a2 = oracle.force(x + 0.5 * hs * v, M, G)
+        a3 = oracle.force(x + 0.5 * hs * v + 0.25 * hs * hs * a1, M, G)
+        a4 = oracle.force(x + hs * v + 0.5 * hs * hs * a2, M, G)
+        x, v = (x + hs * v + hs * hs / 6.0 * (a1 + a2 + a3),
+                v + hs / 6.0 * (a1 + 2.0 * a2 + 2.0 * a3 + a4))
+    d = np.linalg.norm((x - ref["pos"]).reshape(-1, 3), axis=1)
+    n = np.linalg.norm(ref["pos"].reshape(-1, 3), axis=1)
+    ok = n > 0
+    assert np.max(d[ok] / n[ok]) <= 1e-10
+    e0 = oracle.energy(P, V, M, G)
+    assert abs((oracle.energy(fast["pos"], fast["vel"], M, G) - e0) / e0) <= 1e-13
