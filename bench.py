@@ -850,6 +850,8 @@ def run_horizons(args):
     # chaotic, and these give the spread of its own |dE/E|
     sp = np.load(os.path.join(gold, "horizon_ensemble_spread.npz"))["de"]
     ref_all = np.concatenate([ref64, sp.ravel()])
+    # the fast form's arithmetic emulated on the host (same 64 systems)
+    ff = np.load(os.path.join(gold, "horizon_ensemble_fastform.npz"))["de"]
 
     def with_spread(r):
         r["reference_method_with_perturbed_runs_p50_p90_p99_max"] = [
@@ -857,6 +859,9 @@ def run_horizons(args):
         r["reference_method_with_perturbed_runs_samples"] = int(ref_all.size)
         r["reference_method_per_system_max_over_runs_first_64"] = [
             float(x) for x in np.maximum(ref64, sp.max(axis=1))]
+        r["fast_form_arithmetic_on_the_host_p50_p90_p99_max"] = [
+            float(np.percentile(ff, x)) for x in (50, 90, 99, 100)]
+        r["fast_form_arithmetic_on_the_host_at_or_below_1e-12"] = int((ff <= 1e-12).sum())
         return r
 
     if "ens64" in which:
