@@ -37,7 +37,8 @@ Run in a container where the reference sources exist:
   predicted from g with one rounding at the position's scale, the
   single-precision step-size root, g consistent with each step's guess),
   so that the fast form's energy error over 10^4 yr can be set beside the
-  reference method's on the host.
+  reference method's on the host; with two more runs each moved by one
+  unit in the last place, as the reference method's spread runs are.
 
 * ``horizon_cfg3.npz``: the Wisdom-Holman workload (``ics.test_particle_swarm
   (seed=1003)``, heliocentric: 1 MSun star, 5 planets, 1,048,576 test
@@ -193,37 +194,50 @@ def main_ensemble_spread(out=os.path.join(HERE, "horizon_ensemble_spread.npz"), 
           % (T, q[0], q[1], q[2], q[3], res[0]["kind"], time.time() - t0, cores, out))
 
 
-def ens_fastform_run(s):
+def ens_fastform_run(job):
+    s, k = job if isinstance(job, tuple) else (job, 0)
     import oracle
     O = oracle.Oracle()
     P, V, M, offs = ics.ensemble(n_systems=1, seed0=10000 + s)
+    if k:  # the same one-ulp moves as the reference method's perturbed runs
+        P = P.copy()
+        i = (5 * k) % P.size
+        P[i] = np.nextafter(P[i], np.inf if k % 2 else -np.inf)
     T = ENS_HORIZONS[-1]
     e0 = O.energy(P, V, M, G)
     t0 = time.time()
     out = O.radau15(P, V, M, np.zeros(M.size), G, 0.0, T, fastform=True)
     wall = time.time() - t0
     e1 = O.energy(out["pos"], out["vel"], M, G)
-    return {"s": s, "de": abs((e1 - e0) / e0), "wall": wall, "t": out["t"]}
+    return {"s": s, "k": k, "de": abs((e1 - e0) / e0), "wall": wall, "t": out["t"]}
 
 
-def main_ensemble_fastform(out=os.path.join(HERE, "horizon_ensemble_fastform.npz"), cores=None):
+def main_ensemble_fastform(out=os.path.join(HERE, "horizon_ensemble_fastform.npz"), cores=None,
+                           perturbations=(0, 1, 2)):
+    """Run k = 0 is the unperturbed one (``de``); k = 1, 2 move one
+    coordinate by one unit in the last place as in
+    horizon_ensemble_spread.npz (``de_pert``)."""
     _build_checkers()
     cores = cores or max(1, (os.cpu_count() or 2) - 1)
     t0 = time.time()
+    jobs = [(s, k) for k in perturbations for s in range(ENS_SYSTEMS)]
     with mp.get_context("spawn").Pool(cores) as pool:
-        res = pool.map(ens_fastform_run, range(ENS_SYSTEMS), chunksize=1)
-    de = np.zeros(ENS_SYSTEMS)
-    wall = np.zeros(ENS_SYSTEMS)
-    tt = np.zeros(ENS_SYSTEMS)
+        res = pool.map(ens_fastform_run, jobs, chunksize=1)
+    all_de = np.zeros((ENS_SYSTEMS, len(perturbations)))
+    wall = np.zeros_like(all_de)
+    tt = np.zeros_like(all_de)
     for r in res:
-        de[r["s"]], wall[r["s"]], tt[r["s"]] = r["de"], r["wall"], r["t"]
+        j = perturbations.index(r["k"])
+        all_de[r["s"], j], wall[r["s"], j], tt[r["s"], j] = r["de"], r["wall"], r["t"]
+    de = all_de[:, 0]
     np.savez_compressed(out, kind=np.array("oracle-fastform"), seed0=np.array([10000]),
-                        horizon=np.array([ENS_HORIZONS[-1]]), de=de, t=tt, wall=wall)
-    q = np.percentile(de, [50, 90, 99, 100])
-    print("ensemble %g yr, fast-form arithmetic: |dE/E| median %.2g p90 %.2g p99 %.2g max %.2g"
-          "; <=1e-12: %d/%d; %.0f s on %d cores; wrote %s"
-          % (ENS_HORIZONS[-1], q[0], q[1], q[2], q[3], int((de <= 1e-12).sum()), ENS_SYSTEMS,
-             time.time() - t0, cores, out))
+                        horizon=np.array([ENS_HORIZONS[-1]]), de=de, de_pert=all_de[:, 1:],
+                        perturbations=np.array(perturbations), t=tt, wall=wall)
+    q = np.percentile(all_de, [50, 90, 99, 100])
+    print("ensemble %g yr, fast-form arithmetic, %d runs: |dE/E| median %.2g p90 %.2g p99 %.2g "
+          "max %.2g; <=1e-12: %.0f %%; %.0f s on %d cores; wrote %s"
+          % (ENS_HORIZONS[-1], all_de.size, q[0], q[1], q[2], q[3],
+             100.0 * (all_de <= 1e-12).mean(), time.time() - t0, cores, out))
 
 
 CFG3_SAMPLE = 1024
