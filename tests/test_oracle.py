@@ -173,3 +173,24 @@ def test_fastform_emulation_is_the_same_integrator(oracle):
     assert np.max(d[ok] / n[ok]) <= 1e-10
     e0 = oracle.energy(P, V, M, G)
     assert abs((oracle.energy(fast["pos"], fast["vel"], M, G) - e0) / e0) <= 1e-13
+
+
+def test_energy_bar_reading_on_the_committed_runs():
+    """The reading of the 1e-12 energy bar at 10^4 yr on the committed runs
+    (tests/golden/make_horizons.py): over the same 64 ensemble systems, 3
+    runs each (two moved by one unit in the last place), the fast form's
+    arithmetic (the oracle's emulation) ends with at least the reference
+    method's share of runs within 1e-12 and every percentile within 10x of
+    the reference method's."""
+    import os
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    g = np.load(os.path.join(here, "horizon_ensemble.npz"))
+    h = list(g["horizons"]).index(10000.0)
+    ref = np.concatenate([g["de"][:, h],
+                          np.load(os.path.join(here, "horizon_ensemble_spread.npz"))["de"].ravel()])
+    f = np.load(os.path.join(here, "horizon_ensemble_fastform.npz"))
+    fast = np.concatenate([f["de"], f["de_pert"].ravel()])
+    assert ref.size == fast.size == 192
+    assert (fast <= 1e-12).mean() >= (ref <= 1e-12).mean()
+    for q in (50, 90, 99, 100):
+        assert np.percentile(fast, q) <= 10 * np.percentile(ref, q), q
