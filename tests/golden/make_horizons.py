@@ -23,13 +23,13 @@ Run in a container where the reference sources exist:
   compared with.
 
 * ``horizon_ensemble_spread.npz``: the same 64 systems over 10,000 yr,
-  rerun twice by the reference library with one coordinate moved by one
-  unit in the last place (coordinate 5k mod 3n, up for k = 1, down for
-  k = 2).  Over 10^4 yr several of these systems are chaotic, so |dE/E|
+  rerun four times by the reference library with one coordinate moved by
+  one unit in the last place (coordinate 5k mod 3n, up for odd k, down for
+  even k, k = 1 .. 4).  Over 10^4 yr several of these systems are chaotic, so |dE/E|
   of one system depends on the path: the perturbed runs show how far the
   reference method's own result moves (system 10 of the set: 1.4e-11 to
   1.1e-9 over such runs), and together with the unperturbed run they give
-  a 192-sample distribution of the reference method's |dE/E| at 10^4 yr.
+  a 320-sample distribution of the reference method's |dE/E| at 10^4 yr.
 
 * ``horizon_ensemble_fastform.npz``: the same 64 systems over 10,000 yr
   by the oracle with the GPU fast form's arithmetic (``Oracle.radau15(...,
@@ -37,7 +37,7 @@ Run in a container where the reference sources exist:
   predicted from g with one rounding at the position's scale, the
   single-precision step-size root, g consistent with each step's guess),
   so that the fast form's energy error over 10^4 yr can be set beside the
-  reference method's on the host; with two more runs each moved by one
+  reference method's on the host; with four more runs each moved by one
   unit in the last place, as the reference method's spread runs are.
 
 * ``horizon_cfg3.npz``: the Wisdom-Holman workload (``ics.test_particle_swarm
@@ -172,7 +172,7 @@ def main_ensemble(out=os.path.join(HERE, "horizon_ensemble.npz"), cores=None):
 
 
 def main_ensemble_spread(out=os.path.join(HERE, "horizon_ensemble_spread.npz"), cores=None,
-                         perturbations=(1, 2)):
+                         perturbations=(1, 2, 3, 4)):
     _build_checkers()
     cores = cores or max(1, (os.cpu_count() or 2) - 1)
     T = ENS_HORIZONS[-1]
@@ -213,8 +213,8 @@ def ens_fastform_run(job):
 
 
 def main_ensemble_fastform(out=os.path.join(HERE, "horizon_ensemble_fastform.npz"), cores=None,
-                           perturbations=(0, 1, 2)):
-    """Run k = 0 is the unperturbed one (``de``); k = 1, 2 move one
+                           perturbations=(0, 1, 2, 3, 4)):
+    """Run k = 0 is the unperturbed one (``de``); k = 1 .. 4 move one
     coordinate by one unit in the last place as in
     horizon_ensemble_spread.npz (``de_pert``)."""
     _build_checkers()
